@@ -1,0 +1,455 @@
+"""Seeded synthetic ChIMES workloads.
+
+Two things are generated here, both deterministic for a given seed:
+
+* parameter files in the ChIMES text format, i.e. the exact layout that
+  ``chimesFF::read_parameters`` parses (chimesFF/src/chimesFF.cpp:354-1570):
+  ``PAIRTYP: CHEBYSHEV o2 o3 o4``, ``ATOM TYPES``, ``# TYPEIDX #`` rows,
+  ``ATOM PAIRS`` with 8-column ``# PAIRIDX #`` rows (S_DELTA present, MORSE
+  lambda last), ``FCUT TYPE``, ``SPECIAL 3B/4B S_MAXIM/S_MINIM``,
+  ``PAIRTYPE PARAMS`` (exactly o2 ``pow coeff`` lines),
+  ``TRIPLETTYPE PARAMS`` / ``QUADRUPLETYPE PARAMS`` blocks (powers in columns
+  1..P, coefficient in column P+3), ``PAIRMAPS``/``TRIPMAPS``/``QUADMAPS`` whose
+  keys concatenate the proper pair names in ij,ik,jk / ij,ik,il,jk,jl,kl order
+  (chimesFF.cpp:976-1005, 1307-1349), and ``ENDFILE``;
+* periodic configurations: positions by random sequential insertion with a
+  minimum-image rejection radius, and element labels drawn at random.
+
+Many-body power tuples are listed once per orbit of the label-preserving atom
+permutations of the cluster type ("deduplicated"): TOTAL = UNIQUE = number of
+orbit representatives.  ``expand=True`` instead lists every member of each
+orbit with the orbit's shared coefficient, which is how the published ChIMES
+files are laid out (e.g. ``UNIQUE: 30 TOTAL: 112``).
+
+Powers run over [0, order-1]: the reference indexes ``Tn[pow]`` in vectors of
+length order+1 (chimesFF.h:46, chimesFF.cpp:2081), so order-1 is the largest
+power a 3B/4B term may use without reading past its polynomial table.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import itertools
+import math
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+ELEMENTS = ("C", "N", "O")
+MASSES = {"C": 12.011, "N": 14.0067, "O": 15.9994}
+
+
+# ----------------------------------------------------------------------------
+# Cluster-type combinatorics
+# ----------------------------------------------------------------------------
+
+def pair_slots(n_atoms: int) -> List[Tuple[int, int]]:
+    """Pair order of a cluster: ij, ik, jk (3B) / ij, ik, il, jk, jl, kl (4B)."""
+    return [(i, j) for i in range(n_atoms) for j in range(i + 1, n_atoms)]
+
+
+def _label_group(atoms: Sequence[int]) -> List[Tuple[int, ...]]:
+    n = len(atoms)
+    return [s for s in itertools.permutations(range(n))
+            if all(atoms[s[i]] == atoms[i] for i in range(n))]
+
+
+def _pair_permutation(sigma: Sequence[int], n_atoms: int) -> List[int]:
+    slots = pair_slots(n_atoms)
+    index = {p: k for k, p in enumerate(slots)}
+    out = []
+    for (i, j) in slots:
+        a, b = sigma[i], sigma[j]
+        out.append(index[(min(a, b), max(a, b))])
+    return out
+
+
+def power_orbits(atoms: Sequence[int], order: int, min_nonzero: int) -> List[List[Tuple[int, ...]]]:
+    """Orbits of power tuples in [0, order-1]^P with >= min_nonzero nonzero
+    entries under the label-preserving permutations of the cluster's atoms.
+    Each orbit is returned as a list whose first member is its lexicographically
+    smallest tuple (the representative); orbits are ordered by representative."""
+    n = len(atoms)
+    npairs = n * (n - 1) // 2
+    perms = [_pair_permutation(s, n) for s in _label_group(atoms)]
+    seen = set()
+    orbits = []
+    for p in itertools.product(range(order), repeat=npairs):
+        if sum(1 for v in p if v) < min_nonzero or p in seen:
+            continue
+        members = set()
+        for perm in perms:
+            q = [0] * npairs
+            for k in range(npairs):
+                q[perm[k]] = p[k]
+            members.add(tuple(q))
+        seen |= members
+        orbits.append(sorted(members))
+    return orbits
+
+
+# ----------------------------------------------------------------------------
+# Parameter files
+# ----------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class ParamSpec:
+    """Recipe for one synthetic parameter set.
+
+    ``rin``/``rout``/``lam`` are either one value for every pair type or a
+    (low, high) range sampled per pair type.  ``s3max`` etc. are ``None``
+    (keep the 2B-derived defaults), a float (``ALL v``) or a dict mapping a
+    triplet/quadruplet type index to per-pair values (``SPECIFIC``)."""
+    elements: Sequence[str]
+    orders: Tuple[int, int, int] = (12, 8, 0)
+    rin: object = 1.0
+    rout: object = 5.0
+    lam: object = 1.4
+    fcut: Tuple = ("TERSOFF", 0.5)
+    s3max: object = None
+    s3min: object = None
+    s4max: object = None
+    s4min: object = None
+    excluded3: Tuple[int, ...] = ()
+    excluded4: Tuple[int, ...] = ()
+    energy_offsets: Optional[Sequence[float]] = None
+    penalty: Optional[Tuple[float, float]] = None
+    coeff_sigma: float = 0.05
+    expand: bool = False
+    seed: int = 1000
+
+
+def _draw(v, rng):
+    if isinstance(v, (tuple, list)):
+        return float(rng.uniform(v[0], v[1]))
+    return float(v)
+
+
+def _fmt(x: float) -> str:
+    return repr(float(x))
+
+
+def build_param_text(spec: ParamSpec) -> str:
+    rng = np.random.default_rng(spec.seed)
+    el = list(spec.elements)
+    nt = len(el)
+    o2, o3, o4 = spec.orders
+    pairs = [(a, b) for a in range(nt) for b in range(a, nt)]
+    pidx = {p: k for k, p in enumerate(pairs)}
+
+    def proper(a, b):
+        a, b = min(a, b), max(a, b)
+        return el[a] + el[b]
+
+    pair_rin = [_draw(spec.rin, rng) for _ in pairs]
+    pair_rout = [_draw(spec.rout, rng) for _ in pairs]
+    pair_lam = [_draw(spec.lam, rng) for _ in pairs]
+
+    L = []
+    w = L.append
+    w("! Synthetic ChIMES parameter set (seeded generator)")
+    w("! seed = %d" % spec.seed)
+    w("")
+    w("PAIRTYP: CHEBYSHEV  %d %d %d -1 1" % (o2, o3, o4))
+    w("")
+    w("ATOM TYPES: %d" % nt)
+    w("")
+    w("# TYPEIDX #\t# ATM_TYP #\t# ATMCHRG #\t# ATMMASS #")
+    for i, e in enumerate(el):
+        w("%d\t\t%s\t\t0\t\t%s" % (i, e, MASSES.get(e, 10.0)))
+    w("")
+    w("ATOM PAIRS: %d" % len(pairs))
+    w("")
+    w("# PAIRIDX #\t# ATM_TY1 #\t# ATM_TY1 #\t# S_MINIM #\t# S_MAXIM #\t# S_DELTA #\t# CHBDIST #\t# MORSE_LAMBDA #")
+    for k, (a, b) in enumerate(pairs):
+        w("\t%d\t%s\t%s\t%s\t%s\t0.01\tMORSE\t%s" % (k, el[a], el[b], _fmt(pair_rin[k]),
+                                                      _fmt(pair_rout[k]), _fmt(pair_lam[k])))
+    w("")
+    if spec.penalty is not None:
+        w("PAIR CHEBYSHEV PENALTY DIST: %s" % _fmt(spec.penalty[0]))
+        w("PAIR CHEBYSHEV PENALTY SCALING: %s" % _fmt(spec.penalty[1]))
+        w("")
+    if spec.fcut[0] == "TERSOFF":
+        w("FCUT TYPE: TERSOFF %s" % _fmt(spec.fcut[1]))
+    else:
+        w("FCUT TYPE: CUBIC")
+    w("")
+
+    trips = list(itertools.combinations_with_replacement(range(nt), 3)) if o3 > 0 else []
+    quads = list(itertools.combinations_with_replacement(range(nt), 4)) if o4 > 0 else []
+    trip_pairs = [[proper(t[i], t[j]) for (i, j) in pair_slots(3)] for t in trips]
+    quad_pairs = [[proper(q[i], q[j]) for (i, j) in pair_slots(4)] for q in quads]
+
+    def special(tag, val, types, tpairs, maps_key):
+        if val is None:
+            return
+        if isinstance(val, dict):
+            w("%s SPECIFIC %d" % (tag, len(val)))
+            for t, cuts in sorted(val.items()):
+                w("%s %s %s" % (maps_key[t], " ".join(tpairs[t]), " ".join(_fmt(c) for c in cuts)))
+        else:
+            w("%s ALL %s" % (tag, _fmt(val)))
+        w("")
+
+    # SPECIFIC rows are looked up by a map key; use the key of the type's own
+    # (sorted) atom order.
+    trip_key = {ti: "".join(trip_pairs[ti]) for ti in range(len(trips))}
+    quad_key = {qi: "".join(quad_pairs[qi]) for qi in range(len(quads))}
+
+    if o3 > 0:
+        special("SPECIAL 3B S_MAXIM:", spec.s3max, trips, trip_pairs, trip_key)
+        special("SPECIAL 3B S_MINIM:", spec.s3min, trips, trip_pairs, trip_key)
+    if o4 > 0:
+        special("SPECIAL 4B S_MAXIM:", spec.s4max, quads, quad_pairs, quad_key)
+        special("SPECIAL 4B S_MINIM:", spec.s4min, quads, quad_pairs, quad_key)
+
+    if o3 > 0:
+        w("ATOM PAIR TRIPLETS: %d" % len(trips))
+    if o4 > 0:
+        w("ATOM PAIR QUADRUPLETS: %d" % len(quads))
+    w("")
+    w("PAIR CHEBYSHEV PARAMS ")
+    w("")
+    for k, (a, b) in enumerate(pairs):
+        w("PAIRTYPE PARAMS: %d %s %s" % (k, el[a], el[b]))
+        w("")
+        for pw in range(o2):
+            c = rng.normal(0.0, spec.coeff_sigma) / (1.0 + pw)
+            w("%d %s" % (pw, _fmt(c)))
+        w(" ")
+
+    def cluster_block(title, head, idx, atoms, pnames, order, min_nz, excluded):
+        w(title)
+        w("   INDEX: %d ATOMS: %s" % (idx, " ".join(el[a] for a in atoms)))
+        if idx in excluded:
+            w("PAIRS: %s EXCLUDED: 0 TOTAL: 0" % " ".join(pnames))
+            w("")
+            return
+        orbits = power_orbits(atoms, order, min_nz)
+        rows = []
+        for oi, orb in enumerate(orbits):
+            c = rng.normal(0.0, spec.coeff_sigma) / (1.0 + sum(orb[0]))
+            members = orb if spec.expand else orb[:1]
+            for m in members:
+                rows.append((m, oi, c))
+        w("PAIRS: %s UNIQUE: %d TOTAL: %d" % (" ".join(pnames), len(orbits), len(rows)))
+        w(head)
+        w("   " + "-" * 76)
+        for r, (m, oi, c) in enumerate(rows):
+            w("%d %s %d %d %s" % (r, " ".join(str(v) for v in m), oi, oi, _fmt(c)))
+        w("")
+
+    if o3 > 0:
+        w("TRIPLET CHEBYSHEV PARAMS ")
+        w("")
+        for ti, t in enumerate(trips):
+            cluster_block("TRIPLETTYPE PARAMS:",
+                          "     index  |  powers  |  equiv index  |  param index  |       parameter       ",
+                          ti, t, trip_pairs[ti], o3, 2, set(spec.excluded3))
+    if o4 > 0:
+        w("QUADRUPLET CHEBYSHEV PARAMS ")
+        w("")
+        for qi, q in enumerate(quads):
+            cluster_block("QUADRUPLETYPE PARAMS: ",
+                          "     index  |  powers  |  equiv index  |  param index  |       parameter       ",
+                          qi, q, quad_pairs[qi], o4, 3, set(spec.excluded4))
+
+    pmap = {}
+    for a in range(nt):
+        for b in range(nt):
+            pmap[el[a] + el[b]] = pidx[(min(a, b), max(a, b))]
+    w("")
+    w("PAIRMAPS: %d" % len(pmap))
+    for k in sorted(pmap):
+        w("%d %s" % (pmap[k], k))
+    w("")
+    if o3 > 0:
+        tmap = {}
+        for t in itertools.product(range(nt), repeat=3):
+            key = proper(t[0], t[1]) + proper(t[0], t[2]) + proper(t[1], t[2])
+            ti = trips.index(tuple(sorted(t)))
+            tmap[key] = -1 if ti in spec.excluded3 else ti
+        w("TRIPMAPS: %d" % len(tmap))
+        for k in sorted(tmap):
+            w("%d %s" % (tmap[k], k))
+        w("")
+    if o4 > 0:
+        qmap = {}
+        for q in itertools.product(range(nt), repeat=4):
+            key = "".join(proper(q[i], q[j]) for (i, j) in pair_slots(4))
+            qi = quads.index(tuple(sorted(q)))
+            qmap[key] = -1 if qi in spec.excluded4 else qi
+        w("QUADMAPS: %d" % len(qmap))
+        for k in sorted(qmap):
+            w("%d %s" % (qmap[k], k))
+        w("")
+    if spec.energy_offsets is not None:
+        w("NO ENERGY OFFSETS: %d" % nt)
+        for i in range(nt):
+            w("ENERGY OFFSET %d %s" % (i + 1, _fmt(spec.energy_offsets[i])))
+    w("ENDFILE")
+    return "\n".join(L) + "\n"
+
+
+def write_param_file(path: str, spec: ParamSpec) -> str:
+    with open(path, "w") as f:
+        f.write(build_param_text(spec))
+    return path
+
+
+# ----------------------------------------------------------------------------
+# Configurations
+# ----------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Config:
+    types: List[str]
+    pos: np.ndarray          # (N, 3) Cartesian, Angstrom
+    cell: np.ndarray         # (3, 3) rows are the a, b, c lattice vectors
+
+    @property
+    def n_atoms(self) -> int:
+        return len(self.types)
+
+    def xyz_text(self) -> str:
+        c = self.cell.reshape(-1)
+        out = ["%d" % self.n_atoms, " ".join(_fmt(v) for v in c)]
+        for t, p in zip(self.types, self.pos):
+            out.append("%s %s %s %s" % (t, _fmt(p[0]), _fmt(p[1]), _fmt(p[2])))
+        return "\n".join(out) + "\n"
+
+    def write_xyz(self, path: str) -> str:
+        with open(path, "w") as f:
+            f.write(self.xyz_text())
+        return path
+
+
+def read_xyz(path: str) -> Config:
+    """Reads the .xyz layout of the reference's example drivers: atom count,
+    a comment line holding the 9 cell-vector components, then ``type x y z``."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    n = int(lines[0].split()[0])
+    cell = np.array([float(v) for v in lines[1].split()[:9]]).reshape(3, 3)
+    types, pos = [], []
+    for ln in lines[2:2 + n]:
+        w = ln.split()
+        types.append(w[0])
+        pos.append([float(w[1]), float(w[2]), float(w[3])])
+    return Config(types, np.array(pos, dtype=np.float64), cell)
+
+
+def random_config(n_atoms: int, cell, elements: Sequence[str], rmin: float, seed: int,
+                  type_probs: Optional[Sequence[float]] = None, max_tries: int = 200000) -> Config:
+    """Random sequential insertion: uniform fractional coordinates, rejected when
+    the minimum-image distance to any accepted atom is below ``rmin``."""
+    rng = np.random.default_rng(seed)
+    cell = np.asarray(cell, dtype=np.float64).reshape(3, 3)
+    ortho = np.allclose(cell - np.diag(np.diag(cell)), 0.0)
+    frac = np.zeros((n_atoms, 3))
+    n = 0
+    tries = 0
+    if ortho and n_atoms > 1500:
+        lengths = np.diag(cell)
+        ncell = np.maximum((lengths // rmin).astype(int), 1)
+        grid: Dict[Tuple[int, int, int], List[int]] = {}
+        while n < n_atoms:
+            tries += 1
+            if tries > max_tries * 10:
+                raise RuntimeError("random_config: packing too dense")
+            f = rng.random(3)
+            c = tuple((f * ncell).astype(int) % ncell)
+            cand = []
+            for d in itertools.product((-1, 0, 1), repeat=3):
+                cand.extend(grid.get(tuple((np.array(c) + d) % ncell), ()))
+            if cand:
+                df = frac[cand] - f
+                df -= np.round(df)
+                r = np.sqrt(((df * lengths) ** 2).sum(axis=1))
+                if r.min() < rmin:
+                    continue
+            frac[n] = f
+            grid.setdefault(c, []).append(n)
+            n += 1
+    else:
+        while n < n_atoms:
+            tries += 1
+            if tries > max_tries:
+                raise RuntimeError("random_config: packing too dense")
+            f = rng.random(3)
+            if n:
+                df = frac[:n] - f
+                df -= np.round(df)
+                r = np.sqrt(((df @ cell) ** 2).sum(axis=1))
+                if r.min() < rmin:
+                    continue
+            frac[n] = f
+            n += 1
+    pos = frac @ cell
+    probs = None if type_probs is None else np.asarray(type_probs, dtype=np.float64)
+    tidx = rng.choice(len(elements), size=n_atoms, p=probs)
+    return Config([elements[i] for i in tidx], pos, cell)
+
+
+# ----------------------------------------------------------------------------
+# The named workloads (seed = 1000 + workload number)
+# ----------------------------------------------------------------------------
+
+def spec_c1() -> ParamSpec:
+    """1 element; 2B order 12 (rin 1.0, rout 5.0, lambda 1.4); 3B order 8 with
+    outer cutoff 4.0; Tersoff cutoff with offset 0.5; no 4B."""
+    return ParamSpec(elements=["C"], orders=(12, 8, 0), rin=1.0, rout=5.0, lam=1.4,
+                     fcut=("TERSOFF", 0.5), s3max=4.0, seed=1001)
+
+
+def config_c1() -> Config:
+    return random_config(64, np.diag([9.0, 9.0, 9.0]), ["C"], 1.2, seed=1101)
+
+
+def spec_c2(elements=("C", "N"), orders=(12, 8, 4), seed=1002) -> ParamSpec:
+    """Per pair type: 2B order 12, rin 0.9, rout 5.0, lambda ~ U(1.3, 1.6);
+    3B order 8 with outer 4.0; 4B order 4 with outer 3.2."""
+    return ParamSpec(elements=list(elements), orders=orders, rin=0.9, rout=5.0, lam=(1.3, 1.6),
+                     fcut=("TERSOFF", 0.5), s3max=4.0, s4max=3.2, seed=seed)
+
+
+def config_c2(n_atoms=1024, box=22.0, seed=1102) -> Config:
+    return random_config(n_atoms, np.diag([box, box, box]), ["C", "N"], 1.0, seed=seed,
+                         type_probs=[0.5, 0.5])
+
+
+def spec_c3() -> ParamSpec:
+    return spec_c2(orders=(12, 10, 4), seed=1003)
+
+
+def config_c3(n_atoms=32768, box=(70.0, 70.0, 72.0), seed=1103) -> Config:
+    return random_config(n_atoms, np.diag(box), ["C", "N"], 1.0, seed=seed, type_probs=[0.5, 0.5])
+
+
+def spec_c4() -> ParamSpec:
+    """Three-element parameter set of the 12/10/4 recipe; each batched
+    configuration uses one, two or all three of its elements."""
+    return spec_c2(elements=("C", "N", "O"), orders=(12, 10, 4), seed=1004)
+
+
+def configs_c4(n_configs=4096, seed=1104, n_min=8, n_max=512) -> List[Config]:
+    """Atom counts log-uniform in [n_min, n_max], densities U(0.05, 0.12) per
+    cubic Angstrom, 1-3 elements per configuration."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(n_configs):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        rho = rng.uniform(0.05, 0.12)
+        L = (n / rho) ** (1.0 / 3.0)
+        ne = int(rng.integers(1, 4))
+        out.append(random_config(n, np.diag([L, L, L]), list(ELEMENTS[:ne]), 1.0,
+                                 seed=int(rng.integers(1 << 31))))
+    return out
+
+
+def specs_c5() -> List[ParamSpec]:
+    """Three parameter sets for the serving workload: 12/8/4 with one element,
+    12/10/4 with two, 12/8/4 with three."""
+    return [spec_c2(elements=("C",), orders=(12, 8, 4), seed=1051),
+            spec_c2(elements=("C", "N"), orders=(12, 10, 4), seed=1052),
+            spec_c2(elements=("C", "N", "O"), orders=(12, 8, 4), seed=1053)]

@@ -1,0 +1,995 @@
+/*
+ * ORACLE -- test infrastructure only.  Nothing in the product links, loads or
+ * calls this file; only tests/, the smoke check and the bench's CPU-baseline
+ * leg do, as the checker.
+ *
+ * A plain-C restatement of the reference ChIMES calculator's force-evaluation
+ * path (rk-lindsey/chimes_calculator), single-threaded, with the reference's
+ * floating-point operation order kept term by term so that, built with
+ * -ffp-contract=off against the same libm, it reproduces the reference's
+ * results bit for bit.  Each function names the reference code it restates.
+ *
+ *   parameters ....... chimesFF::read_parameters     chimesFF/src/chimesFF.cpp:354-1570
+ *   pair permutations  chimesFF::build_atom_and_pair_mappers  chimesFF/src/chimesFF.h:438-539
+ *                      build_pair_int_trip_map / quad_map     chimesFF.cpp:3023-3080, 2958-3021
+ *   Chebyshev ........ set_cheby_polys               chimesFF.h:542-628
+ *                      set_polys_out_of_range        chimesFF.cpp:1572-1613
+ *   cutoff/penalty ... get_fcut / get_penalty        chimesFF.h:347-419
+ *   cluster terms .... compute_1B/2B/3B/4B           chimesFF.cpp:1636-1775, 1931-2176, 2496-2872
+ *   system set-up .... set_hmat, simulation_system::init, reorient, build_layered_system
+ *                      serial_interface/src/serial_chimes_interface.cpp:85-587
+ *   cluster lists .... simulation_system::build_neigh_lists  serial_chimes_interface.cpp:588-864
+ *   driver ........... serial_chimes_interface::calculate    serial_chimes_interface.cpp:960-1124
+ *
+ * Errors are returned as negative status codes with a message (the reference
+ * prints and calls exit(0)); the oracle never terminates its host process.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORA_PI 3.14159265359 /* chimesFF.h:22 */
+#define MAXTOK 64
+
+typedef struct {
+    int ntypes, npairs, o2, o3, o4;
+    char (*atm)[16];          /* [ntypes] element names                   */
+    char (*pname)[40];        /* [npairs] proper pair name (atm1+atm2)     */
+    char (*pa1)[16], (*pa2)[16];
+    double *rin, *rout, *lam; /* [npairs]                                  */
+    int fcut_tersoff; double fcut_var;
+    double pen_dist, pen_scale, inner_smooth;
+    double *eoff;             /* [ntypes]                                  */
+    int *pows2; double *c2;   /* [npairs][o2]                              */
+    int *pair_map;            /* [nt*nt] atom_int_pair_map                 */
+    int *prpr;                /* [nt*nt] index of proper pair name         */
+    /* 3B */
+    int ntrips; int *n3; int **pw3; double **c3; double *cut3; /* cut3[t][2][3] */
+    char (*t3atm)[3][16]; char (*t3pair)[3][40];
+    int *trip_map; int *trip_perm; /* [nt^3], [nt^3][3] */
+    /* 4B */
+    int nquads; int *n4; int **pw4; double **c4; double *cut4; /* cut4[q][2][6] */
+    char (*q4atm)[4][16]; char (*q4pair)[6][40];
+    int *quad_map; int *quad_perm; /* [nt^4], [nt^4][6] */
+    int badness;
+    long n_penalty, n_below_rin;
+} ora_ff;
+
+typedef struct {
+    int n_atoms, n_ghost, n_repl, n_replicates, n_layers;
+    double *x, *y, *z; int *parent, *rep_parent, *typ;
+    double h[9], hi[9];
+    double la, lb, lc, vol;
+    long cap;
+} ora_sys;
+
+typedef struct {
+    ora_ff ff;
+    char err[512];
+    /* last calculate() cluster lists (neigh/sys ghost indices) */
+    long n2, n3, n4;
+    int *l2, *l3, *l4;
+    long cap2, cap3, cap4;
+} ora_handle;
+
+/* ------------------------------------------------------------------ */
+/* text helpers (chimesFF::split_line, chimesFF.cpp:148-180)           */
+/* ------------------------------------------------------------------ */
+typedef struct { char **lines; int n; char *buf; } ora_text;
+
+static int load_text(const char *path, ora_text *t) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    fseek(f, 0, SEEK_END); long sz = ftell(f); fseek(f, 0, SEEK_SET);
+    t->buf = (char *)malloc(sz + 1);
+    if (fread(t->buf, 1, sz, f) != (size_t)sz) { fclose(f); return -1; }
+    t->buf[sz] = 0; fclose(f);
+    int cap = 1024; t->lines = (char **)malloc(cap * sizeof(char *)); t->n = 0;
+    char *p = t->buf;
+    while (*p) {
+        if (t->n == cap) { cap *= 2; t->lines = (char **)realloc(t->lines, cap * sizeof(char *)); }
+        t->lines[t->n++] = p;
+        char *e = strchr(p, '\n');
+        if (!e) break;
+        *e = 0; p = e + 1;
+    }
+    return 0;
+}
+
+static int split(const char *line, char tok[][MAXTOK], int maxt) {
+    char tmp[4096];
+    strncpy(tmp, line, sizeof(tmp) - 1); tmp[sizeof(tmp) - 1] = 0;
+    char *c = strchr(tmp, '!'); if (c) *c = 0;
+    c = strstr(tmp, "##"); if (c) *c = 0;
+    int n = 0; char *s = tmp;
+    while (*s && n < maxt) {
+        while (*s == ' ' || *s == '\t' || *s == '\r' || *s == '\n' || *s == '\v' || *s == '\f') s++;
+        if (!*s) break;
+        int k = 0;
+        while (*s && !(*s == ' ' || *s == '\t' || *s == '\r' || *s == '\n' || *s == '\v' || *s == '\f')) {
+            if (k < MAXTOK - 1) tok[n][k++] = *s;
+            s++;
+        }
+        tok[n][k] = 0; n++;
+    }
+    return n;
+}
+
+#define FAIL(h, ...) do { snprintf((h)->err, sizeof((h)->err), __VA_ARGS__); return -1; } while (0)
+
+/* get_proper_pair, chimesFF.cpp:69-84 */
+static int proper_pair(ora_ff *ff, const char *a, const char *b) {
+    for (int i = 0; i < ff->npairs; i++) {
+        if (!strcmp(a, ff->pa1[i]) && !strcmp(b, ff->pa2[i])) return i;
+        if (!strcmp(b, ff->pa1[i]) && !strcmp(a, ff->pa2[i])) return i;
+    }
+    return -1;
+}
+
+static int find_atm(ora_ff *ff, const char *name) {
+    for (int i = 0; i < ff->ntypes; i++) if (!strcmp(ff->atm[i], name)) return i;
+    return ff->ntypes;
+}
+
+/* std::next_permutation on a small int array */
+static int next_perm(int *a, int n) {
+    int i = n - 2;
+    while (i >= 0 && a[i] >= a[i + 1]) i--;
+    if (i < 0) { for (int l = 0, r = n - 1; l < r; l++, r--) { int t = a[l]; a[l] = a[r]; a[r] = t; } return 0; }
+    int j = n - 1;
+    while (a[j] <= a[i]) j--;
+    int t = a[i]; a[i] = a[j]; a[j] = t;
+    for (int l = i + 1, r = n - 1; l < r; l++, r--) { t = a[l]; a[l] = a[r]; a[r] = t; }
+    return 1;
+}
+
+/* build_atom_and_pair_mappers, chimesFF.h:438-539.  pair_map carries over
+ * between calls when no permutation matches, as the reference's reused
+ * vector does. */
+static void atom_pair_mapper(ora_ff *ff, int natoms, const int *typ, char (*clu_pairs)[40], int *pair_map) {
+    int npairs = natoms * (natoms - 1) / 2;
+    int perm[4], tmp_pairs[6][2], run_pairs[6][2];
+    memset(run_pairs, 0, sizeof(run_pairs));
+    for (int i = 0; i < natoms; i++) perm[i] = i;
+    int idx = 0;
+    for (int i = 0; i < natoms; i++) for (int j = i + 1; j < natoms; j++) { tmp_pairs[idx][0] = i; tmp_pairs[idx][1] = j; idx++; }
+    do {
+        int match = 1; idx = 0;
+        for (int i = 0; i < natoms && match; i++)
+            for (int j = i + 1; j < natoms; j++) {
+                const char *rt = ff->pname[ff->prpr[typ[perm[i]] * ff->ntypes + typ[perm[j]]]];
+                if (strcmp(clu_pairs[idx], rt)) { match = 0; break; }
+                idx++;
+            }
+        if (match) {
+            idx = 0;
+            for (int i = 0; i < natoms; i++) for (int j = i + 1; j < natoms; j++) { run_pairs[idx][0] = perm[i]; run_pairs[idx][1] = perm[j]; idx++; }
+            break;
+        }
+    } while (next_perm(perm, natoms));
+    for (int i = 0; i < npairs; i++)
+        for (int j = 0; j < npairs; j++)
+            if ((run_pairs[i][0] == tmp_pairs[j][0] && run_pairs[i][1] == tmp_pairs[j][1]) ||
+                (run_pairs[i][0] == tmp_pairs[j][1] && run_pairs[i][1] == tmp_pairs[j][0]))
+                pair_map[j] = i;
+}
+
+/* ------------------------------------------------------------------ */
+/* read_parameters, chimesFF.cpp:354-1570                              */
+/* ------------------------------------------------------------------ */
+static int parse(ora_handle *h, const char *path) {
+    ora_ff *ff = &h->ff;
+    ora_text T;
+    if (load_text(path, &T)) FAIL(h, "cannot open parameter file: %s", path);
+    char tok[MAXTOK][MAXTOK];
+    int L;
+    ff->pen_dist = 0.01; ff->pen_scale = 1.0e4; ff->inner_smooth = 0.01; /* chimesFF.cpp:104-116 */
+    ff->fcut_tersoff = 0;
+    /* pass 1: orders */
+    int found = 0;
+    for (L = 0; L < T.n; L++) {
+        if (strstr(T.lines[L], "ENDFILE")) break;
+        if (strstr(T.lines[L], "PAIRTYP: CHEBYSHEV")) {
+            int n = split(T.lines[L], tok, MAXTOK);
+            if (n < 3) FAIL(h, "PAIRTYP line must contain the 2-body order");
+            ff->o2 = atoi(tok[2]); ff->o3 = n >= 4 ? atoi(tok[3]) : 0; ff->o4 = n >= 5 ? atoi(tok[4]) : 0;
+            found = 1; break;
+        }
+    }
+    if (!found) FAIL(h, "not a ChIMES Chebyshev parameter file");
+    /* pass 2: general */
+    int npairs = 0;
+    for (L = 0; L < T.n; L++) {
+        const char *ln = T.lines[L];
+        if (strstr(ln, "ENDFILE")) break;
+        if (strstr(ln, "ATOM TYPES:")) {
+            split(ln, tok, MAXTOK); ff->ntypes = atoi(tok[2]);
+            ff->eoff = (double *)calloc(ff->ntypes, sizeof(double));
+            ff->atm = calloc(ff->ntypes, sizeof(*ff->atm));
+        }
+        if (strstr(ln, "# TYPEIDX #")) {
+            for (int i = 0; i < ff->ntypes; i++) {
+                if (++L >= T.n) FAIL(h, "truncated TYPEIDX block");
+                split(T.lines[L], tok, MAXTOK); strncpy(ff->atm[i], tok[1], 15);
+            }
+        }
+        if (strstr(ln, "ATOM PAIRS:")) { split(ln, tok, MAXTOK); npairs = atoi(tok[2]); }
+        if (strstr(ln, "# PAIRIDX #")) {
+            if (strstr(ln, "# USEOVRP #")) continue;
+            ff->npairs = npairs;
+            ff->pname = calloc(npairs, sizeof(*ff->pname)); ff->pa1 = calloc(npairs, sizeof(*ff->pa1));
+            ff->pa2 = calloc(npairs, sizeof(*ff->pa2));
+            ff->rin = calloc(npairs, sizeof(double)); ff->rout = calloc(npairs, sizeof(double));
+            ff->lam = calloc(npairs, sizeof(double));
+            for (int i = 0; i < npairs; i++) {
+                if (++L >= T.n) FAIL(h, "truncated PAIRIDX block");
+                int n = split(T.lines[L], tok, MAXTOK);
+                int xf, mo;
+                if (n == 8) { xf = 6; mo = 7; } else if (n == 7) { xf = 5; mo = 6; }
+                else FAIL(h, "pair line: expect 7 or 8 entries");
+                strncpy(ff->pa1[i], tok[1], 15); strncpy(ff->pa2[i], tok[2], 15);
+                snprintf(ff->pname[i], 40, "%s%s", tok[1], tok[2]);
+                ff->rin[i] = strtod(tok[3], 0); ff->rout[i] = strtod(tok[4], 0);
+                if (strcmp(tok[xf], "MORSE")) FAIL(h, "only the MORSE distance transformation is supported");
+                ff->lam[i] = strtod(tok[mo], 0);
+            }
+        }
+        if (strstr(ln, "FCUT TYPE:")) {
+            split(ln, tok, MAXTOK);
+            if (!strcmp(tok[2], "CUBIC")) ff->fcut_tersoff = 0;
+            else if (!strcmp(tok[2], "TERSOFF")) { ff->fcut_tersoff = 1; ff->fcut_var = strtod(tok[3], 0); }
+            else FAIL(h, "unknown FCUT TYPE: %s", tok[2]);
+        }
+        if (strstr(ln, "PAIR CHEBYSHEV PENALTY DIST:")) { split(ln, tok, MAXTOK); ff->pen_dist = strtod(tok[4], 0); }
+        if (strstr(ln, "PAIR CHEBYSHEV PENALTY SCALING:")) { split(ln, tok, MAXTOK); ff->pen_scale = strtod(tok[4], 0); }
+        if (strstr(ln, "NO ENERGY OFFSETS:")) {
+            int n = split(ln, tok, MAXTOK);
+            if (atoi(tok[n - 1]) != ff->ntypes) FAIL(h, "number of energy offsets does not match atom types");
+            for (int i = 0; i < ff->ntypes; i++) {
+                if (++L >= T.n) FAIL(h, "truncated energy offsets");
+                split(T.lines[L], tok, MAXTOK);
+                ff->eoff[atoi(tok[2]) - 1] = strtod(tok[3], 0);
+            }
+        }
+    }
+    int nt = ff->ntypes;
+    if (nt <= 0 || ff->npairs <= 0) FAIL(h, "missing ATOM TYPES or ATOM PAIRS");
+    /* pass 3: 2B parameters and PAIRMAPS */
+    ff->pows2 = calloc((size_t)ff->npairs * (ff->o2 > 0 ? ff->o2 : 1), sizeof(int));
+    ff->c2 = calloc((size_t)ff->npairs * (ff->o2 > 0 ? ff->o2 : 1), sizeof(double));
+    ff->pair_map = calloc(nt * nt, sizeof(int)); ff->prpr = calloc(nt * nt, sizeof(int));
+    int have_pmap = 0;
+    for (L = 0; L < T.n; L++) {
+        const char *ln = T.lines[L];
+        if (strstr(ln, "ENDFILE")) break;
+        if (strstr(ln, "PAIRTYPE PARAMS:")) {
+            split(ln, tok, MAXTOK); int p = atoi(tok[2]);
+            if (p < 0 || p >= ff->npairs) FAIL(h, "pair index out of range");
+            L++;
+            for (int i = 0; i < ff->o2; i++) {
+                if (++L >= T.n) FAIL(h, "truncated 2B parameters");
+                split(T.lines[L], tok, MAXTOK);
+                ff->pows2[p * ff->o2 + i] = atoi(tok[0]); ff->c2[p * ff->o2 + i] = strtod(tok[1], 0);
+            }
+        }
+        if (strstr(ln, "PAIRMAPS:")) {
+            split(ln, tok, MAXTOK); int nm = atoi(tok[1]);
+            int *mi = calloc(nm, sizeof(int)); char (*mk)[64] = calloc(nm, 64);
+            for (int i = 0; i < nm; i++) {
+                if (++L >= T.n) FAIL(h, "truncated PAIRMAPS");
+                split(T.lines[L], tok, MAXTOK); mi[i] = atoi(tok[0]); strncpy(mk[i], tok[1], 63);
+            }
+            for (int i = 0; i < nt; i++)
+                for (int j = 0; j < nt; j++) {
+                    char key[64]; snprintf(key, 64, "%s%s", ff->atm[i], ff->atm[j]);
+                    int k; for (k = 0; k < nm; k++) if (!strcmp(mk[k], key)) break;
+                    if (k == nm) FAIL(h, "could not find element in vector: %s", key);
+                    ff->pair_map[i * nt + j] = mi[k];
+                    int pp = proper_pair(ff, ff->atm[i], ff->atm[j]);
+                    if (pp < 0) FAIL(h, "no proper pair name for %s %s", ff->atm[i], ff->atm[j]);
+                    ff->prpr[i * nt + j] = pp;
+                }
+            free(mi); free(mk); have_pmap = 1;
+        }
+    }
+    if (!have_pmap) FAIL(h, "missing PAIRMAPS");
+    /* passes 4-5: 3B, then 6-7: 4B (same structure) */
+    for (int body = 3; body <= 4; body++) {
+        int order = body == 3 ? ff->o3 : ff->o4;
+        if (order <= 0) continue;
+        int np = body == 3 ? 3 : 6;
+        const char *hdr_count = body == 3 ? "ATOM PAIR TRIPLETS:" : "ATOM PAIR QUADRUPLETS:";
+        const char *hdr_type = body == 3 ? "TRIPLETTYPE PARAMS:" : "QUADRUPLETYPE PARAMS:";
+        const char *hdr_maps = body == 3 ? "TRIPMAPS:" : "QUADMAPS:";
+        int ntyp = 0; int *ncoef = NULL; int **pw = NULL; double **cf = NULL; double *cut = NULL;
+        char (*catm)[16] = NULL; char (*cpair)[40] = NULL; /* [ntyp*body], [ntyp*np] */
+        int *tmap = NULL; int ntup = body == 3 ? nt * nt * nt : nt * nt * nt * nt;
+        int *map_idx = NULL; char (*map_key)[256] = NULL; int nmaps = 0;
+        for (L = 0; L < T.n; L++) {
+            const char *ln = T.lines[L];
+            if (strstr(ln, "ENDFILE")) break;
+            if (strstr(ln, hdr_count)) {
+                split(ln, tok, MAXTOK); ntyp = atoi(tok[3]);
+                ncoef = calloc(ntyp, sizeof(int)); pw = calloc(ntyp, sizeof(int *)); cf = calloc(ntyp, sizeof(double *));
+                cut = calloc((size_t)ntyp * 2 * np, sizeof(double));
+                catm = calloc((size_t)ntyp * body, 16); cpair = calloc((size_t)ntyp * np, 40);
+            }
+            if (strstr(ln, hdr_type)) {
+                if (!ncoef) FAIL(h, "%s before %s", hdr_type, hdr_count);
+                if (++L >= T.n) FAIL(h, "truncated cluster block");
+                split(T.lines[L], tok, MAXTOK);
+                int t = atoi(tok[1]);
+                if (t < 0 || t >= ntyp) FAIL(h, "cluster type index out of range");
+                for (int a = 0; a < body; a++) strncpy(catm[t * body + a], tok[3 + a], 15);
+                if (++L >= T.n) FAIL(h, "truncated cluster block");
+                split(T.lines[L], tok, MAXTOK);
+                for (int p = 0; p < np; p++) strncpy(cpair[t * np + p], tok[1 + p], 39);
+                if (strcmp(tok[1 + np], "EXCLUDED:")) {
+                    int nc = atoi(tok[body == 3 ? 7 : 10]);
+                    ncoef[t] = nc; pw[t] = calloc((size_t)nc * np + 1, sizeof(int)); cf[t] = calloc(nc + 1, sizeof(double));
+                    L += 2;
+                    for (int c = 0; c < nc; c++) {
+                        if (++L >= T.n) FAIL(h, "truncated coefficient list");
+                        split(T.lines[L], tok, MAXTOK);
+                        for (int p = 0; p < np; p++) pw[t][c * np + p] = atoi(tok[1 + p]);
+                        cf[t][c] = strtod(tok[body == 3 ? 6 : 9], 0);
+                    }
+                }
+            }
+            if (strstr(ln, hdr_maps)) {
+                split(ln, tok, MAXTOK); nmaps = atoi(tok[1]);
+                map_idx = calloc(nmaps, sizeof(int)); map_key = calloc(nmaps, 256);
+                for (int i = 0; i < nmaps; i++) {
+                    if (++L >= T.n) FAIL(h, "truncated map block");
+                    split(T.lines[L], tok, MAXTOK); map_idx[i] = atoi(tok[0]); strncpy(map_key[i], tok[1], 255);
+                }
+                tmap = calloc(ntup, sizeof(int));
+                for (int u = 0; u < ntup; u++) {
+                    int a[4], r = u;
+                    for (int k = body - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+                    char key[256] = "";
+                    for (int i = 0; i < body; i++)
+                        for (int j = i + 1; j < body; j++) strcat(key, ff->pname[proper_pair(ff, ff->atm[a[i]], ff->atm[a[j]])]);
+                    int k; for (k = 0; k < nmaps; k++) if (!strcmp(map_key[k], key)) break;
+                    if (k == nmaps) FAIL(h, "could not find element in vector: %s", key);
+                    tmap[u] = map_idx[k];
+                }
+            }
+        }
+        if (!tmap) FAIL(h, "missing %s", hdr_maps);
+        /* default cutoffs: 2B values of each pair of the type's atoms (chimesFF.cpp:947-980, 1280-1325) */
+        for (int t = 0; t < ntyp; t++) {
+            int a[4];
+            for (int k = 0; k < body; k++) a[k] = find_atm(ff, catm[t * body + k]);
+            int p = 0;
+            for (int i = 0; i < body; i++)
+                for (int j = i + 1; j < body; j++, p++) {
+                    int pt = ff->pair_map[a[i] * nt + a[j]];
+                    cut[(t * 2 + 0) * np + p] = ff->rin[pt];
+                    cut[(t * 2 + 1) * np + p] = ff->rout[pt];
+                }
+        }
+        /* SPECIAL S_MAXIM / S_MINIM (chimesFF.cpp:1009-1168, 1353-1566) */
+        const char *smax = body == 3 ? "SPECIAL 3B S_MAXIM:" : "SPECIAL 4B S_MAXIM:";
+        const char *smin = body == 3 ? "SPECIAL 3B S_MINIM:" : "SPECIAL 4B S_MINIM:";
+        for (L = 0; L < T.n; L++) {
+            const char *ln = T.lines[L];
+            if (strstr(ln, "ENDFILE")) break;
+            int which = strstr(ln, smax) ? 1 : (strstr(ln, smin) ? 0 : -1);
+            if (which < 0) continue;
+            split(ln, tok, MAXTOK);
+            if (!strcmp(tok[3], "ALL")) {
+                double v = strtod(tok[4], 0);
+                for (int t = 0; t < ntyp; t++) for (int p = 0; p < np; p++) cut[(t * 2 + which) * np + p] = v;
+            } else {
+                int ne = atoi(tok[4]);
+                if (which == 0 && body == 4)
+                    for (int t = 0; t < ntyp; t++) for (int p = 0; p < np; p++) cut[(t * 2 + 0) * np + p] = -1.0;
+                for (int e = 0; e < ne; e++) {
+                    if (++L >= T.n) FAIL(h, "truncated SPECIAL block");
+                    split(T.lines[L], tok, MAXTOK);
+                    int k; for (k = 0; k < nmaps; k++) if (!strcmp(map_key[k], tok[0])) break;
+                    if (k == nmaps) FAIL(h, "SPECIAL entry names an unknown cluster type: %s", tok[0]);
+                    int t = map_idx[k];
+                    if (t < 0 || t >= ntyp) FAIL(h, "SPECIAL entry maps outside the cluster types");
+                    int disq[6] = {0, 0, 0, 0, 0, 0};
+                    for (int q = 0; q < np; q++) {
+                        int slot = -1;
+                        for (int p = 0; p < np; p++)
+                            if (!strcmp(cpair[t * np + p], tok[1 + q]) && !disq[p]) { disq[p] = 1; slot = p; break; }
+                        if (slot < 0) FAIL(h, "could not find element in vector: %s", tok[1 + q]);
+                        cut[(t * 2 + which) * np + slot] = strtod(tok[1 + np + q], 0);
+                    }
+                }
+            }
+        }
+        /* build_pair_int_trip_map / quad_map */
+        int *perm = calloc((size_t)ntup * np, sizeof(int));
+        int pair_map[6] = {0, 0, 0, 0, 0, 0};
+        for (int u = 0; u < ntup; u++) {
+            int a[4], r = u;
+            for (int k = body - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+            int t = tmap[u];
+            if (t < 0) continue;
+            if (t >= ntyp) FAIL(h, "cluster map entry out of range");
+            atom_pair_mapper(ff, body, a, &cpair[t * np], pair_map);
+            memcpy(&perm[u * np], pair_map, np * sizeof(int));
+        }
+        if (body == 3) {
+            ff->ntrips = ntyp; ff->n3 = ncoef; ff->pw3 = pw; ff->c3 = cf; ff->cut3 = cut;
+            ff->trip_map = tmap; ff->trip_perm = perm;
+        } else {
+            ff->nquads = ntyp; ff->n4 = ncoef; ff->pw4 = pw; ff->c4 = cf; ff->cut4 = cut;
+            ff->quad_map = tmap; ff->quad_perm = perm;
+        }
+        free(map_idx); free(map_key); free(catm); free(cpair);
+    }
+    free(T.lines); free(T.buf);
+    return 0;
+}
+
+/* max_cutoff_2B/3B/4B, chimesFF.cpp:2890-2943 */
+static double max_cut2(ora_ff *ff) {
+    double m = ff->rout[0];
+    for (int i = 0; i < ff->npairs; i++) if (ff->rout[i] > m) m = ff->rout[i];
+    return m;
+}
+static double max_cutn(ora_ff *ff, int body) {
+    int order = body == 3 ? ff->o3 : ff->o4;
+    if (order == 0) return 0.0;
+    int np = body == 3 ? 3 : 6, nty = body == 3 ? ff->ntrips : ff->nquads;
+    double *cut = body == 3 ? ff->cut3 : ff->cut4;
+    double m = cut[(0 * 2 + 1) * np + 0];
+    for (int t = 0; t < nty; t++) for (int p = 0; p < np; p++) if (cut[(t * 2 + 1) * np + p] > m) m = cut[(t * 2 + 1) * np + p];
+    return m;
+}
+
+/* ------------------------------------------------------------------ */
+/* per-cluster math                                                    */
+/* ------------------------------------------------------------------ */
+static void cheby(ora_ff *ff, double *Tn, double *Tnd, double dx, double morse, double rin, double rout, int order) {
+    double x_min = exp(-1 * rin / morse);
+    double x_max = exp(-1 * rout / morse);
+    double x_avg = 0.5 * (x_max + x_min);
+    double x_diff = 0.5 * (x_max - x_min);
+    x_diff *= -1.0;
+    int oor = 0; double dx_orig = dx;
+    if (dx < rin) { oor = 1; dx = rin; }
+    double exprlen = exp(-1 * dx / morse);
+    double x = (exprlen - x_avg) / x_diff;
+    double dx_dr = (-exprlen / morse) / x_diff;
+    Tn[0] = 1.0; Tn[1] = x; Tnd[0] = 1.0; Tnd[1] = 2.0 * x;
+    for (int i = 2; i <= order; i++) {
+        Tn[i] = 2.0 * x * Tn[i - 1] - Tn[i - 2];
+        Tnd[i] = 2.0 * x * Tnd[i - 1] - Tnd[i - 2];
+    }
+    for (int i = order; i >= 1; i--) Tnd[i] = i * dx_dr * Tnd[i - 1];
+    Tnd[0] = 0.0;
+    if (oor) {
+        ff->n_below_rin++;
+        double damp = exp((dx_orig - rin) / ff->inner_smooth);
+        for (int i = 0; i <= order; i++) {
+            Tn[i] += ff->inner_smooth * (damp - 1.0) * Tnd[i];
+            Tnd[i] *= damp;
+        }
+    }
+}
+
+static void fcut_fn(ora_ff *ff, double dx, double rc, double *fc, double *fcd) {
+    if (!ff->fcut_tersoff) {
+        double f0 = (1.0 - dx / rc);
+        *fc = pow(f0, 3.0);
+        *fcd = pow(f0, 2.0);
+        *fcd *= -1.0 * 3.0 / rc;
+    } else {
+        double th = rc - ff->fcut_var * rc;
+        if (dx < th) { *fc = 1.0; *fcd = 0.0; }
+        else if (dx > rc) { *fc = 0.0; *fcd = 0.0; }
+        else {
+            double f0 = (dx - th) / (rc - th) * ORA_PI + ORA_PI / 2.0;
+            double f0d = ORA_PI / (rc - th);
+            *fc = 0.5 + 0.5 * sin(f0);
+            *fcd = 0.5 * cos(f0) * f0d;
+        }
+    }
+}
+
+void ora_compute_1b(void *vh, int t, double *E) { ora_handle *h = vh; *E += h->ff.eoff[t]; }
+
+void ora_compute_2b(void *vh, double dx, const double *dr, int t0, int t1, double *force, double *stress, double *E) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    int p = ff->pair_map[t0 * ff->ntypes + t1];
+    if (dx >= ff->rout[p]) return;
+    double Tn[64], Tnd[64], fc, fcd;
+    cheby(ff, Tn, Tnd, dx, ff->lam[p], ff->rin[p], ff->rout[p], ff->o2);
+    fcut_fn(ff, dx, ff->rout[p], &fc, &fcd);
+    double dx_inv = (dx > 0.0) ? 1.0 / dx : 1e20;
+    for (int c = 0; c < ff->o2; c++) {
+        double cv = ff->c2[p * ff->o2 + c];
+        int pw = ff->pows2[p * ff->o2 + c] + 1;
+        *E += cv * fc * Tn[pw];
+        double deriv = fc * Tnd[pw] + fcd * Tn[pw];
+        double fs = cv * deriv * dx_inv;
+        force[0] += fs * dr[0]; force[1] += fs * dr[1]; force[2] += fs * dr[2];
+        force[3] -= fs * dr[0]; force[4] -= fs * dr[1]; force[5] -= fs * dr[2];
+        stress[0] -= fs * dr[0] * dr[0]; stress[1] -= fs * dr[0] * dr[1]; stress[2] -= fs * dr[0] * dr[2];
+        stress[3] -= fs * dr[1] * dr[1]; stress[4] -= fs * dr[1] * dr[2]; stress[5] -= fs * dr[2] * dr[2];
+    }
+    /* get_penalty, chimesFF.h:388-419 */
+    double rpen = 0.0, Epen = 0.0, fs = 1.0;
+    if (dx - ff->pen_dist < ff->rin[p]) {
+        rpen = ff->rin[p] + ff->pen_dist - dx;
+        if (dx < ff->rin[p]) ff->badness = 2;
+        else if (1 > ff->badness) ff->badness = 1;
+    }
+    if (rpen > 0.0) {
+        Epen = rpen * rpen * rpen * ff->pen_scale;
+        fs = -3.0 * rpen * rpen * ff->pen_scale;
+        ff->n_penalty++;
+    }
+    if (Epen > 0.0) {
+        *E += Epen;
+        fs /= dx;
+        force[0] += fs * dr[0]; force[1] += fs * dr[1]; force[2] += fs * dr[2];
+        force[3] -= fs * dr[0]; force[4] -= fs * dr[1]; force[5] -= fs * dr[2];
+        stress[0] -= fs * dr[0] * dr[0]; stress[1] -= fs * dr[0] * dr[1]; stress[2] -= fs * dr[0] * dr[2];
+        stress[3] -= fs * dr[1] * dr[1]; stress[4] -= fs * dr[1] * dr[2]; stress[5] -= fs * dr[2] * dr[2];
+    }
+}
+
+/* force/stress update of one pair p joining cluster atoms a and b, with the
+ * reference's dr2 distance-tensor product (fs * (dr_a * dr_b)) */
+static inline void pair_update(double fs, const double *d, int a, int b, double *force, double *stress) {
+    force[a * 3 + 0] += fs * d[0]; force[a * 3 + 1] += fs * d[1]; force[a * 3 + 2] += fs * d[2];
+    force[b * 3 + 0] -= fs * d[0]; force[b * 3 + 1] -= fs * d[1]; force[b * 3 + 2] -= fs * d[2];
+    stress[0] -= fs * (d[0] * d[0]); stress[1] -= fs * (d[0] * d[1]); stress[2] -= fs * (d[0] * d[2]);
+    stress[3] -= fs * (d[1] * d[1]); stress[4] -= fs * (d[1] * d[2]); stress[5] -= fs * (d[2] * d[2]);
+}
+
+void ora_compute_3b(void *vh, const double *dx, const double *dr, const int *typ, double *force, double *stress, double *E) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    int nt = ff->ntypes;
+    int u = typ[0] * nt * nt + typ[1] * nt + typ[2];
+    int t = ff->trip_map[u];
+    if (t < 0) return;
+    const int *m = &ff->trip_perm[u * 3];
+    double co[3], ci[3];
+    for (int p = 0; p < 3; p++) {
+        co[p] = ff->cut3[(t * 2 + 1) * 3 + m[p]];
+        ci[p] = ff->cut3[(t * 2 + 0) * 3 + m[p]];
+        if (dx[p] >= co[p]) return;
+    }
+    int pt[3] = {ff->pair_map[typ[0] * nt + typ[1]], ff->pair_map[typ[0] * nt + typ[2]], ff->pair_map[typ[1] * nt + typ[2]]};
+    double Tn[3][64], Tnd[3][64], fc[3], fcd[3];
+    for (int p = 0; p < 3; p++) cheby(ff, Tn[p], Tnd[p], dx[p], ff->lam[pt[p]], ci[p], co[p], ff->o3);
+    for (int p = 0; p < 3; p++) fcut_fn(ff, dx[p], co[p], &fc[p], &fcd[p]);
+    double fall = fc[0] * fc[1] * fc[2];
+    double f2[3] = {fc[1] * fc[2] / dx[0], fc[0] * fc[2] / dx[1], fc[0] * fc[1] / dx[2]};
+    for (int c = 0; c < ff->n3[t]; c++) {
+        double cv = ff->c3[t][c];
+        int p0 = ff->pw3[t][c * 3 + m[0]], p1 = ff->pw3[t][c * 3 + m[1]], p2 = ff->pw3[t][c * 3 + m[2]];
+        *E += cv * fall * Tn[0][p0] * Tn[1][p1] * Tn[2][p2];
+        double d0 = fc[0] * Tnd[0][p0] + fcd[0] * Tn[0][p0];
+        double d1 = fc[1] * Tnd[1][p1] + fcd[1] * Tn[1][p1];
+        double d2 = fc[2] * Tnd[2][p2] + fcd[2] * Tn[2][p2];
+        double fs0 = cv * d0 * f2[0] * Tn[1][p1] * Tn[2][p2];
+        double fs1 = cv * d1 * f2[1] * Tn[0][p0] * Tn[2][p2];
+        double fs2 = cv * d2 * f2[2] * Tn[0][p0] * Tn[1][p1];
+        pair_update(fs0, &dr[0], 0, 1, force, stress);
+        pair_update(fs1, &dr[3], 0, 2, force, stress);
+        pair_update(fs2, &dr[6], 1, 2, force, stress);
+    }
+}
+
+void ora_compute_4b(void *vh, const double *dx, const double *dr, const int *typ, double *force, double *stress, double *E) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    int nt = ff->ntypes;
+    int u = ((typ[0] * nt + typ[1]) * nt + typ[2]) * nt + typ[3];
+    u = typ[0] * nt * nt * nt + typ[1] * nt * nt + typ[2] * nt + typ[3];
+    int t = ff->quad_map[u];
+    if (t < 0) return;
+    const int *m = &ff->quad_perm[u * 6];
+    double co[6], ci[6];
+    for (int p = 0; p < 6; p++) {
+        co[p] = ff->cut4[(t * 2 + 1) * 6 + m[p]];
+        ci[p] = ff->cut4[(t * 2 + 0) * 6 + m[p]];
+        if (dx[p] >= co[p]) return;
+    }
+    static const int A[6] = {0, 0, 0, 1, 1, 2}, B[6] = {1, 2, 3, 2, 3, 3};
+    int pt[6];
+    for (int p = 0; p < 6; p++) pt[p] = ff->pair_map[typ[A[p]] * nt + typ[B[p]]];
+    double Tn[6][64], Tnd[6][64], fc[6], fcd[6];
+    for (int p = 0; p < 6; p++) cheby(ff, Tn[p], Tnd[p], dx[p], ff->lam[pt[p]], ci[p], co[p], ff->o4);
+    for (int p = 0; p < 6; p++) fcut_fn(ff, dx[p], co[p], &fc[p], &fcd[p]);
+    double fall = fc[0] * fc[1] * fc[2] * fc[3] * fc[4] * fc[5];
+    double f5[6] = {fc[1] * fc[2] * fc[3] * fc[4] * fc[5] / dx[0], fc[0] * fc[2] * fc[3] * fc[4] * fc[5] / dx[1],
+                    fc[0] * fc[1] * fc[3] * fc[4] * fc[5] / dx[2], fc[0] * fc[1] * fc[2] * fc[4] * fc[5] / dx[3],
+                    fc[0] * fc[1] * fc[2] * fc[3] * fc[5] / dx[4], fc[0] * fc[1] * fc[2] * fc[3] * fc[4] / dx[5]};
+    for (int c = 0; c < ff->n4[t]; c++) {
+        double cv = ff->c4[t][c];
+        int pw[6];
+        for (int p = 0; p < 6; p++) pw[p] = ff->pw4[t][c * 6 + m[p]];
+        double t012 = Tn[0][pw[0]] * Tn[1][pw[1]] * Tn[2][pw[2]];
+        double t34 = Tn[3][pw[3]] * Tn[4][pw[4]];
+        double t5 = Tn[5][pw[5]];
+        *E += cv * fall * t012 * t34 * t5;
+        double d[6];
+        for (int p = 0; p < 6; p++) d[p] = fc[p] * Tnd[p][pw[p]] + fcd[p] * Tn[p][pw[p]];
+        double fs0 = cv * d[0] * f5[0] * Tn[1][pw[1]] * Tn[2][pw[2]] * t34 * t5;
+        double fs1 = cv * d[1] * f5[1] * Tn[0][pw[0]] * Tn[2][pw[2]] * t34 * t5;
+        double fs2 = cv * d[2] * f5[2] * Tn[0][pw[0]] * Tn[1][pw[1]] * t34 * t5;
+        double fs3 = cv * d[3] * f5[3] * t012 * Tn[4][pw[4]] * t5;
+        double fs4 = cv * d[4] * f5[4] * t012 * Tn[3][pw[3]] * t5;
+        double fs5 = cv * d[5] * f5[5] * t012 * t34;
+        pair_update(fs0, &dr[0], 0, 1, force, stress);
+        pair_update(fs1, &dr[3], 0, 2, force, stress);
+        pair_update(fs2, &dr[6], 0, 3, force, stress);
+        pair_update(fs3, &dr[9], 1, 2, force, stress);
+        pair_update(fs4, &dr[12], 1, 3, force, stress);
+        pair_update(fs5, &dr[15], 2, 3, force, stress);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* periodic system (serial_chimes_interface.cpp:20-587)                */
+/* ------------------------------------------------------------------ */
+static double mag3(const double *a) { double m = 0; for (int i = 0; i < 3; i++) m += a[i] * a[i]; return sqrt(m); }
+static double dot3(const double *a, const double *b) { double d = 0; for (int i = 0; i < 3; i++) d += a[i] * b[i]; return d; }
+static double angle3(const double *a, const double *b) { double g = dot3(a, b); g /= mag3(a); g /= mag3(b); return acos(g); }
+
+static void set_hmat(const double *ca, const double *cb, const double *cc, double *h, double *hi, int rep) {
+    h[0] = ca[0] * (rep + 1); h[3] = ca[1] * (rep + 1); h[6] = ca[2] * (rep + 1);
+    h[1] = cb[0] * (rep + 1); h[4] = cb[1] * (rep + 1); h[7] = cb[2] * (rep + 1);
+    h[2] = cc[0] * (rep + 1); h[5] = cc[1] * (rep + 1); h[8] = cc[2] * (rep + 1);
+    double det = h[0] * (h[4] * h[8] - h[5] * h[7]) - h[1] * (h[3] * h[8] - h[5] * h[6]) + h[2] * (h[3] * h[7] - h[4] * h[6]);
+    double t[9];
+    t[0] = (h[4] * h[8] - h[5] * h[7]); t[3] = -1 * (h[1] * h[8] - h[2] * h[7]); t[6] = (h[1] * h[5] - h[2] * h[4]);
+    t[1] = -1 * (h[3] * h[8] - h[5] * h[6]); t[4] = (h[0] * h[8] - h[2] * h[6]); t[7] = -1 * (h[0] * h[5] - h[2] * h[3]);
+    t[2] = (h[3] * h[7] - h[4] * h[6]); t[5] = -1 * (h[0] * h[7] - h[1] * h[6]); t[8] = (h[0] * h[4] - h[1] * h[3]);
+    hi[0] = t[0]; hi[3] = t[1]; hi[6] = t[2];
+    hi[1] = t[3]; hi[4] = t[4]; hi[7] = t[5];
+    hi[2] = t[6]; hi[5] = t[7]; hi[8] = t[8];
+    for (int i = 0; i < 9; i++) hi[i] /= det;
+}
+
+static void matvec(const double *m, double x, double y, double z, double *o) {
+    o[0] = m[0] * x + m[1] * y + m[2] * z;
+    o[1] = m[3] * x + m[4] * y + m[5] * z;
+    o[2] = m[6] * x + m[7] * y + m[8] * z;
+}
+
+static void sys_reserve(ora_sys *s, long n) {
+    if (n <= s->cap) return;
+    s->cap = n;
+    s->x = realloc(s->x, n * sizeof(double)); s->y = realloc(s->y, n * sizeof(double)); s->z = realloc(s->z, n * sizeof(double));
+    s->parent = realloc(s->parent, n * sizeof(int)); s->rep_parent = realloc(s->rep_parent, n * sizeof(int));
+    s->typ = realloc(s->typ, n * sizeof(int));
+}
+static void sys_free(ora_sys *s) { free(s->x); free(s->y); free(s->z); free(s->parent); free(s->rep_parent); free(s->typ); }
+
+/* simulation_system::init, serial_chimes_interface.cpp:150-341 */
+static void sys_init(ora_sys *s, int n, const int *typ, const double *x, const double *y, const double *z,
+                     const double *ca, const double *cb, const double *cc, double max_cut, int small) {
+    s->n_atoms = n; s->n_ghost = n; s->n_repl = n;
+    double la = mag3(ca), lb = mag3(cb), lc = mag3(cc);
+    double mn = la; if (lb < mn) mn = lb; if (lc < mn) mn = lc;
+    s->n_replicates = small ? (int)ceil(max_cut / mn) - 1 : 0;
+    int nr = s->n_replicates;
+    sys_reserve(s, (long)n * (nr + 1) * (nr + 1) * (nr + 1));
+    for (int a = 0; a < n; a++) { s->x[a] = x[a]; s->y[a] = y[a]; s->z[a] = z[a]; s->parent[a] = a; s->rep_parent[a] = a; s->typ[a] = typ[a]; }
+    set_hmat(ca, cb, cc, s->h, s->hi, 0);
+    for (int i = 0; i <= nr; i++)
+        for (int j = 0; j <= nr; j++)
+            for (int k = 0; k <= nr; k++) {
+                if (i == 0 && j == 0 && k == 0) continue;
+                for (int a = 0; a < n; a++) {
+                    int g = s->n_ghost++; s->n_repl++;
+                    double t[3]; matvec(s->hi, s->x[a], s->y[a], s->z[a], t);
+                    t[0] += i; t[1] += j; t[2] += k;
+                    double o[3]; matvec(s->h, t[0], t[1], t[2], o);
+                    s->x[g] = o[0]; s->y[g] = o[1]; s->z[g] = o[2];
+                    s->parent[g] = s->n_repl - 1; s->rep_parent[g] = a; s->typ[g] = typ[a];
+                }
+            }
+    s->n_atoms = s->n_repl;
+    set_hmat(ca, cb, cc, s->h, s->hi, nr);
+    for (int i = 0; i < s->n_atoms; i++) {
+        double f[3]; matvec(s->hi, s->x[i], s->y[i], s->z[i], f);
+        f[0] -= floor(f[0]); f[1] -= floor(f[1]); f[2] -= floor(f[2]);
+        double o[3]; matvec(s->h, f[0], f[1], f[2], o);
+        s->x[i] = o[0]; s->y[i] = o[1]; s->z[i] = o[2];
+    }
+    double A[3] = {s->h[0], s->h[3], s->h[6]}, B[3] = {s->h[1], s->h[4], s->h[7]}, C[3] = {s->h[2], s->h[5], s->h[8]};
+    s->la = mag3(A); s->lb = mag3(B); s->lc = mag3(C);
+    double al = angle3(B, C), be = angle3(C, A), ga = angle3(A, B);
+    double v = 1;
+    v += 2 * cos(al) * cos(be) * cos(ga);
+    v -= cos(al) * cos(al); v -= cos(be) * cos(be); v -= cos(ga) * cos(ga);
+    s->vol = s->la * s->lb * s->lc * sqrt(v);
+}
+
+/* simulation_system::reorient, serial_chimes_interface.cpp:342-476 (the
+ * extents it also computes are not used by the list build and are omitted) */
+static void sys_reorient(ora_sys *s) {
+    for (int i = 0; i < s->n_atoms; i++) {
+        double f[3]; matvec(s->hi, s->x[i], s->y[i], s->z[i], f);
+        s->x[i] = f[0]; s->y[i] = f[1]; s->z[i] = f[2];
+    }
+    double A[3] = {s->h[0], s->h[3], s->h[6]}, B[3] = {s->h[1], s->h[4], s->h[7]}, C[3] = {s->h[2], s->h[5], s->h[8]};
+    double ma = mag3(A);
+    double u[3] = {0.0 + A[0] / ma, 0.0 + A[1] / ma, 0.0 + A[2] / ma};
+    double cr[3] = {(u[1] * B[2] - u[2] * B[1]), -1 * (u[0] * B[2] - u[2] * B[0]), (u[0] * B[1] - u[1] * B[0])};
+    double ta[3] = {mag3(A), 0, 0};
+    double tb[3] = {dot3(B, u), mag3(cr), 0};
+    double tc[3];
+    tc[0] = dot3(C, u);
+    tc[1] = (dot3(B, C) - tb[0] * tc[0]) / tb[1];
+    tc[2] = sqrt(mag3(C) * mag3(C) - tc[0] * tc[0] - tc[1] * tc[1]);
+    set_hmat(ta, tb, tc, s->h, s->hi, 0);
+    for (int i = 0; i < s->n_atoms; i++) {
+        double o[3]; matvec(s->h, s->x[i], s->y[i], s->z[i], o);
+        s->x[i] = o[0]; s->y[i] = o[1]; s->z[i] = o[2];
+    }
+    double A2[3] = {s->h[0], s->h[3], s->h[6]}, B2[3] = {s->h[1], s->h[4], s->h[7]}, C2[3] = {s->h[2], s->h[5], s->h[8]};
+    s->la = mag3(A2); s->lb = mag3(B2); s->lc = mag3(C2);
+}
+
+/* simulation_system::build_layered_system, serial_chimes_interface.cpp:477-587 */
+static int sys_layers(ora_handle *h, ora_sys *s, double c2, double c3, double c4) {
+    double mn = s->la; if (s->lb < mn) mn = s->lb; if (s->lc < mn) mn = s->lc;
+    s->n_layers = (int)ceil(c2 * 2.0 / mn + 1);
+    int n = s->n_layers;
+    double ex = s->la * (2 * n + 1), ey = s->lb * (2 * n + 1), ez = s->lc * (2 * n + 1);
+    if (c2 > 0.5 * ex || c2 > 0.5 * ey || c2 > 0.5 * ez) FAIL(h, "maximum 2b cutoff is greater than half at least one box length");
+    if (h->ff.o3 > 0 && (c3 > 0.5 * ex || c3 > 0.5 * ey || c3 > 0.5 * ez)) FAIL(h, "maximum 3b cutoff is greater than half at least one box length");
+    if (h->ff.o4 > 0 && (c4 > 0.5 * ex || c4 > 0.5 * ey || c4 > 0.5 * ez)) FAIL(h, "maximum 4b cutoff is greater than half at least one box length");
+    long side = 2 * n + 1;
+    sys_reserve(s, (long)s->n_atoms * side * side * side);
+    s->n_ghost = s->n_atoms;
+    for (int i = -n; i <= n; i++)
+        for (int j = -n; j <= n; j++)
+            for (int k = -n; k <= n; k++) {
+                if (i == 0 && j == 0 && k == 0) continue;
+                for (int a = 0; a < s->n_atoms; a++) {
+                    int g = s->n_ghost++;
+                    double t[3]; matvec(s->hi, s->x[a], s->y[a], s->z[a], t);
+                    t[0] += i; t[1] += j; t[2] += k;
+                    double o[3]; matvec(s->h, t[0], t[1], t[2], o);
+                    s->x[g] = o[0]; s->y[g] = o[1]; s->z[g] = o[2];
+                    s->parent[g] = a; s->typ[g] = s->typ[a];
+                }
+            }
+    return 0;
+}
+
+/* simulation_system::get_dist, serial_chimes_interface.h:141-215 */
+static double sys_dist(const ora_sys *s, int i, int j, double *r) {
+    const double *m = s->hi, *H = s->h;
+    double ix = m[0] * s->x[i] + m[1] * s->y[i] + m[2] * s->z[i];
+    double iy = m[3] * s->x[i] + m[4] * s->y[i] + m[5] * s->z[i];
+    double iz = m[6] * s->x[i] + m[7] * s->y[i] + m[8] * s->z[i];
+    double jx = m[0] * s->x[j] + m[1] * s->y[j] + m[2] * s->z[j];
+    double jy = m[3] * s->x[j] + m[4] * s->y[j] + m[5] * s->z[j];
+    double jz = m[6] * s->x[j] + m[7] * s->y[j] + m[8] * s->z[j];
+    double dx = jx - ix, dy = jy - iy, dz = jz - iz;
+    double rr[3];
+    if (!r) r = rr;
+    r[0] = H[0] * dx + H[1] * dy + H[2] * dz;
+    r[1] = H[3] * dx + H[4] * dy + H[5] * dz;
+    r[2] = H[6] * dx + H[7] * dy + H[8] * dz;
+    return sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+}
+
+static void push(int **v, long *n, long *cap, const int *vals, int k) {
+    if (*n + k > *cap) { *cap = (*cap ? *cap * 2 : 4096) + k; *v = realloc(*v, *cap * sizeof(int)); }
+    memcpy(*v + *n, vals, k * sizeof(int)); *n += k;
+}
+
+/* simulation_system::build_neigh_lists, serial_chimes_interface.cpp:588-864.
+ * l2 holds (i, ghost) pairs; l2_start[i]..l2_start[i+1] is atom i's list. */
+static int build_lists(ora_handle *h, ora_sys *s, double c2, double c3, double c4, long *l2_start) {
+    double mx[3] = {-1.0e100, -1.0e100, -1.0e100}, mn[3] = {1.0e100, 1.0e100, 1.0e100};
+    for (int i = 0; i < s->n_ghost; i++) {
+        if (s->x[i] > mx[0]) mx[0] = s->x[i];
+        if (s->y[i] > mx[1]) mx[1] = s->y[i];
+        if (s->z[i] > mx[2]) mx[2] = s->z[i];
+        if (s->x[i] < mn[0]) mn[0] = s->x[i];
+        if (s->y[i] < mn[1]) mn[1] = s->y[i];
+        if (s->z[i] < mn[2]) mn[2] = s->z[i];
+    }
+    double sd = c2; if (c3 > sd) sd = c3; if (c4 > sd) sd = c4;
+    int nbx = (int)ceil((mx[0] - mn[0]) / sd), nby = (int)ceil((mx[1] - mn[1]) / sd), nbz = (int)ceil((mx[2] - mn[2]) / sd);
+    long tb = (long)nbx * nby * nbz;
+    long *bstart = calloc(tb + 1, sizeof(long));
+    int *bid = malloc(s->n_ghost * sizeof(int));
+    for (int i = 0; i < s->n_ghost; i++) {
+        int bx = (int)floor((s->x[i] - mn[0]) / sd), by = (int)floor((s->y[i] - mn[1]) / sd), bz = (int)floor((s->z[i] - mn[2]) / sd);
+        if (bx < 0 || by < 0 || bz < 0) { free(bstart); free(bid); FAIL(h, "negative bin computed"); }
+        long ib = bx + (long)by * nbx + (long)bz * nbx * nby;
+        if (ib >= tb) { free(bstart); free(bid); FAIL(h, "ibin out of range"); }
+        bid[i] = (int)ib; bstart[ib + 1]++;
+    }
+    for (long b = 0; b < tb; b++) bstart[b + 1] += bstart[b];
+    long *fill = malloc(tb * sizeof(long)); memcpy(fill, bstart, tb * sizeof(long));
+    int *bins = malloc(s->n_ghost * sizeof(int));
+    for (int i = 0; i < s->n_ghost; i++) bins[fill[bid[i]]++] = i;
+    free(fill); free(bid);
+    h->n2 = h->n3 = h->n4 = 0;
+    for (int ai = 0; ai < s->n_atoms; ai++) {
+        l2_start[ai] = h->n2 / 2;
+        int bx = (int)floor((s->x[ai] - mn[0]) / sd), by = (int)floor((s->y[ai] - mn[1]) / sd), bz = (int)floor((s->z[ai] - mn[2]) / sd);
+        if (bx < 1 || by < 1 || bz < 1) { free(bstart); free(bins); FAIL(h, "bad bin computed"); }
+        for (int i = bx - 1; i <= bx + 1; i++)
+            for (int j = by - 1; j <= by + 1; j++)
+                for (int k = bz - 1; k <= bz + 1; k++) {
+                    long ib = i + (long)j * nbx + (long)k * nbx * nby;
+                    if (ib >= tb) { free(bstart); free(bins); FAIL(h, "binning index out of range"); }
+                    for (long q = bstart[ib]; q < bstart[ib + 1]; q++) {
+                        int ajj = bins[q];
+                        if (ajj == ai) continue;
+                        if (ai <= s->parent[ajj] && sys_dist(s, ai, ajj, NULL) < sd) {
+                            int v[2] = {ai, ajj}; push(&h->l2, &h->n2, &h->cap2, v, 2);
+                        }
+                    }
+                }
+    }
+    l2_start[s->n_atoms] = h->n2 / 2;
+    free(bstart); free(bins);
+    if (h->ff.o3 == 0 && h->ff.o4 == 0) return 0;
+    for (int i = 0; i < s->n_atoms; i++) {
+        long b0 = l2_start[i], b1 = l2_start[i + 1];
+        for (long j = b0; j < b1; j++) {
+            int v3 = 1, v4 = 1;
+            int jj = h->l2[2 * j + 1];
+            double dij = sys_dist(s, i, jj, NULL);
+            if (dij >= c3) v3 = 0;
+            if (dij >= c4) v4 = 0;
+            if (!v3 && !v4) continue;
+            for (long k = b0; k < b1; k++) {
+                int kk = h->l2[2 * k + 1];
+                if (jj == kk) continue;
+                if (s->parent[jj] > s->parent[kk]) continue;
+                double dik = sys_dist(s, i, kk, NULL);
+                if (dik >= c3) v3 = 0;
+                if (dik >= c4) v4 = 0;
+                double djk = sys_dist(s, jj, kk, NULL);
+                if (djk >= c3) v3 = 0;
+                if (djk >= c4) v4 = 0;
+                if (!v3 && !v4) {
+                    if (dij < c3) v3 = 1;
+                    if (dij < c4) v4 = 1;
+                    continue;
+                }
+                if (v3) { int v[3] = {i, jj, kk}; push(&h->l3, &h->n3, &h->cap3, v, 3); }
+                if (h->ff.o4 == 0) continue;
+                if (!v4) { if (dij < c4) v4 = 1; continue; }
+                for (long l = b0; l < b1; l++) {
+                    int ll = h->l2[2 * l + 1];
+                    if (jj == ll || kk == ll) continue;
+                    if (s->parent[jj] > s->parent[ll]) continue;
+                    if (s->parent[kk] > s->parent[ll]) continue;
+                    if (sys_dist(s, i, ll, NULL) >= c4) continue;
+                    if (sys_dist(s, jj, ll, NULL) >= c4) continue;
+                    if (sys_dist(s, kk, ll, NULL) >= c4) continue;
+                    if (v4) { int v[4] = {i, jj, kk, ll}; push(&h->l4, &h->n4, &h->cap4, v, 4); }
+                }
+            }
+        }
+    }
+    h->n2 /= 2; h->n3 /= 3; h->n4 /= 4;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* public entry points (ctypes)                                        */
+/* ------------------------------------------------------------------ */
+void *ora_load(const char *path, char *err, int errlen) {
+    ora_handle *h = calloc(1, sizeof(ora_handle));
+    if (parse(h, path)) {
+        if (err && errlen > 0) { strncpy(err, h->err, errlen - 1); err[errlen - 1] = 0; }
+        free(h); return NULL;
+    }
+    return h;
+}
+
+void ora_free(void *vh) {
+    ora_handle *h = vh; if (!h) return;
+    free(h->l2); free(h->l3); free(h->l4);
+    free(h);  /* parameter tables are left to process exit: test-only object */
+}
+
+const char *ora_error(void *vh) { return ((ora_handle *)vh)->err; }
+
+void ora_info(void *vh, int *orders, int *ntypes, double *maxcuts) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    orders[0] = ff->o2; orders[1] = ff->o3; orders[2] = ff->o4; *ntypes = ff->ntypes;
+    maxcuts[0] = max_cut2(ff); maxcuts[1] = max_cutn(ff, 3); maxcuts[2] = max_cutn(ff, 4);
+}
+
+int ora_type_index(void *vh, const char *name) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    for (int i = 0; i < ff->ntypes; i++) if (!strcmp(ff->atm[i], name)) return i;
+    return -1;
+}
+
+int ora_badness(void *vh) { return ((ora_handle *)vh)->ff.badness; }
+
+/* serial_chimes_interface::calculate.  energy/force accumulate into the
+ * caller's values; stress[9] is overwritten.  Returns 0 or -1 (see ora_error). */
+int ora_calculate(void *vh, int n, const double *x, const double *y, const double *z, const int *typ,
+                  const double *ca, const double *cb, const double *cc, int small,
+                  double *energy, double *fx, double *fy, double *fz, double *stress) {
+    ora_handle *h = vh; ora_ff *ff = &h->ff;
+    double c2 = max_cut2(ff), c3 = max_cutn(ff, 3), c4 = max_cutn(ff, 4);
+    double st[6] = {0, 0, 0, 0, 0, 0};
+    ora_sys S = {0}, N = {0};
+    sys_init(&S, n, typ, x, y, z, ca, cb, cc, c2, small);
+    if (sys_layers(h, &S, c2, c3, c4)) { sys_free(&S); return -1; }
+    int body = 2 + (ff->o3 > 0) + (ff->o4 > 0);
+    if (body > S.n_ghost) { sys_free(&S); FAIL(h, "layered system contains too few atoms"); }
+    sys_init(&N, n, typ, x, y, z, ca, cb, cc, c2, small);
+    sys_reorient(&N);
+    if (sys_layers(h, &N, c2, c3, c4)) { sys_free(&S); sys_free(&N); return -1; }
+    long *l2s = malloc((N.n_atoms + 1) * sizeof(long));
+    if (build_lists(h, &N, c2, c3, c4, l2s)) { free(l2s); sys_free(&S); sys_free(&N); return -1; }
+    double *E = energy;
+    double f2[6], f3[9], f4[12], dr[18], dx[6];
+    for (int i = 0; i < S.n_atoms; i++) {
+        ora_compute_1b(h, S.typ[i], E);
+        for (long q = l2s[i]; q < l2s[i + 1]; q++) {
+            int jj = h->l2[2 * q + 1];
+            double d = sys_dist(&S, i, jj, dr);
+            memset(f2, 0, sizeof(f2));
+            ora_compute_2b(h, d, dr, S.typ[i], S.typ[jj], f2, st, E);
+            int a = S.rep_parent[i], b = S.rep_parent[S.parent[jj]];
+            fx[a] += f2[0]; fy[a] += f2[1]; fz[a] += f2[2];
+            fx[b] += f2[3]; fy[b] += f2[4]; fz[b] += f2[5];
+        }
+    }
+    if (ff->o3 > 0)
+        for (long q = 0; q < h->n3; q++) {
+            int id[3] = {h->l3[3 * q], h->l3[3 * q + 1], h->l3[3 * q + 2]};
+            dx[0] = sys_dist(&S, id[0], id[1], &dr[0]);
+            dx[1] = sys_dist(&S, id[0], id[2], &dr[3]);
+            dx[2] = sys_dist(&S, id[1], id[2], &dr[6]);
+            int t[3] = {S.typ[id[0]], S.typ[id[1]], S.typ[id[2]]};
+            memset(f3, 0, sizeof(f3));
+            ora_compute_3b(h, dx, dr, t, f3, st, E);
+            for (int a = 0; a < 3; a++) {
+                int o = S.rep_parent[S.parent[id[a]]];
+                fx[o] += f3[3 * a]; fy[o] += f3[3 * a + 1]; fz[o] += f3[3 * a + 2];
+            }
+        }
+    if (ff->o4 > 0)
+        for (long q = 0; q < h->n4; q++) {
+            int id[4] = {h->l4[4 * q], h->l4[4 * q + 1], h->l4[4 * q + 2], h->l4[4 * q + 3]};
+            static const int A[6] = {0, 0, 0, 1, 1, 2}, B[6] = {1, 2, 3, 2, 3, 3};
+            for (int p = 0; p < 6; p++) dx[p] = sys_dist(&S, id[A[p]], id[B[p]], &dr[3 * p]);
+            int t[4] = {S.typ[id[0]], S.typ[id[1]], S.typ[id[2]], S.typ[id[3]]};
+            memset(f4, 0, sizeof(f4));
+            ora_compute_4b(h, dx, dr, t, f4, st, E);
+            for (int a = 0; a < 4; a++) {
+                int o = S.rep_parent[S.parent[id[a]]];
+                fx[o] += f4[3 * a]; fy[o] += f4[3 * a + 1]; fz[o] += f4[3 * a + 2];
+            }
+        }
+    *E /= pow(S.n_replicates + 1.0, 3.0);
+    stress[0] = st[0]; stress[1] = st[1]; stress[2] = st[2];
+    stress[3] = st[1]; stress[4] = st[3]; stress[5] = st[4];
+    stress[6] = st[2]; stress[7] = st[4]; stress[8] = st[5];
+    for (int k = 0; k < 9; k++) stress[k] /= S.vol;
+    free(l2s); sys_free(&S); sys_free(&N);
+    return 0;
+}
+
+void ora_list_sizes(void *vh, long *n2, long *n3, long *n4) {
+    ora_handle *h = vh; *n2 = h->n2; *n3 = h->n3; *n4 = h->n4;
+}
+
+void ora_get_lists(void *vh, int *l2, int *l3, int *l4) {
+    ora_handle *h = vh;
+    if (l2) memcpy(l2, h->l2, h->n2 * 2 * sizeof(int));
+    if (l3) memcpy(l3, h->l3, h->n3 * 3 * sizeof(int));
+    if (l4) memcpy(l4, h->l4, h->n4 * 4 * sizeof(int));
+}

@@ -1,0 +1,197 @@
+"""ctypes wrapper of the oracle (test infrastructure only).
+
+Loads ``oracle/_build/libchimes_oracle.so`` -- the C restatement of the
+reference calculator in ``oracle/chimes_oracle.c`` -- and exposes a
+``serial_chimes_interface``-like ``calculate`` plus the cluster lists of the
+last call.  ``run_reference`` drives the unmodified reference build in
+``oracle/_ref/ref_driver`` when it exists (only where the reference sources
+were available to compile it).
+
+Only tests, the smoke check and the bench's CPU-baseline leg import this.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libchimes_oracle.so")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+REFROOT = "/root/reference"
+
+_lib = None
+
+
+def build_port(force: bool = False) -> str:
+    if force or not os.path.exists(PORT_SO) or \
+            os.path.getmtime(PORT_SO) < os.path.getmtime(os.path.join(HERE, "chimes_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_SO
+
+
+def build_reference() -> Optional[str]:
+    """Compiles the reference's own sources into oracle/_ref when they exist here."""
+    if not os.path.isdir(REFROOT):
+        return REF_DRIVER if os.path.exists(REF_DRIVER) else None
+    try:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFROOT=" + REFROOT], check=True,
+                       stdout=subprocess.DEVNULL)
+    except subprocess.CalledProcessError:
+        return None
+    return REF_DRIVER
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(build_port())
+        D, I, L, P = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p
+        dp, ip, lp = ctypes.POINTER(D), ctypes.POINTER(I), ctypes.POINTER(L)
+        lib.ora_load.restype = P
+        lib.ora_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, I]
+        lib.ora_free.argtypes = [P]
+        lib.ora_error.restype = ctypes.c_char_p
+        lib.ora_error.argtypes = [P]
+        lib.ora_info.argtypes = [P, ip, ip, dp]
+        lib.ora_type_index.restype = I
+        lib.ora_type_index.argtypes = [P, ctypes.c_char_p]
+        lib.ora_badness.restype = I
+        lib.ora_badness.argtypes = [P]
+        lib.ora_calculate.restype = I
+        lib.ora_calculate.argtypes = [P, I, dp, dp, dp, ip, dp, dp, dp, I, dp, dp, dp, dp, dp]
+        lib.ora_list_sizes.argtypes = [P, lp, lp, lp]
+        lib.ora_get_lists.argtypes = [P, ip, ip, ip]
+        lib.ora_compute_1b.argtypes = [P, I, dp]
+        lib.ora_compute_2b.argtypes = [P, D, dp, I, I, dp, dp, dp]
+        lib.ora_compute_3b.argtypes = [P, dp, dp, ip, dp, dp, dp]
+        lib.ora_compute_4b.argtypes = [P, dp, dp, ip, dp, dp, dp]
+        _lib = lib
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class Oracle:
+    """One parameter set loaded into the C restatement."""
+
+    def __init__(self, param_file: str):
+        self.lib = _load()
+        err = ctypes.create_string_buffer(512)
+        self.h = self.lib.ora_load(param_file.encode(), err, 512)
+        if not self.h:
+            raise ValueError("oracle: " + err.value.decode())
+        orders = (ctypes.c_int * 3)()
+        nt = ctypes.c_int()
+        cuts = (ctypes.c_double * 3)()
+        self.lib.ora_info(self.h, orders, ctypes.byref(nt), cuts)
+        self.orders = tuple(orders)
+        self.ntypes = nt.value
+        self.max_cutoffs = tuple(cuts)
+
+    def type_indices(self, types: Sequence[str]) -> np.ndarray:
+        cache: Dict[str, int] = {}
+        out = np.empty(len(types), dtype=np.int32)
+        for i, t in enumerate(types):
+            if t not in cache:
+                cache[t] = self.lib.ora_type_index(self.h, t.encode())
+                if cache[t] < 0:
+                    raise ValueError("oracle: atom type %s not in parameter file" % t)
+            out[i] = cache[t]
+        return out
+
+    def calculate(self, pos, types, cell, small: bool = False, energy: float = 0.0,
+                  force=None) -> Dict[str, object]:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        n = pos.shape[0]
+        x, y, z = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(3, 3)
+        ca, cb, cc = (np.ascontiguousarray(cell[k]) for k in range(3))
+        typ = self.type_indices(types)
+        f = np.zeros((n, 3)) if force is None else np.array(force, dtype=np.float64)
+        fx, fy, fz = (np.ascontiguousarray(f[:, k]) for k in range(3))
+        e = ctypes.c_double(energy)
+        st = np.zeros(9)
+        rc = self.lib.ora_calculate(self.h, n, _dp(x), _dp(y), _dp(z), _ip(typ), _dp(ca), _dp(cb), _dp(cc),
+                                    int(bool(small)), ctypes.byref(e), _dp(fx), _dp(fy), _dp(fz), _dp(st))
+        if rc != 0:
+            raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
+        return {"energy": e.value, "force": np.stack([fx, fy, fz], axis=1), "stress": st,
+                "badness": self.lib.ora_badness(self.h)}
+
+    def lists(self):
+        n2, n3, n4 = ctypes.c_long(), ctypes.c_long(), ctypes.c_long()
+        self.lib.ora_list_sizes(self.h, ctypes.byref(n2), ctypes.byref(n3), ctypes.byref(n4))
+        l2 = np.zeros((n2.value, 2), dtype=np.int32)
+        l3 = np.zeros((n3.value, 3), dtype=np.int32)
+        l4 = np.zeros((n4.value, 4), dtype=np.int32)
+        self.lib.ora_get_lists(self.h, _ip(l2), _ip(l3), _ip(l4))
+        return l2, l3, l4
+
+    # per-cluster entry points (chimesFF::compute_nB semantics: accumulate)
+    def compute_2b(self, dx, dr, typ, force, stress, energy):
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        e = ctypes.c_double(energy)
+        self.lib.ora_compute_2b(self.h, float(dx), _dp(dr), int(typ[0]), int(typ[1]), _dp(force), _dp(stress),
+                                ctypes.byref(e))
+        return e.value
+
+    def compute_3b(self, dx, dr, typ, force, stress, energy):
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        t = np.ascontiguousarray(typ, dtype=np.int32)
+        e = ctypes.c_double(energy)
+        self.lib.ora_compute_3b(self.h, _dp(dx), _dp(dr), _ip(t), _dp(force), _dp(stress), ctypes.byref(e))
+        return e.value
+
+    def compute_4b(self, dx, dr, typ, force, stress, energy):
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        t = np.ascontiguousarray(typ, dtype=np.int32)
+        e = ctypes.c_double(energy)
+        self.lib.ora_compute_4b(self.h, _dp(dx), _dp(dr), _ip(t), _dp(force), _dp(stress), ctypes.byref(e))
+        return e.value
+
+
+def run_reference(param_file: str, xyz_file: str, small: bool, out_prefix: str, lists: bool = False,
+                  time_reps: int = 0):
+    """Runs the compiled reference driver; returns (result dict, lists or None, timing or None)."""
+    drv = build_reference()
+    if drv is None or not os.path.exists(drv):
+        raise FileNotFoundError("reference driver not available")
+    cmd = [drv, param_file, xyz_file, "1" if small else "0", out_prefix]
+    if lists:
+        cmd.append("--lists")
+    if time_reps:
+        cmd += ["--time", str(time_reps)]
+    p = subprocess.run(cmd, check=True, capture_output=True, text=True)
+    timing = None
+    if time_reps:
+        import json
+        timing = json.loads(p.stdout.strip().splitlines()[-1])
+    with open(out_prefix + ".res") as f:
+        rows = f.read().split("\n")
+    energy = float(rows[0])
+    stress = np.array([float(v) for v in rows[1].split()])
+    force = np.array([[float(v) for v in r.split()] for r in rows[2:] if r.strip()])
+    lst = None
+    if lists:
+        with open(out_prefix + ".lists") as f:
+            head = f.readline().split()
+            n2, n3, n4 = int(head[2]), int(head[3]), int(head[4])
+            flat = np.array(f.read().split(), dtype=np.int64)
+        l2 = flat[:2 * n2].reshape(n2, 2)
+        l3 = flat[2 * n2:2 * n2 + 3 * n3].reshape(n3, 3)
+        l4 = flat[2 * n2 + 3 * n3:].reshape(n4, 4)
+        lst = (l2, l3, l4)
+    return {"energy": energy, "force": force, "stress": stress}, lst, timing
