@@ -1,0 +1,97 @@
+"""ctypes binding of the in-tree native library ``libchimescalc.so``.
+
+The library is the product: every evaluation runs in its CUDA kernels.  There
+is no Python or CPU fallback -- ``load()`` raises when the library has not been
+built, and the library itself reports an error when no GPU is present.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libchimescalc.so")
+
+_lib = None
+
+# Exported C symbols and their signatures: the reference's serial interface
+# (chimescalc_serial_C.h), its per-cluster interface (chimescalc_C.h) and the
+# ck_* extension (chimes_gb300.h).
+D, I, LL, P, S = ctypes.c_double, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_char_p
+DP, IP, LLP = ctypes.POINTER(D), ctypes.POINTER(I), ctypes.POINTER(LL)
+SP = ctypes.POINTER(ctypes.c_char_p)
+
+SIGNATURES = {
+    # serial interface
+    "chimes_open_instance": (P, []),
+    "chimes_close_instance": (None, [P]),
+    "set_chimes_serial": (None, [I]),
+    "set_chimes_serial_instance": (None, [P, I]),
+    "init_chimes_serial": (None, [S, IP]),
+    "init_chimes_serial_instance": (None, [P, S, I]),
+    "calculate_chimes": (None, [I, DP, DP, DP, SP, DP, DP, DP, DP, DP, DP, DP, DP]),
+    "calculate_chimes_instance": (None, [P, I, DP, DP, DP, SP, DP, DP, DP, DP, DP, DP, DP, DP]),
+    # per-cluster interface
+    "get_chimes_max_2b_cutoff": (D, []),
+    "get_chimes_max_3b_cutoff": (D, []),
+    "get_chimes_max_4b_cutoff": (D, []),
+    "get_chimes_2b_order": (I, []),
+    "get_chimes_3b_order": (I, []),
+    "get_chimes_4b_order": (I, []),
+    "set_chimes": (None, []),
+    "init_chimes": (None, [I]),
+    "chimes_read_params": (None, [S]),
+    "chimes_build_pair_int_trip_map": (None, []),
+    "chimes_build_pair_int_quad_map": (None, []),
+    "chimes_compute_2b_props": (None, [D, DP, SP, DP, DP, DP]),
+    "chimes_compute_3b_props": (None, [DP, DP, SP, DP, DP, DP]),
+    "chimes_compute_4b_props": (None, [DP, DP, SP, DP, DP, DP]),
+    "chimes_compute_2b_props_fromf90": (None, [DP, DP, S, S, DP, DP, DP]),
+    "chimes_compute_3b_props_fromf90": (None, [DP, DP, S, S, S, DP, DP, DP]),
+    "chimes_compute_4b_props_fromf90": (None, [DP, DP, S, S, S, S, DP, DP, DP]),
+    # extension
+    "ck_set_error_mode": (I, [I]),
+    "ck_last_error": (S, []),
+    "ck_open": (P, []),
+    "ck_close": (None, [P]),
+    "ck_load_params": (I, [P, S]),
+    "ck_select_params": (I, [P, I]),
+    "ck_param_info": (I, [P, I, IP, IP, DP]),
+    "ck_type_index": (I, [P, I, S]),
+    "ck_set_precision": (I, [P, I]),
+    "ck_set_tuning": (I, [P, I, I, I]),
+    "ck_use_graph": (I, [P, I]),
+    "ck_calculate_batch": (I, [P, I, IP, DP, IP, DP, IP, IP, DP, DP, DP]),
+    "ck_stage_batch": (I, [P, I, IP, DP, IP, DP, IP, IP]),
+    "ck_launch": (I, [P]),
+    "ck_collect": (I, [P, DP, DP, DP]),
+    "ck_stream": (P, [P]),
+    "ck_last_counts": (I, [P, LLP]),
+    "ck_last_diagnostics": (I, [P, IP]),
+    "ck_export_lists": (I, [P, IP, IP, IP]),
+    "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
+}
+
+
+def load() -> ctypes.CDLL:
+    """Loads the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("native library %s is missing: build it with "
+                           "chimes_calculator_gb300.build.build() (there is no CPU fallback)" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(SIGNATURES)

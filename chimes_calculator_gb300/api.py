@@ -1,0 +1,179 @@
+"""Python API over the native library: load parameter sets once, evaluate one
+configuration or a batch of configurations on the GPU.
+
+    calc = Calculator()                       # one CUDA stream + workspace
+    slot = calc.load_params("model.txt")
+    res = calc.evaluate(pos, types, cell)     # energy, forces, stress (one config)
+    res = calc.evaluate_batch(configs)        # many configs in one set of launches
+
+Energies/forces/stress follow serial_chimes_interface::calculate
+(serial_interface/src/serial_chimes_interface.cpp:960-1124) with zero initial
+energy and forces: kcal/mol, kcal/mol/A and the 3x3 stress in kcal/mol/A^3.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+
+FP64 = 0
+MIXED = 1
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class ChimesError(RuntimeError):
+    pass
+
+
+class Calculator:
+    def __init__(self, precision: int = FP64, graph: bool = False):
+        self.lib = _lib.load()
+        self.lib.ck_set_error_mode(1)
+        self.h = self.lib.ck_open()
+        self.slots: List[int] = []
+        self._types: List[Dict[str, int]] = []
+        self.set_precision(precision)
+        self.use_graph(graph)
+
+    def close(self):
+        if self.h:
+            self.lib.ck_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc is not None and rc < 0:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        return rc
+
+    def load_params(self, path: str) -> int:
+        slot = self._check(self.lib.ck_load_params(self.h, path.encode()))
+        self.slots.append(slot)
+        self._types.append({})
+        return slot
+
+    def info(self, slot: int = 0):
+        orders = (ctypes.c_int * 3)()
+        nt = ctypes.c_int()
+        cuts = (ctypes.c_double * 3)()
+        self._check(self.lib.ck_param_info(self.h, slot, orders, ctypes.byref(nt), cuts))
+        return {"orders": tuple(orders), "ntypes": nt.value, "max_cutoffs": tuple(cuts)}
+
+    def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
+        cache = self._types[slot]
+        out = np.empty(len(types), dtype=np.int32)
+        for i, t in enumerate(types):
+            k = cache.get(t)
+            if k is None:
+                k = self.lib.ck_type_index(self.h, slot, t.encode())
+                if k < 0:
+                    raise ChimesError("atom type %s is not in parameter set %d" % (t, slot))
+                cache[t] = k
+            out[i] = k
+        return out
+
+    def set_precision(self, precision: int):
+        self._check(self.lib.ck_set_precision(self.h, int(precision)))
+
+    def set_tuning(self, tpc3: int = 4, tpc4: int = 8, blocks_per_sm: int = 4):
+        self._check(self.lib.ck_set_tuning(self.h, tpc3, tpc4, blocks_per_sm))
+
+    def use_graph(self, on: bool):
+        self._check(self.lib.ck_use_graph(self.h, 1 if on else 0))
+
+    # -- packing -------------------------------------------------------------
+    def pack(self, configs, slots=None, small=None):
+        """configs: sequence of (pos[N,3], types (names or indices), cell[3,3])."""
+        n = len(configs)
+        slots = [0] * n if slots is None else list(slots)
+        natoms = np.array([len(c[0]) for c in configs], dtype=np.int32)
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(c[0], dtype=np.float64).reshape(-1, 3)
+                                                   for c in configs]))
+        tys = []
+        for c, s in zip(configs, slots):
+            t = c[1]
+            if len(t) and isinstance(t[0], str):
+                tys.append(self.type_indices(t, s))
+            else:
+                tys.append(np.asarray(t, dtype=np.int32))
+        types = np.ascontiguousarray(np.concatenate(tys).astype(np.int32))
+        cells = np.ascontiguousarray(np.stack([np.asarray(c[2], dtype=np.float64).reshape(3, 3) for c in configs]))
+        sm = np.zeros(n, dtype=np.int32) if small is None else np.asarray(small, dtype=np.int32).reshape(n)
+        ps = np.asarray(slots, dtype=np.int32)
+        return natoms, pos, types, cells, sm, ps
+
+    def evaluate_batch(self, configs, slots=None, small=None):
+        natoms, pos, types, cells, sm, ps = self.pack(configs, slots, small)
+        n = len(configs)
+        energy = np.zeros(n)
+        force = np.zeros((int(natoms.sum()), 3))
+        stress = np.zeros((n, 9))
+        self._check(self.lib.ck_calculate_batch(self.h, n, _ip(natoms), _dp(pos), _ip(types), _dp(cells), _ip(sm),
+                                                _ip(ps), _dp(energy), _dp(force), _dp(stress)))
+        out = []
+        off = 0
+        for s in range(n):
+            out.append({"energy": energy[s], "force": force[off:off + natoms[s]].copy(),
+                        "stress": stress[s].copy()})
+            off += natoms[s]
+        return out
+
+    def evaluate(self, pos, types, cell, slot: int = 0, small: bool = False):
+        return self.evaluate_batch([(pos, types, cell)], slots=[slot], small=[int(small)])[0]
+
+    # -- split form (device timing) ------------------------------------------
+    def stage(self, packed):
+        natoms, pos, types, cells, sm, ps = packed
+        self._staged_n = (len(natoms), int(natoms.sum()))
+        self._check(self.lib.ck_stage_batch(self.h, len(natoms), _ip(natoms), _dp(pos), _ip(types), _dp(cells),
+                                            _ip(sm), _ip(ps)))
+
+    def launch(self):
+        self._check(self.lib.ck_launch(self.h))
+
+    def collect(self):
+        ns, na = self._staged_n
+        energy = np.zeros(ns)
+        force = np.zeros((na, 3))
+        stress = np.zeros((ns, 9))
+        self._check(self.lib.ck_collect(self.h, _dp(energy), _dp(force), _dp(stress)))
+        return energy, force, stress
+
+    def stream_ptr(self) -> int:
+        return self.lib.ck_stream(self.h) or 0
+
+    def counts(self):
+        out = (ctypes.c_longlong * 5)()
+        self._check(self.lib.ck_last_counts(self.h, out))
+        return {"n2": out[0], "n3": out[1], "n4": out[2], "n_ghost": out[3], "n_atoms": out[4]}
+
+    def diagnostics(self):
+        out = (ctypes.c_int * 3)()
+        self._check(self.lib.ck_last_diagnostics(self.h, out))
+        return {"badness": out[0], "penalty_hits": out[1], "below_rin": out[2]}
+
+    def lists(self):
+        """Cluster lists of the last evaluation in system-local ghost numbering
+        (the reference's indices): l2 (n2,2) [atom, ghost], l3 (n3,3), l4 (n4,4)."""
+        c = self.counts()
+        l2 = np.zeros((c["n2"], 2), dtype=np.int32)
+        l3 = np.zeros((c["n3"], 3), dtype=np.int32)
+        l4 = np.zeros((c["n4"], 4), dtype=np.int32)
+        self._check(self.lib.ck_export_lists(self.h, _ip(l2), _ip(l3), _ip(l4)))
+        return l2, l3, l4

@@ -1,0 +1,357 @@
+// C ABI of the library.
+//
+// 1. The reference's serial-interface symbols (chimescalc_serial_C.h), same
+//    names, arguments and semantics: energy and forces are accumulated into the
+//    caller's values, stress[9] is overwritten, set_chimes_serial must precede
+//    init_chimes_serial, and the handle-based variants work on instances from
+//    chimes_open_instance.  Errors follow the reference (message on stdout,
+//    exit(0)) unless ck_set_error_mode(1) switches to returned status codes.
+// 2. The ck_* extension: batched evaluation of many configurations, precision
+//    and launch tuning, graph replay, split stage/launch/collect for device
+//    timing, diagnostics and cluster-list export.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ck_engine.h"
+
+namespace {
+
+struct Instance {
+    ck::Engine eng;
+    int slot = -1;
+    bool small = true;   // serial_chimes_interface(bool small = true)
+};
+
+Instance* g_static = nullptr;               // the instance of set_chimes_serial
+Instance* g_cur = nullptr;                  // chimes_ptr of chimescalc_serial_C.cpp:22
+int g_errmode = 0;                          // 0: print + exit(0) (reference), 1: return status
+thread_local std::string g_err;
+
+int report(int status, const std::string& msg) {
+    g_err = msg;
+    if (status != ck::kOk && g_errmode == 0) {
+        std::cout << "ERROR: " << msg << std::endl;
+        std::exit(0);
+    }
+    return status;
+}
+
+int check_handle(void* h) {
+    if (!h) return report(ck::kErrState, "no ChIMES instance: call set_chimes_serial / chimes_open_instance first");
+    return ck::kOk;
+}
+
+int ensure_params(Instance* in) {
+    if (in->slot < 0) return report(ck::kErrState, "parameters not initialised: call init_chimes_serial first");
+    return ck::kOk;
+}
+
+int types_to_index(const ck::HostParams& P, int n, char* names[], std::vector<int>& out) {
+    out.resize(n);
+    std::map<std::string, int> cache;
+    for (int i = 0; i < n; i++) {
+        std::string nm(names[i]);
+        auto it = cache.find(nm);
+        if (it == cache.end()) {
+            int t = P.type_index(nm);
+            if (t < 0) return report(ck::kErrInput, "couldn't assign an atom type index for (index/type) " +
+                                                        std::to_string(i) + " " + nm);
+            it = cache.emplace(nm, t).first;
+        }
+        out[i] = it->second;
+    }
+    return ck::kOk;
+}
+
+int calculate_one(Instance* in, int natom, const double* xc, const double* yc, const double* zc, char* atom_types[],
+                     const double* ca, const double* cb, const double* cc, double* energy, double* fx, double* fy,
+                     double* fz, double* stress) {
+    if (int st = ensure_params(in)) return st;
+    const ck::HostParams& P = in->eng.params(in->slot);
+    if (natom <= 0) return report(ck::kErrInput, "natom must be positive");
+    std::vector<int> types;
+    if (int st = types_to_index(P, natom, atom_types, types)) return st;
+    std::vector<double> pos(3 * (size_t)natom), force(3 * (size_t)natom);
+    for (int i = 0; i < natom; i++) {
+        pos[3 * i] = xc[i]; pos[3 * i + 1] = yc[i]; pos[3 * i + 2] = zc[i];
+    }
+    ck::SystemSpec s;
+    s.n = natom;
+    s.pos = pos.data();
+    s.types = types.data();
+    for (int k = 0; k < 3; k++) { s.cell[k] = ca[k]; s.cell[3 + k] = cb[k]; s.cell[6 + k] = cc[k]; }
+    s.small = in->small;
+    s.pset = in->slot;
+    std::vector<ck::SystemResult> res;
+    std::string err;
+    ck::Status st = in->eng.run({s}, force.data(), res, err);
+    if (st != ck::kOk) return report(st, err);
+    const ck::SystemResult& r = res[0];
+    // serial_chimes_interface::calculate: energy accumulates into the caller's
+    // value and the sum is divided by (n_rep+1)^3; forces accumulate; stress
+    // is overwritten with the symmetric tensor divided by the volume.
+    *energy = *energy / std::pow(r.n_rep + 1.0, 3.0) + r.energy;
+    for (int i = 0; i < natom; i++) {
+        fx[i] += force[3 * i]; fy[i] += force[3 * i + 1]; fz[i] += force[3 * i + 2];
+    }
+    const double* v = r.virial;
+    const double full[9] = {v[0], v[1], v[2], v[1], v[3], v[4], v[2], v[4], v[5]};
+    for (int k = 0; k < 9; k++) stress[k] = full[k] / r.vol;
+    g_err.clear();
+    return ck::kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// Reference serial interface (serial_interface/api/chimescalc_serial_C.h:11-18)
+// ---------------------------------------------------------------------------
+void* chimes_open_instance() { return new Instance(); }
+
+void chimes_close_instance(void* handle) { delete static_cast<Instance*>(handle); }
+
+void set_chimes_serial_instance(void* handle, int small) {
+    if (check_handle(handle)) return;
+    if (small != 0 && small != 1) {
+        report(ck::kErrInput, "Small must be set to 0 (false) or 1 (true); received " + std::to_string(small));
+        return;
+    }
+    static_cast<Instance*>(handle)->small = small != 0;
+}
+
+void set_chimes_serial(int small) {
+    if (small != 0 && small != 1) {
+        report(ck::kErrInput, "Small must be set to 0 (false) or 1 (true); received " + std::to_string(small));
+        return;
+    }
+    if (!g_static) g_static = new Instance();
+    g_cur = g_static;
+    set_chimes_serial_instance(g_cur, small);
+}
+
+void init_chimes_serial_instance(void* handle, char* param_file, int /*rank: the reference passes 0*/) {
+    if (check_handle(handle)) return;
+    Instance* in = static_cast<Instance*>(handle);
+    std::string err;
+    int slot = in->eng.load_params(param_file ? param_file : "", err);
+    if (slot < 0) {
+        report(slot, err);
+        return;
+    }
+    in->slot = slot;
+    g_err.clear();
+}
+
+void init_chimes_serial(char* param_file, int* rank) {
+    if (check_handle(g_cur)) return;
+    init_chimes_serial_instance(g_cur, param_file, rank ? *rank : 0);
+}
+
+void calculate_chimes_instance(void* handle, int natom, double* xc, double* yc, double* zc, char* atom_types[],
+                               double ca[3], double cb[3], double cc[3], double* energy, double fx[], double fy[],
+                               double fz[], double stress[9]) {
+    if (check_handle(handle)) return;
+    calculate_one(static_cast<Instance*>(handle), natom, xc, yc, zc, atom_types, ca, cb, cc, energy, fx, fy, fz,
+                     stress);
+}
+
+void calculate_chimes(int natom, double* xc, double* yc, double* zc, char* atom_types[], double ca[3], double cb[3],
+                      double cc[3], double* energy, double fx[], double fy[], double fz[], double stress[9]) {
+    calculate_chimes_instance(g_cur, natom, xc, yc, zc, atom_types, ca, cb, cc, energy, fx, fy, fz, stress);
+}
+
+// ---------------------------------------------------------------------------
+// ck_* extension
+// ---------------------------------------------------------------------------
+int ck_set_error_mode(int mode) {
+    int old = g_errmode;
+    g_errmode = mode ? 1 : 0;
+    return old;
+}
+
+const char* ck_last_error(void) { return g_err.c_str(); }
+
+void* ck_open(void) { return chimes_open_instance(); }
+void ck_close(void* h) { chimes_close_instance(h); }
+
+int ck_load_params(void* h, const char* path) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    std::string err;
+    int slot = in->eng.load_params(path ? path : "", err);
+    if (slot < 0) return report(slot, err);
+    if (in->slot < 0) in->slot = slot;
+    g_err.clear();
+    return slot;
+}
+
+int ck_select_params(void* h, int slot) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    in->slot = slot;
+    return ck::kOk;
+}
+
+int ck_param_info(void* h, int slot, int* orders, int* ntypes, double* maxcuts) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    const ck::HostParams& P = in->eng.params(slot);
+    if (orders) { orders[0] = P.o2; orders[1] = P.o3; orders[2] = P.o4; }
+    if (ntypes) *ntypes = P.ntypes;
+    if (maxcuts) { maxcuts[0] = P.max_cut2(); maxcuts[1] = P.max_cut3(); maxcuts[2] = P.max_cut4(); }
+    return ck::kOk;
+}
+
+int ck_type_index(void* h, int slot, const char* name) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    return in->eng.params(slot).type_index(name ? name : "");
+}
+
+int ck_set_precision(void* h, int precision) {
+    if (int st = check_handle(h)) return st;
+    if (precision != ck::kFP64 && precision != ck::kMixed) return report(ck::kErrInput, "precision must be 0 or 1");
+    static_cast<Instance*>(h)->eng.precision = precision;
+    return ck::kOk;
+}
+
+int ck_set_tuning(void* h, int tpc3, int tpc4, int blocks_per_sm) {
+    if (int st = check_handle(h)) return st;
+    auto ok = [](int t) { return t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32; };
+    if (!ok(tpc3) || !ok(tpc4) || blocks_per_sm < 1 || blocks_per_sm > 64)
+        return report(ck::kErrInput, "threads per cluster must be a power of two <= 32");
+    ck::Engine& e = static_cast<Instance*>(h)->eng;
+    e.tuning.tpc3 = tpc3;
+    e.tuning.tpc4 = tpc4;
+    e.tuning.blocks_per_sm = blocks_per_sm;
+    return ck::kOk;
+}
+
+int ck_use_graph(void* h, int on) {
+    if (int st = check_handle(h)) return st;
+    static_cast<Instance*>(h)->eng.use_graph = on != 0;
+    return ck::kOk;
+}
+
+static int build_specs(Instance* in, int nsys, const int* natoms, const double* pos, const int* types,
+                       const double* cells, const int* small, const int* pset, std::vector<ck::SystemSpec>& specs) {
+    if (nsys <= 0) return report(ck::kErrInput, "nsys must be positive");
+    specs.resize(nsys);
+    long long off = 0;
+    for (int s = 0; s < nsys; s++) {
+        ck::SystemSpec& sp = specs[s];
+        sp.n = natoms[s];
+        sp.pos = pos + 3 * off;
+        sp.types = types + off;
+        for (int k = 0; k < 9; k++) sp.cell[k] = cells[9 * s + k];
+        sp.small = small ? small[s] != 0 : false;
+        sp.pset = pset ? pset[s] : (in->slot < 0 ? 0 : in->slot);
+        off += natoms[s];
+    }
+    return ck::kOk;
+}
+
+int ck_calculate_batch(void* h, int nsys, const int* natoms, const double* pos, const int* types,
+                       const double* cells, const int* small, const int* pset, double* energy, double* force,
+                       double* stress) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    std::vector<ck::SystemSpec> specs;
+    if (int st = build_specs(in, nsys, natoms, pos, types, cells, small, pset, specs)) return st;
+    std::vector<ck::SystemResult> res;
+    std::string err;
+    ck::Status st = in->eng.run(specs, force, res, err);
+    if (st != ck::kOk) return report(st, err);
+    for (int s = 0; s < nsys; s++) {
+        if (energy) energy[s] = res[s].energy;
+        if (stress) {
+            const double* v = res[s].virial;
+            const double full[9] = {v[0], v[1], v[2], v[1], v[3], v[4], v[2], v[4], v[5]};
+            for (int k = 0; k < 9; k++) stress[9 * s + k] = full[k] / res[s].vol;
+        }
+    }
+    g_err.clear();
+    return ck::kOk;
+}
+
+int ck_stage_batch(void* h, int nsys, const int* natoms, const double* pos, const int* types, const double* cells,
+                   const int* small, const int* pset) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    std::vector<ck::SystemSpec> specs;
+    if (int st = build_specs(in, nsys, natoms, pos, types, cells, small, pset, specs)) return st;
+    std::string err;
+    ck::Status st = in->eng.stage(specs, err);
+    if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
+int ck_launch(void* h) {
+    if (int st = check_handle(h)) return st;
+    std::string err;
+    ck::Status st = static_cast<Instance*>(h)->eng.launch(err);
+    if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
+int ck_collect(void* h, double* energy, double* force, double* stress) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    std::vector<ck::SystemResult> res;
+    std::string err;
+    ck::Status st = in->eng.collect(force, res, err);
+    if (st != ck::kOk) return report(st, err);
+    for (size_t s = 0; s < res.size(); s++) {
+        if (energy) energy[s] = res[s].energy;
+        if (stress) {
+            const double* v = res[s].virial;
+            const double full[9] = {v[0], v[1], v[2], v[1], v[3], v[4], v[2], v[4], v[5]};
+            for (int k = 0; k < 9; k++) stress[9 * s + k] = full[k] / res[s].vol;
+        }
+    }
+    return ck::kOk;
+}
+
+void* ck_stream(void* h) {
+    if (!h) return nullptr;
+    return (void*)static_cast<Instance*>(h)->eng.stream();
+}
+
+int ck_last_counts(void* h, long long* out) {
+    if (int st = check_handle(h)) return st;
+    const ck::RunStats& s = static_cast<Instance*>(h)->eng.last;
+    out[0] = s.n2; out[1] = s.n3; out[2] = s.n4; out[3] = s.n_ghost; out[4] = s.n_atoms;
+    return ck::kOk;
+}
+
+int ck_last_diagnostics(void* h, int* out) {
+    if (int st = check_handle(h)) return st;
+    const ck::RunStats& s = static_cast<Instance*>(h)->eng.last;
+    out[0] = s.badness; out[1] = s.penalty_hits; out[2] = s.below_rin;
+    return ck::kOk;
+}
+
+int ck_export_lists(void* h, int* l2, int* l3, int* l4) {
+    if (int st = check_handle(h)) return st;
+    std::vector<int> a, b, c;
+    std::string err;
+    ck::Status st = static_cast<Instance*>(h)->eng.export_lists(a, b, c, err);
+    if (st != ck::kOk) return report(st, err);
+    if (l2 && !a.empty()) std::memcpy(l2, a.data(), sizeof(int) * a.size());
+    if (l3 && !b.empty()) std::memcpy(l3, b.data(), sizeof(int) * b.size());
+    if (l4 && !c.empty()) std::memcpy(l4, c.data(), sizeof(int) * c.size());
+    return ck::kOk;
+}
+
+}  // extern "C"

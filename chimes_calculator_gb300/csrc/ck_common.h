@@ -1,0 +1,139 @@
+// Shared host/device data layout of the GB300 ChIMES force path.
+//
+// Everything the kernels read lives in two kinds of device buffers:
+//   * one parameter-set image per loaded parameter file (DevParamSet and the
+//     arrays it points to), built once by read_parameters;
+//   * one batch workspace per instance (BatchView), holding every system of a
+//     batch back to back: caller atoms, replicated atoms, ghost images, bins,
+//     the 2B neighbour lists, the 3B/4B cluster lists and the accumulators.
+//
+// Index spaces (all int32 inside a batch; offsets are int64):
+//   caller atom  c   : 0 .. sum(n_in)         positions/forces as the caller passed them
+//   atom         a   : 0 .. sum(n_atoms)      after replication (small=true), wrapped
+//   ghost        g   : 0 .. sum(n_atoms*side^3); within a system ghost (img, a) sits at
+//                      ghost_off + img*n_atoms + a, img 0 is the primary cell and
+//                      img>=1 walks (i,j,k) in [-n,n]^3\{0} with i slowest, which is the
+//                      ghost numbering of simulation_system::build_layered_system
+//                      (serial_interface/src/serial_chimes_interface.cpp:546-585).
+#pragma once
+#include <cstdint>
+
+namespace ck {
+
+constexpr int kMaxOrder = 31;      // powers are packed 5 bits per pair
+constexpr int kMaxTypes = 8;       // nt^4 4-body tuple records
+constexpr int kPowBits = 5;
+
+enum Status : int {
+    kOk = 0,
+    kErrParam = -1,       // malformed / unsupported parameter file
+    kErrInput = -2,       // bad caller input (unknown atom type, sizes)
+    kErrGeometry = -3,    // cutoff larger than half the layered box, bad bins
+    kErrCuda = -4,        // CUDA runtime error
+    kErrCapacity = -5,    // a device capacity was exceeded (internal; retried)
+    kErrState = -6,       // call order (e.g. calculate before init)
+    kErrTimeout = -7,     // a bounded device wait expired
+};
+
+// One 2-body pair type (chimes_2b_cutoff / morse_var, chimesFF.h:290-295).
+struct PairRec {
+    double rin, rout, lam;
+    double xavg, xdiff;    // Morse-map constants 0.5*(xmax+xmin), -0.5*(xmax-xmin)
+    int ncoef;             // = 2B order
+    int coef_off;          // offset into c2d/c2f/p2
+};
+
+// One ordered atom-type tuple of a 3- or 4-body cluster.  Cutoffs, lambdas and
+// the packed powers are already permuted into the cluster's own pair order
+// (ij,ik,jk / ij,ik,il,jk,jl,kl) by the tuple's pair_int_{trip,quad}_map entry.
+struct TupleRec {
+    int valid;             // atom_int_{trip,quad}_map >= 0 and the type has coefficients
+    int ncoef;
+    int coef_off;          // offset into the body's coefficient arrays
+    int type_id;           // tripidx / quadidx (for diagnostics)
+    double rin[6], rout[6], lam[6], xavg[6], xdiff[6];
+};
+
+struct DevParamSet {
+    int ntypes, npairs, o2, o3, o4;
+    int tersoff;
+    double fcut_var, pen_dist, pen_scale, inner_smooth;
+    double maxcut2, maxcut3, maxcut4, search;
+    const double* eoff;        // [nt]
+    const int* pair_map;       // [nt*nt]  atom_int_pair_map
+    const PairRec* pairs;      // [npairs]
+    const double* c2d; const float* c2f; const int* p2;
+    const TupleRec* t3;        // [nt^3] (null when o3 == 0)
+    const double* c3d; const float* c3f; const uint32_t* p3;
+    const TupleRec* t4;        // [nt^4] (null when o4 == 0)
+    const double* c4d; const float* c4f; const uint32_t* p4;
+};
+
+// Per-system geometry, written by the host set-up (cell algebra) and
+// completed on the device (bin grid).
+struct SysDesc {
+    double h[9], hi[9];        // cell of the (replicated) system and inverse: r = h * s
+    double hn[9], hni[9];      // reoriented cell used for the neighbour lists
+    double h0[9], h0i[9];      // unreplicated cell (replication step)
+    double search;             // max(rc2, rc3, rc4)
+    double c3, c4;             // max 3B / 4B outer cutoffs (0 when the order is 0)
+    int n_in;                  // caller atoms
+    int n_rep;                 // n_replicates
+    int n_atoms;               // replicated atoms = n_in * (n_rep+1)^3
+    int n_layers, side;        // ghost layers and 2n+1
+    int pset;                  // parameter set slot
+    int has3, has4;
+    long long in_off, atom_off, ghost_off, bin_off;
+    int bin_cap;               // bins reserved for this system
+    int pad0;
+    // device-completed
+    double minpos[3];
+    int nb[3];
+    int err;
+};
+
+// Flat views of a batch workspace (all device pointers).
+struct BatchView {
+    int n_sys;
+    long long n_in_total, n_atoms_total, n_ghost_total, n_bins_total;
+    SysDesc* sys;
+    const DevParamSet* psets;      // device array of parameter sets (by slot)
+    // caller atoms
+    const double* in_pos;          // [n_in_total][3]
+    const int* in_type;            // [n_in_total]
+    // replicated atoms
+    int* atom_sys;                 // [n_atoms_total]
+    int* atom_type;
+    int* atom_orig;                // caller-atom index receiving the force
+    // ghosts (image 0 = the atoms themselves)
+    int* ghost_parent;             // atom index (global)
+    double* ghost_fs;              // [g][3] fractional coords, input cell
+    double* ghost_xn;              // [g][3] Cartesian coords, reoriented cell
+    double* ghost_fn;              // [g][3] fractional coords, reoriented cell
+    // bins (per system, offset bin_off)
+    unsigned long long* minmax;    // [n_sys][6] order-preserving keys
+    int* ghost_bin;                // [g] local bin id
+    int* bin_count;                // [n_bins_total]
+    long long* bin_start;          // [n_bins_total+1] positions in bin_items (global exclusive scan)
+    int* bin_fill;
+    int* bin_items;                // [g] global ghost ids sorted by (bin, id)
+    // 2B lists
+    int* l2_count;                 // [n_atoms_total]
+    long long* l2_off;             // [n_atoms_total+1]
+    int* l2_ghost;                 // [n2] global ghost id of the neighbour
+    double* l2_dist;               // [n2] distance in the reoriented frame
+    long long n2_cap;
+    // 3B/4B enumeration
+    int* e_cnt3; int* e_cnt4;      // [n2]
+    long long* e_off3; long long* e_off4;   // [n2+1]
+    int* c3;                       // [n3][3] global ghost ids (i, j, k)
+    int* c4;                       // [n4][4]
+    long long n3_cap, n4_cap;
+    // results
+    double* force;                 // [n_in_total][3]
+    double* ev;                    // [n_sys][8]: energy, virial xx xy xz yy yz zz, spare
+    int* flags;                    // [8] device error flags: 0 capacity, 1 geometry, 2 badness max,
+                                   //     3 penalty count, 4 below-rin count, 5 timeout
+};
+
+}  // namespace ck

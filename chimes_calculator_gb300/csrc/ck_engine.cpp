@@ -1,0 +1,412 @@
+// Host engine: staging, the launch sequence of the list build and force
+// kernels (optionally replayed as one CUDA graph), capacity growth and result
+// collection.  See ck_engine.h.
+#include "ck_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "ck_geom.h"
+
+namespace ck {
+
+#define CK_TRY(call)                                                              \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            err = std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call; \
+            return kErrCuda;                                                      \
+        }                                                                         \
+    } while (0)
+
+const char* status_name(int s) {
+    switch (s) {
+        case kOk: return "ok";
+        case kErrParam: return "parameter file error";
+        case kErrInput: return "input error";
+        case kErrGeometry: return "geometry error";
+        case kErrCuda: return "CUDA error";
+        case kErrCapacity: return "capacity exceeded";
+        case kErrState: return "call-order error";
+        case kErrTimeout: return "device wait timed out";
+        default: return "error";
+    }
+}
+
+Engine::Engine() {}
+
+Engine::~Engine() {
+    drop_graph();
+    for (auto& s : sets_)
+        if (s.dev) cudaFree(s.dev);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::drop_graph() {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    graph_exec_ = nullptr;
+    graph_ = nullptr;
+    graph_key_.clear();
+}
+
+Status Engine::init_device(std::string& err) {
+    if (ready_) return kOk;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        err = std::string("no CUDA device available: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        return kErrCuda;
+    }
+    CK_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    CK_TRY(h_flags_.reserve(8));
+    CK_TRY(h_counts_.reserve(4));
+    CK_TRY(d_flags_.reserve(8));
+    ready_ = true;
+    return kOk;
+}
+
+int Engine::load_params(const std::string& path, std::string& err) {
+    Status st = init_device(err);
+    if (st != kOk) return st;
+    PSet ps;
+    ps.host.reset(new HostParams());
+    st = parse_parameter_file(path, *ps.host, err);
+    if (st != kOk) return st;
+    ParamImage img = pack_params(*ps.host);
+    cudaError_t e = cudaMalloc(&ps.dev, img.bytes.size());
+    if (e == cudaSuccess) e = cudaMemcpy(ps.dev, img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        err = std::string("CUDA error uploading parameters: ") + cudaGetErrorString(e);
+        if (ps.dev) cudaFree(ps.dev);
+        return kErrCuda;
+    }
+    // relocate the offsets of the header to device pointers
+    DevParamSet h = img.header;
+    const uintptr_t base = (uintptr_t)ps.dev;
+    auto rel = [&](auto& ptr) {
+        if (ptr) ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(base + (uintptr_t)ptr);
+    };
+    rel(h.eoff); rel(h.pair_map); rel(h.pairs); rel(h.c2d); rel(h.c2f); rel(h.p2);
+    rel(h.t3); rel(h.c3d); rel(h.c3f); rel(h.p3);
+    rel(h.t4); rel(h.c4d); rel(h.c4f); rel(h.p4);
+    ps.view = h;
+    sets_.push_back(std::move(ps));
+    std::vector<DevParamSet> all;
+    for (auto& s : sets_) all.push_back(s.view);
+    drop_graph();
+    e = dsets_.reserve(all.size());
+    if (e == cudaSuccess) e = cudaMemcpy(dsets_.p, all.data(), all.size() * sizeof(DevParamSet), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        err = std::string("CUDA error uploading parameter table: ") + cudaGetErrorString(e);
+        return kErrCuda;
+    }
+    return (int)sets_.size() - 1;
+}
+
+Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
+    Status st = init_device(err);
+    if (st != kOk) return st;
+    if (sys.empty()) {
+        err = "empty batch";
+        return kErrInput;
+    }
+    CK_TRY(cudaStreamSynchronize(stream_));   // pinned staging may still feed a previous launch
+    const int S = (int)sys.size();
+    hsys_.assign(S, SysDesc());
+    vols_.assign(S, 0.0);
+    long long in_off = 0, atom_off = 0, ghost_off = 0, bin_off = 0;
+    int stride3 = 0, stride4 = 0;
+    double n2_est = 0.0, n3_est = 0.0, n4_est = 0.0;
+    for (int s = 0; s < S; s++) {
+        const SystemSpec& in = sys[s];
+        if (in.pset < 0 || in.pset >= (int)sets_.size()) {
+            err = "configuration " + std::to_string(s) + ": parameter set not loaded";
+            return kErrState;
+        }
+        const HostParams& P = *sets_[in.pset].host;
+        SysDesc& d = hsys_[s];
+        std::memset(&d, 0, sizeof(d));
+        std::string gerr;
+        st = system_geometry(&in.cell[0], &in.cell[3], &in.cell[6], in.n, in.small, P.max_cut2(), P.max_cut3(),
+                             P.max_cut4(), P.o3 > 0, P.o4 > 0, d, vols_[s], gerr);
+        if (st != kOk) {
+            err = (S > 1 ? "configuration " + std::to_string(s) + ": " : std::string()) + gerr;
+            return st;
+        }
+        for (int a = 0; a < in.n; a++)
+            if (in.types[a] < 0 || in.types[a] >= P.ntypes) {
+                err = "atom type index out of range for the parameter set";
+                return kErrInput;
+            }
+        d.pset = in.pset;
+        d.in_off = in_off; d.atom_off = atom_off; d.ghost_off = ghost_off; d.bin_off = bin_off;
+        in_off += in.n;
+        atom_off += d.n_atoms;
+        ghost_off += (long long)d.n_atoms * d.side * d.side * d.side;
+        bin_off += d.bin_cap;
+        stride3 = std::max(stride3, P.o3 > 0 ? P.o3 + 1 : 0);
+        stride4 = std::max(stride4, P.o4 > 0 ? P.o4 + 1 : 0);
+        // list-size estimates for the first capacity guess
+        const double rho = d.n_atoms / (vols_[s] > 0 ? vols_[s] : 1.0);
+        const double m = rho * 4.18879 * d.search * d.search * d.search;
+        n2_est += d.n_atoms * (0.55 * m + 4);
+        if (d.has3) n3_est += d.n_atoms * (0.3 * m * m * std::pow(d.c3 / d.search, 6.0) + 4);
+        if (d.has4) n4_est += d.n_atoms * (0.1 * m * m * m * std::pow(d.c4 / d.search, 9.0) + 4);
+    }
+    if (ghost_off > 2000000000LL) {
+        err = "batch exceeds 2^31 ghost atoms";
+        return kErrInput;
+    }
+    tuning.stride3 = stride3;
+    tuning.stride4 = stride4;
+    V_ = BatchView();
+    V_.n_sys = S;
+    V_.n_in_total = in_off;
+    V_.n_atoms_total = atom_off;
+    V_.n_ghost_total = ghost_off;
+    V_.n_bins_total = bin_off;
+    n2_cap_ = std::max(n2_cap_, (long long)n2_est + 1024);
+    n3_cap_ = std::max(n3_cap_, (long long)n3_est + 1024);
+    n4_cap_ = std::max(n4_cap_, (long long)n4_est + 1024);
+
+    CK_TRY(d_sys_.reserve(S));
+    CK_TRY(d_in_pos_.reserve(3 * in_off));
+    CK_TRY(d_in_type_.reserve(in_off));
+    CK_TRY(d_atom_sys_.reserve(atom_off));
+    CK_TRY(d_atom_type_.reserve(atom_off));
+    CK_TRY(d_atom_orig_.reserve(atom_off));
+    CK_TRY(d_ghost_parent_.reserve(ghost_off));
+    CK_TRY(d_ghost_bin_.reserve(ghost_off));
+    CK_TRY(d_ghost_fs_.reserve(3 * ghost_off));
+    CK_TRY(d_ghost_xn_.reserve(3 * ghost_off));
+    CK_TRY(d_ghost_fn_.reserve(3 * ghost_off));
+    CK_TRY(d_bin_items_.reserve(ghost_off));
+    CK_TRY(d_minmax_.reserve(6 * S));
+    CK_TRY(d_bin_count_.reserve(bin_off));
+    CK_TRY(d_bin_fill_.reserve(bin_off));
+    CK_TRY(d_bin_start_.reserve(bin_off + 1));
+    CK_TRY(d_l2_count_.reserve(atom_off));
+    CK_TRY(d_l2_off_.reserve(atom_off + 1));
+    CK_TRY(d_force_.reserve(3 * in_off));
+    CK_TRY(d_ev_.reserve(8 * S));
+    CK_TRY(h_in_pos_.reserve(3 * in_off));
+    CK_TRY(h_in_type_.reserve(in_off));
+    CK_TRY(h_force_.reserve(3 * in_off));
+    CK_TRY(h_ev_.reserve(8 * S));
+    st = ensure_lists(err);
+    if (st != kOk) return st;
+
+    for (int s = 0; s < S; s++) {
+        const SystemSpec& in = sys[s];
+        std::memcpy(h_in_pos_.p + 3 * hsys_[s].in_off, in.pos, sizeof(double) * 3 * in.n);
+        std::memcpy(h_in_type_.p + hsys_[s].in_off, in.types, sizeof(int) * in.n);
+    }
+    CK_TRY(cudaMemcpyAsync(d_sys_.p, hsys_.data(), sizeof(SysDesc) * S, cudaMemcpyHostToDevice, stream_));
+    CK_TRY(cudaMemcpyAsync(d_in_pos_.p, h_in_pos_.p, sizeof(double) * 3 * in_off, cudaMemcpyHostToDevice, stream_));
+    CK_TRY(cudaMemcpyAsync(d_in_type_.p, h_in_type_.p, sizeof(int) * in_off, cudaMemcpyHostToDevice, stream_));
+    staged_ = true;
+    return kOk;
+}
+
+Status Engine::ensure_lists(std::string& err) {
+    CK_TRY(d_l2_ghost_.reserve(n2_cap_));
+    CK_TRY(d_l2_owner_.reserve(n2_cap_));
+    CK_TRY(d_l2_dist_.reserve(n2_cap_));
+    CK_TRY(d_e_cnt3_.reserve(n2_cap_));
+    CK_TRY(d_e_cnt4_.reserve(n2_cap_));
+    CK_TRY(d_e_off3_.reserve(n2_cap_ + 1));
+    CK_TRY(d_e_off4_.reserve(n2_cap_ + 1));
+    CK_TRY(d_c3_.reserve(3 * n3_cap_));
+    CK_TRY(d_c4_.reserve(4 * n4_cap_));
+    long long scan_n = std::max(std::max(V_.n_bins_total, V_.n_atoms_total), n2_cap_);
+    CK_TRY(d_scan_tmp_.reserve(scan_tmp_bytes(scan_n)));
+    BatchView& B = V_;
+    B.sys = d_sys_.p;
+    B.psets = dsets_.p;
+    B.in_pos = d_in_pos_.p;
+    B.in_type = d_in_type_.p;
+    B.atom_sys = d_atom_sys_.p; B.atom_type = d_atom_type_.p; B.atom_orig = d_atom_orig_.p;
+    B.ghost_parent = d_ghost_parent_.p;
+    B.ghost_fs = d_ghost_fs_.p; B.ghost_xn = d_ghost_xn_.p; B.ghost_fn = d_ghost_fn_.p;
+    B.minmax = d_minmax_.p;
+    B.ghost_bin = d_ghost_bin_.p;
+    B.bin_count = d_bin_count_.p; B.bin_start = d_bin_start_.p; B.bin_fill = d_bin_fill_.p;
+    B.bin_items = d_bin_items_.p;
+    B.l2_count = d_l2_count_.p; B.l2_off = d_l2_off_.p; B.l2_ghost = d_l2_ghost_.p; B.l2_dist = d_l2_dist_.p;
+    B.n2_cap = n2_cap_;
+    B.e_cnt3 = d_e_cnt3_.p; B.e_cnt4 = d_e_cnt4_.p; B.e_off3 = d_e_off3_.p; B.e_off4 = d_e_off4_.p;
+    B.c3 = d_c3_.p; B.c4 = d_c4_.p;
+    B.n3_cap = n3_cap_; B.n4_cap = n4_cap_;
+    B.force = d_force_.p; B.ev = d_ev_.p; B.flags = d_flags_.p;
+    return kOk;
+}
+
+Status Engine::enqueue(std::string& err) {
+    const BatchView& B = V_;
+    cudaStream_t st = stream_;
+    CK_TRY(cudaMemsetAsync(B.bin_count, 0, sizeof(int) * B.n_bins_total, st));
+    CK_TRY(cudaMemsetAsync(B.bin_fill, 0, sizeof(int) * B.n_bins_total, st));
+    launch_reset(B, st);
+    launch_atoms(B, st);
+    launch_ghosts(B, st);
+    launch_bin_setup(B, st);
+    launch_bin_count(B, st);
+    exclusive_scan(B.bin_count, B.bin_start, B.n_bins_total, d_scan_tmp_.p, st);
+    launch_bin_scatter(B, st);
+    launch_bin_sort(B, st);
+    launch_l2(B, d_l2_owner_.p, false, st);
+    exclusive_scan(B.l2_count, B.l2_off, B.n_atoms_total, d_scan_tmp_.p, st);
+    launch_l2(B, d_l2_owner_.p, true, st);
+    launch_enum(B, d_l2_owner_.p, false, st);
+    exclusive_scan(B.e_cnt3, B.e_off3, B.n2_cap, d_scan_tmp_.p, st);
+    exclusive_scan(B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
+    launch_enum(B, d_l2_owner_.p, true, st);
+    launch_check(B, st);
+    ForceLaunch L = tuning;
+    L.precision = precision;
+    launch_force2(B, d_l2_owner_.p, L, st);
+    if (L.stride3 > 0) launch_force3(B, L, st);
+    if (L.stride4 > 0) launch_force4(B, L, st);
+    CK_TRY(cudaMemcpyAsync(h_force_.p, B.force, sizeof(double) * 3 * B.n_in_total, cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaMemcpyAsync(h_ev_.p, B.ev, sizeof(double) * 8 * B.n_sys, cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaMemcpyAsync(h_flags_.p, B.flags, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaMemcpyAsync(h_counts_.p + 0, B.l2_off + B.n_atoms_total, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaMemcpyAsync(h_counts_.p + 1, B.e_off3 + B.n2_cap, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaMemcpyAsync(h_counts_.p + 2, B.e_off4 + B.n2_cap, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK_TRY(cudaGetLastError());
+    return kOk;
+}
+
+Status Engine::launch(std::string& err) {
+    if (!staged_) {
+        err = "launch before stage";
+        return kErrState;
+    }
+    if (!use_graph) return enqueue(err);
+    std::vector<long long> key = {(long long)V_.n_sys, V_.n_in_total, V_.n_atoms_total, V_.n_ghost_total,
+                                  V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
+                                  tuning.stride3, tuning.stride4, tuning.blocks_per_sm};
+    for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
+                          (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
+                          (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,
+                          (const void*)h_force_.p, (const void*)h_ev_.p, (const void*)V_.bin_count,
+                          (const void*)V_.e_off3, (const void*)V_.psets})
+        key.push_back((long long)(uintptr_t)p);
+    if (key != graph_key_) {
+        drop_graph();
+        CK_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        Status st = enqueue(err);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (st != kOk) { if (g) cudaGraphDestroy(g); return st; }
+        if (e != cudaSuccess) {
+            err = std::string("CUDA graph capture failed: ") + cudaGetErrorString(e);
+            return kErrCuda;
+        }
+        graph_ = g;
+        CK_TRY(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+        graph_key_ = key;
+    }
+    CK_TRY(cudaGraphLaunch(graph_exec_, stream_));
+    return kOk;
+}
+
+Status Engine::collect(double* force_out, std::vector<SystemResult>& res, std::string& err) {
+    CK_TRY(cudaStreamSynchronize(stream_));
+    const int* f = h_flags_.p;
+    const long long* c = h_counts_.p;
+    last.n2 = c[0]; last.n3 = c[1]; last.n4 = c[2];
+    last.n_atoms = V_.n_atoms_total;
+    last.n_ghost = V_.n_ghost_total;
+    if (f[0] & 1) {
+        err = "bin grid larger than its reserved capacity";
+        return kErrGeometry;
+    }
+    if ((f[0] & (2 | 4 | 8)) || c[0] > n2_cap_ || c[1] > n3_cap_ || c[2] > n4_cap_) {
+        if (c[0] > n2_cap_) n2_cap_ = c[0] + c[0] / 8 + 1024;
+        else {
+            if (c[1] > n3_cap_) n3_cap_ = c[1] + c[1] / 8 + 1024;
+            if (c[2] > n4_cap_) n4_cap_ = c[2] + c[2] / 8 + 1024;
+        }
+        err = "list capacity exceeded";
+        return kErrCapacity;
+    }
+    if (f[1]) {
+        err = f[1] == 1 ? "negative bin computed (check box lengths and atom coordinates)"
+                        : f[1] == 3 ? "bad bin computed for a real atom (check box lengths and atom coordinates)"
+                                    : "bin index out of range";
+        return kErrGeometry;
+    }
+    last.badness = f[2];
+    last.penalty_hits = f[3];
+    last.below_rin = f[4];
+    res.assign(V_.n_sys, SystemResult());
+    for (int s = 0; s < V_.n_sys; s++) {
+        const double* ev = h_ev_.p + 8 * s;
+        SystemResult& r = res[s];
+        r.n_rep = hsys_[s].n_rep;
+        r.energy = ev[0] / std::pow(hsys_[s].n_rep + 1.0, 3.0);
+        for (int k = 0; k < 6; k++) r.virial[k] = ev[1 + k];
+        r.vol = vols_[s];
+    }
+    if (force_out) std::memcpy(force_out, h_force_.p, sizeof(double) * 3 * V_.n_in_total);
+    return kOk;
+}
+
+Status Engine::run(const std::vector<SystemSpec>& sys, double* force_out, std::vector<SystemResult>& res,
+                   std::string& err) {
+    Status st = stage(sys, err);
+    if (st != kOk) return st;
+    for (int attempt = 0; attempt < 6; attempt++) {
+        st = launch(err);
+        if (st != kOk) return st;
+        st = collect(force_out, res, err);
+        if (st != kErrCapacity) return st;
+        st = ensure_lists(err);
+        if (st != kOk) return st;
+    }
+    err = "list capacity did not converge";
+    return kErrCapacity;
+}
+
+Status Engine::export_lists(std::vector<int>& l2, std::vector<int>& l3, std::vector<int>& l4, std::string& err) {
+    if (!staged_) {
+        err = "no evaluation to export";
+        return kErrState;
+    }
+    CK_TRY(cudaStreamSynchronize(stream_));
+    const long long n2 = last.n2, n3 = last.n3, n4 = last.n4;
+    std::vector<int> g2(n2), own(n2), g3(3 * n3), g4(4 * n4), asys(V_.n_atoms_total);
+    if (n2) {
+        CK_TRY(cudaMemcpy(g2.data(), V_.l2_ghost, sizeof(int) * n2, cudaMemcpyDeviceToHost));
+        CK_TRY(cudaMemcpy(own.data(), d_l2_owner_.p, sizeof(int) * n2, cudaMemcpyDeviceToHost));
+    }
+    if (n3) CK_TRY(cudaMemcpy(g3.data(), V_.c3, sizeof(int) * 3 * n3, cudaMemcpyDeviceToHost));
+    if (n4) CK_TRY(cudaMemcpy(g4.data(), V_.c4, sizeof(int) * 4 * n4, cudaMemcpyDeviceToHost));
+    if (V_.n_atoms_total)
+        CK_TRY(cudaMemcpy(asys.data(), V_.atom_sys, sizeof(int) * V_.n_atoms_total, cudaMemcpyDeviceToHost));
+    auto sys_of_ghost = [&](long long g) {
+        int lo = 0, hi = V_.n_sys - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) / 2;
+            if (hsys_[mid].ghost_off <= g) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    };
+    l2.resize(2 * n2);
+    for (long long e = 0; e < n2; e++) {
+        const SysDesc& d = hsys_[asys[own[e]]];
+        l2[2 * e] = (int)(own[e] - d.atom_off);
+        l2[2 * e + 1] = (int)(g2[e] - d.ghost_off);
+    }
+    l3.resize(3 * n3);
+    for (long long q = 0; q < 3 * n3; q++) l3[q] = (int)(g3[q] - hsys_[sys_of_ghost(g3[q])].ghost_off);
+    l4.resize(4 * n4);
+    for (long long q = 0; q < 4 * n4; q++) l4[q] = (int)(g4[q] - hsys_[sys_of_ghost(g4[q])].ghost_off);
+    return kOk;
+}
+
+}  // namespace ck

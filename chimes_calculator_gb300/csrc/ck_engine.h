@@ -1,0 +1,168 @@
+// Host engine of the GB300 ChIMES force path: owns one CUDA stream, the
+// device-resident parameter sets and a grow-only batch workspace, and runs the
+// list build and force kernels for a batch of periodic systems.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ck_common.h"
+#include "ck_kernels.h"
+#include "ck_params.h"
+
+namespace ck {
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { if (p) cudaFree(p); }
+    // grows (never shrinks); contents are not preserved
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        size_t want = n + n / 4 + 64;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        cap = e == cudaSuccess ? want : 0;
+        return e;
+    }
+};
+
+template <class T>
+struct PinnedBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { if (p) cudaFreeHost(p); }
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        size_t want = n + n / 4 + 64;
+        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        cap = e == cudaSuccess ? want : 0;
+        return e;
+    }
+};
+
+// One periodic configuration as the caller passes it.
+struct SystemSpec {
+    int n = 0;
+    const double* pos = nullptr;   // [n][3] Cartesian (x,y,z interleaved)
+    const int* types = nullptr;    // [n] atom type index of the parameter set
+    double cell[9] = {0};          // rows: lattice vectors a, b, c
+    bool small = false;            // allow replication of small cells (reference `small`)
+    int pset = 0;                  // parameter-set slot
+};
+
+struct SystemResult {
+    double energy = 0.0;           // 1B+2B+3B+4B energy divided by (n_rep+1)^3
+    double virial[6] = {0, 0, 0, 0, 0, 0};   // packed xx xy xz yy yz zz, not divided by the volume
+    double vol = 0.0;
+    int n_rep = 0;
+};
+
+struct RunStats {
+    long long n2 = 0, n3 = 0, n4 = 0;
+    long long n_atoms = 0, n_ghost = 0;
+    int badness = 0;
+    int penalty_hits = 0, below_rin = 0;
+};
+
+class Engine {
+public:
+    Engine();
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    Status init_device(std::string& err);
+    // Parses a parameter file into a new device-resident slot; returns the slot (>= 0).
+    int load_params(const std::string& path, std::string& err);
+    const HostParams& params(int slot) const { return *sets_[slot].host; }
+    int n_param_sets() const { return (int)sets_.size(); }
+
+    // Full evaluation of a batch: stage + launch + collect, retrying on capacity growth.
+    // force_out: [sum n][3], zeroed and filled (not accumulated).
+    Status run(const std::vector<SystemSpec>& sys, double* force_out, std::vector<SystemResult>& res,
+               std::string& err);
+
+    // Split form (the bench times launch() on device-resident inputs):
+    Status stage(const std::vector<SystemSpec>& sys, std::string& err);   // host geometry + async H2D
+    Status launch(std::string& err);                                       // list build + forces, async
+    Status collect(double* force_out, std::vector<SystemResult>& res, std::string& err);  // D2H + sync
+
+    cudaStream_t stream() const { return stream_; }
+    ForceLaunch tuning;
+    int precision = kFP64;
+    bool use_graph = false;
+    RunStats last;
+
+    // Cluster lists of the last run in system-local ghost numbering (the
+    // reference's sys_parent/ghost indices), for set comparisons.
+    Status export_lists(std::vector<int>& l2, std::vector<int>& l3, std::vector<int>& l4, std::string& err);
+
+private:
+    struct PSet {
+        std::unique_ptr<HostParams> host;
+        void* dev = nullptr;
+        DevParamSet view{};
+    };
+    std::vector<PSet> sets_;
+    DevBuf<DevParamSet> dsets_;
+    cudaStream_t stream_ = nullptr;
+    bool ready_ = false;
+
+    // batch layout of the staged batch
+    std::vector<SysDesc> hsys_;
+    std::vector<double> vols_;
+    BatchView V_{};
+    long long n2_cap_ = 0, n3_cap_ = 0, n4_cap_ = 0;
+    bool staged_ = false;
+
+    DevBuf<SysDesc> d_sys_;
+    DevBuf<double> d_in_pos_;
+    DevBuf<int> d_in_type_;
+    DevBuf<int> d_atom_sys_, d_atom_type_, d_atom_orig_;
+    DevBuf<int> d_ghost_parent_, d_ghost_bin_;
+    DevBuf<double> d_ghost_fs_, d_ghost_xn_, d_ghost_fn_;
+    DevBuf<unsigned long long> d_minmax_;
+    DevBuf<int> d_bin_count_, d_bin_fill_, d_bin_items_;
+    DevBuf<long long> d_bin_start_;
+    DevBuf<int> d_l2_count_, d_l2_ghost_, d_l2_owner_;
+    DevBuf<long long> d_l2_off_;
+    DevBuf<double> d_l2_dist_;
+    DevBuf<int> d_e_cnt3_, d_e_cnt4_;
+    DevBuf<long long> d_e_off3_, d_e_off4_;
+    DevBuf<int> d_c3_, d_c4_;
+    DevBuf<double> d_force_, d_ev_;
+    DevBuf<int> d_flags_;
+    DevBuf<unsigned char> d_scan_tmp_;
+
+    PinnedBuf<double> h_in_pos_;
+    PinnedBuf<int> h_in_type_;
+    PinnedBuf<double> h_force_;
+    PinnedBuf<double> h_ev_;
+    PinnedBuf<int> h_flags_;
+    PinnedBuf<long long> h_counts_;
+
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    std::vector<long long> graph_key_;
+
+    Status ensure_lists(std::string& err);
+    Status enqueue(std::string& err);
+    void drop_graph();
+};
+
+const char* status_name(int s);
+
+}  // namespace ck

@@ -1,0 +1,478 @@
+// Cluster force kernels: Morse/Chebyshev stage, coefficient contraction and
+// energy / force / virial reduction for 2-, 3- and 4-body clusters.
+//
+// Math (restated from chimesFF, chimesFF/src/chimesFF.cpp:1644-1775 (2B),
+// 1931-2176 (3B), 2496-2872 (4B); set_cheby_polys chimesFF.h:542-628; get_fcut
+// chimesFF.h:347-386; get_penalty chimesFF.h:388-419):
+//   s = exp(-r/lambda), x = (s - xavg)/xdiff, dx/dr = -s/(lambda*xdiff)
+//   T_0 = 1, T_1 = x, T_n = 2x T_{n-1} - T_{n-2};  dT_n/dr = n U_{n-1}(x) dx/dr
+//   2B:  E += fc * sum_c a_c T_{p_c+1};   many-body: E += fc_all * S,
+//        S   = sum_c a_c prod_q T_q[p_cq]
+//        G_p = sum_c a_c dT_p[p_cp] prod_{q!=p} T_q[p_cq]
+//   force scalar of pair p = (prod_{q!=p} fc_q / r_p) (fc_p G_p + fc'_p S),
+//   which equals the reference's per-coefficient sum of force_scalar[p];
+//   F_i += f_p dr_p, F_j -= f_p dr_p, virial -= f_p dr_p (x) dr_p.
+// Only the summation order differs from the reference (sums are formed per
+// cluster first), which moves results by rounding only.
+//
+// Work mapping: a warp takes 32/TPC clusters per step, TPC lanes per cluster.
+// Lanes of a cluster compute its pair geometry (FP64) and Chebyshev tables
+// (compute type CT) into shared memory, then split the coefficient list
+// (lane l takes coefficients l, l+TPC, ...) and combine S and G_p by xor
+// shuffles.  The group leader turns them into forces (FP64 atomics on the
+// caller's atoms) and accumulates energy and virial per system in FP64.
+// CT = double is the plain FP64 path; CT = float is the mixed path (FP32
+// Chebyshev recursion, cutoff and contraction; FP64 geometry and accumulation).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ck_common.h"
+#include "ck_kernels.h"
+
+namespace ck {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr double kPi = 3.14159265359;   // the reference's `pi` macro (chimesFF.h:22)
+
+template <typename CT> __device__ __forceinline__ void csincos(CT x, CT* s, CT* c);
+template <> __device__ __forceinline__ void csincos<double>(double x, double* s, double* c) { sincos(x, s, c); }
+template <> __device__ __forceinline__ void csincos<float>(float x, float* s, float* c) { sincosf(x, s, c); }
+
+template <typename CT> __device__ __forceinline__ const CT* coef2(const DevParamSet& P);
+template <> __device__ __forceinline__ const double* coef2<double>(const DevParamSet& P) { return P.c2d; }
+template <> __device__ __forceinline__ const float* coef2<float>(const DevParamSet& P) { return P.c2f; }
+template <typename CT, int NB> __device__ __forceinline__ const CT* coefn(const DevParamSet& P);
+template <> __device__ __forceinline__ const double* coefn<double, 3>(const DevParamSet& P) { return P.c3d; }
+template <> __device__ __forceinline__ const float* coefn<float, 3>(const DevParamSet& P) { return P.c3f; }
+template <> __device__ __forceinline__ const double* coefn<double, 4>(const DevParamSet& P) { return P.c4d; }
+template <> __device__ __forceinline__ const float* coefn<float, 4>(const DevParamSet& P) { return P.c4f; }
+
+// get_fcut (chimesFF.h:347-386), evaluated in CT
+template <typename CT>
+__device__ __forceinline__ void fcut_eval(const DevParamSet& P, double r, double rc, CT& fc, CT& fcd) {
+    if (!P.tersoff) {
+        CT f0 = CT(1.0) - CT(r) / CT(rc);
+        fc = f0 * f0 * f0;
+        fcd = f0 * f0 * (CT(-3.0) / CT(rc));
+    } else {
+        const double th = rc - P.fcut_var * rc;
+        if (r < th) { fc = CT(1); fcd = CT(0); }
+        else if (r > rc) { fc = CT(0); fcd = CT(0); }
+        else {
+            const CT inv = CT(1.0) / CT(rc - th);
+            const CT f0 = CT(r - th) * inv * CT(kPi) + CT(kPi / 2.0);
+            CT sn, cs;
+            csincos<CT>(f0, &sn, &cs);
+            fc = CT(0.5) + CT(0.5) * sn;
+            fcd = CT(0.5) * cs * (CT(kPi) * inv);
+        }
+    }
+}
+
+// Morse coordinate: x and dx/dr at r (clamped to rin below the inner cutoff).
+// The exponential and the map are taken in FP64 in both precision modes: the
+// polynomial recursion magnifies an error in x by up to n^2.
+__device__ __forceinline__ void morse_x(double r, double rin, double lam, double xavg, double xdiff,
+                                        double& x, double& dxdr, bool& oor) {
+    oor = r < rin;
+    const double rr = oor ? rin : r;
+    const double e = exp(-rr / lam);
+    x = (e - xavg) / xdiff;
+    dxdr = (-e / lam) / xdiff;
+}
+
+// Chebyshev table T[0..o], dT/dr[0..o] (set_cheby_polys and
+// set_polys_out_of_range, chimesFF.cpp:1572-1613) into a strided array.
+template <typename CT>
+__device__ __forceinline__ void cheby_table(CT* T, CT* D, double r, double rin, double lam, double xavg,
+                                            double xdiff, int order, double inner_smooth, int* flags) {
+    double xd, dxdr;
+    bool oor;
+    morse_x(r, rin, lam, xavg, xdiff, xd, dxdr, oor);
+    const CT x = CT(xd), tx = CT(2) * x, g = CT(dxdr);
+    CT t0 = CT(1), t1 = x, u0 = CT(1), u1 = tx;
+    T[0] = t0; D[0] = CT(0);
+    if (order >= 1) { T[1] = t1; D[1] = g * u0; }
+    for (int n = 2; n <= order; n++) {
+        const CT t2 = tx * t1 - t0;
+        const CT u2 = tx * u1 - u0;
+        T[n] = t2;
+        D[n] = CT(n) * g * u1;
+        t0 = t1; t1 = t2; u0 = u1; u1 = u2;
+    }
+    if (oor) {
+        atomicAdd(&flags[4], 1);
+        const double damp = exp((r - rin) / inner_smooth);
+        const CT k = CT(inner_smooth * (damp - 1.0)), dm = CT(damp);
+        for (int n = 0; n <= order; n++) {
+            T[n] = T[n] + k * D[n];
+            D[n] = D[n] * dm;
+        }
+    }
+}
+
+__device__ __forceinline__ void pair_geom(const BatchView& B, const double* h, int ga, int gb, double* dr, double& r) {
+    const double* fa = &B.ghost_fs[3 * (long long)ga];
+    const double* fb = &B.ghost_fs[3 * (long long)gb];
+    const double dx = fb[0] - fa[0], dy = fb[1] - fa[1], dz = fb[2] - fa[2];
+    dr[0] = h[0] * dx + h[1] * dy + h[2] * dz;
+    dr[1] = h[3] * dx + h[4] * dy + h[5] * dz;
+    dr[2] = h[6] * dx + h[7] * dy + h[8] * dz;
+    r = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+}
+
+__device__ __forceinline__ void add_force(const BatchView& B, int ghost, double fx, double fy, double fz) {
+    const int o = B.atom_orig[B.ghost_parent[ghost]];
+    atomicAdd(&B.force[3 * (long long)o + 0], fx);
+    atomicAdd(&B.force[3 * (long long)o + 1], fy);
+    atomicAdd(&B.force[3 * (long long)o + 2], fz);
+}
+
+// Per-lane energy/virial accumulator for one system at a time.
+struct EVAcc {
+    int s = -1;
+    double v[7] = {0, 0, 0, 0, 0, 0, 0};
+    __device__ void flush(const BatchView& B) {
+        if (s >= 0)
+            for (int k = 0; k < 7; k++) atomicAdd(&B.ev[8 * s + k], v[k]);
+        s = -1;
+        for (int k = 0; k < 7; k++) v[k] = 0;
+    }
+    __device__ void add(const BatchView& B, int sys, double e, const double* vir) {
+        if (sys != s) { flush(B); s = sys; }
+        v[0] += e;
+        for (int k = 0; k < 6; k++) v[1 + k] += vir[k];
+    }
+    // end of kernel: one set of atomics per warp when the warp holds one system
+    __device__ void flush_warp(const BatchView& B) {
+        const int lane = threadIdx.x & 31;
+        int key = s;
+        int s0 = -1;
+        for (int l = 0; l < 32; l++) {
+            int t = __shfl_sync(kFull, key, l);
+            if (t >= 0) { s0 = t; break; }
+        }
+        const bool uniform = __all_sync(kFull, s < 0 || s == s0);
+        if (uniform) {
+            for (int k = 0; k < 7; k++) {
+                double x = v[k];
+                for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(kFull, x, off);
+                v[k] = x;
+            }
+            if (lane == 0 && s0 >= 0)
+                for (int k = 0; k < 7; k++) atomicAdd(&B.ev[8 * s0 + k], v[k]);
+        } else {
+            flush(B);
+        }
+    }
+};
+
+__device__ __forceinline__ void virial_add(double* vir, double f, const double* d) {
+    vir[0] -= f * d[0] * d[0];
+    vir[1] -= f * d[0] * d[1];
+    vir[2] -= f * d[0] * d[2];
+    vir[3] -= f * d[1] * d[1];
+    vir[4] -= f * d[1] * d[2];
+    vir[5] -= f * d[2] * d[2];
+}
+
+// ---------------------------------------------------------------------------
+// 1-body + 2-body: one thread per neighbour-list entry (and per atom for 1B).
+// The 2B coefficients are summed along the recursion with the dense
+// per-pair-type table a_n = sum of coefficients whose power+1 is n.
+// ---------------------------------------------------------------------------
+template <typename CT>
+__global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner) {
+    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
+    EVAcc acc;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long ntot = n2 > B.n_atoms_total ? n2 : B.n_atoms_total;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ntot; e += stride) {
+        double vir[6] = {0, 0, 0, 0, 0, 0};
+        if (e < B.n_atoms_total) {   // compute_1B (chimesFF.cpp:1636-1641)
+            const int s = B.atom_sys[e];
+            const DevParamSet& P = B.psets[B.sys[s].pset];
+            acc.add(B, s, P.eoff[B.atom_type[e]], vir);
+        }
+        if (e >= n2) continue;
+        const int r = l2_owner[e];
+        const int s = B.atom_sys[r];
+        const SysDesc& d = B.sys[s];
+        const DevParamSet& P = B.psets[d.pset];
+        const int gi = (int)(d.ghost_off + (r - d.atom_off));
+        const int gj = B.l2_ghost[e];
+        const int t0 = B.atom_type[r], t1 = B.atom_type[B.ghost_parent[gj]];
+        const PairRec pr = P.pairs[P.pair_map[t0 * P.ntypes + t1]];
+        double dr[3], dist;
+        pair_geom(B, d.h, gi, gj, dr, dist);
+        if (dist >= pr.rout) continue;
+        double xd, dxdr;
+        bool oor;
+        morse_x(dist, pr.rin, pr.lam, pr.xavg, pr.xdiff, xd, dxdr, oor);
+        const CT* a = coef2<CT>(P) + pr.coef_off;   // dense a_n, n = 0..o2
+        const CT x = CT(xd), tx = CT(2) * x;
+        CT t0c = CT(1), t1c = x, u0 = CT(1), u1 = tx;
+        CT S = a[0] * t0c + a[1] * t1c;
+        CT GD = a[1] * u0;                     // sum a_n n U_{n-1}
+        for (int n = 2; n <= P.o2; n++) {
+            const CT t2 = tx * t1c - t0c;
+            const CT u2 = tx * u1 - u0;
+            S += a[n] * t2;
+            GD += a[n] * CT(n) * u1;
+            t0c = t1c; t1c = t2; u0 = u1; u1 = u2;
+        }
+        double Sd = double(S), Gd = double(GD) * dxdr;
+        if (oor) {
+            atomicAdd(&B.flags[4], 1);
+            const double damp = exp((dist - pr.rin) / P.inner_smooth);
+            Sd += P.inner_smooth * (damp - 1.0) * Gd;
+            Gd *= damp;
+        }
+        CT fcc, fcdc;
+        fcut_eval<CT>(P, dist, pr.rout, fcc, fcdc);
+        const double fc = double(fcc), fcd = double(fcdc);
+        double E = fc * Sd;
+        const double dx_inv = dist > 0.0 ? 1.0 / dist : 1e20;
+        double fs = (fc * Gd + fcd * Sd) * dx_inv;
+        // get_penalty (chimesFF.h:388-419)
+        if (dist - P.pen_dist < pr.rin) {
+            const double rp = pr.rin + P.pen_dist - dist;
+            atomicMax(&B.flags[2], dist < pr.rin ? 2 : 1);
+            if (rp > 0.0) {
+                atomicAdd(&B.flags[3], 1);
+                E += rp * rp * rp * P.pen_scale;
+                fs += (-3.0 * rp * rp * P.pen_scale) / dist;
+            }
+        }
+        add_force(B, gi, fs * dr[0], fs * dr[1], fs * dr[2]);
+        add_force(B, gj, -fs * dr[0], -fs * dr[1], -fs * dr[2]);
+        virial_add(vir, fs, dr);
+        acc.add(B, s, E, vir);
+    }
+    acc.flush_warp(B);
+}
+
+// ---------------------------------------------------------------------------
+// 3-body and 4-body clusters
+// ---------------------------------------------------------------------------
+template <int NB>
+struct Topo;
+template <>
+struct Topo<3> {
+    static constexpr int NP = 3;
+    __device__ static int a(int p) { return p == 2 ? 1 : 0; }
+    __device__ static int b(int p) { return p == 0 ? 1 : 2; }
+};
+template <>
+struct Topo<4> {
+    static constexpr int NP = 6;
+    __device__ static int a(int p) { return p < 3 ? 0 : (p < 5 ? 1 : 2); }
+    __device__ static int b(int p) { return p < 3 ? p + 1 : (p == 3 ? 2 : 3); }
+};
+
+template <int NB, typename CT, int TPC>
+__global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters, const long long* n_ptr,
+                                                long long cap, int stride) {
+    const long long n = min(*n_ptr, cap);
+    constexpr int NP = Topo<NB>::NP;
+    constexpr int G = 32 / TPC;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int warp_in_block = threadIdx.x >> 5;
+    const int grp = lane / TPC, gl = lane % TPC;
+    // per-group shared layout: T[NP*stride], D[NP*stride] (CT); geo[NP][4], fc[NP], fcd[NP] (double)
+    const size_t tbytes = ((size_t)2 * NP * stride * sizeof(CT) + 15) & ~size_t(15);
+    const size_t gbytes = tbytes + sizeof(double) * NP * 6;
+    unsigned char* gbase = smem + ((size_t)warp_in_block * G + grp) * gbytes;
+    CT* T = reinterpret_cast<CT*>(gbase);
+    CT* D = T + NP * stride;
+    double* geo = reinterpret_cast<double*>(gbase + tbytes);
+    double* fcs = geo + 4 * NP;
+    double* fcds = fcs + NP;
+
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long wid = (long long)blockIdx.x * (blockDim.x >> 5) + warp_in_block;
+    const long long steps = (n + G - 1) / G;
+    const long long chunk = (steps + nwarps - 1) / nwarps;
+    const long long st0 = wid * chunk, st1 = min(steps, st0 + chunk);
+    EVAcc acc;
+
+    for (long long step = st0; step < st1; step++) {
+        const long long c = step * G + grp;
+        const bool have = c < n;
+        int id[NB];
+        int s = 0;
+        const SysDesc* d = nullptr;
+        const DevParamSet* P = nullptr;
+        const TupleRec* R = nullptr;
+        int nc = 0;
+        if (have) {
+            for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
+            s = B.atom_sys[B.ghost_parent[id[0]]];
+            d = &B.sys[s];
+            P = &B.psets[d->pset];
+            int u = 0;
+            for (int k = 0; k < NB; k++) u = u * P->ntypes + B.atom_type[B.ghost_parent[id[k]]];
+            R = (NB == 3 ? P->t3 : P->t4) + u;
+            if (R->valid) nc = R->ncoef;
+            // geometry of this lane's pairs
+            for (int p = gl; p < NP; p += TPC) {
+                double dr[3], r;
+                pair_geom(B, d->h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+                geo[4 * p + 0] = dr[0]; geo[4 * p + 1] = dr[1]; geo[4 * p + 2] = dr[2]; geo[4 * p + 3] = r;
+            }
+        }
+        __syncwarp();
+        if (nc > 0) {   // compute_3B/4B early-outs on the per-pair outer cutoffs
+            for (int p = 0; p < NP; p++)
+                if (geo[4 * p + 3] >= R->rout[p]) { nc = 0; break; }
+        }
+        const int order = NB == 3 ? (P ? P->o3 : 0) : (P ? P->o4 : 0);
+        if (nc > 0) {
+            for (int p = gl; p < NP; p += TPC) {
+                const double r = geo[4 * p + 3];
+                cheby_table<CT>(T + p * stride, D + p * stride, r, R->rin[p], R->lam[p], R->xavg[p], R->xdiff[p],
+                                order, P->inner_smooth, B.flags);
+                CT fc, fcd;
+                fcut_eval<CT>(*P, r, R->rout[p], fc, fcd);
+                fcs[p] = double(fc);
+                fcds[p] = double(fcd);
+            }
+        }
+        __syncwarp();
+        // contraction
+        CT S = CT(0), Gp[NP];
+        for (int p = 0; p < NP; p++) Gp[p] = CT(0);
+        if (nc > 0) {
+            const CT* cf = coefn<CT, NB>(*P) + R->coef_off;
+            const uint32_t* pw = (NB == 3 ? P->p3 : P->p4) + R->coef_off;
+            for (int k = gl; k < nc; k += TPC) {
+                const CT a = cf[k];
+                const uint32_t pk = pw[k];
+                CT t[NP], dd[NP];
+#pragma unroll
+                for (int p = 0; p < NP; p++) {
+                    const int q = (pk >> (kPowBits * p)) & 31u;
+                    t[p] = T[p * stride + q];
+                    dd[p] = D[p * stride + q];
+                }
+                // prefix/suffix products of the T's
+                CT pre[NP + 1], suf[NP + 1];
+                pre[0] = a;
+#pragma unroll
+                for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * t[p];
+                suf[NP] = CT(1);
+#pragma unroll
+                for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * t[p];
+                S += pre[NP];
+#pragma unroll
+                for (int p = 0; p < NP; p++) Gp[p] += pre[p] * dd[p] * suf[p + 1];
+            }
+        }
+        // combine the TPC partial sums of each cluster
+#pragma unroll
+        for (int off = TPC / 2; off > 0; off >>= 1) {
+            S += __shfl_xor_sync(kFull, S, off);
+#pragma unroll
+            for (int p = 0; p < NP; p++) Gp[p] += __shfl_xor_sync(kFull, Gp[p], off);
+        }
+        if (nc > 0 && gl == 0) {
+            double fc[NP], fcd[NP], pre[NP + 1], suf[NP + 1];
+            for (int p = 0; p < NP; p++) { fc[p] = fcs[p]; fcd[p] = fcds[p]; }
+            pre[0] = 1.0;
+            for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * fc[p];
+            suf[NP] = 1.0;
+            for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * fc[p];
+            const double Sd = double(S);
+            double f[NB][3];
+            for (int k = 0; k < NB; k++) f[k][0] = f[k][1] = f[k][2] = 0.0;
+            double vir[6] = {0, 0, 0, 0, 0, 0};
+            for (int p = 0; p < NP; p++) {
+                const double* dr = &geo[4 * p];
+                const double fsp = pre[p] * suf[p + 1] / dr[3] * (fc[p] * double(Gp[p]) + fcd[p] * Sd);
+                const int a = Topo<NB>::a(p), b = Topo<NB>::b(p);
+                for (int k = 0; k < 3; k++) {
+                    f[a][k] += fsp * dr[k];
+                    f[b][k] -= fsp * dr[k];
+                }
+                virial_add(vir, fsp, dr);
+            }
+            for (int k = 0; k < NB; k++) add_force(B, id[k], f[k][0], f[k][1], f[k][2]);
+            acc.add(B, s, pre[NP] * Sd, vir);
+        }
+        __syncwarp();
+    }
+    acc.flush_warp(B);
+}
+
+template <int NB, typename CT>
+void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, long long n, int tpc, int stride,
+              const ForceLaunch& L, cudaStream_t st) {
+    if (n <= 0) return;
+    constexpr int NP = NB * (NB - 1) / 2;
+    const int block = 128;
+    const size_t tbytes = ((size_t)2 * NP * stride * sizeof(CT) + 15) & ~size_t(15);
+    const size_t gbytes = tbytes + sizeof(double) * NP * 6;
+    const int G = 32 / tpc;
+    const size_t smem = gbytes * G * (block / 32);
+    const long long steps = (n + G - 1) / G;
+    long long want = (long long)sm_count() * L.blocks_per_sm;
+    long long need = (steps + (block / 32) - 1) / (block / 32);
+    const unsigned grid = (unsigned)(want < need ? want : need);
+#define CK_LAUNCH(T_)                                                                          \
+    do {                                                                                       \
+        auto kern = k_forcen<NB, CT, T_>;                                                      \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<grid, block, smem, st>>>(B, clusters, n_ptr, n, stride);                               \
+    } while (0)
+    switch (tpc) {
+        case 1: CK_LAUNCH(1); break;
+        case 2: CK_LAUNCH(2); break;
+        case 4: CK_LAUNCH(4); break;
+        case 8: CK_LAUNCH(8); break;
+        case 16: CK_LAUNCH(16); break;
+        default: CK_LAUNCH(32); break;
+    }
+#undef CK_LAUNCH
+}
+
+}  // namespace
+
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L, cudaStream_t st) {
+    const long long n2 = B.n2_cap;
+    const long long ntot = n2 > B.n_atoms_total ? n2 : B.n_atoms_total;
+    if (ntot <= 0) return;
+    long long want = (long long)sm_count() * 8;
+    long long need = (ntot + 255) / 256;
+    const unsigned grid = (unsigned)(want < need ? want : need);
+    if (L.precision == kMixed) k_force2<float><<<grid, 256, 0, st>>>(B, l2_owner);
+    else k_force2<double><<<grid, 256, 0, st>>>(B, l2_owner);
+}
+
+void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    const long long* np = B.e_off3 + B.n2_cap;
+    if (L.precision == kMixed) launch_n<3, float>(B, B.c3, np, B.n3_cap, L.tpc3, L.stride3, L, st);
+    else launch_n<3, double>(B, B.c3, np, B.n3_cap, L.tpc3, L.stride3, L, st);
+}
+
+void launch_force4(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    const long long* np = B.e_off4 + B.n2_cap;
+    if (L.precision == kMixed) launch_n<4, float>(B, B.c4, np, B.n4_cap, L.tpc4, L.stride4, L, st);
+    else launch_n<4, double>(B, B.c4, np, B.n4_cap, L.tpc4, L.stride4, L, st);
+}
+
+}  // namespace ck

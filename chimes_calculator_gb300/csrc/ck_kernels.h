@@ -1,0 +1,50 @@
+// Kernel launchers of the GB300 ChIMES force path.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ck_common.h"
+
+namespace ck {
+
+// ---- cluster-list build (ck_lists.cu) -------------------------------------
+void launch_atoms(const BatchView& B, cudaStream_t st);
+void launch_ghosts(const BatchView& B, cudaStream_t st);
+void launch_bin_setup(const BatchView& B, cudaStream_t st);
+void launch_bin_count(const BatchView& B, cudaStream_t st);
+void launch_bin_scatter(const BatchView& B, cudaStream_t st);
+void launch_bin_sort(const BatchView& B, cudaStream_t st);
+void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st);
+// Runs over the list capacity B.n2_cap; the live count is read on the device.
+void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_t st);
+// Sets capacity flags when a live count exceeds its buffer.
+void launch_check(const BatchView& B, cudaStream_t st);
+// Clears bounding boxes, accumulators and flags.
+void launch_reset(const BatchView& B, cudaStream_t st);
+
+// Exclusive scan of n ints into n+1 int64 (out[n] = total).  `tmp` must hold
+// scan_tmp_bytes(n) bytes.
+size_t scan_tmp_bytes(long long n);
+void exclusive_scan(const int* in, long long* out, long long n, void* tmp, cudaStream_t st);
+
+// ---- forces (ck_force.cu) ------------------------------------------------
+enum Precision : int { kFP64 = 0, kMixed = 1 };
+
+struct ForceLaunch {
+    int precision = kFP64;
+    int tpc3 = 4;          // threads per 3-body cluster
+    int tpc4 = 8;          // threads per 4-body cluster
+    int block = 256;
+    int blocks_per_sm = 4;
+    int stride3 = 0;       // polynomial table stride (max 3B order + 1 over the batch's sets)
+    int stride4 = 0;
+};
+
+// Cluster counts are read on the device (l2_off[n_atoms], e_off3/4[n2_cap]) and
+// clamped to the capacities, so launches need no host round trip.
+void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L, cudaStream_t st);
+void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+void launch_force4(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+
+int sm_count();
+
+}  // namespace ck

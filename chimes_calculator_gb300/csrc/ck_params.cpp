@@ -1,0 +1,597 @@
+// Parsing of the ChIMES parameter-file format and packing of the device tables.
+//
+// The parse follows chimesFF::read_parameters (chimesFF/src/chimesFF.cpp:354-1570)
+// pass for pass: the same keywords, token positions, rewinds and defaults, so
+// a file reads into the same tables.  Differences: errors are returned as
+// status codes with a message instead of printing and calling exit(0), the
+// per-coefficient echo to stdout is not reproduced, and inputs that would make
+// the reference read outside its polynomial tables (a power larger than the
+// order) are rejected.
+#include "ck_params.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+namespace ck {
+
+namespace {
+
+// chimesFF::split_line (chimesFF.cpp:148-180): strip '!' and '##' comments,
+// split on whitespace.
+std::vector<std::string> tokens(const std::string& raw) {
+    std::string line = raw;
+    size_t p = line.find('!');
+    if (p != std::string::npos) line.erase(p);
+    p = line.find("##");
+    if (p != std::string::npos) line.erase(p);
+    std::vector<std::string> out;
+    std::istringstream ss(line);
+    std::string t;
+    while (ss >> t) out.push_back(t);
+    return out;
+}
+
+bool has(const std::string& line, const char* key) { return line.find(key) != std::string::npos; }
+
+struct Lines {
+    std::vector<std::string> v;
+    size_t i = 0;
+    bool next(std::string& out) {
+        if (i >= v.size()) return false;
+        out = v[i++];
+        return true;
+    }
+    void rewind() { i = 0; }
+};
+
+struct ParseError {
+    std::string msg;
+};
+
+[[noreturn]] void fail(const std::string& m) { throw ParseError{m}; }
+
+int to_int(const std::vector<std::string>& t, size_t k, const char* what) {
+    if (k >= t.size()) fail(std::string("missing integer field in ") + what);
+    try {
+        return std::stoi(t[k]);
+    } catch (...) {
+        fail(std::string("bad integer '") + t[k] + "' in " + what);
+    }
+}
+
+double to_dbl(const std::vector<std::string>& t, size_t k, const char* what) {
+    if (k >= t.size()) fail(std::string("missing number field in ") + what);
+    try {
+        return std::stod(t[k]);
+    } catch (...) {
+        fail(std::string("bad number '") + t[k] + "' in " + what);
+    }
+}
+
+const std::string& tok(const std::vector<std::string>& t, size_t k, const char* what) {
+    if (k >= t.size()) fail(std::string("missing field in ") + what);
+    return t[k];
+}
+
+// get_proper_pair (chimesFF.cpp:69-84)
+int proper_pair(const HostParams& P, const std::string& a, const std::string& b) {
+    for (int i = 0; i < P.npairs; i++) {
+        if (a == P.pa1[i] && b == P.pa2[i]) return i;
+        if (b == P.pa1[i] && a == P.pa2[i]) return i;
+    }
+    fail("no proper pair name found for atom types " + a + ", " + b);
+}
+
+// build_atom_and_pair_mappers (chimesFF/src/chimesFF.h:438-539): the first
+// permutation (std::next_permutation order) of the cluster's atom slots whose
+// runtime pair names equal the parameter type's pair names gives, for each
+// cluster pair j, the parameter pair index mapped[j].  `mapped` keeps its
+// previous contents when no permutation matches, like the reference's reused
+// vector.
+void atom_pair_mapper(const HostParams& P, int natoms, const int* typ,
+                      const std::vector<std::string>& clu_pairs, std::vector<int>& mapped) {
+    const int npairs = natoms * (natoms - 1) / 2;
+    std::vector<int> perm(natoms);
+    for (int i = 0; i < natoms; i++) perm[i] = i;
+    std::vector<std::pair<int, int>> slots, run(npairs, {0, 0});
+    for (int i = 0; i < natoms; i++)
+        for (int j = i + 1; j < natoms; j++) slots.push_back({i, j});
+    do {
+        bool match = true;
+        for (int p = 0; p < npairs && match; p++) {
+            int a = typ[perm[slots[p].first]], b = typ[perm[slots[p].second]];
+            if (clu_pairs[p] != P.pair_name(P.prpr[a * P.ntypes + b])) match = false;
+        }
+        if (match) {
+            for (int p = 0; p < npairs; p++) run[p] = {perm[slots[p].first], perm[slots[p].second]};
+            break;
+        }
+    } while (std::next_permutation(perm.begin(), perm.end()));
+    for (int i = 0; i < npairs; i++)
+        for (int j = 0; j < npairs; j++)
+            if ((run[i].first == slots[j].first && run[i].second == slots[j].second) ||
+                (run[i].first == slots[j].second && run[i].second == slots[j].first))
+                mapped[j] = i;
+}
+
+void parse_lines(Lines& L, HostParams& P) {
+    std::string line;
+    // pass 1: PAIRTYP: CHEBYSHEV o2 [o3 [o4]]  (chimesFF.cpp:390-437)
+    bool found = false;
+    while (L.next(line)) {
+        if (has(line, "ENDFILE")) fail("could not find line containing \"PAIRTYP: CHEBYSHEV\"");
+        if (has(line, "PAIRTYP: CHEBYSHEV")) {
+            auto t = tokens(line);
+            if (t.size() < 3) fail("\"PAIRTYP: CHEBYSHEV\" line must at least contain the 2-body order");
+            P.o2 = to_int(t, 2, "PAIRTYP");
+            P.o3 = t.size() >= 4 ? to_int(t, 3, "PAIRTYP") : 0;
+            P.o4 = t.size() >= 5 ? to_int(t, 4, "PAIRTYP") : 0;
+            found = true;
+            break;
+        }
+    }
+    if (!found) fail("error reading line: no ENDFILE and no PAIRTYP line");
+    if (P.o2 < 1 || P.o2 > kMaxOrder || P.o3 < 0 || P.o3 > kMaxOrder || P.o4 < 0 || P.o4 > kMaxOrder)
+        fail("polynomial orders must lie in [1,31] (2B) and [0,31] (3B, 4B)");
+
+    // pass 2: types, pairs, cutoff style, penalty, energy offsets (chimesFF.cpp:445-686)
+    L.rewind();
+    int no_pairs = 0;
+    while (true) {
+        if (!L.next(line)) fail("error reading line: missing ENDFILE");
+        if (has(line, "ENDFILE")) break;
+        if (has(line, "ATOM TYPES:")) {
+            auto t = tokens(line);
+            P.ntypes = to_int(t, 2, "ATOM TYPES");
+            if (P.ntypes < 1 || P.ntypes > kMaxTypes) fail("number of atom types must lie in [1,8]");
+            P.eoff.assign(P.ntypes, 0.0);
+        }
+        if (has(line, "# TYPEIDX #")) {
+            P.atm.assign(P.ntypes, "");
+            P.mass.assign(P.ntypes, 0.0);
+            for (int i = 0; i < P.ntypes; i++) {
+                if (!L.next(line)) fail("error reading line: truncated TYPEIDX block");
+                auto t = tokens(line);
+                P.atm[i] = tok(t, 1, "TYPEIDX row");
+                P.mass[i] = to_dbl(t, 3, "TYPEIDX row");
+            }
+        }
+        if (has(line, "ATOM PAIRS:")) {
+            auto t = tokens(line);
+            no_pairs = to_int(t, 2, "ATOM PAIRS");
+        }
+        if (has(line, "# PAIRIDX #")) {
+            if (has(line, "# USEOVRP #")) continue;
+            if (no_pairs <= 0) fail("PAIRIDX block before ATOM PAIRS");
+            P.npairs = no_pairs;
+            P.pa1.assign(no_pairs, ""); P.pa2.assign(no_pairs, "");
+            P.rin.assign(no_pairs, 0.0); P.rout.assign(no_pairs, 0.0); P.lam.assign(no_pairs, 0.0);
+            std::string style;
+            for (int i = 0; i < no_pairs; i++) {
+                if (!L.next(line)) fail("error reading line: truncated PAIRIDX block");
+                auto t = tokens(line);
+                int xf, mo;
+                if (t.size() == 8) { xf = 6; mo = 7; }
+                else if (t.size() == 7) { xf = 5; mo = 6; }
+                else fail("incorrect input in pair line (expect 7 or 8 entries): " + line);
+                P.pa1[i] = t[1]; P.pa2[i] = t[2];
+                P.rin[i] = to_dbl(t, 3, "pair line");
+                P.rout[i] = to_dbl(t, 4, "pair line");
+                if (i == 0) style = t[xf];
+                else if (t[xf] != style) fail("distance transformation style must be the same for all pair types");
+                if (style != "MORSE") fail("only the MORSE distance transformation is supported: " + style);
+                P.lam[i] = to_dbl(t, mo, "pair line (MORSE lambda)");
+            }
+        }
+        if (has(line, "FCUT TYPE:")) {
+            auto t = tokens(line);
+            const std::string& s = tok(t, 2, "FCUT TYPE");
+            if (s == "CUBIC") P.tersoff = false;
+            else if (s == "TERSOFF") { P.tersoff = true; P.fcut_var = to_dbl(t, 3, "FCUT TYPE"); }
+            else fail("unknown FCUT TYPE: " + s);
+        }
+        if (has(line, "PAIR CHEBYSHEV PENALTY DIST:")) P.pen_dist = to_dbl(tokens(line), 4, "PENALTY DIST");
+        if (has(line, "PAIR CHEBYSHEV PENALTY SCALING:")) P.pen_scale = to_dbl(tokens(line), 4, "PENALTY SCALING");
+        if (has(line, "NO ENERGY OFFSETS:")) {
+            auto t = tokens(line);
+            if (t.empty() || to_int(t, t.size() - 1, "NO ENERGY OFFSETS") != P.ntypes)
+                fail("number of energy offsets does not match number of atom types");
+            for (int i = 0; i < P.ntypes; i++) {
+                if (!L.next(line)) fail("error reading line: truncated energy offsets");
+                auto u = tokens(line);
+                int k = to_int(u, 2, "ENERGY OFFSET");
+                if (k < 1 || k > P.ntypes) fail("energy offset index out of range");
+                P.eoff[k - 1] = to_dbl(u, 3, "ENERGY OFFSET");
+            }
+        }
+    }
+    if (P.ntypes < 1 || (int)P.atm.size() != P.ntypes) fail("missing ATOM TYPES / TYPEIDX block");
+    if (P.npairs < 1) fail("missing ATOM PAIRS / PAIRIDX block");
+    const int nt = P.ntypes;
+
+    // pass 3: 2B coefficients and PAIRMAPS (chimesFF.cpp:694-830)
+    L.rewind();
+    P.pows2.assign(P.npairs, {});
+    P.coef2.assign(P.npairs, {});
+    bool have_pmap = false;
+    while (true) {
+        if (!L.next(line)) fail("error reading line: missing ENDFILE");
+        if (has(line, "ENDFILE")) break;
+        if (has(line, "PAIRTYPE PARAMS:")) {
+            auto t = tokens(line);
+            int p = to_int(t, 2, "PAIRTYPE PARAMS");
+            if (p < 0 || p >= P.npairs) fail("PAIRTYPE PARAMS index out of range");
+            if (!L.next(line)) fail("error reading line");
+            P.pows2[p].clear(); P.coef2[p].clear();
+            for (int i = 0; i < P.o2; i++) {
+                if (!L.next(line)) fail("error reading line: truncated 2B parameters");
+                auto u = tokens(line);
+                int pw = to_int(u, 0, "2B parameter");
+                if (pw < 0 || pw + 1 > P.o2) fail("2B power out of range for the 2B order");
+                P.pows2[p].push_back(pw);
+                P.coef2[p].push_back(to_dbl(u, 1, "2B parameter"));
+            }
+        }
+        if (has(line, "PAIRMAPS:")) {
+            auto t = tokens(line);
+            int nm = to_int(t, 1, "PAIRMAPS");
+            std::map<std::string, int> m;
+            std::vector<std::string> order;
+            for (int i = 0; i < nm; i++) {
+                if (!L.next(line)) fail("error reading line: truncated PAIRMAPS");
+                auto u = tokens(line);
+                const std::string& key = tok(u, 1, "PAIRMAPS row");
+                if (!m.count(key)) m[key] = to_int(u, 0, "PAIRMAPS row");
+            }
+            P.pair_map.assign(nt * nt, 0);
+            P.prpr.assign(nt * nt, 0);
+            for (int i = 0; i < nt; i++)
+                for (int j = 0; j < nt; j++) {
+                    auto it = m.find(P.atm[i] + P.atm[j]);
+                    if (it == m.end()) fail("could not find element in vector: " + P.atm[i] + P.atm[j]);
+                    if (it->second < 0 || it->second >= P.npairs) fail("PAIRMAPS index out of range");
+                    P.pair_map[i * nt + j] = it->second;
+                    P.prpr[i * nt + j] = proper_pair(P, P.atm[i], P.atm[j]);
+                }
+            have_pmap = true;
+        }
+    }
+    if (!have_pmap) fail("missing PAIRMAPS block");
+    for (int p = 0; p < P.npairs; p++)
+        if ((int)P.coef2[p].size() != P.o2) fail("missing PAIRTYPE PARAMS block for a pair type");
+
+    // passes 4-7: 3B and 4B blocks (chimesFF.cpp:834-1567)
+    for (int nb = 3; nb <= 4; nb++) {
+        HostParams::Body& B = nb == 3 ? P.b3 : P.b4;
+        const int order = nb == 3 ? P.o3 : P.o4;
+        B.nbody = nb;
+        B.npair = nb * (nb - 1) / 2;
+        if (order <= 0) continue;
+        const int np = B.npair;
+        const char* h_count = nb == 3 ? "ATOM PAIR TRIPLETS:" : "ATOM PAIR QUADRUPLETS:";
+        const char* h_type = nb == 3 ? "TRIPLETTYPE PARAMS:" : "QUADRUPLETYPE PARAMS:";
+        const char* h_maps = nb == 3 ? "TRIPMAPS:" : "QUADMAPS:";
+        std::map<std::string, int> keys;   // map key -> type index
+        int ntup = 1;
+        for (int k = 0; k < nb; k++) ntup *= nt;
+        L.rewind();
+        bool have_map = false;
+        while (true) {
+            if (!L.next(line)) fail("error reading line: missing ENDFILE");
+            if (has(line, "ENDFILE")) break;
+            if (has(line, h_count)) {
+                auto t = tokens(line);
+                B.ntyp = to_int(t, 3, h_count);
+                if (B.ntyp < 0) fail("negative cluster type count");
+                B.ncoef.assign(B.ntyp, 0);
+                B.pows.assign(B.ntyp, {});
+                B.coef.assign(B.ntyp, {});
+                B.cut_in.assign(B.ntyp, std::vector<double>(np, 0.0));
+                B.cut_out.assign(B.ntyp, std::vector<double>(np, 0.0));
+                B.atoms.assign(B.ntyp, {});
+                B.pairs.assign(B.ntyp, {});
+            }
+            if (has(line, h_type)) {
+                if (!L.next(line)) fail("error reading line");
+                auto t = tokens(line);
+                int ti = to_int(t, 1, h_type);
+                if (ti < 0 || ti >= B.ntyp) fail("cluster type index out of range");
+                B.atoms[ti].clear();
+                for (int a = 0; a < nb; a++) B.atoms[ti].push_back(tok(t, 3 + a, h_type));
+                if (!L.next(line)) fail("error reading line");
+                auto u = tokens(line);
+                B.pairs[ti].clear();
+                for (int p = 0; p < np; p++) B.pairs[ti].push_back(tok(u, 1 + p, "PAIRS line"));
+                if (tok(u, 1 + np, "PAIRS line") != "EXCLUDED:") {
+                    int nc = to_int(u, nb == 3 ? 7 : 10, "PAIRS line (TOTAL)");
+                    if (nc < 0) fail("negative coefficient count");
+                    B.ncoef[ti] = nc;
+                    if (!L.next(line) || !L.next(line)) fail("error reading line");
+                    B.pows[ti].assign((size_t)nc * np, 0);
+                    B.coef[ti].assign(nc, 0.0);
+                    for (int c = 0; c < nc; c++) {
+                        if (!L.next(line)) fail("error reading line: truncated coefficient list");
+                        auto w = tokens(line);
+                        for (int p = 0; p < np; p++) {
+                            int pw = to_int(w, 1 + p, "coefficient row");
+                            if (pw < 0 || pw > order) fail("many-body power larger than its order");
+                            B.pows[ti][(size_t)c * np + p] = pw;
+                        }
+                        B.coef[ti][c] = to_dbl(w, nb == 3 ? 6 : 9, "coefficient row");
+                    }
+                }
+            }
+            if (has(line, h_maps)) {
+                auto t = tokens(line);
+                int nm = to_int(t, 1, h_maps);
+                for (int i = 0; i < nm; i++) {
+                    if (!L.next(line)) fail("error reading line: truncated map block");
+                    auto u = tokens(line);
+                    const std::string& key = tok(u, 1, "map row");
+                    if (!keys.count(key)) keys[key] = to_int(u, 0, "map row");
+                }
+                B.map.assign(ntup, 0);
+                for (int uidx = 0; uidx < ntup; uidx++) {
+                    int a[4], r = uidx;
+                    for (int k = nb - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+                    std::string key;
+                    for (int i = 0; i < nb; i++)
+                        for (int j = i + 1; j < nb; j++) key += P.pair_name(proper_pair(P, P.atm[a[i]], P.atm[a[j]]));
+                    auto it = keys.find(key);
+                    if (it == keys.end()) fail("could not find element in vector: " + key);
+                    if (it->second >= B.ntyp) fail("cluster map index out of range");
+                    B.map[uidx] = it->second;
+                }
+                have_map = true;
+            }
+        }
+        if (!have_map) fail(std::string("missing ") + h_maps + " block");
+        for (int ti = 0; ti < B.ntyp; ti++)
+            if ((int)B.atoms[ti].size() != nb || (int)B.pairs[ti].size() != np) fail("missing cluster type block");
+        // default cutoffs from the 2B pair types of the type's atoms (chimesFF.cpp:947-980, 1280-1325)
+        for (int ti = 0; ti < B.ntyp; ti++) {
+            int a[4];
+            for (int k = 0; k < nb; k++) {
+                a[k] = P.type_index(B.atoms[ti][k]);
+                if (a[k] < 0) fail("cluster type names an unknown atom type: " + B.atoms[ti][k]);
+            }
+            int p = 0;
+            for (int i = 0; i < nb; i++)
+                for (int j = i + 1; j < nb; j++, p++) {
+                    int pt = P.pair_map[a[i] * nt + a[j]];
+                    B.cut_in[ti][p] = P.rin[pt];
+                    B.cut_out[ti][p] = P.rout[pt];
+                }
+        }
+        // SPECIAL nB S_MAXIM / S_MINIM: ALL v | SPECIFIC n (chimesFF.cpp:1009-1168, 1353-1566)
+        const std::string smax = nb == 3 ? "SPECIAL 3B S_MAXIM:" : "SPECIAL 4B S_MAXIM:";
+        const std::string smin = nb == 3 ? "SPECIAL 3B S_MINIM:" : "SPECIAL 4B S_MINIM:";
+        L.rewind();
+        while (true) {
+            if (!L.next(line)) fail("error reading line: missing ENDFILE");
+            if (has(line, "ENDFILE")) break;
+            int which = has(line, smax.c_str()) ? 1 : (has(line, smin.c_str()) ? 0 : -1);
+            if (which < 0) continue;
+            auto t = tokens(line);
+            auto& dst = which ? B.cut_out : B.cut_in;
+            if (tok(t, 3, "SPECIAL") == "ALL") {
+                double v = to_dbl(t, 4, "SPECIAL ALL");
+                for (auto& row : dst) std::fill(row.begin(), row.end(), v);
+            } else {
+                int ne = to_int(t, 4, "SPECIAL SPECIFIC");
+                if (which == 0 && nb == 4)
+                    for (auto& row : dst) std::fill(row.begin(), row.end(), -1.0);
+                for (int e = 0; e < ne; e++) {
+                    if (!L.next(line)) fail("error reading line: truncated SPECIAL block");
+                    auto u = tokens(line);
+                    auto it = keys.find(tok(u, 0, "SPECIAL row"));
+                    if (it == keys.end() || it->second < 0 || it->second >= B.ntyp)
+                        fail("SPECIAL row names an unknown cluster type");
+                    int ti = it->second;
+                    std::vector<bool> disq(np, false);
+                    for (int q = 0; q < np; q++) {
+                        const std::string& nm = tok(u, 1 + q, "SPECIAL row");
+                        int slot = -1;
+                        for (int p = 0; p < np; p++)
+                            if (B.pairs[ti][p] == nm && !disq[p]) { disq[p] = true; slot = p; break; }
+                        if (slot < 0) fail("could not find element in vector: " + nm);
+                        dst[ti][slot] = to_dbl(u, 1 + np + q, "SPECIAL row");
+                    }
+                }
+            }
+        }
+        // pair_int_{trip,quad}_map
+        B.perm.assign(ntup, std::vector<int>(np, 0));
+        std::vector<int> pm(np, 0);
+        for (int uidx = 0; uidx < ntup; uidx++) {
+            int a[4], r = uidx;
+            for (int k = nb - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+            int ti = B.map[uidx];
+            if (ti < 0) continue;
+            atom_pair_mapper(P, nb, a, B.pairs[ti], pm);
+            B.perm[uidx] = pm;
+        }
+    }
+}
+
+}  // namespace
+
+double HostParams::max_cut2() const {
+    double m = rout[0];
+    for (double v : rout) if (v > m) m = v;
+    return m;
+}
+
+static double max_cut_body(const HostParams::Body& B, int order) {
+    if (order == 0 || B.ntyp == 0) return 0.0;
+    double m = B.cut_out[0][0];
+    for (auto& row : B.cut_out) for (double v : row) if (v > m) m = v;
+    return m;
+}
+double HostParams::max_cut3() const { return max_cut_body(b3, o3); }
+double HostParams::max_cut4() const { return max_cut_body(b4, o4); }
+
+int HostParams::type_index(const std::string& name) const {
+    for (int i = 0; i < ntypes; i++) if (atm[i] == name) return i;
+    return -1;
+}
+
+Status parse_parameter_file(const std::string& path, HostParams& P, std::string& err) {
+    std::ifstream f(path);
+    if (!f.is_open()) {
+        err = "cannot open parameter file: " + path;
+        return kErrParam;
+    }
+    Lines L;
+    std::string line;
+    while (std::getline(f, line)) L.v.push_back(line);
+    P = HostParams();
+    try {
+        parse_lines(L, P);
+    } catch (const ParseError& e) {
+        err = e.msg;
+        return kErrParam;
+    }
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Device image
+// ---------------------------------------------------------------------------
+namespace {
+struct Blob {
+    std::vector<unsigned char> b;
+    template <class T>
+    size_t add(const T* p, size_t n) {
+        size_t off = (b.size() + 255) & ~size_t(255);
+        b.resize(off + n * sizeof(T));
+        if (n) std::memcpy(b.data() + off, p, n * sizeof(T));
+        return off;
+    }
+};
+template <class T>
+T* as_off(size_t off) { return reinterpret_cast<T*>(off); }
+
+// set_cheby_polys' Morse-map constants (chimesFF.h:553-559)
+void morse_consts(double rin, double rout, double lam, double& xavg, double& xdiff) {
+    double x_min = std::exp(-1 * rin / lam);
+    double x_max = std::exp(-1 * rout / lam);
+    xavg = 0.5 * (x_max + x_min);
+    xdiff = 0.5 * (x_max - x_min);
+    xdiff *= -1.0;
+}
+}  // namespace
+
+ParamImage pack_params(const HostParams& P) {
+    ParamImage img;
+    Blob B;
+    B.b.resize(256);   // no array at offset 0, so a zero offset can mean "absent"
+    DevParamSet& H = img.header;
+    const int nt = P.ntypes;
+    H.ntypes = nt; H.npairs = P.npairs; H.o2 = P.o2; H.o3 = P.o3; H.o4 = P.o4;
+    H.tersoff = P.tersoff ? 1 : 0;
+    H.fcut_var = P.fcut_var; H.pen_dist = P.pen_dist; H.pen_scale = P.pen_scale; H.inner_smooth = P.inner_smooth;
+    H.maxcut2 = P.max_cut2(); H.maxcut3 = P.max_cut3(); H.maxcut4 = P.max_cut4();
+    H.search = H.maxcut2;
+    if (H.maxcut3 > H.search) H.search = H.maxcut3;
+    if (H.maxcut4 > H.search) H.search = H.maxcut4;
+
+    H.eoff = as_off<const double>(B.add(P.eoff.data(), P.eoff.size()));
+    H.pair_map = as_off<const int>(B.add(P.pair_map.data(), P.pair_map.size()));
+    std::vector<PairRec> pr(P.npairs);
+    std::vector<double> c2d;
+    std::vector<float> c2f;
+    std::vector<int> p2;
+    for (int p = 0; p < P.npairs; p++) {
+        pr[p].rin = P.rin[p]; pr[p].rout = P.rout[p]; pr[p].lam = P.lam[p];
+        morse_consts(P.rin[p], P.rout[p], P.lam[p], pr[p].xavg, pr[p].xdiff);
+        // dense table a_n (n = 0..o2) with a_{pow+1} = sum of the coefficients of
+        // that power: the 2B kernel sums along the Chebyshev recursion
+        pr[p].ncoef = P.o2 + 1;
+        pr[p].coef_off = (int)c2d.size();
+        std::vector<double> dense(P.o2 + 1, 0.0);
+        for (int c = 0; c < P.o2; c++) {
+            dense[P.pows2[p][c] + 1] += P.coef2[p][c];
+            p2.push_back(P.pows2[p][c]);
+        }
+        for (int n = 0; n <= P.o2; n++) {
+            c2d.push_back(dense[n]);
+            c2f.push_back((float)dense[n]);
+        }
+    }
+    H.pairs = as_off<const PairRec>(B.add(pr.data(), pr.size()));
+    H.c2d = as_off<const double>(B.add(c2d.data(), c2d.size()));
+    H.c2f = as_off<const float>(B.add(c2f.data(), c2f.size()));
+    H.p2 = as_off<const int>(B.add(p2.data(), p2.size()));
+
+    for (int nb = 3; nb <= 4; nb++) {
+        const HostParams::Body& Bd = nb == 3 ? P.b3 : P.b4;
+        const int order = nb == 3 ? P.o3 : P.o4;
+        if (order <= 0) continue;
+        const int np = Bd.npair;
+        int ntup = 1;
+        for (int k = 0; k < nb; k++) ntup *= nt;
+        std::vector<TupleRec> tr(ntup);
+        std::vector<double> cd;
+        std::vector<float> cf;
+        std::vector<uint32_t> pw;
+        std::map<std::pair<int, std::vector<int>>, int> shared;  // (type, mapping) -> coef_off
+        for (int u = 0; u < ntup; u++) {
+            TupleRec& R = tr[u];
+            std::memset(&R, 0, sizeof(R));
+            int a[4], r = u;
+            for (int k = nb - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+            int ti = Bd.map[u];
+            R.type_id = ti;
+            if (ti < 0) continue;
+            const std::vector<int>& m = Bd.perm[u];
+            int p = 0;
+            for (int i = 0; i < nb; i++)
+                for (int j = i + 1; j < nb; j++, p++) {
+                    R.rin[p] = Bd.cut_in[ti][m[p]];
+                    R.rout[p] = Bd.cut_out[ti][m[p]];
+                    R.lam[p] = P.lam[P.pair_map[a[i] * nt + a[j]]];
+                    morse_consts(R.rin[p], R.rout[p], R.lam[p], R.xavg[p], R.xdiff[p]);
+                }
+            R.ncoef = Bd.ncoef[ti];
+            R.valid = R.ncoef > 0 ? 1 : 0;
+            auto key = std::make_pair(ti, m);
+            auto it = shared.find(key);
+            if (it != shared.end()) {
+                R.coef_off = it->second;
+                continue;
+            }
+            R.coef_off = (int)cd.size();
+            shared[key] = R.coef_off;
+            for (int c = 0; c < R.ncoef; c++) {
+                cd.push_back(Bd.coef[ti][c]);
+                cf.push_back((float)Bd.coef[ti][c]);
+                uint32_t packed = 0;
+                for (int q = 0; q < np; q++)
+                    packed |= uint32_t(Bd.pows[ti][(size_t)c * np + m[q]]) << (kPowBits * q);
+                pw.push_back(packed);
+            }
+        }
+        size_t tro = B.add(tr.data(), tr.size());
+        size_t cdo = B.add(cd.data(), cd.size());
+        size_t cfo = B.add(cf.data(), cf.size());
+        size_t pwo = B.add(pw.data(), pw.size());
+        if (nb == 3) {
+            H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
+            H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);
+        } else {
+            H.t4 = as_off<const TupleRec>(tro); H.c4d = as_off<const double>(cdo);
+            H.c4f = as_off<const float>(cfo); H.p4 = as_off<const uint32_t>(pwo);
+        }
+    }
+    img.header_off = B.add(&H, 1);
+    img.bytes = std::move(B.b);
+    return img;
+}
+
+}  // namespace ck
