@@ -27,11 +27,11 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CXX_SOURCES = ["ck_params.cpp", "ck_geom.cpp", "ck_engine.cpp", "ck_capi.cpp"]
-CU_SOURCES = ["ck_lists.cu", "ck_force.cu"]
+CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_direct.cu"]
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(REPO, "include", "*.h"))
+    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(REPO, "include", "*.h"))
 
 
 def _stale(obj: str, src: str, headers) -> bool:

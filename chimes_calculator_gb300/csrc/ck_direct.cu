@@ -1,0 +1,180 @@
+// Per-cluster kernels: the chimesFF::compute_2B/3B/4B entry points, where the
+// caller owns the cluster loop and passes distances, displacement vectors and
+// type indices (chimesFF/src/chimesFF.cpp:1644-1775, 1931-2176, 2496-2872).
+// One thread per cluster, FP64, any number of clusters per launch; outputs are
+// per-cluster (the host adds them into the caller's accumulators).
+//
+// Besides energy, forces and the packed stress, each cluster reports the
+// reference's `force_scalar_in` value: for 2B the penalty force scalar over r
+// (1.0 without a penalty), for 3B/4B the per-pair force scalars of the LAST
+// coefficient of the list, as the reference's loop leaves them.  status bits:
+// 1 = the cluster passed the type and cutoff checks, 2 = penalty region
+// (badness 1), 4 = below the inner cutoff (badness 2), 8 = a many-body pair below
+// its inner cutoff (the reference prints a warning; badness is unchanged).
+#include <cuda_runtime.h>
+
+#include "ck_common.h"
+#include "ck_kernels.h"
+#include "ck_math.cuh"
+
+namespace ck {
+
+namespace {
+
+__global__ void k_direct2(const DevParamSet* Pp, int n, const double* dx, const double* dr, const int* typ,
+                          double* force, double* stress, double* energy, double* fscal, int* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const DevParamSet& P = *Pp;
+    for (int k = 0; k < 6; k++) { force[6 * c + k] = 0.0; stress[6 * c + k] = 0.0; }
+    energy[c] = 0.0;
+    fscal[c] = 0.0;
+    status[c] = 0;
+    const int t0 = typ[2 * c], t1 = typ[2 * c + 1];
+    const PairRec pr = P.pairs[P.pair_map[t0 * P.ntypes + t1]];
+    const double r = dx[c];
+    const double* d = &dr[3 * c];
+    if (r >= pr.rout) return;
+    int st = 1;
+    double xd, dxdr;
+    bool oor;
+    morse_x(r, pr.rin, pr.lam, pr.xavg, pr.xdiff, xd, dxdr, oor);
+    const double* a = P.c2d + pr.coef_off;
+    const double tx = 2.0 * xd;
+    double t0c = 1.0, t1c = xd, u0 = 1.0, u1 = tx;
+    double S = a[0] * t0c + a[1] * t1c, GD = a[1] * u0;
+    for (int k = 2; k <= P.o2; k++) {
+        const double t2 = tx * t1c - t0c, u2 = tx * u1 - u0;
+        S += a[k] * t2;
+        GD += a[k] * k * u1;
+        t0c = t1c; t1c = t2; u0 = u1; u1 = u2;
+    }
+    double G = GD * dxdr;
+    if (oor) {
+        const double damp = exp((r - pr.rin) / P.inner_smooth);
+        S += P.inner_smooth * (damp - 1.0) * G;
+        G *= damp;
+    }
+    double fc, fcd;
+    fcut_eval<double>(P, r, pr.rout, fc, fcd);
+    double E = fc * S;
+    const double dx_inv = r > 0.0 ? 1.0 / r : 1e20;
+    double fs = (fc * G + fcd * S) * dx_inv;
+    double fs_out = 1.0;
+    if (r - P.pen_dist < pr.rin) {
+        st |= r < pr.rin ? 4 : 2;
+        const double rp = pr.rin + P.pen_dist - r;
+        if (rp > 0.0) {
+            E += rp * rp * rp * P.pen_scale;
+            fs_out = (-3.0 * rp * rp * P.pen_scale) / r;
+            fs += fs_out;
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        force[6 * c + k] = fs * d[k];
+        force[6 * c + 3 + k] = -fs * d[k];
+    }
+    stress[6 * c + 0] = -fs * d[0] * d[0];
+    stress[6 * c + 1] = -fs * d[0] * d[1];
+    stress[6 * c + 2] = -fs * d[0] * d[2];
+    stress[6 * c + 3] = -fs * d[1] * d[1];
+    stress[6 * c + 4] = -fs * d[1] * d[2];
+    stress[6 * c + 5] = -fs * d[2] * d[2];
+    energy[c] = E;
+    fscal[c] = fs_out;
+    status[c] = st;
+}
+
+template <int NB>
+__global__ void k_directn(const DevParamSet* Pp, int n, const double* dx, const double* dr, const int* typ,
+                          double* force, double* stress, double* energy, double* fscal, int* status) {
+    constexpr int NP = Topo<NB>::NP;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const DevParamSet& P = *Pp;
+    for (int k = 0; k < 3 * NB; k++) force[3 * NB * c + k] = 0.0;
+    for (int k = 0; k < 6; k++) stress[6 * c + k] = 0.0;
+    for (int k = 0; k < NP; k++) fscal[NP * c + k] = 0.0;
+    energy[c] = 0.0;
+    status[c] = 0;
+    int u = 0;
+    for (int k = 0; k < NB; k++) u = u * P.ntypes + typ[NB * c + k];
+    const TupleRec* R = (NB == 3 ? P.t3 : P.t4) + u;
+    if (R->type_id < 0) return;   // excluded cluster type
+    const double* r = &dx[NP * c];
+    const double* d = &dr[3 * NP * c];
+    for (int p = 0; p < NP; p++)
+        if (r[p] >= R->rout[p]) return;
+    const int order = NB == 3 ? P.o3 : P.o4;
+    double T[NP][kMaxOrder + 1], D[NP][kMaxOrder + 1], fc[NP], fcd[NP];
+    for (int p = 0; p < NP; p++) {
+        cheby_table<double>(T[p], D[p], r[p], R->rin[p], R->lam[p], R->xavg[p], R->xdiff[p], order,
+                            P.inner_smooth, nullptr);
+        fcut_eval<double>(P, r[p], R->rout[p], fc[p], fcd[p]);
+    }
+    int st = 1;
+    for (int p = 0; p < NP; p++)
+        if (r[p] < R->rin[p]) st |= 8;   // below-rin warning only (badness is a 2B notion)
+    double pre[NP + 1], suf[NP + 1];
+    pre[0] = 1.0;
+    for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * fc[p];
+    suf[NP] = 1.0;
+    for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * fc[p];
+    double S = 0.0, G[NP];
+    for (int p = 0; p < NP; p++) G[p] = 0.0;
+    const double* cf = (NB == 3 ? P.c3d : P.c4d) + R->coef_off;
+    const uint32_t* pw = (NB == 3 ? P.p3 : P.p4) + R->coef_off;
+    double last[NP];
+    for (int p = 0; p < NP; p++) last[p] = 0.0;
+    for (int k = 0; k < R->ncoef; k++) {
+        double t[NP], dd[NP];
+        for (int p = 0; p < NP; p++) {
+            const int q = (pw[k] >> (kPowBits * p)) & 31u;
+            t[p] = T[p][q];
+            dd[p] = D[p][q];
+        }
+        double tp[NP + 1], ts[NP + 1];
+        tp[0] = 1.0;
+        for (int p = 0; p < NP; p++) tp[p + 1] = tp[p] * t[p];
+        ts[NP] = 1.0;
+        for (int p = NP - 1; p >= 0; p--) ts[p] = ts[p + 1] * t[p];
+        S += cf[k] * tp[NP];
+        for (int p = 0; p < NP; p++) G[p] += cf[k] * dd[p] * tp[p] * ts[p + 1];
+        if (k == R->ncoef - 1)
+            for (int p = 0; p < NP; p++)
+                last[p] = cf[k] * (fc[p] * dd[p] + fcd[p] * t[p]) * (pre[p] * suf[p + 1] / r[p]) * tp[p] * ts[p + 1];
+    }
+    double vir[6] = {0, 0, 0, 0, 0, 0};
+    for (int p = 0; p < NP; p++) {
+        const double fsp = pre[p] * suf[p + 1] / r[p] * (fc[p] * G[p] + fcd[p] * S);
+        const double* dp = &d[3 * p];
+        const int a = Topo<NB>::a(p), b = Topo<NB>::b(p);
+        for (int k = 0; k < 3; k++) {
+            force[3 * NB * c + 3 * a + k] += fsp * dp[k];
+            force[3 * NB * c + 3 * b + k] -= fsp * dp[k];
+        }
+        vir[0] -= fsp * dp[0] * dp[0];
+        vir[1] -= fsp * dp[0] * dp[1];
+        vir[2] -= fsp * dp[0] * dp[2];
+        vir[3] -= fsp * dp[1] * dp[1];
+        vir[4] -= fsp * dp[1] * dp[2];
+        vir[5] -= fsp * dp[2] * dp[2];
+    }
+    for (int k = 0; k < 6; k++) stress[6 * c + k] = vir[k];
+    for (int p = 0; p < NP; p++) fscal[NP * c + p] = last[p];
+    energy[c] = pre[NP] * S;
+    status[c] = st;
+}
+
+}  // namespace
+
+void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st) {
+    if (n <= 0) return;
+    const unsigned grid = (unsigned)((n + 63) / 64);
+    if (nbody == 2) k_direct2<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    else if (nbody == 3) k_directn<3><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    else k_directn<4><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+}
+
+}  // namespace ck

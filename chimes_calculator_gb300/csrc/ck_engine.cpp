@@ -372,6 +372,57 @@ Status Engine::run(const std::vector<SystemSpec>& sys, double* force_out, std::v
     return kErrCapacity;
 }
 
+Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                                double* force, double* stress, double* energy, double* fscal, int* status,
+                                std::string& err) {
+    Status st = init_device(err);
+    if (st != kOk) return st;
+    if (slot < 0 || slot >= (int)sets_.size()) {
+        err = "parameters not initialised";
+        return kErrState;
+    }
+    if (nbody < 2 || nbody > 4) {
+        err = "clusters have 2, 3 or 4 atoms";
+        return kErrInput;
+    }
+    if (n <= 0) return kOk;
+    const HostParams& P = *sets_[slot].host;
+    if ((nbody == 3 && P.o3 <= 0) || (nbody == 4 && P.o4 <= 0)) {
+        err = "the parameter set has no " + std::to_string(nbody) + "-body terms";
+        return kErrInput;
+    }
+    for (long long i = 0; i < (long long)n * nbody; i++)
+        if (typ[i] < 0 || typ[i] >= P.ntypes) {
+            err = "atom type index out of range for the parameter set";
+            return kErrInput;
+        }
+    const int np = nbody * (nbody - 1) / 2;
+    const size_t nd_in = (size_t)n * np * 4;                       // dx + dr
+    const size_t nd_out = (size_t)n * (3 * nbody + 6 + 1 + np);    // force, stress, energy, fscal
+    CK_TRY(d_dir_d_.reserve(nd_in + nd_out));
+    CK_TRY(d_dir_i_.reserve((size_t)n * (nbody + 1)));
+    double* ddx = d_dir_d_.p;
+    double* ddr = ddx + (size_t)n * np;
+    double* dforce = ddr + (size_t)n * np * 3;
+    double* dstress = dforce + (size_t)n * 3 * nbody;
+    double* denergy = dstress + (size_t)n * 6;
+    double* dfscal = denergy + n;
+    int* dtyp = d_dir_i_.p;
+    int* dstatus = dtyp + (size_t)n * nbody;
+    CK_TRY(cudaMemcpyAsync(ddx, dx, sizeof(double) * n * np, cudaMemcpyHostToDevice, stream_));
+    CK_TRY(cudaMemcpyAsync(ddr, dr, sizeof(double) * n * np * 3, cudaMemcpyHostToDevice, stream_));
+    CK_TRY(cudaMemcpyAsync(dtyp, typ, sizeof(int) * n * nbody, cudaMemcpyHostToDevice, stream_));
+    launch_direct(dsets_.p + slot, nbody, n, ddx, ddr, dtyp, dforce, dstress, denergy, dfscal, dstatus, stream_);
+    CK_TRY(cudaGetLastError());
+    CK_TRY(cudaMemcpyAsync(force, dforce, sizeof(double) * n * 3 * nbody, cudaMemcpyDeviceToHost, stream_));
+    CK_TRY(cudaMemcpyAsync(stress, dstress, sizeof(double) * n * 6, cudaMemcpyDeviceToHost, stream_));
+    CK_TRY(cudaMemcpyAsync(energy, denergy, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_));
+    if (fscal) CK_TRY(cudaMemcpyAsync(fscal, dfscal, sizeof(double) * n * np, cudaMemcpyDeviceToHost, stream_));
+    if (status) CK_TRY(cudaMemcpyAsync(status, dstatus, sizeof(int) * n, cudaMemcpyDeviceToHost, stream_));
+    CK_TRY(cudaStreamSynchronize(stream_));
+    return kOk;
+}
+
 Status Engine::export_lists(std::vector<int>& l2, std::vector<int>& l3, std::vector<int>& l4, std::string& err) {
     if (!staged_) {
         err = "no evaluation to export";

@@ -106,6 +106,15 @@ public:
     bool use_graph = false;
     RunStats last;
 
+    // Per-cluster evaluation (the chimesFF::compute_nB entry points): n
+    // clusters of `nbody` atoms given as distances dx[n][P], displacement
+    // vectors dr[n][P][3] (atom2 - atom1) and type indices typ[n][nbody].
+    // Writes per-cluster force[n][nbody][3], packed stress[n][6], energy[n],
+    // force scalars fscal[n][P] and status[n] (see ck_direct.cu).
+    Status compute_clusters(int slot, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                            double* force, double* stress, double* energy, double* fscal, int* status,
+                            std::string& err);
+
     // Cluster lists of the last run in system-local ghost numbering (the
     // reference's sys_parent/ghost indices), for set comparisons.
     Status export_lists(std::vector<int>& l2, std::vector<int>& l3, std::vector<int>& l4, std::string& err);
@@ -146,6 +155,8 @@ private:
     DevBuf<double> d_force_, d_ev_;
     DevBuf<int> d_flags_;
     DevBuf<unsigned char> d_scan_tmp_;
+    DevBuf<double> d_dir_d_;      // per-cluster inputs and outputs (doubles)
+    DevBuf<int> d_dir_i_;         // per-cluster types and status
 
     PinnedBuf<double> h_in_pos_;
     PinnedBuf<int> h_in_type_;

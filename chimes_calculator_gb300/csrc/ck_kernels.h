@@ -45,6 +45,10 @@ void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L
 void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 void launch_force4(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 
+// Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
+void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st);
+
 int sm_count();
 
 }  // namespace ck
