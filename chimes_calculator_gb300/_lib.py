@@ -57,6 +57,7 @@ SIGNATURES = {
     "ck_close": (None, [P]),
     "ck_load_params": (I, [P, S]),
     "ck_select_params": (I, [P, I]),
+    "ck_check_params": (I, [S, IP, IP, DP]),
     "ck_param_info": (I, [P, I, IP, IP, DP]),
     "ck_type_index": (I, [P, I, S]),
     "ck_set_precision": (I, [P, I]),

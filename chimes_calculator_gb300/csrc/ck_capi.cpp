@@ -33,14 +33,7 @@ Instance* g_cur = nullptr;                  // chimes_ptr of chimescalc_serial_C
 int g_errmode = 0;                          // 0: print + exit(0) (reference), 1: return status
 thread_local std::string g_err;
 
-int report(int status, const std::string& msg) {
-    g_err = msg;
-    if (status != ck::kOk && g_errmode == 0) {
-        std::cout << "ERROR: " << msg << std::endl;
-        std::exit(0);
-    }
-    return status;
-}
+int report(int status, const std::string& msg) { return ck::report_error(status, msg); }
 
 int check_handle(void* h) {
     if (!h) return report(ck::kErrState, "no ChIMES instance: call set_chimes_serial / chimes_open_instance first");
@@ -108,6 +101,18 @@ int calculate_one(Instance* in, int natom, const double* xc, const double* yc, c
 }
 
 }  // namespace
+
+namespace ck {
+int report_error(int status, const std::string& msg) {
+    g_err = msg;
+    if (status != kOk && g_errmode == 0) {
+        std::cout << "ERROR: " << msg << std::endl;
+        std::exit(0);
+    }
+    return status;
+}
+void clear_error() { g_err.clear(); }
+}  // namespace ck
 
 extern "C" {
 
@@ -191,6 +196,18 @@ int ck_load_params(void* h, const char* path) {
     if (in->slot < 0) in->slot = slot;
     g_err.clear();
     return slot;
+}
+
+int ck_check_params(const char* path, int* orders, int* ntypes, double* maxcuts) {
+    ck::HostParams P;
+    std::string err;
+    ck::Status st = ck::parse_parameter_file(path ? path : "", P, err);
+    if (st != ck::kOk) return report(st, err);
+    if (orders) { orders[0] = P.o2; orders[1] = P.o3; orders[2] = P.o4; }
+    if (ntypes) *ntypes = P.ntypes;
+    if (maxcuts) { maxcuts[0] = P.max_cut2(); maxcuts[1] = P.max_cut3(); maxcuts[2] = P.max_cut4(); }
+    g_err.clear();
+    return ck::kOk;
 }
 
 int ck_select_params(void* h, int slot) {
@@ -339,6 +356,21 @@ int ck_last_diagnostics(void* h, int* out) {
     if (int st = check_handle(h)) return st;
     const ck::RunStats& s = static_cast<Instance*>(h)->eng.last;
     out[0] = s.badness; out[1] = s.penalty_hits; out[2] = s.below_rin;
+    return ck::kOk;
+}
+
+int ck_compute_cluster_batch(void* h, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                             double* force, double* stress, double* energy, double* fscal) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    std::vector<int> status(n > 0 ? n : 1);
+    std::vector<double> fs;
+    if (!fscal) fs.resize((size_t)(n > 0 ? n : 1) * 6);
+    std::string err;
+    ck::Status st = in->eng.compute_clusters(in->slot, nbody, n, dx, dr, typ, force, stress, energy,
+                                             fscal ? fscal : fs.data(), status.data(), err);
+    if (st != ck::kOk) return report(st, err);
     return ck::kOk;
 }
 

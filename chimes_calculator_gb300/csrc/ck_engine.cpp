@@ -136,11 +136,17 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
             err = (S > 1 ? "configuration " + std::to_string(s) + ": " : std::string()) + gerr;
             return st;
         }
-        for (int a = 0; a < in.n; a++)
+        for (int a = 0; a < in.n; a++) {
             if (in.types[a] < 0 || in.types[a] >= P.ntypes) {
                 err = "atom type index out of range for the parameter set";
                 return kErrInput;
             }
+            if (!std::isfinite(in.pos[3 * a]) || !std::isfinite(in.pos[3 * a + 1]) ||
+                !std::isfinite(in.pos[3 * a + 2])) {
+                err = "atom coordinates must be finite";
+                return kErrInput;
+            }
+        }
         d.pset = in.pset;
         d.in_off = in_off; d.atom_off = atom_off; d.ghost_off = ghost_off; d.bin_off = bin_off;
         in_off += in.n;

@@ -176,4 +176,10 @@ private:
 
 const char* status_name(int s);
 
+// Error reporting of the public interfaces: records the message for
+// ck_last_error() and, in the default (reference) mode, prints it on stdout
+// and calls exit(0); in return mode it only returns `status`.
+int report_error(int status, const std::string& msg);
+void clear_error();
+
 }  // namespace ck

@@ -90,6 +90,23 @@ Status system_geometry(const double* ca, const double* cb, const double* cc, int
     double mn = la;
     if (lb < mn) mn = lb;
     if (lc < mn) mn = lc;
+    if (!(mn > 0.0) || !std::isfinite(la) || !std::isfinite(lb) || !std::isfinite(lc)) {
+        err = "cell vectors must be finite and nonzero";
+        return kErrInput;
+    }
+    {
+        double h[9], hi[9];
+        set_hmat(ca, cb, cc, h, hi, 0);
+        for (double v : hi)
+            if (!std::isfinite(v)) {
+                err = "cell vectors are linearly dependent";
+                return kErrInput;
+            }
+    }
+    if (c2 * 2.0 / mn + 1 > 1000.0) {
+        err = "cell is too small for the cutoffs (more than 1000 ghost layers)";
+        return kErrInput;
+    }
     int n_rep = small ? (int)std::ceil(c2 / mn) - 1 : 0;
     if (n_rep < 0) n_rep = 0;
     set_hmat(ca, cb, cc, d.h0, d.h0i, 0);

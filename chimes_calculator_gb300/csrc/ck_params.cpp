@@ -246,7 +246,9 @@ void parse_lines(Lines& L, HostParams& P) {
                 if (!L.next(line)) fail("error reading line: truncated PAIRMAPS");
                 auto u = tokens(line);
                 const std::string& key = tok(u, 1, "PAIRMAPS row");
-                if (!m.count(key)) m[key] = to_int(u, 0, "PAIRMAPS row");
+                const int idx = to_int(u, 0, "PAIRMAPS row");
+                P.pair_map_file_idx.push_back(idx);
+                if (!m.count(key)) m[key] = idx;
             }
             P.pair_map.assign(nt * nt, 0);
             P.prpr.assign(nt * nt, 0);

@@ -26,6 +26,7 @@ struct HostParams {
     std::vector<std::vector<double>> coef2;
     std::vector<int> pair_map;          // atom_int_pair_map [nt*nt]
     std::vector<int> prpr;              // proper pair index [nt*nt] (atom_int_prpr_map)
+    std::vector<int> pair_map_file_idx; // PAIRMAPS indices in file order (atom_idx_pair_map)
 
     struct Body {
         int nbody = 0, npair = 0, ntyp = 0;

@@ -1,0 +1,100 @@
+/*
+ * GB300 extension of the ChIMES C interface (libchimescalc.so).
+ *
+ * These entry points have no counterpart in the reference, whose serial
+ * interface evaluates one configuration per call on one CPU core
+ * (serial_interface/api/chimescalc_serial_C.h).  They add: returned status
+ * codes, several device-resident parameter sets per handle, batched
+ * evaluation of many configurations in one set of launches, the mixed
+ * FP32/FP64 precision mode, launch tuning, CUDA-graph replay, a split
+ * stage/launch/collect form for device timing, diagnostics, cluster-list
+ * export and batched per-cluster evaluation.
+ *
+ * Status codes: 0 ok; -1 parameter file; -2 input; -3 geometry (cutoff vs box,
+ * bins); -4 CUDA; -5 capacity (retried internally); -6 call order; -7 device
+ * wait timed out.  ck_last_error() returns the message of the last failure on
+ * the calling thread.
+ *
+ * Layouts: positions and forces are [atom][xyz] doubles, concatenated over the
+ * configurations of a batch; cells are [config][a,b,c][xyz] (rows are the
+ * lattice vectors); types are indices into the parameter set's atom types;
+ * stress is [config][9] (xx xy xz yx yy yz zx zy zz) divided by the volume.
+ * Batched results are written, not accumulated.
+ */
+#ifndef CHIMES_GB300_H
+#define CHIMES_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 0 (default): print + exit(0) on errors like the reference; 1: return status. Returns the old mode. */
+int ck_set_error_mode(int mode);
+const char *ck_last_error(void);
+
+/* Handles (same object as chimes_open_instance / chimes_close_instance). */
+void *ck_open(void);
+void ck_close(void *h);
+
+/* Parses and uploads a parameter file into a new slot; returns the slot (>= 0)
+ * or a negative status.  The first slot loaded becomes the handle's current one. */
+int ck_load_params(void *h, const char *path);
+int ck_select_params(void *h, int slot);
+/* Parses a parameter file on the host only (no device needed): validation and
+ * inspection.  Same outputs as ck_param_info. */
+int ck_check_params(const char *path, int *orders, int *ntypes, double *maxcuts);
+/* orders[3] = 2B/3B/4B orders, *ntypes, maxcuts[3] = max outer cutoffs. */
+int ck_param_info(void *h, int slot, int *orders, int *ntypes, double *maxcuts);
+/* index of an atom type name in a slot, or -1 */
+int ck_type_index(void *h, int slot, const char *name);
+
+/* 0: FP64 throughout (default); 1: FP32 Chebyshev/cutoff/contraction with FP64
+ * distances and FP64 energy/force/virial accumulation. */
+int ck_set_precision(void *h, int precision);
+/* threads per 3-body and 4-body cluster (1,2,4,8,16,32) and resident blocks per SM */
+int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
+/* replay the whole list-build + force sequence as one CUDA graph (1) or launch it stream-ordered (0) */
+int ck_use_graph(void *h, int on);
+
+/* Evaluates nsys configurations in one set of launches.  small[s] (or NULL for
+ * all 0) allows replication of small cells, pset[s] (or NULL for the current
+ * slot) picks each configuration's parameter set.  energy[nsys], force[sum
+ * natoms][3], stress[nsys][9] are written. */
+int ck_calculate_batch(void *h, int nsys, const int *natoms, const double *pos, const int *types,
+                       const double *cells, const int *small, const int *pset, double *energy, double *force,
+                       double *stress);
+
+/* Split form of ck_calculate_batch: stage copies the inputs to the device,
+ * launch enqueues the list build and force kernels on the handle's stream
+ * (no host synchronisation), collect waits and writes the results.  A
+ * capacity overflow is reported by collect as -5 (call launch again). */
+int ck_stage_batch(void *h, int nsys, const int *natoms, const double *pos, const int *types, const double *cells,
+                   const int *small, const int *pset);
+int ck_launch(void *h);
+int ck_collect(void *h, double *energy, double *force, double *stress);
+/* the handle's cudaStream_t */
+void *ck_stream(void *h);
+
+/* out[5] = pairs, triplets, quadruplets, ghost atoms, atoms of the last evaluation */
+int ck_last_counts(void *h, long long *out);
+/* out[3] = badness (0 good, 1 penalty region, 2 below the inner cutoff), penalty hits, pairs below rin */
+int ck_last_diagnostics(void *h, int *out);
+/* Cluster lists of the last evaluation in each configuration's ghost numbering
+ * (the reference's neighlist_2b/3b/4b order and indices): l2[n2][2] = (atom,
+ * neighbour), l3[n3][3], l4[n4][4].  Sizes from ck_last_counts. */
+int ck_export_lists(void *h, int *l2, int *l3, int *l4);
+
+/* Batched per-cluster evaluation (chimesFF::compute_nB semantics, FP64) with
+ * the handle's current parameter set: n clusters of nbody = 2, 3 or 4 atoms,
+ * dx[n][P] distances, dr[n][P][3] vectors (atom2 - atom1, pairs ij / ij,ik,jk /
+ * ij,ik,il,jk,jl,kl), typ[n][nbody].  Writes force[n][nbody][3], packed
+ * stress[n][6], energy[n] and the reference's force scalars fscal[n][P]
+ * (may be NULL); clusters of excluded types or beyond a cutoff get zeros. */
+int ck_compute_cluster_batch(void *h, int nbody, int n, const double *dx, const double *dr, const int *typ,
+                             double *force, double *stress, double *energy, double *fscal);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

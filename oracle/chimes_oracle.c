@@ -229,7 +229,7 @@ static int parse(ora_handle *h, const char *path) {
                 if (n == 8) { xf = 6; mo = 7; } else if (n == 7) { xf = 5; mo = 6; }
                 else FAIL(h, "pair line: expect 7 or 8 entries");
                 strncpy(ff->pa1[i], tok[1], 15); strncpy(ff->pa2[i], tok[2], 15);
-                snprintf(ff->pname[i], 40, "%s%s", tok[1], tok[2]);
+                snprintf(ff->pname[i], 40, "%.19s%.19s", tok[1], tok[2]);
                 ff->rin[i] = strtod(tok[3], 0); ff->rout[i] = strtod(tok[4], 0);
                 if (strcmp(tok[xf], "MORSE")) FAIL(h, "only the MORSE distance transformation is supported");
                 ff->lam[i] = strtod(tok[mo], 0);
@@ -836,7 +836,7 @@ static int build_lists(ora_handle *h, ora_sys *s, double c2, double c3, double c
     }
     l2_start[s->n_atoms] = h->n2 / 2;
     free(bstart); free(bins);
-    if (h->ff.o3 == 0 && h->ff.o4 == 0) return 0;
+    if (h->ff.o3 == 0 && h->ff.o4 == 0) { h->n2 /= 2; return 0; }
     for (int i = 0; i < s->n_atoms; i++) {
         long b0 = l2_start[i], b1 = l2_start[i + 1];
         for (long j = b0; j < b1; j++) {

@@ -1,0 +1,74 @@
+"""GPU parity against the reference on every golden case: cluster lists
+identical to the reference's (same members, same order), FP64 energies,
+forces and stress within the stated tolerances, and the mixed-precision path
+within its error budget."""
+
+import numpy as np
+import pytest
+
+from conftest import (E_REL_TOL, F_ABS_TOL, MIXED_E_REL_TOL, MIXED_F_ABS_TOL, S_ABS_TOL, golden_names,
+                      list_digest)
+
+pytestmark = pytest.mark.gpu
+
+
+def evaluate(g, precision=0, graph=False, tpc=None):
+    from chimes_calculator_gb300 import Calculator
+    c = Calculator(precision=precision, graph=graph)
+    if tpc:
+        c.set_tuning(*tpc)
+    c.load_params(g.params)
+    r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell, small=g.small)
+    return c, r
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_fp64_matches_reference(golden, native_lib, name):
+    g = golden[name]
+    c, r = evaluate(g)
+    assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
+    assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+    assert np.abs(r["stress"] - g.stress).max() <= S_ABS_TOL
+    l2, l3, l4 = c.lists()
+    for key, arr in (("l2", l2), ("l3", l3), ("l4", l4)):
+        assert arr.shape[0] == g.lists[key]["n"], key
+        assert list_digest(arr) == g.lists[key]["sha256"], key
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_lists_match_oracle(golden, native_lib, name):
+    from oracle.oracle import Oracle
+    g = golden[name]
+    c, _ = evaluate(g)
+    o = Oracle(g.params)
+    o.calculate(g.cfg.pos, g.cfg.types, g.cfg.cell, small=g.small)
+    for a, b in zip(c.lists(), o.lists()):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_mixed_precision_error(golden, native_lib, name):
+    g = golden[name]
+    _, r64 = evaluate(g, precision=0)
+    _, r32 = evaluate(g, precision=1)
+    assert abs(r32["energy"] - r64["energy"]) <= MIXED_E_REL_TOL * max(1.0, abs(r64["energy"]))
+    assert np.abs(r32["force"] - r64["force"]).max() <= MIXED_F_ABS_TOL
+
+
+@pytest.mark.parametrize("tpc", [(1, 1, 2), (2, 4, 4), (8, 16, 4), (32, 32, 2)])
+def test_threads_per_cluster_variants(golden, native_lib, tpc):
+    g = golden["c2_small"]
+    _, r = evaluate(g, tpc=tpc)
+    assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
+    assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+
+
+def test_graph_replay(golden, native_lib):
+    from chimes_calculator_gb300 import Calculator
+    g = golden["c2"]
+    c = Calculator(graph=True)
+    c.load_params(g.params)
+    for _ in range(3):
+        r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell)
+        assert abs(r["energy"] - g.energy) <= E_REL_TOL * abs(g.energy)
+        assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
