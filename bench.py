@@ -1,0 +1,508 @@
+"""Benchmark of the GB300 ChIMES force path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (per GPU): one periodic configuration of 1024 atoms of 2 elements in
+a 22 A cubic box, ChIMES 2B order 12 / 3B order 8 (outer 4.0 A) / 4B order 4
+(outer 3.2 A), Tersoff cutoff, seeded synthetic positions and coefficients --
+the plain FP64 single-configuration workload.  A step is one full evaluation
+(ghost images, cluster lists, Chebyshev stage, contraction, energy/force/virial
+reduction and the copy of the results to pinned host memory).
+
+value : atom-evaluations/s with the inputs resident in HBM, CUDA events on
+        the library's stream around each step, L2 flushed (256 MB write)
+        before every step;
+e2e   : the same metric through the reference-facing C ABI
+        (calculate_chimes_instance) with host arrays, timed on the host.
+Under torchrun each rank runs an independent replica (weak scaling; the path
+has no exchange step, so there is no collective on the data path).
+
+--impl reference times the CPU implementation of the same path (the
+reference build when it can run here, else the oracle's C restatement of it)
+on all host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+N_ATOMS = 1024
+METRIC = "atom-evals/s (E+F+virial), plain FP64 single configuration"
+UNIT = "atom-evals/s"
+WORKLOAD = ("C2: 1024 atoms, 2 elements (50/50), cubic 22.0 A, ChIMES 12/8/4, Tersoff fcut, "
+            "3B outer 4.0 A, 4B outer 3.2 A, plain FP64, one configuration per launch")
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_workload(tmpdir):
+    from chimes_calculator_gb300 import synth
+    params = synth.write_param_file(os.path.join(tmpdir, "c2.params"), synth.spec_c2())
+    cfg = synth.config_c2()
+    return params, cfg
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for ln in open(self.path).read().splitlines():
+            w = [x.strip() for x in ln.split(",")]
+            if len(w) >= 9:
+                rows.append(w)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+# algorithmic work of one evaluation (flop model of the force kernels)
+# ----------------------------------------------------------------------------
+def algorithmic_flops(calc, cfg, params_path):
+    """Per-launch algorithmic FLOPs of the 3B and 4B force kernels:
+        flops(cluster) = P*(6*o + 15) + n_c*(5*P + 1) + P*21
+    over the clusters that pass the per-type outer cutoffs (exp/sin/cos count
+    as one flop).  Cluster geometry is rebuilt here from the exported lists."""
+    from chimes_calculator_gb300 import synth  # noqa: F401
+    info = calc.info(0)
+    o2, o3, o4 = info["orders"]
+    l2, l3, l4 = calc.lists()
+    cell = np.asarray(cfg.cell, dtype=np.float64)
+    inv = np.linalg.inv(cell)
+    f = cfg.pos @ inv
+    f -= np.floor(f)
+    n = cfg.n_atoms
+    maxc = max(info["max_cutoffs"])
+    L = np.linalg.norm(cell, axis=1).min()
+    nl = int(math.ceil(2 * info["max_cutoffs"][0] / L + 1))
+    side = 2 * nl + 1
+
+    def ghost_pos(g):
+        img = g // n
+        a = g % n
+        full = img - 1
+        center = (nl * side + nl) * side + nl
+        full = np.where(full >= center, full + 1, full)
+        sh = np.stack([full // (side * side) - nl, (full // side) % side - nl, full % side - nl], axis=-1)
+        sh = np.where((img == 0)[..., None], 0, sh)
+        return (f[a] + sh) @ cell
+
+    tup = calc.tuple_table(0)
+    out = {}
+    for nb, lst, order in ((3, l3, o3), (4, l4, o4)):
+        if lst.shape[0] == 0 or order == 0:
+            out[nb] = (0, 0.0)
+            continue
+        P = nb * (nb - 1) // 2
+        pairs = [(i, j) for i in range(nb) for j in range(i + 1, nb)]
+        pos = ghost_pos(lst)
+        r = np.stack([np.linalg.norm(pos[:, b] - pos[:, a], axis=1) for a, b in pairs], axis=1)
+        t = np.asarray(cfg_types_idx(calc, cfg))[lst % n]
+        u = np.zeros(lst.shape[0], dtype=np.int64)
+        nt = info["ntypes"]
+        for k in range(nb):
+            u = u * nt + t[:, k]
+        valid, ncoef, rout = tup[nb]
+        ok = valid[u].astype(bool) & np.all(r < rout[u][:, :P], axis=1)
+        nc = ncoef[u][ok].astype(np.float64)
+        flops = ok.sum() * (P * (6 * order + 15) + P * 21) + (nc * (5 * P + 1)).sum()
+        out[nb] = (int(ok.sum()), float(flops))
+    del maxc
+    return out
+
+
+_type_cache = {}
+
+
+def cfg_types_idx(calc, cfg):
+    key = id(cfg)
+    if key not in _type_cache:
+        _type_cache[key] = calc.type_indices(cfg.types, 0)
+    return _type_cache[key]
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    from chimes_calculator_gb300 import FP64, Calculator, _lib
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    tmp = tempfile.mkdtemp(prefix="ckbench")
+    params, cfg = make_workload(tmp)
+    calc = Calculator(precision=args.precision, graph=True)
+    calc.load_params(params)
+    packed = calc.pack([(cfg.pos, cfg.types, cfg.cell)])
+    calc.stage(packed)
+    stream = torch.cuda.ExternalStream(calc.stream_ptr(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def one_step():
+        calc.launch()
+
+    # warm-up (also sizes the capacities and captures the graph)
+    for _ in range(max(3, args.warmup)):
+        one_step()
+        e, fo, so = calc.collect()
+    # correctness of the timed configuration against the committed reference output
+    check = None
+    gpath = os.path.join(REPO, "tests", "golden", "c2", "expected.json")
+    if os.path.exists(gpath):
+        g = json.load(open(gpath))
+        ge = float(g["energy"])
+        gf = np.array([[float(v) for v in r] for r in g["force"]])
+        check = {"dE_rel": abs(e[0] - ge) / abs(ge), "dF_max": float(np.abs(fo - gf).max()),
+                 "reference_energy": ge}
+
+    lib = _lib.load()
+    lib.ck_set_profiling(calc.h, 1)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    stage_ms = (ctypes.c_double * 4)()
+    nlaunch = ctypes.c_longlong()
+    kpl = ctypes.c_int()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))          # evict L2 (256 MB > 129 MB) before every step
+            starts[k].record(stream)
+        one_step()
+        ends[k].record(stream)
+        lib.ck_read_stage_times(calc.h, stage_ms, ctypes.byref(nlaunch), ctypes.byref(kpl))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    calc.collect()
+    from chimes_calculator_gb300.replicas import job_time_and_throughput
+    total_ms, value = job_time_and_throughput(sum(step_ms), N_ATOMS, args.steps)
+    if world > 1:
+        torch.distributed.barrier()
+    ms_per_step = total_ms / args.steps
+
+    # roofline of the dominant kernel (from the in-library stage events)
+    stage = [stage_ms[k] / max(1, nlaunch.value) for k in range(4)]
+    names = ["list build", "force 1B+2B", "force 3B", "force 4B"]
+    counts = calc.counts()
+    work = algorithmic_flops(calc, cfg, params)
+    peak64 = ctypes.c_double()
+    lib.ck_fma_peak(0, ctypes.byref(peak64))
+    dom = int(np.argmax(stage))
+    roof = None
+    if dom in (2, 3):
+        nb = 3 if dom == 2 else 4
+        achieved = work[nb][1] / (stage[dom] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": "k_forcen<%d,double>" % nb, "achieved": achieved,
+                "peak": peak64.value, "unit": "TFLOP/s", "frac": achieved / peak64.value,
+                "traffic": None, "peak_source": "measured in-run FP64 FMA probe (ck_fma_peak); "
+                "MEASURED_PEAKS.json has no CUDA-core FP64 figure",
+                "flops_per_launch": work[nb][1], "clusters_evaluated": work[nb][0],
+                "kernel_ms": stage[dom]}
+    else:
+        roof = {"bound": "hbm", "kernel": names[dom], "achieved": None, "peak": None, "unit": "GB/s",
+                "frac": None, "traffic": None}
+
+    # end to end through the reference-facing C ABI with host buffers
+    e2e = None
+    if not args.profile_run:
+        lib.ck_set_error_mode(1)
+        h = lib.chimes_open_instance()
+        lib.set_chimes_serial_instance(h, 0)
+        lib.init_chimes_serial_instance(h, params.encode(), 0)
+        n = cfg.n_atoms
+        arr = lambda v: (ctypes.c_double * len(v))(*v)
+        x, y, z = (arr(cfg.pos[:, k]) for k in range(3))
+        ty = (ctypes.c_char_p * n)(*[t.encode() for t in cfg.types])
+        ca, cb, cc = (arr(cfg.cell[k]) for k in range(3))
+        fx, fy, fz, st = arr([0.0] * n), arr([0.0] * n), arr([0.0] * n), arr([0.0] * 9)
+        en = ctypes.c_double(0.0)
+        for _ in range(3):
+            lib.calculate_chimes_instance(h, n, x, y, z, ty, ca, cb, cc, ctypes.byref(en), fx, fy, fz, st)
+        reps = max(20, min(200, args.steps))
+        ts = []
+        for _ in range(reps):
+            en.value = 0.0
+            a = time.perf_counter()
+            lib.calculate_chimes_instance(h, n, x, y, z, ty, ca, cb, cc, ctypes.byref(en), fx, fy, fz, st)
+            ts.append(time.perf_counter() - a)
+        err = lib.ck_last_error().decode()
+        lib.chimes_close_instance(h)
+        sec = sum(ts) / len(ts)
+        e2e = {"value": world * n / sec, "unit": UNIT, "h2d_bytes_per_step": n * 24 + n * 4 + 1024,
+               "d2h_bytes_per_step": n * 24 + 8 * 8 + 8 * 4 + 3 * 8, "ms_per_call": sec * 1e3,
+               "p50_ms": 1e3 * statistics.median(ts), "p99_ms": 1e3 * float(np.percentile(ts, 99)),
+               "api": "calculate_chimes_instance", "error": err or None}
+
+    # CPU baseline: the oracle's C restatement of the reference path on one host core
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(params, cfg, seconds=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": counts["n2"], "triplets": counts["n3"],
+                       "quadruplets": counts["n4"], "ghost_atoms": counts["n_ghost"],
+                       "l2_flush": "256 MB write before every timed step", "graph": True,
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": e2e,
+            "roofline": roof,
+            "stage_ms": dict(zip(names, stage)),
+            "gpu_launches": kpl.value * args.steps,
+            "kernels_per_step": kpl.value,
+            "clocks": clk,
+            "wall_s_timed_region": wall,
+            "cpu_baseline": cpu,
+            "check": check,
+        }
+        if args.extras:
+            ex = extras(args)
+            ex["batched_mixed_over_plain_fp64"] = ex["batched_mixed"]["value"] / (value / world)
+            line["extras"] = ex
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def extras(args):
+    """Other paths on the same GPU, for context (not the headline): the mixed
+    path on the same configuration, and batched FP64 / mixed evaluation of the
+    mixed-size workload (configurations of 8-512 atoms)."""
+    from chimes_calculator_gb300 import FP64, MIXED, Calculator, synth
+    out = {}
+    tmp = tempfile.mkdtemp(prefix="ckx")
+    params, cfg = make_workload(tmp)
+    for prec, name in ((MIXED, "c2_mixed"),):
+        c = Calculator(precision=prec, graph=True)
+        c.load_params(params)
+        c.stage(c.pack([(cfg.pos, cfg.types, cfg.cell)]))
+        out[name] = time_steps(c, N_ATOMS, 50)
+    p4 = synth.write_param_file(os.path.join(tmp, "c4.params"), synth.spec_c4())
+    cfgs = synth.configs_c4(n_configs=args.batch_configs)
+    atoms = sum(c.n_atoms for c in cfgs)
+    for prec, name in ((FP64, "batched_fp64"), (MIXED, "batched_mixed")):
+        c = Calculator(precision=prec, graph=True)
+        c.load_params(p4)
+        c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
+        r = time_steps(c, atoms, 3)
+        r["configs"] = len(cfgs)
+        out[name] = r
+    return out
+
+
+def time_steps(c, atoms, steps):
+    import torch
+    stream = torch.cuda.ExternalStream(c.stream_ptr())
+    for _ in range(3):
+        c.launch()
+        c.collect()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record(stream)
+        c.launch()
+        b.record(stream)
+    torch.cuda.synchronize()
+    c.collect()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    return {"value": atoms / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "counts": c.counts()}
+
+
+# ----------------------------------------------------------------------------
+# CPU paths (the oracle is the checker and the CPU baseline only)
+# ----------------------------------------------------------------------------
+def _cpu_worker(job):
+    params, xyz, reps = job
+    sys.path.insert(0, REPO)
+    from chimes_calculator_gb300 import synth
+    from oracle.oracle import Oracle
+    cfg = synth.read_xyz(xyz)
+    o = Oracle(params)
+    o.calculate(cfg.pos, cfg.types, cfg.cell)     # load + first call
+    ts = []
+    for _ in range(reps):
+        a = time.perf_counter()
+        o.calculate(cfg.pos, cfg.types, cfg.cell)
+        ts.append(time.perf_counter() - a)
+    return ts
+
+
+def cpu_kind():
+    ref = os.path.join(REPO, "oracle", "_ref", "ref_driver")
+    if os.path.exists(ref) and os.access(ref, os.X_OK):
+        try:
+            subprocess.run([ref], capture_output=True, timeout=10)
+            return "reference", ref
+        except Exception:
+            pass
+    return "port", None
+
+
+def cpu_baseline(params, cfg, seconds=10.0):
+    from oracle.oracle import build_port
+    build_port()
+    tmp = tempfile.mkdtemp(prefix="ckcpu")
+    xyz = cfg.write_xyz(os.path.join(tmp, "c2.xyz"))
+    kind, ref = cpu_kind()
+    if kind == "reference":
+        from oracle.oracle import run_reference
+        t0 = time.perf_counter()
+        _, _, tm = run_reference(params, xyz, False, os.path.join(tmp, "r"), time_reps=3)
+        sec = tm["best_s"]
+        reps = 3
+    else:
+        t0 = time.perf_counter()
+        ts = _cpu_worker((params, xyz, 1))
+        reps = max(2, min(50, int(seconds / max(ts[0], 1e-3))))
+        ts = _cpu_worker((params, xyz, reps))
+        sec = statistics.median(ts)
+    import platform
+    return {"value": N_ATOMS / sec, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": "%d evaluations of the full 1024-atom workload on one core (median %.3f s each); %s" % (
+                reps, sec, platform.processor() or platform.machine()),
+            "wall_s": time.perf_counter() - t0}
+
+
+def run_reference_arm(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    tmp = tempfile.mkdtemp(prefix="ckref")
+    params, cfg = make_workload(tmp)
+    xyz = cfg.write_xyz(os.path.join(tmp, "c2.xyz"))
+    kind, _ = cpu_kind()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    from oracle.oracle import build_port
+    build_port()
+    # bounded sample: every core evaluates the workload once per step; the number
+    # of timed steps is capped so the run ends within a few minutes
+    with ctx.Pool(cores) as pool:
+        t = time.perf_counter()
+        pool.map(_cpu_worker, [(params, xyz, 1)] * cores)
+        one = (time.perf_counter() - t) / 2.0
+        steps = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
+        warm = min(args.warmup, 1)
+        for _ in range(warm):
+            pool.map(_cpu_worker, [(params, xyz, 1)] * cores)
+        t0 = time.perf_counter()
+        per = pool.map(_cpu_worker, [(params, xyz, steps)] * cores)
+        wall = time.perf_counter() - t0
+    evals = cores * steps
+    sec_per_eval = statistics.median([x for ts in per for x in ts])
+    value = cores * N_ATOMS / sec_per_eval
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * sec_per_eval, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "parallelism": "%d independent processes" % cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": "%d evaluations (%d per core) of the 1024-atom workload, %s; wall %.1f s" % (
+                                 evals, steps, "oracle C restatement of the reference path (the reference "
+                                 "sources are not on this machine)" if kind == "port" else "reference build",
+                                 wall)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--extras", action="store_true", help="also time the mixed and batched paths")
+    ap.add_argument("--batch-configs", type=int, default=4096)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--precision", type=int, default=0, help="0 FP64 (headline), 1 mixed")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="minimal run for a profiler: 3 warm-up + 2 steps, no e2e / CPU legs")
+    args = ap.parse_args()
+    if args.profile_run:
+        args.steps, args.warmup, args.no_cpu, args.extras = 2, 3, True, False
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -60,6 +60,7 @@ SIGNATURES = {
     "ck_check_params": (I, [S, IP, IP, DP]),
     "ck_param_info": (I, [P, I, IP, IP, DP]),
     "ck_type_index": (I, [P, I, S]),
+    "ck_tuple_table": (I, [P, I, I, IP, IP, DP]),
     "ck_set_precision": (I, [P, I]),
     "ck_set_tuning": (I, [P, I, I, I]),
     "ck_use_graph": (I, [P, I]),
@@ -69,6 +70,9 @@ SIGNATURES = {
     "ck_collect": (I, [P, DP, DP, DP]),
     "ck_stream": (P, [P]),
     "ck_last_counts": (I, [P, LLP]),
+    "ck_set_profiling": (I, [P, I]),
+    "ck_fma_peak": (I, [I, DP]),
+    "ck_read_stage_times": (I, [P, DP, LLP, IP]),
     "ck_last_diagnostics": (I, [P, IP]),
     "ck_export_lists": (I, [P, IP, IP, IP]),
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),

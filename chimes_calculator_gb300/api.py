@@ -75,6 +75,19 @@ class Calculator:
         self._check(self.lib.ck_param_info(self.h, slot, orders, ctypes.byref(nt), cuts))
         return {"orders": tuple(orders), "ntypes": nt.value, "max_cutoffs": tuple(cuts)}
 
+    def tuple_table(self, slot: int = 0):
+        """{nbody: (valid[nt^nbody], ncoef[...], rout[..., 6])} of a parameter set."""
+        nt = self.info(slot)["ntypes"]
+        out = {}
+        for nb in (3, 4):
+            n = nt ** nb
+            valid = np.zeros(n, dtype=np.int32)
+            ncoef = np.zeros(n, dtype=np.int32)
+            rout = np.zeros((n, 6))
+            self._check(self.lib.ck_tuple_table(self.h, slot, nb, _ip(valid), _ip(ncoef), _dp(rout)))
+            out[nb] = (valid, ncoef, rout)
+        return out
+
     def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
         cache = self._types[slot]
         out = np.empty(len(types), dtype=np.int32)

@@ -229,6 +229,26 @@ int ck_param_info(void* h, int slot, int* orders, int* ntypes, double* maxcuts) 
     return ck::kOk;
 }
 
+int ck_tuple_table(void* h, int slot, int nbody, int* valid, int* ncoef, double* rout) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    if (nbody != 3 && nbody != 4) return report(ck::kErrInput, "nbody must be 3 or 4");
+    const ck::HostParams& P = in->eng.params(slot);
+    const ck::HostParams::Body& B = nbody == 3 ? P.b3 : P.b4;
+    const int order = nbody == 3 ? P.o3 : P.o4;
+    int ntup = 1;
+    for (int k = 0; k < nbody; k++) ntup *= P.ntypes;
+    for (int u = 0; u < ntup; u++) {
+        const int ti = order > 0 ? B.map[u] : -1;
+        valid[u] = ti >= 0 && B.ncoef[ti] > 0 ? 1 : 0;
+        ncoef[u] = ti >= 0 ? B.ncoef[ti] : 0;
+        for (int p = 0; p < 6; p++)
+            rout[6 * u + p] = (ti >= 0 && p < B.npair) ? B.cut_out[ti][B.perm[u][p]] : 0.0;
+    }
+    return ck::kOk;
+}
+
 int ck_type_index(void* h, int slot, const char* name) {
     if (int st = check_handle(h)) return st;
     Instance* in = static_cast<Instance*>(h);
@@ -349,6 +369,34 @@ int ck_last_counts(void* h, long long* out) {
     if (int st = check_handle(h)) return st;
     const ck::RunStats& s = static_cast<Instance*>(h)->eng.last;
     out[0] = s.n2; out[1] = s.n3; out[2] = s.n4; out[3] = s.n_ghost; out[4] = s.n_atoms;
+    return ck::kOk;
+}
+
+int ck_fma_peak(int precision, double* tflops) {
+    double t = ck::fma_peak_tflops(precision);
+    if (tflops) *tflops = t;
+    if (t <= 0) return report(ck::kErrCuda, "FMA probe failed");
+    return ck::kOk;
+}
+
+int ck_set_profiling(void* h, int on) {
+    if (int st = check_handle(h)) return st;
+    ck::Engine& e = static_cast<Instance*>(h)->eng;
+    e.profile = on != 0;
+    for (double& v : e.stage_ms) v = 0.0;
+    e.stage_launches = 0;
+    return ck::kOk;
+}
+
+int ck_read_stage_times(void* h, double* ms, long long* launches, int* kernels_per_launch) {
+    if (int st = check_handle(h)) return st;
+    ck::Engine& e = static_cast<Instance*>(h)->eng;
+    std::string err;
+    ck::Status st = e.read_stage_times(err);
+    if (st != ck::kOk) return report(st, err);
+    if (ms) for (int k = 0; k < 4; k++) ms[k] = e.stage_ms[k];
+    if (launches) *launches = e.stage_launches;
+    if (kernels_per_launch) *kernels_per_launch = e.kernels_per_launch;
     return ck::kOk;
 }
 

@@ -172,9 +172,9 @@ void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, con
                    double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st) {
     if (n <= 0) return;
     const unsigned grid = (unsigned)((n + 63) / 64);
-    if (nbody == 2) k_direct2<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
-    else if (nbody == 3) k_directn<3><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
-    else k_directn<4><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    if (nbody == 2) count_launch(), k_direct2<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    else if (nbody == 3) count_launch(), k_directn<3><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    else count_launch(), k_directn<4><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
 }
 
 }  // namespace ck

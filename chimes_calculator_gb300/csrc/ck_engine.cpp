@@ -39,6 +39,8 @@ Engine::Engine() {}
 
 Engine::~Engine() {
     drop_graph();
+    for (auto& e : ev_)
+        if (e) cudaEventDestroy(e);
     for (auto& s : sets_)
         if (s.dev) cudaFree(s.dev);
     if (stream_) cudaStreamDestroy(stream_);
@@ -253,6 +255,12 @@ Status Engine::ensure_lists(std::string& err) {
 Status Engine::enqueue(std::string& err) {
     const BatchView& B = V_;
     cudaStream_t st = stream_;
+    const long long k0 = launch_counter();
+    if (profile) {
+        for (auto& e : ev_)
+            if (!e) CK_TRY(cudaEventCreate(&e));
+        CK_TRY(cudaEventRecordWithFlags(ev_[0], st, cudaEventRecordExternal));
+    }
     CK_TRY(cudaMemsetAsync(B.bin_count, 0, sizeof(int) * B.n_bins_total, st));
     CK_TRY(cudaMemsetAsync(B.bin_fill, 0, sizeof(int) * B.n_bins_total, st));
     launch_reset(B, st);
@@ -271,11 +279,17 @@ Status Engine::enqueue(std::string& err) {
     exclusive_scan(B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
     launch_enum(B, d_l2_owner_.p, true, st);
     launch_check(B, st);
+    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[1], st, cudaEventRecordExternal));
     ForceLaunch L = tuning;
     L.precision = precision;
     launch_force2(B, d_l2_owner_.p, L, st);
+    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[2], st, cudaEventRecordExternal));
     if (L.stride3 > 0) launch_force3(B, L, st);
+    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[3], st, cudaEventRecordExternal));
     if (L.stride4 > 0) launch_force4(B, L, st);
+    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[4], st, cudaEventRecordExternal));
+    ev_recorded_ = profile;
+    kernels_per_launch = (int)(launch_counter() - k0);
     CK_TRY(cudaMemcpyAsync(h_force_.p, B.force, sizeof(double) * 3 * B.n_in_total, cudaMemcpyDeviceToHost, st));
     CK_TRY(cudaMemcpyAsync(h_ev_.p, B.ev, sizeof(double) * 8 * B.n_sys, cudaMemcpyDeviceToHost, st));
     CK_TRY(cudaMemcpyAsync(h_flags_.p, B.flags, sizeof(int) * 8, cudaMemcpyDeviceToHost, st));
@@ -283,6 +297,18 @@ Status Engine::enqueue(std::string& err) {
     CK_TRY(cudaMemcpyAsync(h_counts_.p + 1, B.e_off3 + B.n2_cap, sizeof(long long), cudaMemcpyDeviceToHost, st));
     CK_TRY(cudaMemcpyAsync(h_counts_.p + 2, B.e_off4 + B.n2_cap, sizeof(long long), cudaMemcpyDeviceToHost, st));
     CK_TRY(cudaGetLastError());
+    return kOk;
+}
+
+Status Engine::read_stage_times(std::string& err) {
+    if (!ev_recorded_) return kOk;
+    CK_TRY(cudaEventSynchronize(ev_[4]));
+    for (int k = 0; k < 4; k++) {
+        float ms = 0.f;
+        CK_TRY(cudaEventElapsedTime(&ms, ev_[k], ev_[k + 1]));
+        stage_ms[k] += ms;
+    }
+    stage_launches++;
     return kOk;
 }
 
@@ -294,7 +320,7 @@ Status Engine::launch(std::string& err) {
     if (!use_graph) return enqueue(err);
     std::vector<long long> key = {(long long)V_.n_sys, V_.n_in_total, V_.n_atoms_total, V_.n_ghost_total,
                                   V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
-                                  tuning.stride3, tuning.stride4, tuning.blocks_per_sm};
+                                  tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,

@@ -106,6 +106,14 @@ public:
     bool use_graph = false;
     RunStats last;
 
+    // Stage timing: CUDA events recorded on the engine's stream between the
+    // list build, the 1B+2B, 3B and 4B force kernels, accumulated over launches.
+    bool profile = false;
+    double stage_ms[4] = {0, 0, 0, 0};   // list build, 2B, 3B, 4B
+    long long stage_launches = 0;
+    int kernels_per_launch = 0;          // kernels one launch() enqueues
+    Status read_stage_times(std::string& err);   // adds the last launch's event intervals
+
     // Per-cluster evaluation (the chimesFF::compute_nB entry points): n
     // clusters of `nbody` atoms given as distances dx[n][P], displacement
     // vectors dr[n][P][3] (atom2 - atom1) and type indices typ[n][nbody].
@@ -168,6 +176,8 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     std::vector<long long> graph_key_;
+    cudaEvent_t ev_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool ev_recorded_ = false;
 
     Status ensure_lists(std::string& err);
     Status enqueue(std::string& err);

@@ -333,7 +333,7 @@ void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, l
     do {                                                                                       \
         auto kern = k_forcen<NB, CT, T_>;                                                      \
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        kern<<<grid, block, smem, st>>>(B, clusters, n_ptr, n, stride);                               \
+        count_launch(), kern<<<grid, block, smem, st>>>(B, clusters, n_ptr, n, stride);                               \
     } while (0)
     switch (tpc) {
         case 1: CK_LAUNCH(1); break;
@@ -346,7 +346,52 @@ void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, l
 #undef CK_LAUNCH
 }
 
+// Throughput probe for the roofline denominator: 8 independent FMA chains per
+// thread over every SM; the result is only stored if it hits an impossible
+// value, which keeps the chains live.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_probe(T* out, int iters, T b, T c) {
+    T a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = T(threadIdx.x + k) * T(1e-3);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = fma(a[k], b, c);
+    }
+    T s = a[0] + a[1] + a[2] + a[3] + a[4] + a[5] + a[6] + a[7];
+    if (s == T(-1.2345e-7)) out[0] = s;
+}
+
 }  // namespace
+
+double fma_peak_tflops(int precision) {
+    const int blocks = sm_count() * 8, threads = 256;
+    const int iters = precision == kMixed ? 1 << 16 : 1 << 12;
+    void* out = nullptr;
+    if (cudaMalloc(&out, 16) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(e0);
+        if (precision == kMixed)
+            count_launch(), k_fma_probe<float><<<blocks, threads>>>((float*)out, iters, 1.0000001f, 1e-7f);
+        else
+            count_launch(), k_fma_probe<double><<<blocks, threads>>>((double*)out, iters, 1.0000000001, 1e-12);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return -1.0;
+    const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    return flops / (best * 1e-3) / 1e12;
+}
 
 int sm_count() {
     static int n = 0;
@@ -366,8 +411,8 @@ void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L
     long long want = (long long)sm_count() * 8;
     long long need = (ntot + 255) / 256;
     const unsigned grid = (unsigned)(want < need ? want : need);
-    if (L.precision == kMixed) k_force2<float><<<grid, 256, 0, st>>>(B, l2_owner);
-    else k_force2<double><<<grid, 256, 0, st>>>(B, l2_owner);
+    if (L.precision == kMixed) count_launch(), k_force2<float><<<grid, 256, 0, st>>>(B, l2_owner);
+    else count_launch(), k_force2<double><<<grid, 256, 0, st>>>(B, l2_owner);
 }
 
 void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {

@@ -51,4 +51,12 @@ void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, con
 
 int sm_count();
 
+// Measured CUDA-core FMA throughput (TFLOP/s) in FP64 (precision 0) or FP32 (1).
+double fma_peak_tflops(int precision);
+
+// Host-side count of kernel launches enqueued by the launchers above (for
+// reporting how many of the library's kernels one evaluation runs).
+void count_launch();
+long long launch_counter();
+
 }  // namespace ck

@@ -472,16 +472,20 @@ void scan_rec(const int* in, const long long* in64, long long* out, long long n,
     const long long nb = (n + kScanBlock - 1) / kScanBlock;
     long long* sums = tmp;
     long long* sums_scan = tmp + nb;
-    k_scan_block<<<(unsigned)nb, kScanBlock, 0, st>>>(in, in64, out, n, sums);
+    count_launch(), k_scan_block<<<(unsigned)nb, kScanBlock, 0, st>>>(in, in64, out, n, sums);
     if (nb > 1) {
         scan_rec(nullptr, sums, sums_scan, nb, tmp + 2 * nb, st);
-        k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, sums_scan);
+        count_launch(), k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(out, n, sums_scan);
     }
 }
 
 unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
+
+static long long g_launches = 0;
+void count_launch() { g_launches++; }
+long long launch_counter() { return g_launches; }
 
 size_t scan_tmp_bytes(long long n) {
     size_t total = 0;
@@ -496,47 +500,47 @@ size_t scan_tmp_bytes(long long n) {
 
 void exclusive_scan(const int* in, long long* out, long long n, void* tmp, cudaStream_t st) {
     scan_rec(in, nullptr, out, n, (long long*)tmp, st);
-    k_scan_total<<<1, 1, 0, st>>>(out, n, in, nullptr);
+    count_launch(), k_scan_total<<<1, 1, 0, st>>>(out, n, in, nullptr);
 }
 
 void launch_atoms(const BatchView& B, cudaStream_t st) {
-    if (B.n_atoms_total) k_atoms<<<grid_for(B.n_atoms_total, 256), 256, 0, st>>>(B);
+    if (B.n_atoms_total) count_launch(), k_atoms<<<grid_for(B.n_atoms_total, 256), 256, 0, st>>>(B);
 }
 void launch_ghosts(const BatchView& B, cudaStream_t st) {
-    if (B.n_ghost_total) k_ghosts<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B);
+    if (B.n_ghost_total) count_launch(), k_ghosts<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B);
 }
 void launch_bin_setup(const BatchView& B, cudaStream_t st) {
-    k_bin_setup<<<grid_for(B.n_sys, 128), 128, 0, st>>>(B);
+    count_launch(), k_bin_setup<<<grid_for(B.n_sys, 128), 128, 0, st>>>(B);
 }
 void launch_bin_count(const BatchView& B, cudaStream_t st) {
-    if (B.n_ghost_total) k_bin_count<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B);
+    if (B.n_ghost_total) count_launch(), k_bin_count<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B);
 }
 void launch_bin_scatter(const BatchView& B, cudaStream_t st) {
-    if (B.n_ghost_total) k_bin_scatter<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B, B.bin_start);
+    if (B.n_ghost_total) count_launch(), k_bin_scatter<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B, B.bin_start);
 }
 void launch_bin_sort(const BatchView& B, cudaStream_t st) {
-    if (B.n_bins_total) k_bin_sort<<<grid_for(B.n_bins_total, 128), 128, 0, st>>>(B, B.bin_start);
+    if (B.n_bins_total) count_launch(), k_bin_sort<<<grid_for(B.n_bins_total, 128), 128, 0, st>>>(B, B.bin_start);
 }
 void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n_atoms_total) return;
     const unsigned grid = grid_for(B.n_atoms_total * 32, 256);
-    if (fill) k_l2<true><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
-    else k_l2<false><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
+    if (fill) count_launch(), k_l2<true><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
+    else count_launch(), k_l2<false><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
 }
 void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n2_cap) return;
     long long want = (long long)sm_count() * 16;
     long long need = (B.n2_cap + 127) / 128;
     const unsigned grid = (unsigned)(want < need ? want : need);
-    if (fill) k_enum<true><<<grid, 128, 0, st>>>(B, l2_owner);
-    else k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
+    if (fill) count_launch(), k_enum<true><<<grid, 128, 0, st>>>(B, l2_owner);
+    else count_launch(), k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
 }
-void launch_check(const BatchView& B, cudaStream_t st) { k_check<<<1, 1, 0, st>>>(B); }
+void launch_check(const BatchView& B, cudaStream_t st) { count_launch(), k_check<<<1, 1, 0, st>>>(B); }
 void launch_reset(const BatchView& B, cudaStream_t st) {
     long long n = 8LL * B.n_sys;
     if (3 * B.n_in_total > n) n = 3 * B.n_in_total;
     if (n < 8) n = 8;
-    k_reset<<<grid_for(n, 256), 256, 0, st>>>(B);
+    count_launch(), k_reset<<<grid_for(n, 256), 256, 0, st>>>(B);
 }
 
 }  // namespace ck

@@ -45,6 +45,10 @@ int ck_select_params(void *h, int slot);
 int ck_check_params(const char *path, int *orders, int *ntypes, double *maxcuts);
 /* orders[3] = 2B/3B/4B orders, *ntypes, maxcuts[3] = max outer cutoffs. */
 int ck_param_info(void *h, int slot, int *orders, int *ntypes, double *maxcuts);
+/* Per ordered atom-type tuple u (nbody = 3: nt^3 entries, 4: nt^4) of a slot:
+ * valid[u] (an included type with coefficients), ncoef[u] and rout[u][6], the
+ * outer cutoffs in the cluster's own pair order. */
+int ck_tuple_table(void *h, int slot, int nbody, int *valid, int *ncoef, double *rout);
 /* index of an atom type name in a slot, or -1 */
 int ck_type_index(void *h, int slot, const char *name);
 
@@ -74,6 +78,17 @@ int ck_launch(void *h);
 int ck_collect(void *h, double *energy, double *force, double *stress);
 /* the handle's cudaStream_t */
 void *ck_stream(void *h);
+
+/* Stage timing with CUDA events recorded on the handle's stream around the
+ * list build, the 1B+2B, 3B and 4B force kernels.  ck_set_profiling(h, 1)
+ * enables and resets it; after each launch ck_read_stage_times waits for the
+ * events and adds the intervals: ms[4] (accumulated milliseconds), the number
+ * of launches accumulated, and the kernels one launch enqueues. */
+int ck_set_profiling(void *h, int on);
+/* Measured CUDA-core FMA throughput of this GPU in TFLOP/s, FP64 (precision 0)
+ * or FP32 (1): the roofline denominator of the force kernels. */
+int ck_fma_peak(int precision, double *tflops);
+int ck_read_stage_times(void *h, double *ms, long long *launches, int *kernels_per_launch);
 
 /* out[5] = pairs, triplets, quadruplets, ghost atoms, atoms of the last evaluation */
 int ck_last_counts(void *h, long long *out);

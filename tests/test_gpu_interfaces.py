@@ -65,17 +65,19 @@ def _clusters_from(g, nb, count, rng):
     inv = np.linalg.inv(cell)
     out = []
     pairs = [(i, j) for i in range(nb) for j in range(i + 1, nb)]
+    reach = {2: 5.5, 3: 4.2, 4: 3.3}[nb]
     while len(out) < count:
-        ids = rng.choice(len(pos), size=nb, replace=False)
-        p = [pos[ids[0]]]
-        for k in ids[1:]:
-            d = (pos[k] - pos[ids[0]]) @ inv
-            d -= np.round(d)
-            p.append(pos[ids[0]] + d @ cell)
+        i0 = int(rng.integers(len(pos)))
+        d = (pos - pos[i0]) @ inv
+        d -= np.round(d)
+        r = np.sqrt(((d @ cell) ** 2).sum(1))
+        near = np.where((r > 0) & (r < reach))[0]
+        if len(near) < nb - 1:
+            continue
+        ids = np.concatenate([[i0], rng.choice(near, size=nb - 1, replace=False)])
+        p = [pos[i0] + d[k] @ cell for k in ids]
         dr = np.array([p[j] - p[i] for i, j in pairs])
         dx = np.sqrt((dr ** 2).sum(1))
-        if dx.max() > 6.0:
-            continue
         out.append((dx, dr, ids))
     return out
 
@@ -129,7 +131,7 @@ def test_per_cluster_c_interface(golden, native_lib):
     for dx, dr, ids in cl:
         names = [g.cfg.types[i] for i in ids]
         f = (ctypes.c_double * 9)(); st = arr([1.0] * 9); e = ctypes.c_double(5.0)
-        dist = ((ctypes.c_double * 3) * 3)(*[(ctypes.c_double * 3)(*row) for row in dr])
+        dist = ctypes.cast(arr(dr.reshape(-1)), ctypes.POINTER(ctypes.c_double))
         lib.chimes_compute_3b_props(arr(dx), dist, (ctypes.c_char_p * 3)(*[n.encode() for n in names]), f, st,
                                     ctypes.byref(e))
         fo = np.zeros(9); so = np.zeros(6)
