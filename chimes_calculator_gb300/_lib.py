@@ -76,6 +76,7 @@ SIGNATURES = {
     "ck_last_diagnostics": (I, [P, IP]),
     "ck_export_lists": (I, [P, IP, IP, IP]),
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
+    "ck_calculate_noalloc": (I, [P, I, P, P, DP, I, P, P, P, P]),
 }
 
 

@@ -372,6 +372,19 @@ int ck_last_counts(void* h, long long* out) {
     return ck::kOk;
 }
 
+int ck_calculate_noalloc(void* h, int natom, const double* d_pos, const int* d_types, const double* cell,
+                         int small, double* d_energy, double* d_force, double* d_stress, void* stream) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    std::string err;
+    ck::Status st = ck::calculate_noalloc(in->eng, in->slot, natom, d_pos, d_types, cell, small != 0, d_energy,
+                                          d_force, d_stress, static_cast<cudaStream_t>(stream), err);
+    if (st != ck::kOk) return report(st, err);
+    g_err.clear();
+    return ck::kOk;
+}
+
 int ck_fma_peak(int precision, double* tflops) {
     double t = ck::fma_peak_tflops(precision);
     if (tflops) *tflops = t;

@@ -89,6 +89,7 @@ public:
     int load_params(const std::string& path, std::string& err);
     const HostParams& params(int slot) const { return *sets_[slot].host; }
     int n_param_sets() const { return (int)sets_.size(); }
+    const DevParamSet* device_params() const { return dsets_.p; }   // device array, by slot
 
     // Full evaluation of a batch: stage + launch + collect, retrying on capacity growth.
     // force_out: [sum n][3], zeroed and filled (not accumulated).
@@ -185,6 +186,13 @@ private:
 };
 
 const char* status_name(int s);
+
+// One configuration evaluated with every intermediate array in a static
+// device array instead of allocated memory (ck_noalloc.cu); inputs and
+// outputs are the caller's device buffers.  Synchronises `st` before returning.
+Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, const int* d_types,
+                         const double* cell, bool small, double* d_energy, double* d_force, double* d_stress,
+                         cudaStream_t st, std::string& err);
 
 // Error reporting of the public interfaces: records the message for
 // ck_last_error() and, in the default (reference) mode, prints it on stdout

@@ -99,6 +99,31 @@ int ck_last_diagnostics(void *h, int *out);
  * neighbour), l3[n3][3], l4[n4][4].  Sizes from ck_last_counts. */
 int ck_export_lists(void *h, int *l2, int *l3, int *l4);
 
+/* Evaluation of one periodic configuration that allocates no device memory.
+ * No counterpart in the reference (which has no device memory at all).  For
+ * callers that cannot call cudaMalloc while they compute forces -- an MD code
+ * or framework that reserves the GPU's memory up front and hands out only its
+ * own buffers, or a step loop where an allocation could fail or stall.
+ * Inputs and outputs are the caller's DEVICE buffers: d_pos[natom][3]
+ * Cartesian positions, d_types[natom] type indices of the handle's current
+ * parameter set; cell[9] (host) = lattice vectors a, b, c; small allows
+ * replication.  Written (not accumulated): *d_energy (divided by
+ * (n_replicates+1)^3 as in serial_chimes_interface::calculate),
+ * d_force[natom][3], d_stress[9] (virial over volume).  Work is enqueued on
+ * `stream` (a cudaStream_t, 0 = legacy default) and the call waits for it.
+ * Every intermediate array lives in one static device array of about 17 MiB
+ * that each GPU loading the library holds until the process exits; limits per
+ * call: 2048 atoms after replication, 131072 ghost atoms, 65536 bin cells,
+ * 65536 pairs, 131072 triplets, 65536 quadruplets.  Larger inputs return -2
+ * (sizes known before the launch) or -5 (list sizes found on the device; the
+ * outputs are then invalid), with the message in ck_last_error().  The first
+ * call on each device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  Calls share the array and
+ * each clears what must start at zero; calls whose GPU work overlaps (other
+ * streams, threads or handles) race on it and corrupt each other's results. */
+int ck_calculate_noalloc(void *h, int natom, const double *d_pos, const int *d_types, const double *cell,
+                         int small, double *d_energy, double *d_force, double *d_stress, void *stream);
+
 /* Batched per-cluster evaluation (chimesFF::compute_nB semantics, FP64) with
  * the handle's current parameter set: n clusters of nbody = 2, 3 or 4 atoms,
  * dx[n][P] distances, dr[n][P][3] vectors (atom2 - atom1, pairs ij / ij,ik,jk /
