@@ -10,11 +10,18 @@
 // Index spaces (all int32 inside a batch; offsets are int64):
 //   caller atom  c   : 0 .. sum(n_in)         positions/forces as the caller passed them
 //   atom         a   : 0 .. sum(n_atoms)      after replication (small=true), wrapped
-//   ghost        g   : 0 .. sum(n_atoms*side^3); within a system ghost (img, a) sits at
-//                      ghost_off + img*n_atoms + a, img 0 is the primary cell and
-//                      img>=1 walks (i,j,k) in [-n,n]^3\{0} with i slowest, which is the
-//                      ghost numbering of simulation_system::build_layered_system
-//                      (serial_interface/src/serial_chimes_interface.cpp:546-585).
+//   ghost slot   q   : 0 .. sum(n_atoms*gstride); atom a of a system owns the slots
+//                      ghost_off + a*gstride + [0, gstride) and fills them with its
+//                      images that can lie within the search radius of the primary
+//                      cell (the atom itself included); unused slots carry id -1.
+//   ghost id         : the reference's numbering of a system's ghost atoms,
+//                      img*n_atoms + a, img 0 the primary cell and img>=1 walking
+//                      (i,j,k) in [-n,n]^3\{0} with i slowest
+//                      (simulation_system::build_layered_system,
+//                      serial_interface/src/serial_chimes_interface.cpp:546-585).
+//                      Images farther than the search radius from every atom of the
+//                      cell never enter a list, so only the kept ones get slots;
+//                      bins, lists and clusters hold slots and order them by id.
 #pragma once
 #include <cstdint>
 
@@ -85,7 +92,9 @@ struct SysDesc {
     int has3, has4;
     long long in_off, atom_off, ghost_off, bin_off;
     int bin_cap;               // bins reserved for this system
-    int pad0;
+    int gstride;               // ghost slots per atom (upper bound of its kept images, itself included)
+    double ulo[3], uhi[3];     // kept fractional range per axis of the reoriented cell
+    double eps;                // margin of the FP32 distance prefilter (Angstrom)
     // device-completed
     double minpos[3];
     int nb[3];
@@ -105,11 +114,14 @@ struct BatchView {
     int* atom_sys;                 // [n_atoms_total]
     int* atom_type;
     int* atom_orig;                // caller-atom index receiving the force
-    // ghosts (image 0 = the atoms themselves)
-    int* ghost_parent;             // atom index (global)
-    double* ghost_fs;              // [g][3] fractional coords, input cell
-    double* ghost_xn;              // [g][3] Cartesian coords, reoriented cell
-    double* ghost_fn;              // [g][3] fractional coords, reoriented cell
+    // ghost slots (an atom's own slot holds the atom itself)
+    int* atom_self;                // [n_atoms_total] slot of the atom itself
+    int* ghost_id;                 // [q] ghost id within its system, -1 = unused slot
+    int* ghost_parent;             // [q] atom index (global)
+    double* ghost_fs;              // [q][3] fractional coords, input cell
+    double* ghost_xn;              // [q][3] Cartesian coords, reoriented cell
+    double* ghost_fn;              // [q][3] fractional coords, reoriented cell
+    float* ghost_xf;               // [q][3] ghost_xn rounded to FP32 (distance prefilter)
     // bins (per system, offset bin_off)
     unsigned long long* minmax;    // [n_sys][6] order-preserving keys
     int* ghost_bin;                // [g] local bin id
@@ -120,13 +132,14 @@ struct BatchView {
     // 2B lists
     int* l2_count;                 // [n_atoms_total]
     long long* l2_off;             // [n_atoms_total+1]
-    int* l2_ghost;                 // [n2] global ghost id of the neighbour
+    int* l2_ghost;                 // [n2] ghost slot of the neighbour
     double* l2_dist;               // [n2] distance in the reoriented frame
+    float* l2_vec;                 // [n2][4] displacement from the list's atom (FP32), for the prefilter
     long long n2_cap;
     // 3B/4B enumeration
     int* e_cnt3; int* e_cnt4;      // [n2]
     long long* e_off3; long long* e_off4;   // [n2+1]
-    int* c3;                       // [n3][3] global ghost ids (i, j, k)
+    int* c3;                       // [n3][3] ghost slots (i, j, k)
     int* c4;                       // [n4][4]
     long long n3_cap, n4_cap;
     // results

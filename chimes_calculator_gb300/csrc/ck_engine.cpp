@@ -153,7 +153,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
         d.in_off = in_off; d.atom_off = atom_off; d.ghost_off = ghost_off; d.bin_off = bin_off;
         in_off += in.n;
         atom_off += d.n_atoms;
-        ghost_off += (long long)d.n_atoms * d.side * d.side * d.side;
+        ghost_off += (long long)d.n_atoms * d.gstride;
         bin_off += d.bin_cap;
         stride3 = std::max(stride3, P.o3 > 0 ? P.o3 + 1 : 0);
         stride4 = std::max(stride4, P.o4 > 0 ? P.o4 + 1 : 0);
@@ -165,7 +165,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
         if (d.has4) n4_est += d.n_atoms * (0.1 * m * m * m * std::pow(d.c4 / d.search, 9.0) + 4);
     }
     if (ghost_off > 2000000000LL) {
-        err = "batch exceeds 2^31 ghost atoms";
+        err = "batch exceeds 2^31 ghost slots";
         return kErrInput;
     }
     tuning.stride3 = stride3;
@@ -186,6 +186,9 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     CK_TRY(d_atom_sys_.reserve(atom_off));
     CK_TRY(d_atom_type_.reserve(atom_off));
     CK_TRY(d_atom_orig_.reserve(atom_off));
+    CK_TRY(d_atom_self_.reserve(atom_off));
+    CK_TRY(d_ghost_id_.reserve(ghost_off));
+    CK_TRY(d_ghost_xf_.reserve(3 * ghost_off));
     CK_TRY(d_ghost_parent_.reserve(ghost_off));
     CK_TRY(d_ghost_bin_.reserve(ghost_off));
     CK_TRY(d_ghost_fs_.reserve(3 * ghost_off));
@@ -223,6 +226,7 @@ Status Engine::ensure_lists(std::string& err) {
     CK_TRY(d_l2_ghost_.reserve(n2_cap_));
     CK_TRY(d_l2_owner_.reserve(n2_cap_));
     CK_TRY(d_l2_dist_.reserve(n2_cap_));
+    CK_TRY(d_l2_vec_.reserve(4 * n2_cap_));
     CK_TRY(d_e_cnt3_.reserve(n2_cap_));
     CK_TRY(d_e_cnt4_.reserve(n2_cap_));
     CK_TRY(d_e_off3_.reserve(n2_cap_ + 1));
@@ -237,6 +241,9 @@ Status Engine::ensure_lists(std::string& err) {
     B.in_pos = d_in_pos_.p;
     B.in_type = d_in_type_.p;
     B.atom_sys = d_atom_sys_.p; B.atom_type = d_atom_type_.p; B.atom_orig = d_atom_orig_.p;
+    B.atom_self = d_atom_self_.p;
+    B.ghost_id = d_ghost_id_.p;
+    B.ghost_xf = d_ghost_xf_.p;
     B.ghost_parent = d_ghost_parent_.p;
     B.ghost_fs = d_ghost_fs_.p; B.ghost_xn = d_ghost_xn_.p; B.ghost_fn = d_ghost_fn_.p;
     B.minmax = d_minmax_.p;
@@ -244,6 +251,7 @@ Status Engine::ensure_lists(std::string& err) {
     B.bin_count = d_bin_count_.p; B.bin_start = d_bin_start_.p; B.bin_fill = d_bin_fill_.p;
     B.bin_items = d_bin_items_.p;
     B.l2_count = d_l2_count_.p; B.l2_off = d_l2_off_.p; B.l2_ghost = d_l2_ghost_.p; B.l2_dist = d_l2_dist_.p;
+    B.l2_vec = d_l2_vec_.p;
     B.n2_cap = n2_cap_;
     B.e_cnt3 = d_e_cnt3_.p; B.e_cnt4 = d_e_cnt4_.p; B.e_off3 = d_e_off3_.p; B.e_off4 = d_e_off4_.p;
     B.c3 = d_c3_.p; B.c4 = d_c4_.p;
@@ -471,24 +479,20 @@ Status Engine::export_lists(std::vector<int>& l2, std::vector<int>& l3, std::vec
     if (n4) CK_TRY(cudaMemcpy(g4.data(), V_.c4, sizeof(int) * 4 * n4, cudaMemcpyDeviceToHost));
     if (V_.n_atoms_total)
         CK_TRY(cudaMemcpy(asys.data(), V_.atom_sys, sizeof(int) * V_.n_atoms_total, cudaMemcpyDeviceToHost));
-    auto sys_of_ghost = [&](long long g) {
-        int lo = 0, hi = V_.n_sys - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) / 2;
-            if (hsys_[mid].ghost_off <= g) lo = mid; else hi = mid - 1;
-        }
-        return lo;
-    };
+    // slots -> the reference's ghost numbering within each system
+    std::vector<int> gid(V_.n_ghost_total);
+    if (V_.n_ghost_total)
+        CK_TRY(cudaMemcpy(gid.data(), V_.ghost_id, sizeof(int) * V_.n_ghost_total, cudaMemcpyDeviceToHost));
     l2.resize(2 * n2);
     for (long long e = 0; e < n2; e++) {
         const SysDesc& d = hsys_[asys[own[e]]];
         l2[2 * e] = (int)(own[e] - d.atom_off);
-        l2[2 * e + 1] = (int)(g2[e] - d.ghost_off);
+        l2[2 * e + 1] = gid[g2[e]];
     }
     l3.resize(3 * n3);
-    for (long long q = 0; q < 3 * n3; q++) l3[q] = (int)(g3[q] - hsys_[sys_of_ghost(g3[q])].ghost_off);
+    for (long long q = 0; q < 3 * n3; q++) l3[q] = gid[g3[q]];
     l4.resize(4 * n4);
-    for (long long q = 0; q < 4 * n4; q++) l4[q] = (int)(g4[q] - hsys_[sys_of_ghost(g4[q])].ghost_off);
+    for (long long q = 0; q < 4 * n4; q++) l4[q] = gid[g4[q]];
     return kOk;
 }
 

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner
         const int s = B.atom_sys[r];
         const SysDesc& d = B.sys[s];
         const DevParamSet& P = B.psets[d.pset];
-        const int gi = (int)(d.ghost_off + (r - d.atom_off));
+        const int gi = B.atom_self[r];
         const int gj = B.l2_ghost[e];
         const int t0 = B.atom_type[r], t1 = B.atom_type[B.ghost_parent[gj]];
         const PairRec pr = P.pairs[P.pair_map[t0 * P.ntypes + t1]];

@@ -173,6 +173,45 @@ Status system_geometry(const double* ca, const double* cb, const double* cc, int
     d.side = side;
     d.has3 = has3 ? 1 : 0;
     d.has4 = has4 ? 1 : 0;
+    // Kept images.  Every list member lies within `search` of a real atom, and
+    // real atoms have reoriented fractional coordinates in [0,1).  Along axis k
+    // the distance between points whose fractional coordinates differ by du is
+    // at least |du| * h_k, h_k the cell height normal to the other two axes, so
+    // an image whose coordinate falls outside [-search/h_k, 1 + search/h_k] is
+    // never a neighbour.  The 1e-6 slack covers rounding of the stored coordinates.
+    {
+        const double* H = d.hn;
+        const double A[3] = {H[0], H[3], H[6]}, B[3] = {H[1], H[4], H[7]}, C[3] = {H[2], H[5], H[8]};
+        auto cross = [](const double* x, const double* y, double* o) {
+            o[0] = x[1] * y[2] - x[2] * y[1];
+            o[1] = x[2] * y[0] - x[0] * y[2];
+            o[2] = x[0] * y[1] - x[1] * y[0];
+        };
+        double bc[3], ca[3], ab[3];
+        cross(B, C, bc);
+        cross(C, A, ca);
+        cross(A, B, ab);
+        const double V = std::fabs(A[0] * bc[0] + A[1] * bc[1] + A[2] * bc[2]);
+        const double hgt[3] = {V / mag3(bc), V / mag3(ca), V / mag3(ab)};
+        int stride = 1;
+        double ext = 0.0;
+        for (int k = 0; k < 3; k++) {
+            const double w = d.search / hgt[k];
+            d.ulo[k] = -w - 1e-6;
+            d.uhi[k] = 1.0 + w + 1e-6;
+            int cnt = (int)std::floor(d.uhi[k] - d.ulo[k] + 1e-9) + 1;
+            if (cnt > side) cnt = side;
+            stride *= cnt;
+            for (int j = 0; j < 3; j++) ext += std::fabs(H[3 * k + j]) * (d.n_layers + 1);
+        }
+        d.gstride = stride;
+        // FP32 copies of coordinates up to `ext` carry errors below 2e-7 * ext
+        d.eps = 2e-3 + 1e-6 * ext;
+    }
+    if ((long long)n_atoms * d.gstride > 2000000000LL) {
+        err = "ghost slots exceed 2^31";
+        return kErrInput;
+    }
     // Bin-grid capacity: the ghost cloud spans at most (2n+1) * sum_j |hn_ij| per axis.
     long long cap = 1;
     for (int i = 0; i < 3; i++) {

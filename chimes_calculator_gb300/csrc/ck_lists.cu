@@ -3,12 +3,25 @@
 //
 // The lists must be the reference's lists exactly (same members, same order),
 // because cluster membership is decided by floating-point distance tests.
-// Every floating-point step here therefore uses explicit round-to-nearest
-// intrinsics (__dmul_rn/__dadd_rn/__dsub_rn/__ddiv_rn/__dsqrt_rn), which the
-// compiler never fuses, in the reference's evaluation order:
+// Every floating-point step whose result decides membership therefore uses
+// explicit round-to-nearest intrinsics (__dmul_rn/__dadd_rn/__dsub_rn/
+// __ddiv_rn/__dsqrt_rn), which the compiler never fuses, in the reference's
+// evaluation order:
 //   set-up, wrap, reorient, ghosts ... serial_interface/src/serial_chimes_interface.cpp:150-587
 //   bins and lists ................... serial_chimes_interface.cpp:588-864
 //   get_dist ......................... serial_interface/src/serial_chimes_interface.h:141-215
+//
+// Two shortcuts keep the result exact while doing less work than the
+// reference:
+//  * only the ghost images that can lie within the search radius of the
+//    primary cell are generated (host bound in ck_geom.cpp); the bin grid still
+//    spans the bounding box of ALL images, which is exact from the corner
+//    images alone: a ghost coordinate is a composition of IEEE-rounded sums and
+//    products, each monotone in the image shift, so over the shift box its
+//    extremes sit at the corners;
+//  * distances are first tested in FP32 with a margin (SysDesc::eps) far above
+//    the FP32 error; only a distance within the margin of a cutoff, and every
+//    distance that is stored, is evaluated exactly in FP64.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -33,12 +46,13 @@ __device__ __forceinline__ void mv(const double* m, double x, double y, double z
     o[2] = add(add(mul(m[6], x), mul(m[7], y)), mul(m[8], z));
 }
 
-// get_dist on stored fractional coordinates: |H (f_j - f_i)|
-__device__ __forceinline__ double dist_frac(const double* H, const double* fi, const double* fj) {
+// get_dist on stored fractional coordinates: |H (f_j - f_i)|; r = H (f_j - f_i)
+__device__ __forceinline__ double dist_frac(const double* H, const double* fi, const double* fj, double* r = nullptr) {
     double dx = sub(fj[0], fi[0]), dy = sub(fj[1], fi[1]), dz = sub(fj[2], fi[2]);
     double r0 = add(add(mul(H[0], dx), mul(H[1], dy)), mul(H[2], dz));
     double r1 = add(add(mul(H[3], dx), mul(H[4], dy)), mul(H[5], dz));
     double r2 = add(add(mul(H[6], dx), mul(H[7], dy)), mul(H[8], dz));
+    if (r) { r[0] = r0; r[1] = r1; r[2] = r2; }
     return __dsqrt_rn(add(add(mul(r0, r0), mul(r1, r1)), mul(r2, r2)));
 }
 
@@ -58,6 +72,7 @@ __device__ __forceinline__ int find_sys_ghost(const SysDesc* sys, int n, long lo
     }
     return lo;
 }
+
 // order-preserving unsigned key of a double (for atomicMin/atomicMax)
 __device__ __forceinline__ unsigned long long okey(double v) {
     unsigned long long u = (unsigned long long)__double_as_longlong(v);
@@ -68,89 +83,94 @@ __device__ __forceinline__ double okey_inv(unsigned long long k) {
     return __longlong_as_double((long long)u);
 }
 
-__device__ __forceinline__ void ghost_shift(int img, int n, int side, int& i, int& j, int& k) {
-    int full = img - 1;
-    int center = (n * side + n) * side + n;
-    if (full >= center) full++;
-    i = full / (side * side) - n;
-    j = (full / side) % side - n;
-    k = full % side - n;
+// reference ghost image number of shift (i,j,k): 1.. for the images of
+// build_layered_system's (i,j,k) loop, skipping (0,0,0)
+__device__ __forceinline__ int image_index(int i, int j, int k, int n, int side) {
+    const int full = ((i + n) * side + (j + n)) * side + (k + n);
+    const int center = (n * side + n) * side + n;
+    return full < center ? full + 1 : full;
 }
 
-// --- 1. atoms: replicate (small=true), wrap, reorient -----------------------
-// simulation_system::init (:196-322) and reorient (:352-405)
+// kept image shifts of an atom with reoriented fractional coordinates fn:
+// s_k in [lo_k, lo_k + cnt_k), shift 0 (the atom itself) always included
+struct ShiftBox {
+    int lo[3], cnt[3], count;
+};
+__device__ __forceinline__ void shift_box(const SysDesc& d, const double* fn, ShiftBox& b) {
+    const int n = d.n_layers;
+    b.count = 1;
+    for (int k = 0; k < 3; k++) {
+        int lo = (int)ceil(d.ulo[k] - fn[k]), hi = (int)floor(d.uhi[k] - fn[k]);
+        lo = lo < -n ? -n : lo;
+        hi = hi > n ? n : hi;
+        lo = lo > 0 ? 0 : lo;
+        hi = hi < 0 ? 0 : hi;
+        b.lo[k] = lo;
+        b.cnt[k] = hi - lo + 1;
+        b.count *= b.cnt[k];
+    }
+}
+
+// --- 1. atoms: replicate (small=true), wrap, reorient, bounding box --------
+// simulation_system::init (:196-322) and reorient (:352-405).  The bounding box
+// of all ghost images (build_neigh_lists :590-610) comes from each atom, its
+// two corner images per axis, reduced per system.
 __global__ void k_atoms(BatchView B) {
-    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= B.n_atoms_total) return;
-    const int s = find_sys_atom(B.sys, B.n_sys, r);
-    const SysDesc& d = B.sys[s];
-    const int rl = (int)(r - d.atom_off);
-    const int a = rl % d.n_in, blk = rl / d.n_in;
-    const double* xin = B.in_pos + 3 * (d.in_off + a);
-    double x[3] = {xin[0], xin[1], xin[2]};
-    if (blk > 0) {
-        const int nr1 = d.n_rep + 1;
-        const int i = blk / (nr1 * nr1), j = (blk / nr1) % nr1, k = blk % nr1;
-        double t[3];
-        mv(d.h0i, x[0], x[1], x[2], t);
-        t[0] = add(t[0], (double)i); t[1] = add(t[1], (double)j); t[2] = add(t[2], (double)k);
-        mv(d.h0, t[0], t[1], t[2], x);
-    }
-    double f[3], xw[3], fa[3], xn[3], fn[3];
-    mv(d.hi, x[0], x[1], x[2], f);
-    f[0] = sub(f[0], floor(f[0])); f[1] = sub(f[1], floor(f[1])); f[2] = sub(f[2], floor(f[2]));
-    mv(d.h, f[0], f[1], f[2], xw);
-    mv(d.hi, xw[0], xw[1], xw[2], fa);
-    mv(d.hn, fa[0], fa[1], fa[2], xn);
-    mv(d.hni, xn[0], xn[1], xn[2], fn);
-    const long long g = d.ghost_off + rl;
-    for (int c = 0; c < 3; c++) {
-        B.ghost_fs[3 * g + c] = fa[c];
-        B.ghost_xn[3 * g + c] = xn[c];
-        B.ghost_fn[3 * g + c] = fn[c];
-    }
-    B.ghost_parent[g] = (int)r;
-    B.atom_sys[r] = s;
-    B.atom_type[r] = B.in_type[d.in_off + a];
-    B.atom_orig[r] = (int)(d.in_off + a);
-}
-
-// --- 2. ghosts + bounding box ------------------------------------------------
-// build_layered_system (:546-585) for both the input-cell system (fractional
-// coordinates for the force evaluation) and the reoriented system (Cartesian and
-// fractional coordinates for the lists); the min/max of the reoriented cloud
-// (build_neigh_lists :590-610) is reduced on the fly.
-__global__ void k_ghosts(BatchView B) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = g < B.n_ghost_total;
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = r < B.n_atoms_total;
     int s = -1;
-    double xn[3] = {0, 0, 0};
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     if (valid) {
-        s = find_sys_ghost(B.sys, B.n_sys, g);
+        s = find_sys_atom(B.sys, B.n_sys, r);
         const SysDesc& d = B.sys[s];
-        const long long gl = g - d.ghost_off;
-        const int img = (int)(gl / d.n_atoms), a = (int)(gl % d.n_atoms);
-        if (img == 0) {
-            xn[0] = B.ghost_xn[3 * g]; xn[1] = B.ghost_xn[3 * g + 1]; xn[2] = B.ghost_xn[3 * g + 2];
-        } else {
-            int i, j, k;
-            ghost_shift(img, d.n_layers, d.side, i, j, k);
-            const long long src = d.ghost_off + a;
-            double t[3], p[3], o[3];
-            t[0] = add(B.ghost_fs[3 * src], (double)i);
-            t[1] = add(B.ghost_fs[3 * src + 1], (double)j);
-            t[2] = add(B.ghost_fs[3 * src + 2], (double)k);
-            mv(d.h, t[0], t[1], t[2], p);
-            mv(d.hi, p[0], p[1], p[2], o);
-            B.ghost_fs[3 * g] = o[0]; B.ghost_fs[3 * g + 1] = o[1]; B.ghost_fs[3 * g + 2] = o[2];
-            t[0] = add(B.ghost_fn[3 * src], (double)i);
-            t[1] = add(B.ghost_fn[3 * src + 1], (double)j);
-            t[2] = add(B.ghost_fn[3 * src + 2], (double)k);
-            mv(d.hn, t[0], t[1], t[2], xn);
-            mv(d.hni, xn[0], xn[1], xn[2], o);
-            B.ghost_xn[3 * g] = xn[0]; B.ghost_xn[3 * g + 1] = xn[1]; B.ghost_xn[3 * g + 2] = xn[2];
-            B.ghost_fn[3 * g] = o[0]; B.ghost_fn[3 * g + 1] = o[1]; B.ghost_fn[3 * g + 2] = o[2];
-            B.ghost_parent[g] = (int)(d.atom_off + a);
+        const int rl = (int)(r - d.atom_off);
+        const int a = rl % d.n_in, blk = rl / d.n_in;
+        const double* xin = B.in_pos + 3 * (d.in_off + a);
+        double x[3] = {xin[0], xin[1], xin[2]};
+        if (blk > 0) {
+            const int nr1 = d.n_rep + 1;
+            const int i = blk / (nr1 * nr1), j = (blk / nr1) % nr1, k = blk % nr1;
+            double t[3];
+            mv(d.h0i, x[0], x[1], x[2], t);
+            t[0] = add(t[0], (double)i); t[1] = add(t[1], (double)j); t[2] = add(t[2], (double)k);
+            mv(d.h0, t[0], t[1], t[2], x);
+        }
+        double f[3], xw[3], fa[3], xn[3], fn[3];
+        mv(d.hi, x[0], x[1], x[2], f);
+        f[0] = sub(f[0], floor(f[0])); f[1] = sub(f[1], floor(f[1])); f[2] = sub(f[2], floor(f[2]));
+        mv(d.h, f[0], f[1], f[2], xw);
+        mv(d.hi, xw[0], xw[1], xw[2], fa);
+        mv(d.hn, fa[0], fa[1], fa[2], xn);
+        mv(d.hni, xn[0], xn[1], xn[2], fn);
+        ShiftBox sb;
+        shift_box(d, fn, sb);
+        if (sb.count > d.gstride) atomicOr(&B.flags[0], 16);   // slot bound violated (cannot happen)
+        const int j0 = ((0 - sb.lo[0]) * sb.cnt[1] + (0 - sb.lo[1])) * sb.cnt[2] + (0 - sb.lo[2]);
+        const long long q = d.ghost_off + (long long)rl * d.gstride + (j0 < d.gstride ? j0 : 0);
+        for (int c = 0; c < 3; c++) {
+            B.ghost_fs[3 * q + c] = fa[c];
+            B.ghost_xn[3 * q + c] = xn[c];
+            B.ghost_fn[3 * q + c] = fn[c];
+            B.ghost_xf[3 * q + c] = (float)xn[c];
+        }
+        B.ghost_parent[q] = (int)r;
+        B.ghost_id[q] = rl;
+        B.atom_self[r] = (int)q;
+        B.atom_sys[r] = s;
+        B.atom_type[r] = B.in_type[d.in_off + a];
+        B.atom_orig[r] = (int)(d.in_off + a);
+        const int n = d.n_layers;
+        for (int c = 0; c < 3; c++) {
+            double tl[3], th[3];
+            for (int k = 0; k < 3; k++) {
+                const bool up = d.hn[3 * c + k] >= 0.0;
+                tl[k] = add(fn[k], (double)(up ? -n : n));
+                th[k] = add(fn[k], (double)(up ? n : -n));
+            }
+            const double vl = add(add(mul(d.hn[3 * c], tl[0]), mul(d.hn[3 * c + 1], tl[1])), mul(d.hn[3 * c + 2], tl[2]));
+            const double vh = add(add(mul(d.hn[3 * c], th[0]), mul(d.hn[3 * c + 1], th[1])), mul(d.hn[3 * c + 2], th[2]));
+            lo[c] = vl < xn[c] ? vl : xn[c];
+            hi[c] = vh > xn[c] ? vh : xn[c];
         }
     }
     const int lane = threadIdx.x & 31;
@@ -159,8 +179,8 @@ __global__ void k_ghosts(BatchView B) {
     const bool uniform = __all_sync(kFull, !valid || s == s0);
     unsigned long long kmin[3], kmax[3];
     for (int c = 0; c < 3; c++) {
-        kmin[c] = valid ? okey(xn[c]) : ~0ull;
-        kmax[c] = valid ? okey(xn[c]) : 0ull;
+        kmin[c] = valid ? okey(lo[c]) : ~0ull;
+        kmax[c] = valid ? okey(hi[c]) : 0ull;
     }
     if (uniform) {
         for (int off = 16; off; off >>= 1)
@@ -183,6 +203,48 @@ __global__ void k_ghosts(BatchView B) {
     }
 }
 
+// --- 2. kept ghost images, one thread per slot -----------------------------
+// build_layered_system (:546-585) for both the input-cell system (fractional
+// coordinates for the force evaluation) and the reoriented system (Cartesian
+// and fractional coordinates for the lists).
+__global__ void k_ghosts(BatchView B) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= B.n_ghost_total) return;
+    const int s = find_sys_ghost(B.sys, B.n_sys, q);
+    const SysDesc& d = B.sys[s];
+    const long long ql = q - d.ghost_off;
+    const int rl = (int)(ql / d.gstride), j = (int)(ql % d.gstride);
+    const long long r = d.atom_off + rl;
+    const long long qs = B.atom_self[r];
+    if (q == qs) return;   // the atom itself, written by k_atoms
+    const double fa[3] = {B.ghost_fs[3 * qs], B.ghost_fs[3 * qs + 1], B.ghost_fs[3 * qs + 2]};
+    const double fn[3] = {B.ghost_fn[3 * qs], B.ghost_fn[3 * qs + 1], B.ghost_fn[3 * qs + 2]};
+    ShiftBox sb;
+    shift_box(d, fn, sb);
+    if (j >= sb.count) {
+        B.ghost_id[q] = -1;
+        return;
+    }
+    const int i0 = sb.lo[0] + j / (sb.cnt[1] * sb.cnt[2]);
+    const int i1 = sb.lo[1] + (j / sb.cnt[2]) % sb.cnt[1];
+    const int i2 = sb.lo[2] + j % sb.cnt[2];
+    double t[3], p[3], o[3], xn[3];
+    t[0] = add(fa[0], (double)i0); t[1] = add(fa[1], (double)i1); t[2] = add(fa[2], (double)i2);
+    mv(d.h, t[0], t[1], t[2], p);
+    mv(d.hi, p[0], p[1], p[2], o);
+    B.ghost_fs[3 * q] = o[0]; B.ghost_fs[3 * q + 1] = o[1]; B.ghost_fs[3 * q + 2] = o[2];
+    t[0] = add(fn[0], (double)i0); t[1] = add(fn[1], (double)i1); t[2] = add(fn[2], (double)i2);
+    mv(d.hn, t[0], t[1], t[2], xn);
+    mv(d.hni, xn[0], xn[1], xn[2], o);
+    for (int c = 0; c < 3; c++) {
+        B.ghost_xn[3 * q + c] = xn[c];
+        B.ghost_fn[3 * q + c] = o[c];
+        B.ghost_xf[3 * q + c] = (float)xn[c];
+    }
+    B.ghost_parent[q] = (int)r;
+    B.ghost_id[q] = image_index(i0, i1, i2, d.n_layers, d.side) * d.n_atoms + rl;
+}
+
 // --- 3. bin grid per system (build_neigh_lists :622-642) -------------------
 __global__ void k_bin_setup(BatchView B) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,47 +261,47 @@ __global__ void k_bin_setup(BatchView B) {
     }
     if (total > d.bin_cap) {
         d.err = kErrCapacity;
-        atomicExch(&B.flags[0], 1);
+        atomicOr(&B.flags[0], 1);
     }
 }
 
-__device__ __forceinline__ bool bin_of(const SysDesc& d, const double* x, int& bx, int& by, int& bz) {
+__device__ __forceinline__ void bin_of(const SysDesc& d, const double* x, int& bx, int& by, int& bz) {
     bx = (int)floor(__ddiv_rn(sub(x[0], d.minpos[0]), d.search));
     by = (int)floor(__ddiv_rn(sub(x[1], d.minpos[1]), d.search));
     bz = (int)floor(__ddiv_rn(sub(x[2], d.minpos[2]), d.search));
-    return true;
 }
 
 // --- 4. bin population (:644-678) -------------------------------------------
 __global__ void k_bin_count(BatchView B) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= B.n_ghost_total) return;
-    const int s = find_sys_ghost(B.sys, B.n_sys, g);
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= B.n_ghost_total) return;
+    if (B.ghost_id[q] < 0) { B.ghost_bin[q] = -1; return; }
+    const int s = find_sys_ghost(B.sys, B.n_sys, q);
     const SysDesc& d = B.sys[s];
-    if (d.err) { B.ghost_bin[g] = -1; return; }
+    if (d.err) { B.ghost_bin[q] = -1; return; }
     int bx, by, bz;
-    bin_of(d, &B.ghost_xn[3 * g], bx, by, bz);
+    bin_of(d, &B.ghost_xn[3 * q], bx, by, bz);
     const long long total = (long long)d.nb[0] * d.nb[1] * d.nb[2];
-    if (bx < 0 || by < 0 || bz < 0) { atomicExch(&B.flags[1], 1); B.ghost_bin[g] = -1; return; }
+    if (bx < 0 || by < 0 || bz < 0) { atomicExch(&B.flags[1], 1); B.ghost_bin[q] = -1; return; }
     const long long ib = bx + (long long)by * d.nb[0] + (long long)bz * d.nb[0] * d.nb[1];
-    if (ib >= total) { atomicExch(&B.flags[1], 2); B.ghost_bin[g] = -1; return; }
-    B.ghost_bin[g] = (int)ib;
+    if (ib >= total) { atomicExch(&B.flags[1], 2); B.ghost_bin[q] = -1; return; }
+    B.ghost_bin[q] = (int)ib;
     atomicAdd(&B.bin_count[d.bin_off + ib], 1);
 }
 
 __global__ void k_bin_scatter(BatchView B, const long long* bin_start) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= B.n_ghost_total) return;
-    const int ib = B.ghost_bin[g];
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= B.n_ghost_total) return;
+    const int ib = B.ghost_bin[q];
     if (ib < 0) return;
-    const int s = find_sys_ghost(B.sys, B.n_sys, g);
+    const int s = find_sys_ghost(B.sys, B.n_sys, q);
     const long long b = B.sys[s].bin_off + ib;
     const long long pos = bin_start[b] + atomicAdd(&B.bin_fill[b], 1);
-    B.bin_items[pos] = (int)g;
+    B.bin_items[pos] = (int)q;
 }
 
-// each bin's members in ascending ghost order (the reference pushes ghosts
-// into bins in index order)
+// each bin's members in ascending ghost id (the reference pushes ghosts into
+// bins in index order)
 __global__ void k_bin_sort(BatchView B, const long long* bin_start) {
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B.n_bins_total) return;
@@ -247,8 +309,9 @@ __global__ void k_bin_sort(BatchView B, const long long* bin_start) {
     const int n = B.bin_count[b];
     int* v = B.bin_items + s0;
     for (int i = 1; i < n; i++) {
-        int key = v[i], j = i - 1;
-        while (j >= 0 && v[j] > key) { v[j + 1] = v[j]; j--; }
+        const int key = v[i], kid = B.ghost_id[key];
+        int j = i - 1;
+        while (j >= 0 && B.ghost_id[v[j]] > kid) { v[j + 1] = v[j]; j--; }
         v[j + 1] = key;
     }
 }
@@ -263,11 +326,13 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     const int s = B.atom_sys[r];
     const SysDesc& d = B.sys[s];
     if (d.err) { if (!FILL && lane == 0) B.l2_count[r] = 0; return; }
-    const long long gi = d.ghost_off + (r - d.atom_off);
+    const long long gi = B.atom_self[r];
     const double fi[3] = {B.ghost_fn[3 * gi], B.ghost_fn[3 * gi + 1], B.ghost_fn[3 * gi + 2]};
+    const float xi[3] = {B.ghost_xf[3 * gi], B.ghost_xf[3 * gi + 1], B.ghost_xf[3 * gi + 2]};
     double hn[9];
     for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
     const double sd = d.search;
+    const float far2 = (float)((sd + d.eps) * (sd + d.eps));
     int bx, by, bz;
     bin_of(d, &B.ghost_xn[3 * gi], bx, by, bz);
     if (bx < 1 || by < 1 || bz < 1) {
@@ -289,15 +354,19 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
                 const long long st = bin_start[b];
                 const int nb = B.bin_count[b];
                 for (int q0 = 0; q0 < nb; q0 += 32) {
-                    const int q = q0 + lane;
+                    const int qq = q0 + lane;
                     bool pred = false;
                     int ajj = -1;
-                    double dd = 0.0;
-                    if (q < nb) {
-                        ajj = B.bin_items[st + q];
+                    double dd = 0.0, rv[3] = {0, 0, 0};
+                    if (qq < nb) {
+                        ajj = B.bin_items[st + qq];
                         if (ajj != gi && r <= B.ghost_parent[ajj]) {
-                            dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj]);
-                            pred = dd < sd;
+                            const float* xj = &B.ghost_xf[3 * (long long)ajj];
+                            const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
+                            if (ex * ex + ey * ey + ez * ez < far2) {   // else certainly >= sd
+                                dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj], rv);
+                                pred = dd < sd;
+                            }
                         }
                     }
                     const unsigned bal = __ballot_sync(kFull, pred);
@@ -307,6 +376,8 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
                             B.l2_ghost[pos] = ajj;
                             B.l2_dist[pos] = dd;
                             l2_owner[pos] = (int)r;
+                            float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], (float)dd);
+                            reinterpret_cast<float4*>(B.l2_vec)[pos] = v;
                         }
                     }
                     count += __popc(bal);
@@ -315,25 +386,31 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     if (!FILL && lane == 0) B.l2_count[r] = count;
 }
 
+// Exact test "distance >= c" for a ghost pair of one atom's list, deciding
+// from the FP32 displacement difference when it is farther than eps from c.
+struct PairDist {
+    const double* hn;
+    const double* fa;
+    const double* fb;
+    float df;
+    double exact;
+    bool have;
+    __device__ bool ge(double c, double eps) {
+        if ((double)df < c - eps) return false;
+        if ((double)df >= c + eps) return true;
+        if (!have) { exact = dist_frac(hn, fa, fb); have = true; }
+        return exact >= c;
+    }
+};
+
+__device__ __forceinline__ float vdist(const float4& a, const float4& b) {
+    const float x = b.x - a.x, y = b.y - a.y, z = b.z - a.z;
+    return sqrtf(x * x + y * y + z * z);
+}
+
 // --- 6. 3B/4B enumeration (:735-855): one thread per (i, j) list entry -----
 // The valid_3mer / valid_4mer flags carry over between k iterations exactly as
 // in the reference, so the emitted sets and their order match it.
-template <bool FILL>
-__device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e);
-
-template <bool FILL>
-__global__ void k_enum(BatchView B, const int* l2_owner) {
-    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < B.n2_cap;
-         e += (long long)gridDim.x * blockDim.x) {
-        if (e >= n2) {
-            if (!FILL) { B.e_cnt3[e] = 0; B.e_cnt4[e] = 0; }
-            continue;
-        }
-        enum_entry<FILL>(B, l2_owner, e);
-    }
-}
-
 template <bool FILL>
 __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e) {
     const int r = l2_owner[e];
@@ -341,20 +418,21 @@ __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e)
     int n3 = 0, n4 = 0;
     long long o3 = 0, o4 = 0;
     if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
-    const double c3 = d.c3, c4 = d.c4;
+    const double c3 = d.c3, c4 = d.c4, eps = d.eps;
     if (d.has3 || d.has4) {
         double hn[9];
         for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
-        const int gi = (int)(d.ghost_off + (r - d.atom_off));
+        const int gi = B.atom_self[r];
         const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
+        const float4* vec = reinterpret_cast<const float4*>(B.l2_vec);
         const int jj = B.l2_ghost[e];
         const double dij = B.l2_dist[e];
         bool v3 = true, v4 = true;
         if (dij >= c3) v3 = false;
         if (dij >= c4) v4 = false;
         if (v3 || v4) {
-            const double fj[3] = {B.ghost_fn[3 * (long long)jj], B.ghost_fn[3 * (long long)jj + 1],
-                                  B.ghost_fn[3 * (long long)jj + 2]};
+            const double* fj = &B.ghost_fn[3 * (long long)jj];
+            const float4 vj = vec[e];
             const int pj = B.ghost_parent[jj];
             for (long long k = b0; k < b1; k++) {
                 const int kk = B.l2_ghost[k];
@@ -364,10 +442,11 @@ __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e)
                 const double dik = B.l2_dist[k];
                 if (dik >= c3) v3 = false;
                 if (dik >= c4) v4 = false;
+                const float4 vk = vec[k];
                 const double* fk = &B.ghost_fn[3 * (long long)kk];
-                const double djk = dist_frac(hn, fj, fk);
-                if (djk >= c3) v3 = false;
-                if (djk >= c4) v4 = false;
+                PairDist jk{hn, fj, fk, vdist(vj, vk), 0.0, false};
+                if (jk.ge(c3, eps)) v3 = false;
+                if (jk.ge(c4, eps)) v4 = false;
                 if (!v3 && !v4) {
                     if (dij < c3) v3 = true;
                     if (dij < c4) v4 = true;
@@ -385,7 +464,6 @@ __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e)
                     if (dij < c4) v4 = true;
                     continue;
                 }
-                const double fkk[3] = {fk[0], fk[1], fk[2]};
                 for (long long l = b0; l < b1; l++) {
                     const int ll = B.l2_ghost[l];
                     if (jj == ll || kk == ll) continue;
@@ -393,9 +471,12 @@ __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e)
                     if (pj > pl) continue;
                     if (pk > pl) continue;
                     if (B.l2_dist[l] >= c4) continue;
+                    const float4 vl = vec[l];
                     const double* fl = &B.ghost_fn[3 * (long long)ll];
-                    if (dist_frac(hn, fj, fl) >= c4) continue;
-                    if (dist_frac(hn, fkk, fl) >= c4) continue;
+                    PairDist jl{hn, fj, fl, vdist(vj, vl), 0.0, false};
+                    if (jl.ge(c4, eps)) continue;
+                    PairDist kl{hn, fk, fl, vdist(vk, vl), 0.0, false};
+                    if (kl.ge(c4, eps)) continue;
                     if (v4) {
                         if (FILL && o4 + n4 < B.n4_cap) {
                             int* out = B.c4 + 4 * (o4 + n4);
@@ -408,6 +489,19 @@ __device__ void enum_entry(const BatchView& B, const int* l2_owner, long long e)
         }
     }
     if (!FILL) { B.e_cnt3[e] = n3; B.e_cnt4[e] = n4; }
+}
+
+template <bool FILL>
+__global__ void k_enum(BatchView B, const int* l2_owner) {
+    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < B.n2_cap;
+         e += (long long)gridDim.x * blockDim.x) {
+        if (e >= n2) {
+            if (!FILL) { B.e_cnt3[e] = 0; B.e_cnt4[e] = 0; }
+            continue;
+        }
+        enum_entry<FILL>(B, l2_owner, e);
+    }
 }
 
 // --- capacity checks and accumulator reset ---------------------------------

@@ -8,7 +8,7 @@
 // inputs and outputs, and every intermediate array of the evaluation -- ghost
 // images, bin grid, neighbour and cluster lists, scan workspace, accumulators
 // -- lives in one file-scope device array of fixed size (kScratchBytes, about
-// 17 MiB), which every GPU that loads the library holds until the process
+// 13.4 MiB), which every GPU that loads the library holds until the process
 // exits.  The kernels are the same ones the allocating entry points run.
 //
 // The array is shared by all calls on a device and keeps the previous call's
@@ -31,7 +31,7 @@ namespace {
 
 // Maximum sizes of one call (after replication of small cells).
 constexpr long long kNaAtoms = 2048;      // atoms
-constexpr long long kNaGhosts = 131072;   // atoms x ghost images
+constexpr long long kNaGhosts = 65536;    // ghost-image slots (atoms x kept images per atom)
 constexpr long long kNaBins = 65536;      // bin-grid cells
 constexpr long long kNaPairs = 65536;     // 2-body list entries
 constexpr long long kNaTrip = 131072;     // triplets
@@ -41,13 +41,13 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // byte layout of the scratch array
 struct Layout {
-    size_t sys, minmax, ev, flags, in_pos, in_type, atom_sys, atom_type, atom_orig;
-    size_t ghost_parent, ghost_bin, ghost_fs, ghost_xn, ghost_fn, bin_items;
+    size_t sys, minmax, ev, flags, in_pos, in_type, atom_sys, atom_type, atom_orig, atom_self;
+    size_t ghost_id, ghost_parent, ghost_bin, ghost_fs, ghost_xn, ghost_fn, ghost_xf, bin_items;
     size_t bin_count, bin_fill, bin_start, l2_count, l2_off;
-    size_t l2_ghost, l2_owner, l2_dist, e_cnt3, e_cnt4, e_off3, e_off4, c3, c4, force, scan, total;
+    size_t l2_ghost, l2_owner, l2_dist, l2_vec, e_cnt3, e_cnt4, e_off3, e_off4, c3, c4, force, scan, total;
 };
 
-constexpr size_t kScanBytes = 8192;   // >= scan_tmp_bytes of the largest scan below (131072 entries)
+constexpr size_t kScanBytes = 8192;   // >= scan_tmp_bytes of the largest scan below (65536 entries)
 
 constexpr Layout make_layout() {
     Layout L{};
@@ -62,11 +62,14 @@ constexpr Layout make_layout() {
     L.atom_sys = take(kNaAtoms * sizeof(int));
     L.atom_type = take(kNaAtoms * sizeof(int));
     L.atom_orig = take(kNaAtoms * sizeof(int));
+    L.atom_self = take(kNaAtoms * sizeof(int));
+    L.ghost_id = take(kNaGhosts * sizeof(int));
     L.ghost_parent = take(kNaGhosts * sizeof(int));
     L.ghost_bin = take(kNaGhosts * sizeof(int));
     L.ghost_fs = take(3 * kNaGhosts * sizeof(double));
     L.ghost_xn = take(3 * kNaGhosts * sizeof(double));
     L.ghost_fn = take(3 * kNaGhosts * sizeof(double));
+    L.ghost_xf = take(3 * kNaGhosts * sizeof(float));
     L.bin_items = take(kNaGhosts * sizeof(int));
     L.bin_count = take(kNaBins * sizeof(int));
     L.bin_fill = take(kNaBins * sizeof(int));
@@ -76,6 +79,7 @@ constexpr Layout make_layout() {
     L.l2_ghost = take(kNaPairs * sizeof(int));
     L.l2_owner = take(kNaPairs * sizeof(int));
     L.l2_dist = take(kNaPairs * sizeof(double));
+    L.l2_vec = take(4 * kNaPairs * sizeof(float));
     L.e_cnt3 = take(kNaPairs * sizeof(int));
     L.e_cnt4 = take(kNaPairs * sizeof(int));
     L.e_off3 = take((kNaPairs + 1) * sizeof(long long));
@@ -160,10 +164,10 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     Status s = system_geometry(&cell[0], &cell[3], &cell[6], natom, small, P.max_cut2(), P.max_cut3(),
                                P.max_cut4(), P.o3 > 0, P.o4 > 0, d, vol, err);
     if (s != kOk) return s;
-    const long long n_ghost = (long long)d.n_atoms * d.side * d.side * d.side;
+    const long long n_ghost = (long long)d.n_atoms * d.gstride;
     if (d.n_atoms > kNaAtoms || n_ghost > kNaGhosts || d.bin_cap > kNaBins) {
         err = "ck_calculate_noalloc: configuration exceeds the static maximum (" + std::to_string(d.n_atoms) +
-              " atoms, " + std::to_string(n_ghost) + " ghost atoms, " + std::to_string(d.bin_cap) +
+              " atoms, " + std::to_string(n_ghost) + " ghost slots, " + std::to_string(d.bin_cap) +
               " bins; limits " + std::to_string(kNaAtoms) + ", " + std::to_string(kNaGhosts) + ", " +
               std::to_string(kNaBins) + ")";
         return kErrInput;
@@ -188,6 +192,9 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     B.atom_sys = reinterpret_cast<int*>(base + kLayout.atom_sys);
     B.atom_type = reinterpret_cast<int*>(base + kLayout.atom_type);
     B.atom_orig = reinterpret_cast<int*>(base + kLayout.atom_orig);
+    B.atom_self = reinterpret_cast<int*>(base + kLayout.atom_self);
+    B.ghost_id = reinterpret_cast<int*>(base + kLayout.ghost_id);
+    B.ghost_xf = reinterpret_cast<float*>(base + kLayout.ghost_xf);
     B.ghost_parent = reinterpret_cast<int*>(base + kLayout.ghost_parent);
     B.ghost_fs = reinterpret_cast<double*>(base + kLayout.ghost_fs);
     B.ghost_xn = reinterpret_cast<double*>(base + kLayout.ghost_xn);
@@ -202,6 +209,7 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     B.l2_off = reinterpret_cast<long long*>(base + kLayout.l2_off);
     B.l2_ghost = reinterpret_cast<int*>(base + kLayout.l2_ghost);
     B.l2_dist = reinterpret_cast<double*>(base + kLayout.l2_dist);
+    B.l2_vec = reinterpret_cast<float*>(base + kLayout.l2_vec);
     B.n2_cap = kNaPairs;
     B.e_cnt3 = reinterpret_cast<int*>(base + kLayout.e_cnt3);
     B.e_cnt4 = reinterpret_cast<int*>(base + kLayout.e_cnt4);

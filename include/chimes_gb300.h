@@ -111,9 +111,9 @@ int ck_export_lists(void *h, int *l2, int *l3, int *l4);
  * (n_replicates+1)^3 as in serial_chimes_interface::calculate),
  * d_force[natom][3], d_stress[9] (virial over volume).  Work is enqueued on
  * `stream` (a cudaStream_t, 0 = legacy default) and the call waits for it.
- * Every intermediate array lives in one static device array of about 17 MiB
+ * Every intermediate array lives in one static device array of about 13.4 MiB
  * that each GPU loading the library holds until the process exits; limits per
- * call: 2048 atoms after replication, 131072 ghost atoms, 65536 bin cells,
+ * call: 2048 atoms after replication, 65536 ghost-image slots, 65536 bin cells,
  * 65536 pairs, 131072 triplets, 65536 quadruplets.  Larger inputs return -2
  * (sizes known before the launch) or -5 (list sizes found on the device; the
  * outputs are then invalid), with the message in ck_last_error().  The first
