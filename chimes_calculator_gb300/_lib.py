@@ -64,6 +64,7 @@ SIGNATURES = {
     "ck_set_precision": (I, [P, I]),
     "ck_set_tuning": (I, [P, I, I, I]),
     "ck_use_graph": (I, [P, I]),
+    "ck_autotune": (I, [P, IP]),
     "ck_calculate_batch": (I, [P, I, IP, DP, IP, DP, IP, IP, DP, DP, DP]),
     "ck_stage_batch": (I, [P, I, IP, DP, IP, DP, IP, IP]),
     "ck_launch": (I, [P]),
@@ -77,6 +78,12 @@ SIGNATURES = {
     "ck_export_lists": (I, [P, IP, IP, IP]),
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
     "ck_calculate_noalloc": (I, [P, I, P, P, DP, I, P, P, P, P]),
+    "ck_server_open": (P, [I, D, LL, I]),
+    "ck_server_close": (None, [P]),
+    "ck_server_load_params": (I, [P, S]),
+    "ck_server_submit": (LL, [P, I, I, DP, IP, DP, I]),
+    "ck_server_take": (I, [P, LL, I, D, DP, DP, DP, DP]),
+    "ck_server_stats": (I, [P, LLP]),
 }
 
 

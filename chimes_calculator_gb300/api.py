@@ -107,6 +107,15 @@ class Calculator:
     def set_tuning(self, tpc3: int = 4, tpc4: int = 8, blocks_per_sm: int = 4):
         self._check(self.lib.ck_set_tuning(self.h, tpc3, tpc4, blocks_per_sm))
 
+    def autotune(self, packed=None):
+        """Picks threads per cluster and resident blocks for the staged batch
+        (stages `packed` first when given); returns (tpc3, tpc4, blocks_per_sm)."""
+        if packed is not None:
+            self.stage(packed)
+        out = (ctypes.c_int * 3)()
+        self._check(self.lib.ck_autotune(self.h, out))
+        return tuple(out)
+
     def use_graph(self, on: bool):
         self._check(self.lib.ck_use_graph(self.h, 1 if on else 0))
 

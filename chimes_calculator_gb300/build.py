@@ -26,7 +26,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CXX_SOURCES = ["ck_params.cpp", "ck_geom.cpp", "ck_engine.cpp", "ck_capi.cpp", "ck_chimesff.cpp"]
+CXX_SOURCES = ["ck_params.cpp", "ck_geom.cpp", "ck_engine.cpp", "ck_capi.cpp", "ck_chimesff.cpp", "ck_server.cpp"]
 CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_direct.cu", "ck_noalloc.cu"]
 
 
@@ -82,7 +82,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     print(err, file=sys.stderr)
     if jobs or force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
-        _compile([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt"])
+        _compile([NVCC, *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt"])
         shutil.move(tmp, LIB)
     return LIB
 

@@ -275,6 +275,14 @@ int ck_set_tuning(void* h, int tpc3, int tpc4, int blocks_per_sm) {
     return ck::kOk;
 }
 
+int ck_autotune(void* h, int* chosen) {
+    if (int st = check_handle(h)) return st;
+    std::string err;
+    ck::Status st = static_cast<Instance*>(h)->eng.autotune(chosen, err);
+    if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
 int ck_use_graph(void* h, int on) {
     if (int st = check_handle(h)) return st;
     static_cast<Instance*>(h)->eng.use_graph = on != 0;

@@ -147,6 +147,7 @@ struct BatchView {
     double* ev;                    // [n_sys][8]: energy, virial xx xy xz yy yz zz, spare
     int* flags;                    // [8] device error flags: 0 capacity, 1 geometry, 2 badness max,
                                    //     3 penalty count, 4 below-rin count, 5 timeout
+    unsigned long long* queue;     // [2] work-queue heads of the 3-body and 4-body force kernels
 };
 
 }  // namespace ck

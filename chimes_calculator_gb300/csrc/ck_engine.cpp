@@ -66,6 +66,7 @@ Status Engine::init_device(std::string& err) {
     CK_TRY(h_flags_.reserve(8));
     CK_TRY(h_counts_.reserve(4));
     CK_TRY(d_flags_.reserve(8));
+    CK_TRY(d_queue_.reserve(2));
     ready_ = true;
     return kOk;
 }
@@ -256,8 +257,19 @@ Status Engine::ensure_lists(std::string& err) {
     B.e_cnt3 = d_e_cnt3_.p; B.e_cnt4 = d_e_cnt4_.p; B.e_off3 = d_e_off3_.p; B.e_off4 = d_e_off4_.p;
     B.c3 = d_c3_.p; B.c4 = d_c4_.p;
     B.n3_cap = n3_cap_; B.n4_cap = n4_cap_;
-    B.force = d_force_.p; B.ev = d_ev_.p; B.flags = d_flags_.p;
+    B.force = d_force_.p; B.ev = d_ev_.p; B.flags = d_flags_.p; B.queue = d_queue_.p;
     return kOk;
+}
+
+// Stage events: inside a stream capture they become external event-record
+// nodes of the graph (so each replay records them); outside a capture the
+// external flag is refused, and a plain record is used.
+static cudaError_t record_stage_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+    return cudaEventRecord(ev, st);
 }
 
 Status Engine::enqueue(std::string& err) {
@@ -267,7 +279,7 @@ Status Engine::enqueue(std::string& err) {
     if (profile) {
         for (auto& e : ev_)
             if (!e) CK_TRY(cudaEventCreate(&e));
-        CK_TRY(cudaEventRecordWithFlags(ev_[0], st, cudaEventRecordExternal));
+        CK_TRY(record_stage_event(ev_[0], st));
     }
     CK_TRY(cudaMemsetAsync(B.bin_count, 0, sizeof(int) * B.n_bins_total, st));
     CK_TRY(cudaMemsetAsync(B.bin_fill, 0, sizeof(int) * B.n_bins_total, st));
@@ -287,15 +299,15 @@ Status Engine::enqueue(std::string& err) {
     exclusive_scan(B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
     launch_enum(B, d_l2_owner_.p, true, st);
     launch_check(B, st);
-    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[1], st, cudaEventRecordExternal));
+    if (profile) CK_TRY(record_stage_event(ev_[1], st));
     ForceLaunch L = tuning;
     L.precision = precision;
     launch_force2(B, d_l2_owner_.p, L, st);
-    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[2], st, cudaEventRecordExternal));
+    if (profile) CK_TRY(record_stage_event(ev_[2], st));
     if (L.stride3 > 0) launch_force3(B, L, st);
-    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[3], st, cudaEventRecordExternal));
+    if (profile) CK_TRY(record_stage_event(ev_[3], st));
     if (L.stride4 > 0) launch_force4(B, L, st);
-    if (profile) CK_TRY(cudaEventRecordWithFlags(ev_[4], st, cudaEventRecordExternal));
+    if (profile) CK_TRY(record_stage_event(ev_[4], st));
     ev_recorded_ = profile;
     kernels_per_launch = (int)(launch_counter() - k0);
     CK_TRY(cudaMemcpyAsync(h_force_.p, B.force, sizeof(double) * 3 * B.n_in_total, cudaMemcpyDeviceToHost, st));
@@ -410,6 +422,105 @@ Status Engine::run(const std::vector<SystemSpec>& sys, double* force_out, std::v
     }
     err = "list capacity did not converge";
     return kErrCapacity;
+}
+
+std::string Engine::tune_key() const {
+    std::string k = "p" + std::to_string(precision);
+    std::vector<int> seen;
+    for (const SysDesc& d : hsys_)
+        if (std::find(seen.begin(), seen.end(), d.pset) == seen.end()) seen.push_back(d.pset);
+    for (int s : seen) {
+        const HostParams& P = *sets_[s].host;
+        k += "|" + std::to_string(P.ntypes) + ":" + std::to_string(P.o2) + "/" + std::to_string(P.o3) + "/" +
+             std::to_string(P.o4);
+    }
+    auto lg = [](long long v) { int b = 0; while (v > 1) { v >>= 1; b++; } return b; };
+    k += "|a" + std::to_string(lg(V_.n_atoms_total)) + "|s" + std::to_string(lg(V_.n_sys));
+    return k;
+}
+
+Status Engine::autotune(int* chosen, std::string& err) {
+    if (!staged_) {
+        err = "autotune needs a staged batch";
+        return kErrState;
+    }
+    const std::string key = tune_key();
+    for (auto& kv : tune_cache_)
+        if (kv.first == key) {
+            tuning.tpc3 = kv.second.tpc3;
+            tuning.tpc4 = kv.second.tpc4;
+            tuning.blocks_per_sm = kv.second.blocks_per_sm;
+            if (chosen) { chosen[0] = tuning.tpc3; chosen[1] = tuning.tpc4; chosen[2] = tuning.blocks_per_sm; }
+            return kOk;
+        }
+    const bool save_profile = profile, save_graph = use_graph;
+    profile = true;
+    use_graph = false;
+    std::vector<SystemResult> res;
+    auto run_once = [&](double& ms3, double& ms4) -> Status {
+        for (int attempt = 0; attempt < 6; attempt++) {
+            for (double& v : stage_ms) v = 0.0;
+            stage_launches = 0;
+            Status st = launch(err);
+            if (st != kOk) return st;
+            st = collect(nullptr, res, err);
+            if (st == kErrCapacity) {
+                st = ensure_lists(err);
+                if (st != kOk) return st;
+                continue;
+            }
+            if (st != kOk) return st;
+            st = read_stage_times(err);
+            if (st != kOk) return st;
+            ms3 = stage_ms[2];
+            ms4 = stage_ms[3];
+            return kOk;
+        }
+        err = "list capacity did not converge";
+        return kErrCapacity;
+    };
+    double a, b;
+    Status st = run_once(a, b);   // warm-up and list sizing
+    const int tpcs[] = {1, 2, 4, 8, 16, 32};
+    double best3 = 1e300, best4 = 1e300;
+    int t3 = tuning.tpc3, t4 = tuning.tpc4;
+    for (int t : tpcs) {
+        if (st != kOk) break;
+        tuning.tpc3 = t;
+        tuning.tpc4 = t;
+        double m3 = 1e300, m4 = 1e300;
+        for (int rep = 0; rep < 2 && st == kOk; rep++) {
+            st = run_once(a, b);
+            m3 = std::min(m3, a);
+            m4 = std::min(m4, b);
+        }
+        if (m3 < best3) { best3 = m3; t3 = t; }
+        if (m4 < best4) { best4 = m4; t4 = t; }
+    }
+    tuning.tpc3 = t3;
+    tuning.tpc4 = t4;
+    double bestb = 1e300;
+    int bb = tuning.blocks_per_sm;
+    const int bps[] = {1, 2, 4, 8};
+    for (int v : bps) {
+        if (st != kOk) break;
+        tuning.blocks_per_sm = v;
+        double m = 1e300;
+        for (int rep = 0; rep < 2 && st == kOk; rep++) {
+            st = run_once(a, b);
+            m = std::min(m, a + b);
+        }
+        if (m < bestb) { bestb = m; bb = v; }
+    }
+    tuning.blocks_per_sm = bb;
+    profile = save_profile;
+    use_graph = save_graph;
+    for (double& v : stage_ms) v = 0.0;
+    stage_launches = 0;
+    if (st != kOk) return st;
+    tune_cache_.push_back({key, tuning});
+    if (chosen) { chosen[0] = tuning.tpc3; chosen[1] = tuning.tpc4; chosen[2] = tuning.blocks_per_sm; }
+    return kOk;
 }
 
 Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, const double* dr, const int* typ,

@@ -115,6 +115,13 @@ public:
     int kernels_per_launch = 0;          // kernels one launch() enqueues
     Status read_stage_times(std::string& err);   // adds the last launch's event intervals
 
+    // Autotuner for the staged batch: times the 3-body and 4-body force stages
+    // (CUDA events on the engine's stream) for each threads-per-cluster value
+    // and then each resident-blocks value, keeps the fastest, and caches the
+    // choice by the batch's shape (precision, parameter orders, atom and system
+    // counts in powers of two).  chosen = {tpc3, tpc4, blocks_per_sm}.
+    Status autotune(int* chosen, std::string& err);
+
     // Per-cluster evaluation (the chimesFF::compute_nB entry points): n
     // clusters of `nbody` atoms given as distances dx[n][P], displacement
     // vectors dr[n][P][3] (atom2 - atom1) and type indices typ[n][nbody].
@@ -165,6 +172,7 @@ private:
     DevBuf<int> d_c3_, d_c4_;
     DevBuf<double> d_force_, d_ev_;
     DevBuf<int> d_flags_;
+    DevBuf<unsigned long long> d_queue_;
     DevBuf<unsigned char> d_scan_tmp_;
     DevBuf<double> d_dir_d_;      // per-cluster inputs and outputs (doubles)
     DevBuf<int> d_dir_i_;         // per-cluster types and status
@@ -185,6 +193,8 @@ private:
     Status ensure_lists(std::string& err);
     Status enqueue(std::string& err);
     void drop_graph();
+    std::string tune_key() const;
+    std::vector<std::pair<std::string, ForceLaunch>> tune_cache_;
 };
 
 const char* status_name(int s);

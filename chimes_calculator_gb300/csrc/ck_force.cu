@@ -200,13 +200,19 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
     double* fcs = geo + 4 * NP;
     double* fcds = fcs + NP;
 
-    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    const long long wid = (long long)blockIdx.x * (blockDim.x >> 5) + warp_in_block;
+    // work queue: each warp claims kChunk consecutive steps (G clusters each) at a
+    // time, so warps that drew cheap clusters come back for more
     const long long steps = (n + G - 1) / G;
-    const long long chunk = (steps + nwarps - 1) / nwarps;
-    const long long st0 = wid * chunk, st1 = min(steps, st0 + chunk);
+    constexpr long long kChunk = 2;
+    unsigned long long* head = &B.queue[NB - 3];
     EVAcc acc;
 
+    for (;;) {
+    long long st0 = 0;
+    if (lane == 0) st0 = (long long)atomicAdd(head, (unsigned long long)kChunk);
+    st0 = __shfl_sync(kFull, st0, 0);
+    if (st0 >= steps) break;
+    const long long st1 = min(steps, st0 + kChunk);
     for (long long step = st0; step < st1; step++) {
         const long long c = step * G + grp;
         const bool have = c < n;
@@ -312,6 +318,7 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
         }
         __syncwarp();
     }
+    }
     acc.flush_warp(B);
 }
 
@@ -394,13 +401,12 @@ double fma_peak_tflops(int precision) {
 }
 
 int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
+    static const int n = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
     return n;
 }
 

@@ -24,6 +24,7 @@
 //    distance that is stored, is evaluated exactly in FP64.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "ck_common.h"
@@ -517,6 +518,7 @@ __global__ void k_reset(BatchView B) {
     if (i < 8LL * B.n_sys) B.ev[i] = 0.0;
     if (i < 3 * B.n_in_total) B.force[i] = 0.0;
     if (i < 8) B.flags[i] = 0;
+    if (i < 2) B.queue[i] = 0ull;
     if (i < B.n_sys) B.sys[i].err = 0;
 }
 
@@ -577,9 +579,11 @@ unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / 
 
 }  // namespace
 
-static long long g_launches = 0;
-void count_launch() { g_launches++; }
-long long launch_counter() { return g_launches; }
+// Kernel launches enqueued by this library (all threads; a per-engine count
+// is the difference across one enqueue sequence on that engine's thread).
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_counter() { return g_launches.load(std::memory_order_relaxed); }
 
 size_t scan_tmp_bytes(long long n) {
     size_t total = 0;

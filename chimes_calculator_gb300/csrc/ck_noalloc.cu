@@ -41,7 +41,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // byte layout of the scratch array
 struct Layout {
-    size_t sys, minmax, ev, flags, in_pos, in_type, atom_sys, atom_type, atom_orig, atom_self;
+    size_t sys, minmax, ev, flags, queue, in_pos, in_type, atom_sys, atom_type, atom_orig, atom_self;
     size_t ghost_id, ghost_parent, ghost_bin, ghost_fs, ghost_xn, ghost_fn, ghost_xf, bin_items;
     size_t bin_count, bin_fill, bin_start, l2_count, l2_off;
     size_t l2_ghost, l2_owner, l2_dist, l2_vec, e_cnt3, e_cnt4, e_off3, e_off4, c3, c4, force, scan, total;
@@ -57,6 +57,7 @@ constexpr Layout make_layout() {
     L.minmax = take(6 * sizeof(unsigned long long));
     L.ev = take(8 * sizeof(double));
     L.flags = take(8 * sizeof(int));
+    L.queue = take(2 * sizeof(unsigned long long));
     L.in_pos = take(3 * kNaAtoms * sizeof(double));
     L.in_type = take(kNaAtoms * sizeof(int));
     L.atom_sys = take(kNaAtoms * sizeof(int));
@@ -222,6 +223,7 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     B.force = reinterpret_cast<double*>(base + kLayout.force);
     B.ev = reinterpret_cast<double*>(base + kLayout.ev);
     B.flags = reinterpret_cast<int*>(base + kLayout.flags);
+    B.queue = reinterpret_cast<unsigned long long*>(base + kLayout.queue);
     int* l2_owner = reinterpret_cast<int*>(base + kLayout.l2_owner);
     void* scan = base + kLayout.scan;
 

@@ -1,0 +1,359 @@
+// Continuous-batching request server.
+//
+// Single-point energy/force/stress requests (one periodic configuration each)
+// are submitted from any thread and queue in arrival order.  Each worker
+// thread owns one Engine -- its own CUDA stream, device-resident parameter
+// sets and grow-only workspace -- and loops: take the oldest waiting requests
+// while the batch stays under the atom limit and the device-memory estimate of
+// everything in flight stays under the HBM budget, evaluate them as one batch
+// (one set of launches, see ck_engine.h), publish the results, repeat.  With
+// several workers, a batch forms and starts while earlier ones still run, so
+// requests that arrive during a batch are admitted as soon as a worker and
+// memory free up, and their work overlaps on the device.  Latency is measured
+// per request from submit to published result.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ck_engine.h"
+#include "ck_geom.h"
+
+namespace ck {
+
+namespace {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    long long id = 0;
+    int slot = 0;
+    int n = 0;
+    std::vector<double> pos;
+    std::vector<int> types;
+    double cell[9] = {0};
+    bool small = false;
+    double est_bytes = 0.0;
+    // results
+    bool done = false;
+    int status = 0;
+    std::string err;
+    double energy = 0.0, stress[9] = {0};
+    std::vector<double> force;
+    double t_submit = 0.0, t_done = 0.0;
+};
+
+}  // namespace
+
+class Server {
+public:
+    Server(int n_workers, double budget_bytes, long long max_batch_atoms, int precision)
+        : budget_(budget_bytes), max_atoms_(max_batch_atoms) {
+        if (n_workers < 1) n_workers = 1;
+        for (int w = 0; w < n_workers; w++) {
+            engines_.emplace_back(new Engine());
+            engines_.back()->precision = precision;
+            engine_mu_.emplace_back(new std::mutex());
+        }
+    }
+
+    ~Server() { stop(); }
+
+    Status start(std::string& err) {
+        for (auto& e : engines_) {
+            Status st = e->init_device(err);
+            if (st != kOk) return st;
+        }
+        for (size_t w = 0; w < engines_.size(); w++) threads_.emplace_back([this, w] { worker((int)w); });
+        return kOk;
+    }
+
+    void stop() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stopping_ = true;
+        }
+        cv_work_.notify_all();
+        for (auto& t : threads_)
+            if (t.joinable()) t.join();
+        threads_.clear();
+    }
+
+    // Loads a parameter file into every worker's engine (same slot everywhere).
+    int load_params(const std::string& path, std::string& err) {
+        std::lock_guard<std::mutex> g(load_mu_);
+        int slot = -1;
+        for (size_t w = 0; w < engines_.size(); w++) {
+            std::lock_guard<std::mutex> ge(*engine_mu_[w]);
+            int s = engines_[w]->load_params(path, err);
+            if (s < 0) return s;
+            if (slot >= 0 && s != slot) {
+                err = "parameter slots diverged between workers";
+                return kErrState;
+            }
+            slot = s;
+        }
+        nslots_ = slot + 1;
+        return slot;
+    }
+
+    long long submit(int slot, int n, const double* pos, const int* types, const double* cell, bool small,
+                     std::string& err) {
+        if (slot < 0 || slot >= nslots_) {
+            err = "parameter set not loaded";
+            return kErrState;
+        }
+        if (n <= 0) {
+            err = "natom must be positive";
+            return kErrInput;
+        }
+        std::unique_ptr<Request> r(new Request());
+        r->slot = slot;
+        r->n = n;
+        r->pos.assign(pos, pos + 3 * (size_t)n);
+        r->types.assign(types, types + n);
+        std::memcpy(r->cell, cell, sizeof(r->cell));
+        r->small = small;
+        r->est_bytes = estimate_bytes(*r);
+        r->t_submit = now_s();
+        std::lock_guard<std::mutex> g(mu_);
+        r->id = next_id_++;
+        const long long id = r->id;
+        queue_.push_back(r.get());
+        all_[id] = std::move(r);
+        submitted_++;
+        cv_work_.notify_one();
+        return id;
+    }
+
+    // 1 done (results copied, request released), 0 pending, < 0 failed (released)
+    int take(long long id, bool wait, double timeout_s, double* energy, double* force, double* stress,
+             double* latency, std::string& err) {
+        std::unique_lock<std::mutex> g(mu_);
+        auto it = all_.find(id);
+        if (it == all_.end()) {
+            err = "unknown request id";
+            return kErrInput;
+        }
+        Request* r = it->second.get();
+        if (!r->done && wait) {
+            const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+            cv_done_.wait_until(g, deadline, [r] { return r->done; });
+        }
+        if (!r->done) return 0;
+        int st = r->status;
+        if (st == kOk) {
+            if (energy) *energy = r->energy;
+            if (force) std::memcpy(force, r->force.data(), sizeof(double) * r->force.size());
+            if (stress) std::memcpy(stress, r->stress, sizeof(r->stress));
+            if (latency) *latency = r->t_done - r->t_submit;
+        } else {
+            err = r->err;
+        }
+        all_.erase(it);
+        return st == kOk ? 1 : st;
+    }
+
+    void stats(long long* out) {
+        std::lock_guard<std::mutex> g(mu_);
+        out[0] = submitted_;
+        out[1] = completed_;
+        out[2] = batches_;
+        out[3] = max_batch_;
+        out[4] = (long long)inflight_bytes_;
+        out[5] = (long long)peak_inflight_bytes_;
+    }
+
+private:
+    // Device bytes a request needs while in flight: ghost-image slots, bins,
+    // lists and clusters, from the same host geometry the engine uses.
+    double estimate_bytes(const Request& r) {
+        std::lock_guard<std::mutex> g(load_mu_);
+        const HostParams& P = engines_[0]->params(r.slot);
+        SysDesc d;
+        std::memset(&d, 0, sizeof(d));
+        double vol = 0.0;
+        std::string e;
+        if (system_geometry(&r.cell[0], &r.cell[3], &r.cell[6], r.n, r.small, P.max_cut2(), P.max_cut3(),
+                            P.max_cut4(), P.o3 > 0, P.o4 > 0, d, vol, e) != kOk)
+            return 0.0;   // rejected later by the engine with its message
+        const double rho = d.n_atoms / (vol > 0 ? vol : 1.0);
+        const double m = rho * 4.18879 * d.search * d.search * d.search;
+        const double n2 = d.n_atoms * (0.55 * m + 4);
+        const double n3 = d.has3 ? d.n_atoms * (0.3 * m * m * std::pow(d.c3 / d.search, 6.0) + 4) : 0.0;
+        const double n4 = d.has4 ? d.n_atoms * (0.1 * m * m * m * std::pow(d.c4 / d.search, 9.0) + 4) : 0.0;
+        return (double)d.n_atoms * d.gstride * 110.0 + (double)d.bin_cap * 20.0 + n2 * 70.0 + n3 * 12.0 +
+               n4 * 16.0 + d.n_atoms * 120.0;
+    }
+
+    void worker(int w) {
+        for (;;) {
+            std::vector<Request*> batch;
+            double bytes = 0.0;
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_work_.wait(g, [this] { return stopping_ || admissible(); });
+                if (stopping_ && queue_.empty()) return;
+                long long atoms = 0;
+                while (!queue_.empty()) {
+                    Request* r = queue_.front();
+                    const bool first = batch.empty();
+                    if (!first && atoms + r->n > max_atoms_) break;
+                    if (inflight_bytes_ + bytes + r->est_bytes > budget_ && !(first && inflight_bytes_ == 0.0)) break;
+                    queue_.pop_front();
+                    batch.push_back(r);
+                    atoms += r->n;
+                    bytes += r->est_bytes;
+                }
+                if (batch.empty()) continue;
+                inflight_bytes_ += bytes;
+                peak_inflight_bytes_ = std::max(peak_inflight_bytes_, inflight_bytes_);
+            }
+            run_batch(w, batch);
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                inflight_bytes_ -= bytes;
+                if (inflight_bytes_ < 1e-6) inflight_bytes_ = 0.0;
+                batches_++;
+                max_batch_ = std::max(max_batch_, (long long)batch.size());
+                completed_ += (long long)batch.size();
+            }
+            cv_done_.notify_all();
+            cv_work_.notify_all();
+        }
+    }
+
+    // the oldest waiting request fits the budget (always true when nothing is in flight)
+    bool admissible() const {
+        if (queue_.empty()) return false;
+        return inflight_bytes_ == 0.0 || inflight_bytes_ + queue_.front()->est_bytes <= budget_;
+    }
+
+    void run_batch(int w, const std::vector<Request*>& batch) {
+        Engine& eng = *engines_[w];
+        std::vector<SystemSpec> specs(batch.size());
+        long long total = 0;
+        for (size_t i = 0; i < batch.size(); i++) {
+            SystemSpec& s = specs[i];
+            s.n = batch[i]->n;
+            s.pos = batch[i]->pos.data();
+            s.types = batch[i]->types.data();
+            std::memcpy(s.cell, batch[i]->cell, sizeof(s.cell));
+            s.small = batch[i]->small;
+            s.pset = batch[i]->slot;
+            total += s.n;
+        }
+        std::vector<double> force(3 * (size_t)total);
+        std::vector<SystemResult> res;
+        std::string err;
+        Status st;
+        {
+            std::lock_guard<std::mutex> ge(*engine_mu_[w]);
+            st = eng.run(specs, force.data(), res, err);
+        }
+        if (st != kOk && batch.size() > 1) {
+            // isolate the failing request(s): evaluate each one alone
+            for (Request* r : batch) run_batch(w, {r});
+            return;
+        }
+        std::lock_guard<std::mutex> g(mu_);
+        long long off = 0;
+        const double t = now_s();
+        for (size_t i = 0; i < batch.size(); i++) {
+            Request* r = batch[i];
+            r->status = st;
+            if (st == kOk) {
+                const SystemResult& q = res[i];
+                r->energy = q.energy;
+                const double* v = q.virial;
+                const double full[9] = {v[0], v[1], v[2], v[1], v[3], v[4], v[2], v[4], v[5]};
+                for (int k = 0; k < 9; k++) r->stress[k] = full[k] / q.vol;
+                r->force.assign(force.begin() + 3 * off, force.begin() + 3 * (off + r->n));
+            } else {
+                r->err = err;
+            }
+            r->t_done = t;
+            r->done = true;
+            off += r->n;
+        }
+    }
+
+    std::vector<std::unique_ptr<Engine>> engines_;
+    std::vector<std::unique_ptr<std::mutex>> engine_mu_;
+    std::vector<std::thread> threads_;
+    std::mutex mu_, load_mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::deque<Request*> queue_;
+    std::map<long long, std::unique_ptr<Request>> all_;
+    long long next_id_ = 1;
+    int nslots_ = 0;
+    bool stopping_ = false;
+    double budget_;
+    long long max_atoms_;
+    double inflight_bytes_ = 0.0, peak_inflight_bytes_ = 0.0;
+    long long submitted_ = 0, completed_ = 0, batches_ = 0, max_batch_ = 0;
+};
+
+}  // namespace ck
+
+extern "C" {
+
+void* ck_server_open(int n_workers, double hbm_budget_gb, long long max_batch_atoms, int precision) {
+    if (max_batch_atoms <= 0) max_batch_atoms = 1 << 20;
+    if (!(hbm_budget_gb > 0)) hbm_budget_gb = 150.0;
+    ck::Server* s = new ck::Server(n_workers, hbm_budget_gb * 1e9, max_batch_atoms, precision ? 1 : 0);
+    std::string err;
+    if (s->start(err) != ck::kOk) {
+        delete s;
+        ck::report_error(ck::kErrCuda, err);
+        return nullptr;
+    }
+    return s;
+}
+
+void ck_server_close(void* s) { delete static_cast<ck::Server*>(s); }
+
+int ck_server_load_params(void* s, const char* path) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    std::string err;
+    int slot = static_cast<ck::Server*>(s)->load_params(path ? path : "", err);
+    if (slot < 0) return ck::report_error(slot, err);
+    return slot;
+}
+
+long long ck_server_submit(void* s, int slot, int natom, const double* pos, const int* types, const double* cell,
+                           int small) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    std::string err;
+    long long id = static_cast<ck::Server*>(s)->submit(slot, natom, pos, types, cell, small != 0, err);
+    if (id < 0) return ck::report_error((int)id, err);
+    return id;
+}
+
+int ck_server_take(void* s, long long id, int wait, double timeout_s, double* energy, double* force, double* stress,
+                   double* latency_s) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    std::string err;
+    int st = static_cast<ck::Server*>(s)->take(id, wait != 0, timeout_s, energy, force, stress, latency_s, err);
+    if (st < 0) return ck::report_error(st, err);
+    return st;
+}
+
+int ck_server_stats(void* s, long long* out) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    static_cast<ck::Server*>(s)->stats(out);
+    return ck::kOk;
+}
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+"""Continuous-batching serving of single-point energy/force/stress requests.
+
+``Server`` wraps the library's request server (ck_server_* in
+include/chimes_gb300.h): worker threads, each with its own CUDA stream and
+device-resident parameter sets, batch the waiting requests under an atom limit
+and an HBM budget and overlap their batches on the GPU.  ``poisson_run``
+offers requests at Poisson-distributed arrival times and reports per-request
+latency percentiles and throughput; ``serial_run`` is the plain per-request
+path (one evaluation at a time through ``Calculator``) for comparison.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import threading
+import time
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from .api import FP64, Calculator, ChimesError
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class Server:
+    def __init__(self, workers: int = 2, hbm_budget_gb: float = 150.0, max_batch_atoms: int = 1 << 16,
+                 precision: int = FP64):
+        self.lib = _lib.load()
+        self.lib.ck_set_error_mode(1)
+        self.h = self.lib.ck_server_open(workers, hbm_budget_gb, max_batch_atoms, precision)
+        if not self.h:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        self._natoms: Dict[int, int] = {}
+        self._lock = threading.Lock()
+
+    def close(self):
+        if self.h:
+            self.lib.ck_server_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_params(self, path: str) -> int:
+        slot = self.lib.ck_server_load_params(self.h, path.encode())
+        if slot < 0:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        return slot
+
+    def submit(self, pos, types, cell, slot: int = 0, small: bool = False) -> int:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        rid = self.lib.ck_server_submit(self.h, slot, pos.shape[0], _dp(pos), _ip(types), _dp(cell), int(small))
+        if rid < 0:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        with self._lock:
+            self._natoms[rid] = pos.shape[0]
+        return rid
+
+    def take(self, rid: int, wait: bool = True, timeout: float = 120.0) -> Optional[dict]:
+        with self._lock:
+            n = self._natoms[rid]
+        e = ctypes.c_double()
+        lat = ctypes.c_double()
+        force = np.zeros((n, 3))
+        stress = np.zeros(9)
+        st = self.lib.ck_server_take(self.h, rid, int(wait), timeout, ctypes.byref(e), _dp(force), _dp(stress),
+                                     ctypes.byref(lat))
+        if st == 0:
+            return None
+        with self._lock:
+            self._natoms.pop(rid, None)
+        if st < 0:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        return {"energy": e.value, "force": force, "stress": stress, "latency": lat.value}
+
+    def stats(self) -> dict:
+        out = (ctypes.c_longlong * 6)()
+        self.lib.ck_server_stats(self.h, out)
+        return {"submitted": out[0], "completed": out[1], "batches": out[2], "largest_batch": out[3],
+                "bytes_in_flight": out[4], "peak_bytes_in_flight": out[5]}
+
+
+def serving_workload(n_requests: int, seed: int = 1105, n_min: int = 16, n_max: int = 4096):
+    """Requests of the serving workload: each draws one of three parameter
+    sets (12/8/4 with one element, 12/10/4 with two, 12/8/4 with three); atom
+    counts log-uniform in [n_min, n_max]; density U(0.05, 0.12) per A^3."""
+    from . import synth
+    rng = np.random.default_rng(seed)
+    specs = synth.specs_c5()
+    reqs = []
+    for q in range(n_requests):
+        slot = int(rng.integers(len(specs)))
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        rho = rng.uniform(0.05, 0.12)
+        L = (n / rho) ** (1.0 / 3.0)
+        els = list(specs[slot].elements)
+        cfg = synth.random_config(n, np.diag([L, L, L]), els, 1.0, seed=int(rng.integers(1 << 31)))
+        reqs.append((slot, cfg))
+    return specs, reqs
+
+
+def poisson_run(server: Server, requests: Sequence[Tuple[int, object]], type_idx, rate_hz: float,
+                seed: int = 7) -> dict:
+    """Submits requests at Poisson arrival times (mean rate rate_hz) from one
+    thread while another collects them; returns latency percentiles and
+    throughput.  type_idx(slot, cfg) -> int32 type indices."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_hz, size=len(requests))
+    ids: List[int] = [0] * len(requests)
+    ready = [threading.Event() for _ in requests]
+    prepared = [(slot, cfg.pos, type_idx(slot, cfg), cfg.cell) for slot, cfg in requests]
+
+    def submitter():
+        t_next = time.perf_counter()
+        for q, (slot, pos, ty, cell) in enumerate(prepared):
+            t_next += gaps[q]
+            while True:
+                dt = t_next - time.perf_counter()
+                if dt <= 0:
+                    break
+                time.sleep(min(dt, 0.002))
+            ids[q] = server.submit(pos, ty, cell, slot=slot)
+            ready[q].set()
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat = []
+    atoms = 0
+    for q in range(len(requests)):
+        ready[q].wait()
+        r = server.take(ids[q], wait=True)
+        lat.append(r["latency"])
+        atoms += requests[q][1].n_atoms
+    wall = time.perf_counter() - t0
+    th.join()
+    lat = np.array(lat)
+    return {"offered_rate_hz": rate_hz, "requests": len(requests), "wall_s": wall,
+            "throughput_atoms_per_s": atoms / wall, "throughput_req_per_s": len(requests) / wall,
+            "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "mean_ms": 1e3 * float(lat.mean()), "stats": server.stats()}
+
+
+def serial_run(calc: Calculator, requests: Sequence[Tuple[int, object]], type_idx) -> dict:
+    """The plain per-request GPU path: one evaluation at a time."""
+    lat = []
+    atoms = 0
+    t0 = time.perf_counter()
+    for slot, cfg in requests:
+        ty = type_idx(slot, cfg)
+        a = time.perf_counter()
+        calc.evaluate(cfg.pos, ty, cfg.cell, slot=slot)
+        lat.append(time.perf_counter() - a)
+        atoms += cfg.n_atoms
+    wall = time.perf_counter() - t0
+    lat = np.array(lat)
+    return {"requests": len(requests), "wall_s": wall, "throughput_atoms_per_s": atoms / wall,
+            "throughput_req_per_s": len(requests) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99))}

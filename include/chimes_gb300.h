@@ -57,6 +57,12 @@ int ck_type_index(void *h, int slot, const char *name);
 int ck_set_precision(void *h, int precision);
 /* threads per 3-body and 4-body cluster (1,2,4,8,16,32) and resident blocks per SM */
 int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
+/* Autotuner for the batch staged with ck_stage_batch: times the 3-body and
+ * 4-body force kernels (CUDA events) for threads per cluster 1..32 and then
+ * 1, 2, 4, 8 resident blocks per SM, keeps the fastest and caches it by the
+ * batch's shape (precision, parameter orders, atom and configuration counts
+ * rounded to powers of two).  chosen[3] = tpc3, tpc4, blocks_per_sm. */
+int ck_autotune(void *h, int *chosen);
 /* replay the whole list-build + force sequence as one CUDA graph (1) or launch it stream-ordered (0) */
 int ck_use_graph(void *h, int on);
 
@@ -123,6 +129,30 @@ int ck_export_lists(void *h, int *l2, int *l3, int *l4);
  * streams, threads or handles) race on it and corrupt each other's results. */
 int ck_calculate_noalloc(void *h, int natom, const double *d_pos, const int *d_types, const double *cell,
                          int small, double *d_energy, double *d_force, double *d_stress, void *stream);
+
+/* Continuous-batching request server (no counterpart in the reference).
+ * n_workers threads each own an engine (CUDA stream, device-resident
+ * parameter sets, workspace); each takes the oldest waiting requests while the
+ * batch stays under max_batch_atoms and the estimated device memory of all
+ * batches in flight stays under hbm_budget_gb, evaluates them in one set of
+ * launches and publishes the results.  Requests submitted while batches run
+ * join the next batch a worker forms; batches of different workers overlap on
+ * the GPU.  precision: 0 FP64, 1 mixed.  Returns NULL on failure. */
+void *ck_server_open(int n_workers, double hbm_budget_gb, long long max_batch_atoms, int precision);
+void ck_server_close(void *server);
+/* loads a parameter file into every worker; returns its slot */
+int ck_server_load_params(void *server, const char *path);
+/* queues one configuration (host arrays are copied); returns a request id > 0 */
+long long ck_server_submit(void *server, int slot, int natom, const double *pos, const int *types,
+                           const double *cell, int small);
+/* Results of a request: returns 1 when done (outputs written: energy, force[natom][3],
+ * stress[9], latency from submit to completion in seconds; the request is
+ * released), 0 while pending (wait = 1 blocks up to timeout_s), or a negative
+ * status if the request failed (released; message in ck_last_error). */
+int ck_server_take(void *server, long long id, int wait, double timeout_s, double *energy, double *force,
+                   double *stress, double *latency_s);
+/* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
+int ck_server_stats(void *server, long long *out);
 
 /* Batched per-cluster evaluation (chimesFF::compute_nB semantics, FP64) with
  * the handle's current parameter set: n clusters of nbody = 2, 3 or 4 atoms,

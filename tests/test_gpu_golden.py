@@ -63,6 +63,21 @@ def test_threads_per_cluster_variants(golden, native_lib, tpc):
     assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
 
 
+def test_autotune_keeps_results(golden, native_lib):
+    from chimes_calculator_gb300 import MIXED, Calculator
+    g = golden["c2_small"]
+    for prec in (0, MIXED):
+        c = Calculator(precision=prec)
+        c.load_params(g.params)
+        packed = c.pack([(g.cfg.pos, g.cfg.types, g.cfg.cell)])
+        t3, t4, bps = c.autotune(packed)
+        assert t3 in (1, 2, 4, 8, 16, 32) and t4 in (1, 2, 4, 8, 16, 32) and bps in (1, 2, 4, 8)
+        assert c.autotune() == (t3, t4, bps)          # cached for the same batch shape
+        r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell)
+        tol = E_REL_TOL if prec == 0 else 1e-6
+        assert abs(r["energy"] - g.energy) <= tol * max(1.0, abs(g.energy))
+
+
 def test_graph_replay(golden, native_lib):
     from chimes_calculator_gb300 import Calculator
     g = golden["c2"]
