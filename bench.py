@@ -147,10 +147,11 @@ def algorithmic_flops(calc, cfg, params_path):
         return (f[a] + sh) @ cell
 
     tup = calc.tuple_table(0)
+    fac = calc.tuple_factored(0)
     out = {}
     for nb, lst, order in ((3, l3, o3), (4, l4, o4)):
         if lst.shape[0] == 0 or order == 0:
-            out[nb] = (0, 0.0)
+            out[nb] = (0, 0.0, 0.0)
             continue
         P = nb * (nb - 1) // 2
         pairs = [(i, j) for i in range(nb) for j in range(i + 1, nb)]
@@ -165,7 +166,18 @@ def algorithmic_flops(calc, cfg, params_path):
         ok = valid[u].astype(bool) & np.all(r < rout[u][:, :P], axis=1)
         nc = ncoef[u][ok].astype(np.float64)
         flops = ok.sum() * (P * (6 * order + 15) + P * 21) + (nc * (5 * P + 1)).sum()
-        out[nb] = (int(ok.sum()), float(flops))
+        # operations the factored kernel performs instead of n_c*(5P+1): two
+        # multiply-adds per coefficient per pass, the row/column products and
+        # the per-row and per-column gradient terms
+        nrow, ncol, R = fac[nb]
+        K = 1 if nb == 3 else 3
+        C = P - K
+        per_row = 4 if K == 1 else 15
+        per_col = 6 if C == 2 else 12
+        ex = ok.sum() * (P * (6 * order + 15) + P * 21 + R ** C * (C - 1) + R ** K * (K - 1)) \
+            + (4.0 * nc).sum() + (per_row * nrow[u][ok].astype(np.float64)).sum() \
+            + (per_col * ncol[u][ok].astype(np.float64)).sum()
+        out[nb] = (int(ok.sum()), float(flops), float(ex))
     del maxc
     return out
 
@@ -266,14 +278,21 @@ def run_ours(args):
     # force stage is one kernel, so the longest force stage is the top kernel
     dom = 1 + int(np.argmax(stage[1:]))
     roof = None
+    tun = calc.tuning()
     if dom in (2, 3):
         nb = 3 if dom == 2 else 4
+        fact = tun["fact%d" % nb]
+        tpc = tun[("ftpc%d" if fact else "tpc%d") % nb]
+        kname = ("k_forcef<%d,double,%d>" if fact else "k_forcen<%d,double,%d>") % (nb, tpc)
         achieved = work[nb][1] / (stage[dom] * 1e-3) / 1e12
-        roof = {"bound": "fp64", "kernel": "k_forcen<%d,double>" % nb, "achieved": achieved,
+        executed = (work[nb][2] if fact else work[nb][1]) / (stage[dom] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": kname, "achieved": achieved,
                 "peak": peak64.value, "unit": "TFLOP/s", "frac": achieved / peak64.value,
                 "traffic": None, "peak_source": "measured in-run FP64 FMA probe (ck_fma_peak); "
                 "MEASURED_PEAKS.json has no CUDA-core FP64 figure",
                 "flops_per_launch": work[nb][1], "clusters_evaluated": work[nb][0],
+                "executed_flops_per_launch": work[nb][2] if fact else work[nb][1],
+                "executed_tflops": executed, "executed_frac": executed / peak64.value,
                 "kernel_ms": stage[dom], "share_of_step": stage[dom] / sum(stage)}
     else:
         roof = {"bound": "fp64", "kernel": names[dom], "achieved": None, "peak": peak64.value,
@@ -323,7 +342,7 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": counts["n2"], "triplets": counts["n3"],
                        "quadruplets": counts["n4"], "ghost_atoms": counts["n_ghost"],
                        "l2_flush": "256 MB write before every timed step", "graph": True,
-                       "autotuned": {"tpc3": tuning[0], "tpc4": tuning[1], "blocks_per_sm": tuning[2]},
+                       "autotuned": tun,
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": e2e,
             "roofline": roof,
@@ -356,9 +375,9 @@ def extras(args):
         c = Calculator(precision=prec, graph=True)
         c.load_params(params)
         c.stage(c.pack([(cfg.pos, cfg.types, cfg.cell)]))
-        t = c.autotune()
+        c.autotune()
         out[name] = time_steps(c, N_ATOMS, 50)
-        out[name]["autotuned"] = t
+        out[name]["autotuned"] = c.tuning()
     p4 = synth.write_param_file(os.path.join(tmp, "c4.params"), synth.spec_c4())
     cfgs = synth.configs_c4(n_configs=args.batch_configs)
     atoms = sum(c.n_atoms for c in cfgs)
@@ -366,10 +385,10 @@ def extras(args):
         c = Calculator(precision=prec, graph=True)
         c.load_params(p4)
         c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
-        t = c.autotune()
+        c.autotune()
         r = time_steps(c, atoms, 3)
         r["configs"] = len(cfgs)
-        r["autotuned"] = t
+        r["autotuned"] = c.tuning()
         out[name] = r
     out["serving"] = serving(args)
     return out
@@ -409,6 +428,8 @@ def serving(args):
 
 def time_steps(c, atoms, steps):
     import torch
+    from chimes_calculator_gb300 import _lib
+    lib = _lib.load()
     stream = torch.cuda.ExternalStream(c.stream_ptr())
     for _ in range(3):
         c.launch()
@@ -421,7 +442,17 @@ def time_steps(c, atoms, steps):
     torch.cuda.synchronize()
     c.collect()
     ms = sum(a.elapsed_time(b) for a, b in ev) / steps
-    return {"value": atoms / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "counts": c.counts()}
+    # stage split from one more launch with the in-library stage events
+    lib.ck_set_profiling(c.h, 1)
+    stage_ms = (ctypes.c_double * 4)()
+    nl, kpl = ctypes.c_longlong(), ctypes.c_int()
+    c.launch()
+    lib.ck_read_stage_times(c.h, stage_ms, ctypes.byref(nl), ctypes.byref(kpl))
+    c.collect()
+    lib.ck_set_profiling(c.h, 0)
+    names = ["list build", "force 1B+2B", "force 3B", "force 4B"]
+    return {"value": atoms / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "counts": c.counts(),
+            "stage_ms": {k: stage_ms[i] / max(1, nl.value) for i, k in enumerate(names)}}
 
 
 # ----------------------------------------------------------------------------

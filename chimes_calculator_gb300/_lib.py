@@ -61,8 +61,11 @@ SIGNATURES = {
     "ck_param_info": (I, [P, I, IP, IP, DP]),
     "ck_type_index": (I, [P, I, S]),
     "ck_tuple_table": (I, [P, I, I, IP, IP, DP]),
+    "ck_tuple_factored": (I, [P, I, I, IP, IP, IP]),
+    "ck_get_tuning": (I, [P, IP]),
     "ck_set_precision": (I, [P, I]),
     "ck_set_tuning": (I, [P, I, I, I]),
+    "ck_set_contraction": (I, [P, I]),
     "ck_use_graph": (I, [P, I]),
     "ck_autotune": (I, [P, IP]),
     "ck_calculate_batch": (I, [P, I, IP, DP, IP, DP, IP, IP, DP, DP, DP]),

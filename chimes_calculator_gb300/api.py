@@ -88,6 +88,25 @@ class Calculator:
             out[nb] = (valid, ncoef, rout)
         return out
 
+    def tuple_factored(self, slot: int = 0):
+        """{nbody: (nrow[nt^nbody], ncol[...], R)} of the factored coefficient lists."""
+        nt = self.info(slot)["ntypes"]
+        out = {}
+        for nb in (3, 4):
+            n = nt ** nb
+            nrow = np.zeros(n, dtype=np.int32)
+            ncol = np.zeros(n, dtype=np.int32)
+            R = ctypes.c_int()
+            self._check(self.lib.ck_tuple_factored(self.h, slot, nb, _ip(nrow), _ip(ncol), ctypes.byref(R)))
+            out[nb] = (nrow, ncol, R.value)
+        return out
+
+    def tuning(self) -> dict:
+        v = np.zeros(9, dtype=np.int32)
+        self._check(self.lib.ck_get_tuning(self.h, _ip(v)))
+        keys = ["tpc3", "tpc4", "blocks_per_sm", "fact3", "fact4", "ftpc3", "ftpc4", "fbps3", "fbps4"]
+        return {k: int(x) for k, x in zip(keys, v)}
+
     def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
         cache = self._types[slot]
         out = np.empty(len(types), dtype=np.int32)
@@ -106,6 +125,10 @@ class Calculator:
 
     def set_tuning(self, tpc3: int = 4, tpc4: int = 8, blocks_per_sm: int = 4):
         self._check(self.lib.ck_set_tuning(self.h, tpc3, tpc4, blocks_per_sm))
+
+    def set_contraction(self, factored: bool = True):
+        """Factored (default) or per-coefficient 3-/4-body contraction kernels."""
+        self._check(self.lib.ck_set_contraction(self.h, int(bool(factored))))
 
     def autotune(self, packed=None):
         """Picks threads per cluster and resident blocks for the staged batch

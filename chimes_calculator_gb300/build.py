@@ -27,7 +27,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CXX_SOURCES = ["ck_params.cpp", "ck_geom.cpp", "ck_engine.cpp", "ck_capi.cpp", "ck_chimesff.cpp", "ck_server.cpp"]
-CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_direct.cu", "ck_noalloc.cu"]
+CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_factored.cu", "ck_direct.cu", "ck_noalloc.cu"]
 
 
 def _headers():

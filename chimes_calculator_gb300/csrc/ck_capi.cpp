@@ -249,6 +249,32 @@ int ck_tuple_table(void* h, int slot, int nbody, int* valid, int* ncoef, double*
     return ck::kOk;
 }
 
+int ck_tuple_factored(void* h, int slot, int nbody, int* nrow, int* ncol, int* R) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    if (nbody != 3 && nbody != 4) return report(ck::kErrInput, "nbody must be 3 or 4");
+    const ck::DevParamSet& V = in->eng.param_view(slot);
+    *R = nbody == 3 ? V.R3 : V.R4;
+    const std::vector<ck::TupleRec>& t = in->eng.tuples(slot, nbody);
+    int ntup = 1;
+    for (int k = 0; k < nbody; k++) ntup *= V.ntypes;
+    for (int u = 0; u < ntup; u++) {
+        const bool ok = u < (int)t.size() && t[u].valid && *R > 0;
+        nrow[u] = ok ? t[u].f_nrow : 0;
+        ncol[u] = ok ? t[u].f_ncol : 0;
+    }
+    return ck::kOk;
+}
+
+int ck_get_tuning(void* h, int* out) {
+    if (int st = check_handle(h)) return st;
+    const ck::ForceLaunch& L = static_cast<Instance*>(h)->eng.tuning;
+    const int v[9] = {L.tpc3, L.tpc4, L.blocks_per_sm, L.fact3, L.fact4, L.ftpc3, L.ftpc4, L.fbps3, L.fbps4};
+    for (int k = 0; k < 9; k++) out[k] = v[k];
+    return ck::kOk;
+}
+
 int ck_type_index(void* h, int slot, const char* name) {
     if (int st = check_handle(h)) return st;
     Instance* in = static_cast<Instance*>(h);
@@ -272,6 +298,16 @@ int ck_set_tuning(void* h, int tpc3, int tpc4, int blocks_per_sm) {
     e.tuning.tpc3 = tpc3;
     e.tuning.tpc4 = tpc4;
     e.tuning.blocks_per_sm = blocks_per_sm;
+    // factored kernels: 1, 2 or 4 lanes per cluster, one-warp blocks
+    e.tuning.ftpc3 = tpc3 < 4 ? tpc3 : 4;
+    e.tuning.ftpc4 = tpc4 < 4 ? tpc4 : 4;
+    e.tuning.fbps3 = e.tuning.fbps4 = 4 * blocks_per_sm;
+    return ck::kOk;
+}
+
+int ck_set_contraction(void* h, int factored) {
+    if (int st = check_handle(h)) return st;
+    static_cast<Instance*>(h)->eng.factored = factored != 0;
     return ck::kOk;
 }
 

@@ -58,8 +58,31 @@ struct TupleRec {
     int ncoef;
     int coef_off;          // offset into the body's coefficient arrays
     int type_id;           // tripidx / quadidx (for diagnostics)
+    // factored form (see FactRow): rows at fr[f_row .. f_row+f_nrow), columns
+    // right after them (f_ncol); row entries at [f_ent, f_ent+ncoef), column
+    // entries at [f_ent+ncoef, f_ent+2*ncoef)
+    int f_row, f_nrow, f_ncol, f_ent;
     double rin[6], rout[6], lam[6], xavg[6], xdiff[6];
+    // reciprocals for the factored kernels: 1/lam, 1/xdiff, and the cutoff's
+    // 1/rc (cubic) or Tersoff threshold rc - f*rc and 1/(rc - threshold)
+    double inv_lam[6], inv_xdiff[6], fc_th[6], fc_inv[6];
 };
+
+// Factored coefficient lists of one tuple.  The cluster's pairs split into
+// row pairs (the first K: K = 1 for 3-body, 3 for 4-body) and column pairs
+// (the rest); with R powers per pair (0..R-1), a coefficient with powers
+// (q_0..q_{P-1}) sits at row I = sum_{p<K} q_p R^{K-1-p} and column
+// J = sum_{p>=K} q_p R^{P-1-p}, so that
+//   E-sum S = sum_I X_I sum_J a_IJ Y_J,   X_I = prod_{p<K} T_p[q_p],  Y_J = prod_{p>=K} T_p[q_p].
+// Row entries (sorted by I, then J) hold (a, J); column entries (sorted by J,
+// then I) hold (a, I).  A record gives the row's powers (or the column's),
+// packed kPowBits per pair from the first pair of its side up, and the end of
+// its entries; each starts where the previous one ended.
+struct FactRow {
+    int pows;
+    int end;
+};
+constexpr int kFactMaxDim = 128;   // largest R^K and R^(P-K) kept in shared memory per cluster
 
 struct DevParamSet {
     int ntypes, npairs, o2, o3, o4;
@@ -74,6 +97,12 @@ struct DevParamSet {
     const double* c3d; const float* c3f; const uint32_t* p3;
     const TupleRec* t4;        // [nt^4] (null when o4 == 0)
     const double* c4d; const float* c4f; const uint32_t* p4;
+    // factored lists (FactRow); R3/R4 = powers per pair, 0 when the tables are
+    // absent (R^K or R^(P-K) above kFactMaxDim)
+    int R3, R4;
+    int bk3, bk4;              // first cluster bucket of this set (per engine; see BatchView)
+    const FactRow* fr3; const double* fe3d; const float* fe3f; const uint16_t* fe3i;
+    const FactRow* fr4; const double* fe4d; const float* fe4f; const uint16_t* fe4i;
 };
 
 // Per-system geometry, written by the host set-up (cell algebra) and
@@ -142,12 +171,22 @@ struct BatchView {
     int* c3;                       // [n3][3] ghost slots (i, j, k)
     int* c4;                       // [n4][4]
     long long n3_cap, n4_cap;
+    int enum_serial;               // 1: some system has 3B and 4B terms with rc4 > rc3 (sequential enumeration)
     // results
     double* force;                 // [n_in_total][3]
     double* ev;                    // [n_sys][8]: energy, virial xx xy xz yy yz zz, spare
     int* flags;                    // [8] device error flags: 0 capacity, 1 geometry, 2 badness max,
                                    //     3 penalty count, 4 below-rin count, 5 timeout
     unsigned long long* queue;     // [2] work-queue heads of the 3-body and 4-body force kernels
+    // cluster buckets by (parameter set, ordered type tuple), for the factored
+    // contraction: bucket key = pset.bk{3,4} + tuple index; each bucket padded
+    // to a multiple of 32 slots with -1, so a warp's clusters share one tuple
+    int nbk3, nbk4;
+    int* bk_count;                 // [nbk3 + nbk4]
+    int* bk_fill;                  // [nbk3 + nbk4]
+    long long* bk_start;           // [nbk3 + 1] then [nbk4 + 1]; last = slots in use
+    int* perm3; int* perm4;        // [perm*_cap] cluster index or -1
+    long long perm3_cap, perm4_cap;
 };
 
 }  // namespace ck

@@ -86,6 +86,17 @@ int Engine::load_params(const std::string& path, std::string& err) {
         if (ps.dev) cudaFree(ps.dev);
         return kErrCuda;
     }
+    // host copies of the tuple records (inspection, work models)
+    {
+        const int nt = img.header.ntypes;
+        if (img.header.t3)
+            ps.t3.assign(reinterpret_cast<const TupleRec*>(img.bytes.data() + (uintptr_t)img.header.t3),
+                         reinterpret_cast<const TupleRec*>(img.bytes.data() + (uintptr_t)img.header.t3) + nt * nt * nt);
+        if (img.header.t4)
+            ps.t4.assign(reinterpret_cast<const TupleRec*>(img.bytes.data() + (uintptr_t)img.header.t4),
+                         reinterpret_cast<const TupleRec*>(img.bytes.data() + (uintptr_t)img.header.t4) +
+                             nt * nt * nt * nt);
+    }
     // relocate the offsets of the header to device pointers
     DevParamSet h = img.header;
     const uintptr_t base = (uintptr_t)ps.dev;
@@ -95,6 +106,14 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.eoff); rel(h.pair_map); rel(h.pairs); rel(h.c2d); rel(h.c2f); rel(h.p2);
     rel(h.t3); rel(h.c3d); rel(h.c3f); rel(h.p3);
     rel(h.t4); rel(h.c4d); rel(h.c4f); rel(h.p4);
+    rel(h.fr3); rel(h.fe3d); rel(h.fe3f); rel(h.fe3i);
+    rel(h.fr4); rel(h.fe4d); rel(h.fe4f); rel(h.fe4i);
+    // this set's cluster buckets follow those of the sets loaded before it
+    int nt3 = h.ntypes * h.ntypes * h.ntypes;
+    h.bk3 = nbk3_;
+    h.bk4 = nbk4_;
+    if (h.o3 > 0) nbk3_ += nt3;
+    if (h.o4 > 0) nbk4_ += nt3 * h.ntypes;
     ps.view = h;
     sets_.push_back(std::move(ps));
     std::vector<DevParamSet> all;
@@ -122,6 +141,9 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     vols_.assign(S, 0.0);
     long long in_off = 0, atom_off = 0, ghost_off = 0, bin_off = 0;
     int stride3 = 0, stride4 = 0;
+    bool fact3 = factored, fact4 = factored;
+    int rf3 = 0, rf4 = 0;
+    bool enum_serial = false;
     double n2_est = 0.0, n3_est = 0.0, n4_est = 0.0;
     for (int s = 0; s < S; s++) {
         const SystemSpec& in = sys[s];
@@ -151,6 +173,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
             }
         }
         d.pset = in.pset;
+        if (d.has3 && d.has4 && d.c4 > d.c3) enum_serial = true;
         d.in_off = in_off; d.atom_off = atom_off; d.ghost_off = ghost_off; d.bin_off = bin_off;
         in_off += in.n;
         atom_off += d.n_atoms;
@@ -158,6 +181,9 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
         bin_off += d.bin_cap;
         stride3 = std::max(stride3, P.o3 > 0 ? P.o3 + 1 : 0);
         stride4 = std::max(stride4, P.o4 > 0 ? P.o4 + 1 : 0);
+        const DevParamSet& V = sets_[in.pset].view;
+        if (P.o3 > 0) { fact3 = fact3 && V.R3 > 0; rf3 = std::max(rf3, V.R3); }
+        if (P.o4 > 0) { fact4 = fact4 && V.R4 > 0; rf4 = std::max(rf4, V.R4); }
         // list-size estimates for the first capacity guess
         const double rho = d.n_atoms / (vols_[s] > 0 ? vols_[s] : 1.0);
         const double m = rho * 4.18879 * d.search * d.search * d.search;
@@ -171,12 +197,19 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     }
     tuning.stride3 = stride3;
     tuning.stride4 = stride4;
+    tuning.fact3 = fact3 && rf3 > 0 && tuning.want_fact3 ? 1 : 0;
+    tuning.fact4 = fact4 && rf4 > 0 && tuning.want_fact4 ? 1 : 0;
+    avail_fact3_ = fact3 && rf3 > 0;
+    avail_fact4_ = fact4 && rf4 > 0;
+    tuning.rf3 = rf3;
+    tuning.rf4 = rf4;
     V_ = BatchView();
     V_.n_sys = S;
     V_.n_in_total = in_off;
     V_.n_atoms_total = atom_off;
     V_.n_ghost_total = ghost_off;
     V_.n_bins_total = bin_off;
+    enum_serial_ = enum_serial;
     n2_cap_ = std::max(n2_cap_, (long long)n2_est + 1024);
     n3_cap_ = std::max(n3_cap_, (long long)n3_est + 1024);
     n4_cap_ = std::max(n4_cap_, (long long)n4_est + 1024);
@@ -234,6 +267,14 @@ Status Engine::ensure_lists(std::string& err) {
     CK_TRY(d_e_off4_.reserve(n2_cap_ + 1));
     CK_TRY(d_c3_.reserve(3 * n3_cap_));
     CK_TRY(d_c4_.reserve(4 * n4_cap_));
+    // buckets pad each (set, tuple) to 32 slots
+    const long long p3cap = nbk3_ > 0 ? n3_cap_ + 32LL * nbk3_ : 0;
+    const long long p4cap = nbk4_ > 0 ? n4_cap_ + 32LL * nbk4_ : 0;
+    CK_TRY(d_perm3_.reserve(std::max(1LL, p3cap)));
+    CK_TRY(d_perm4_.reserve(std::max(1LL, p4cap)));
+    CK_TRY(d_bk_count_.reserve(nbk3_ + nbk4_ + 1));
+    CK_TRY(d_bk_fill_.reserve(nbk3_ + nbk4_ + 1));
+    CK_TRY(d_bk_start_.reserve(nbk3_ + nbk4_ + 2));
     long long scan_n = std::max(std::max(V_.n_bins_total, V_.n_atoms_total), n2_cap_);
     CK_TRY(d_scan_tmp_.reserve(scan_tmp_bytes(scan_n)));
     BatchView& B = V_;
@@ -258,6 +299,11 @@ Status Engine::ensure_lists(std::string& err) {
     B.c3 = d_c3_.p; B.c4 = d_c4_.p;
     B.n3_cap = n3_cap_; B.n4_cap = n4_cap_;
     B.force = d_force_.p; B.ev = d_ev_.p; B.flags = d_flags_.p; B.queue = d_queue_.p;
+    B.enum_serial = enum_serial_ ? 1 : 0;
+    B.nbk3 = nbk3_; B.nbk4 = nbk4_;
+    B.bk_count = d_bk_count_.p; B.bk_fill = d_bk_fill_.p; B.bk_start = d_bk_start_.p;
+    B.perm3 = d_perm3_.p; B.perm4 = d_perm4_.p;
+    B.perm3_cap = p3cap; B.perm4_cap = p4cap;
     return kOk;
 }
 
@@ -304,9 +350,27 @@ Status Engine::enqueue(std::string& err) {
     L.precision = precision;
     launch_force2(B, d_l2_owner_.p, L, st);
     if (profile) CK_TRY(record_stage_event(ev_[2], st));
-    if (L.stride3 > 0) launch_force3(B, L, st);
+    if ((L.stride3 > 0 && L.fact3) || (L.stride4 > 0 && L.fact4)) {
+        CK_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
+        CK_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
+    }
+    if (L.stride3 > 0) {
+        if (L.fact3) {
+            launch_bucket(B, 3, st);
+            launch_force3f(B, L, st);
+        } else {
+            launch_force3(B, L, st);
+        }
+    }
     if (profile) CK_TRY(record_stage_event(ev_[3], st));
-    if (L.stride4 > 0) launch_force4(B, L, st);
+    if (L.stride4 > 0) {
+        if (L.fact4) {
+            launch_bucket(B, 4, st);
+            launch_force4f(B, L, st);
+        } else {
+            launch_force4(B, L, st);
+        }
+    }
     if (profile) CK_TRY(record_stage_event(ev_[4], st));
     ev_recorded_ = profile;
     kernels_per_launch = (int)(launch_counter() - k0);
@@ -340,12 +404,16 @@ Status Engine::launch(std::string& err) {
     if (!use_graph) return enqueue(err);
     std::vector<long long> key = {(long long)V_.n_sys, V_.n_in_total, V_.n_atoms_total, V_.n_ghost_total,
                                   V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
-                                  tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0};
+                                  tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0,
+                                  tuning.fact3, tuning.fact4, tuning.rf3, tuning.rf4, tuning.ftpc3, tuning.ftpc4,
+                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,
                           (const void*)h_force_.p, (const void*)h_ev_.p, (const void*)V_.bin_count,
-                          (const void*)V_.e_off3, (const void*)V_.psets})
+                          (const void*)V_.e_off3, (const void*)V_.psets, (const void*)V_.perm3,
+                          (const void*)V_.perm4, (const void*)V_.bk_count, (const void*)V_.bk_fill,
+                          (const void*)V_.bk_start})
         key.push_back((long long)(uintptr_t)p);
     if (key != graph_key_) {
         drop_graph();
@@ -425,7 +493,7 @@ Status Engine::run(const std::vector<SystemSpec>& sys, double* force_out, std::v
 }
 
 std::string Engine::tune_key() const {
-    std::string k = "p" + std::to_string(precision);
+    std::string k = "p" + std::to_string(precision) + (factored ? "f" : "c");
     std::vector<int> seen;
     for (const SysDesc& d : hsys_)
         if (std::find(seen.begin(), seen.end(), d.pset) == seen.end()) seen.push_back(d.pset);
@@ -445,12 +513,27 @@ Status Engine::autotune(int* chosen, std::string& err) {
         return kErrState;
     }
     const std::string key = tune_key();
+    auto report = [&]() {
+        if (chosen) {
+            chosen[0] = tuning.fact3 ? tuning.ftpc3 : tuning.tpc3;
+            chosen[1] = tuning.fact4 ? tuning.ftpc4 : tuning.tpc4;
+            chosen[2] = tuning.blocks_per_sm;
+        }
+    };
     for (auto& kv : tune_cache_)
         if (kv.first == key) {
             tuning.tpc3 = kv.second.tpc3;
             tuning.tpc4 = kv.second.tpc4;
             tuning.blocks_per_sm = kv.second.blocks_per_sm;
-            if (chosen) { chosen[0] = tuning.tpc3; chosen[1] = tuning.tpc4; chosen[2] = tuning.blocks_per_sm; }
+            tuning.ftpc3 = kv.second.ftpc3;
+            tuning.ftpc4 = kv.second.ftpc4;
+            tuning.fbps3 = kv.second.fbps3;
+            tuning.fbps4 = kv.second.fbps4;
+            tuning.want_fact3 = kv.second.want_fact3;
+            tuning.want_fact4 = kv.second.want_fact4;
+            tuning.fact3 = avail_fact3_ && tuning.want_fact3;
+            tuning.fact4 = avail_fact4_ && tuning.want_fact4;
+            report();
             return kOk;
         }
     const bool save_profile = profile, save_graph = use_graph;
@@ -481,45 +564,80 @@ Status Engine::autotune(int* chosen, std::string& err) {
     };
     double a, b;
     Status st = run_once(a, b);   // warm-up and list sizing
-    const int tpcs[] = {1, 2, 4, 8, 16, 32};
+    const bool do3 = tuning.stride3 > 0, do4 = tuning.stride4 > 0;
+    // candidates per body order: factored kernels (1, 2, 4 lanes per cluster)
+    // where the tables exist, then the per-coefficient kernels (1..32 lanes)
+    struct Cand { int fact, tpc; };
+    auto cands = [](bool can_fact) {
+        std::vector<Cand> v;
+        if (can_fact)
+            for (int t : {1, 2, 4}) v.push_back({1, t});
+        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t});
+        return v;
+    };
+    const std::vector<Cand> c3 = cands(avail_fact3_), c4 = cands(avail_fact4_);
+    auto apply = [&](int nb, const Cand& c) {
+        if (nb == 3) {
+            tuning.fact3 = c.fact;
+            (c.fact ? tuning.ftpc3 : tuning.tpc3) = c.tpc;
+        } else {
+            tuning.fact4 = c.fact;
+            (c.fact ? tuning.ftpc4 : tuning.tpc4) = c.tpc;
+        }
+    };
     double best3 = 1e300, best4 = 1e300;
-    int t3 = tuning.tpc3, t4 = tuning.tpc4;
-    for (int t : tpcs) {
-        if (st != kOk) break;
-        tuning.tpc3 = t;
-        tuning.tpc4 = t;
+    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3};
+    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4};
+    const size_t nc = std::max(c3.size(), c4.size());
+    for (size_t i = 0; i < nc && st == kOk; i++) {
+        const bool need3 = do3 && i < c3.size(), need4 = do4 && i < c4.size();
+        if (!need3 && !need4) break;
+        apply(3, c3[std::min(i, c3.size() - 1)]);
+        apply(4, c4[std::min(i, c4.size() - 1)]);
         double m3 = 1e300, m4 = 1e300;
         for (int rep = 0; rep < 2 && st == kOk; rep++) {
             st = run_once(a, b);
             m3 = std::min(m3, a);
             m4 = std::min(m4, b);
         }
-        if (m3 < best3) { best3 = m3; t3 = t; }
-        if (m4 < best4) { best4 = m4; t4 = t; }
+        if (need3 && m3 < best3) { best3 = m3; b3 = c3[i]; }
+        if (need4 && m4 < best4) { best4 = m4; b4 = c4[i]; }
     }
-    tuning.tpc3 = t3;
-    tuning.tpc4 = t4;
-    double bestb = 1e300;
-    int bb = tuning.blocks_per_sm;
+    apply(3, b3);
+    apply(4, b4);
+    tuning.want_fact3 = b3.fact;
+    tuning.want_fact4 = b4.fact;
+    const bool f3 = tuning.fact3 != 0, f4 = tuning.fact4 != 0;
+    // resident blocks per SM: 4-warp blocks for the per-coefficient kernels,
+    // one-warp blocks for the factored ones (capped by their occupancy)
     const int bps[] = {1, 2, 4, 8};
-    for (int v : bps) {
-        if (st != kOk) break;
-        tuning.blocks_per_sm = v;
-        double m = 1e300;
+    const int fbps[] = {2, 4, 8, 16};
+    double bestb = 1e300, bestf3 = 1e300, bestf4 = 1e300;
+    int bb = tuning.blocks_per_sm, bf3 = tuning.fbps3, bf4 = tuning.fbps4;
+    for (int i = 0; i < 4 && st == kOk; i++) {
+        tuning.blocks_per_sm = bps[i];
+        tuning.fbps3 = tuning.fbps4 = fbps[i];
+        double m3 = 1e300, m4 = 1e300;
         for (int rep = 0; rep < 2 && st == kOk; rep++) {
             st = run_once(a, b);
-            m = std::min(m, a + b);
+            m3 = std::min(m3, a);
+            m4 = std::min(m4, b);
         }
-        if (m < bestb) { bestb = m; bb = v; }
+        const double mold = (do3 && !f3 ? m3 : 0.0) + (do4 && !f4 ? m4 : 0.0);
+        if (mold < bestb) { bestb = mold; bb = bps[i]; }
+        if (f3 && m3 < bestf3) { bestf3 = m3; bf3 = fbps[i]; }
+        if (f4 && m4 < bestf4) { bestf4 = m4; bf4 = fbps[i]; }
     }
     tuning.blocks_per_sm = bb;
+    tuning.fbps3 = bf3;
+    tuning.fbps4 = bf4;
     profile = save_profile;
     use_graph = save_graph;
     for (double& v : stage_ms) v = 0.0;
     stage_launches = 0;
     if (st != kOk) return st;
     tune_cache_.push_back({key, tuning});
-    if (chosen) { chosen[0] = tuning.tpc3; chosen[1] = tuning.tpc4; chosen[2] = tuning.blocks_per_sm; }
+    report();
     return kOk;
 }
 

@@ -90,6 +90,10 @@ public:
     const HostParams& params(int slot) const { return *sets_[slot].host; }
     int n_param_sets() const { return (int)sets_.size(); }
     const DevParamSet* device_params() const { return dsets_.p; }   // device array, by slot
+    const DevParamSet& param_view(int slot) const { return sets_[slot].view; }
+    const std::vector<TupleRec>& tuples(int slot, int nbody) const {
+        return nbody == 3 ? sets_[slot].t3 : sets_[slot].t4;
+    }
 
     // Full evaluation of a batch: stage + launch + collect, retrying on capacity growth.
     // force_out: [sum n][3], zeroed and filled (not accumulated).
@@ -103,6 +107,9 @@ public:
 
     cudaStream_t stream() const { return stream_; }
     ForceLaunch tuning;
+    // 3-/4-body contraction: true = factored kernels wherever every parameter
+    // set of the batch has factored tables, false = per-coefficient kernels
+    bool factored = true;
     int precision = kFP64;
     bool use_graph = false;
     RunStats last;
@@ -140,6 +147,7 @@ private:
         std::unique_ptr<HostParams> host;
         void* dev = nullptr;
         DevParamSet view{};
+        std::vector<TupleRec> t3, t4;   // host copies of the tuple records
     };
     std::vector<PSet> sets_;
     DevBuf<DevParamSet> dsets_;
@@ -170,6 +178,11 @@ private:
     DevBuf<int> d_e_cnt3_, d_e_cnt4_;
     DevBuf<long long> d_e_off3_, d_e_off4_;
     DevBuf<int> d_c3_, d_c4_;
+    int nbk3_ = 0, nbk4_ = 0;     // cluster buckets over all loaded parameter sets
+    bool avail_fact3_ = false, avail_fact4_ = false;   // staged batch has factored tables
+    bool enum_serial_ = false;                         // staged batch needs the sequential enumeration
+    DevBuf<int> d_bk_count_, d_bk_fill_, d_perm3_, d_perm4_;
+    DevBuf<long long> d_bk_start_;
     DevBuf<double> d_force_, d_ev_;
     DevBuf<int> d_flags_;
     DevBuf<unsigned long long> d_queue_;

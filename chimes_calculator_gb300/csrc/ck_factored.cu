@@ -1,0 +1,474 @@
+// Factored 3-body and 4-body contraction.
+//
+// The per-coefficient form (k_forcen in ck_force.cu) spends about 2P+P FP64
+// operations on every coefficient term: the product of P Chebyshev values and
+// P gradient terms.  Here a cluster's pairs are split into row pairs (the
+// first K) and column pairs (the rest), and the coefficient list of each
+// ordered type tuple is stored twice, grouped by row and grouped by column
+// (FactRow, ck_common.h).  With X_I = prod_{p<K} T_p, Y_J = prod_{p>=K} T_p:
+//   S        = sum_I X_I z_I,            z_I = sum_J a_IJ Y_J     (row pass)
+//   G_p, p<K = sum_I dX_I/dT_p.dT_p z_I                           (row pass)
+//   G_p, p>=K= sum_J dY_J/dT_p.dT_p w_J, w_J = sum_I a_IJ X_I     (column pass)
+// so a coefficient costs two multiply-adds, and the products are formed once
+// per row or column.  The sums are the reference's (compute_3B/4B,
+// chimesFF.cpp:1931-2176, 2496-2872) in another association order.
+//
+// Clusters are first bucketed by (parameter set, ordered type tuple), each
+// bucket padded with -1 to a multiple of 32 slots, so every warp works on one
+// tuple: loop bounds and coefficient loads are uniform across the warp (the
+// loads are broadcasts).  TPC lanes share a cluster (TPC = 1, 2 or 4) and
+// split each row's and column's entries; per-cluster tables (T, dT/dr per
+// pair, Y and X) sit in shared memory interleaved by cluster, [entry][cluster].
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ck_common.h"
+#include "ck_force_common.cuh"
+#include "ck_kernels.h"
+#include "ck_math.cuh"
+
+namespace ck {
+
+namespace {
+
+template <int NB>
+struct Split;
+template <>
+struct Split<3> {
+    static constexpr int K = 1;
+};
+template <>
+struct Split<4> {
+    static constexpr int K = 3;
+};
+
+template <typename CT, int NB>
+__device__ __forceinline__ const CT* fact_coef(const DevParamSet& P);
+template <> __device__ __forceinline__ const double* fact_coef<double, 3>(const DevParamSet& P) { return P.fe3d; }
+template <> __device__ __forceinline__ const float* fact_coef<float, 3>(const DevParamSet& P) { return P.fe3f; }
+template <> __device__ __forceinline__ const double* fact_coef<double, 4>(const DevParamSet& P) { return P.fe4d; }
+template <> __device__ __forceinline__ const float* fact_coef<float, 4>(const DevParamSet& P) { return P.fe4f; }
+
+// Ordered type tuple of cluster c: its ghost slots, system, parameter set and tuple index.
+template <int NB>
+__device__ __forceinline__ const TupleRec* cluster_tuple(const BatchView& B, const int* clusters, long long c,
+                                                         int* id, int& s, const DevParamSet*& P, int& u) {
+    for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
+    s = B.atom_sys[B.ghost_parent[id[0]]];
+    P = &B.psets[B.sys[s].pset];
+    u = 0;
+    for (int k = 0; k < NB; k++) u = u * P->ntypes + B.atom_type[B.ghost_parent[id[k]]];
+    return (NB == 3 ? P->t3 : P->t4) + u;
+}
+
+// Chebyshev tables and cutoff of pair p of a tuple (set_cheby_polys,
+// chimesFF.h:542-628; get_fcut, chimesFF.h:347-386) with the tuple's
+// precomputed reciprocals in place of the divisions.
+template <typename CT>
+__device__ __forceinline__ void pair_setup(const DevParamSet& P, const TupleRec& R, int p, double r, CT* T, CT* D,
+                                           int stride, int nT, CT& fc, CT& fcd, int* flags) {
+    const double rin = R.rin[p];
+    const bool oor = r < rin;
+    const double rr = oor ? rin : r;
+    const double e = exp(-rr * R.inv_lam[p]);
+    const double xd = (e - R.xavg[p]) * R.inv_xdiff[p];
+    const double dxdr = -e * R.inv_lam[p] * R.inv_xdiff[p];
+    cheby_fill_strided<CT>(T, D, stride, nT, xd, dxdr, oor, r, rin, P.inner_smooth, flags);
+    const double finv = R.fc_inv[p];
+    if (!P.tersoff) {
+        const CT f0 = CT(1.0) - CT(r) * CT(finv);
+        fc = f0 * f0 * f0;
+        fcd = f0 * f0 * (CT(-3.0) * CT(finv));
+    } else {
+        const double th = R.fc_th[p];
+        if (r < th) { fc = CT(1); fcd = CT(0); }
+        else if (r > R.rout[p]) { fc = CT(0); fcd = CT(0); }
+        else {
+            const CT f0 = CT(r - th) * CT(finv) * CT(kPi) + CT(kPi / 2.0);
+            CT sn, cs;
+            csincos<CT>(f0, &sn, &cs);
+            fc = CT(0.5) + CT(0.5) * sn;
+            fcd = CT(0.5) * cs * (CT(kPi) * CT(finv));
+        }
+    }
+}
+
+// Bucket key of cluster c, or -1 when its tuple has no coefficients.
+template <int NB>
+__device__ __forceinline__ int bucket_key(const BatchView& B, const int* clusters, long long c) {
+    int id[NB], s, u;
+    const DevParamSet* P;
+    const TupleRec* R = cluster_tuple<NB>(B, clusters, c, id, s, P, u);
+    if (!R->valid || (NB == 3 ? P->R3 : P->R4) <= 0) return -1;
+    return (NB == 3 ? P->bk3 : P->bk4) + u;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(256) k_bucket_count(BatchView B, const int* clusters, const long long* n_ptr,
+                                                      long long cap) {
+    const long long n = min(*n_ptr, cap);
+    int* count = B.bk_count + (NB == 3 ? 0 : B.nbk3);
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // base is uniform over the block, so whole warps take part in the match
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long c = base + threadIdx.x;
+        const int key = c < n ? bucket_key<NB>(B, clusters, c) : -1;
+        const unsigned peers = __match_any_sync(kFull, key);
+        if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
+    }
+}
+
+// Exclusive scan of the bucket sizes rounded up to 32; the total goes to
+// start[nbk] and the padding slots of every bucket are set to -1.  One block.
+__global__ void __launch_bounds__(1024) k_bucket_scan(BatchView B, int nb) {
+    const int nbk = nb == 3 ? B.nbk3 : B.nbk4;
+    const int* count = B.bk_count + (nb == 3 ? 0 : B.nbk3);
+    long long* start = B.bk_start + (nb == 3 ? 0 : B.nbk3 + 1);
+    int* perm = nb == 3 ? B.perm3 : B.perm4;
+    const long long pcap = nb == 3 ? B.perm3_cap : B.perm4_cap;
+    __shared__ long long wsum[32];
+    __shared__ long long carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nbk; base += blockDim.x) {
+        const int k = base + threadIdx.x;
+        const long long v = k < nbk ? (long long)((count[k] + 31) & ~31) : 0;
+        long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = lane < nwarps ? wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(kFull, w, o);
+                if (lane >= o) w += y;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const long long incl = x + (warp > 0 ? wsum[warp - 1] : 0);
+        if (k < nbk) start[k] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += wsum[nwarps - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) start[nbk] = carry;
+    __syncthreads();
+    for (int k = threadIdx.x; k < nbk; k += blockDim.x) {
+        const long long s1 = k + 1 < nbk ? start[k + 1] : carry;
+        for (long long q = start[k] + count[k]; q < s1 && q < pcap; q++) perm[q] = -1;
+    }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(256) k_bucket_scatter(BatchView B, const int* clusters, const long long* n_ptr,
+                                                        long long cap) {
+    const long long n = min(*n_ptr, cap);
+    int* fill = B.bk_fill + (NB == 3 ? 0 : B.nbk3);
+    const long long* start = B.bk_start + (NB == 3 ? 0 : B.nbk3 + 1);
+    int* perm = NB == 3 ? B.perm3 : B.perm4;
+    const long long pcap = NB == 3 ? B.perm3_cap : B.perm4_cap;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long c = base + threadIdx.x;
+        const int key = c < n ? bucket_key<NB>(B, clusters, c) : -1;
+        const unsigned peers = __match_any_sync(kFull, key);
+        const int leader = __ffs(peers) - 1;
+        int b = 0;
+        if (key >= 0 && lane == leader) b = atomicAdd(&fill[key], __popc(peers));
+        b = __shfl_sync(kFull, b, leader);
+        if (key >= 0) {
+            const long long slot = start[key] + b + __popc(peers & ((1u << lane) - 1u));
+            if (slot < pcap) perm[slot] = (int)c;
+        }
+    }
+}
+
+// Shared-memory layout of one warp (one block), G = 32/TPC clusters,
+// interleaved [entry][cluster]:
+//   double geo[NP*4][G] (dr, r), fc[NP][G], fcd[NP][G]
+//   CT     T[NP*rs][G], D[NP*rs][G], Y[ys][G], X[xs][G]
+template <int NB, typename CT, int TPC>
+__global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters, const int* perm,
+                                               const long long* perm_n, long long perm_cap, int rs, int ys,
+                                               int xs) {
+    constexpr int NP = Topo<NB>::NP;
+    constexpr int K = Split<NB>::K;
+    constexpr int G = 32 / TPC;
+    const long long n = min(*perm_n, perm_cap);
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int grp = lane / TPC, gl = lane % TPC;
+    double* geo = reinterpret_cast<double*>(smem);
+    double* fcs = geo + NP * 4 * G;
+    double* fcds = fcs + NP * G;
+    CT* Tt = reinterpret_cast<CT*>(fcds + NP * G);
+    CT* Dt = Tt + NP * rs * G;
+    CT* Y = Dt + NP * rs * G;
+    CT* X = Y + ys * G;
+    CT* const Xv = K > 1 ? X : Tt;   // the row-side products (3-body: pair 0's T itself)
+
+    const long long steps = n / G;
+    unsigned long long* head = &B.queue[NB - 3];
+    EVAcc acc;
+
+    for (;;) {
+        long long step = 0;
+        if (lane == 0) step = (long long)atomicAdd(head, 1ull);
+        step = __shfl_sync(kFull, step, 0);
+        if (step >= steps) break;
+        const long long base = step * G;
+        const int c0 = perm[base];
+        if (c0 < 0) continue;   // uniform: a chunk never starts in a bucket's padding
+        // the warp's tuple (shared by all its clusters)
+        int id0[NB], s0, u0;
+        const DevParamSet* P;
+        const TupleRec* R = cluster_tuple<NB>(B, clusters, c0, id0, s0, P, u0);
+        const int Rp = NB == 3 ? P->R3 : P->R4;
+        const int c = perm[base + grp];
+        bool active = c >= 0;
+        int id[NB];
+        int s = 0;
+        if (active) {
+            for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
+            s = B.atom_sys[B.ghost_parent[id[0]]];
+            const double* h = B.sys[s].h;
+            for (int p = gl; p < NP; p += TPC) {
+                double dr[3], r;
+                pair_geom(B, h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+                geo[(4 * p + 0) * G + grp] = dr[0];
+                geo[(4 * p + 1) * G + grp] = dr[1];
+                geo[(4 * p + 2) * G + grp] = dr[2];
+                geo[(4 * p + 3) * G + grp] = r;
+            }
+        }
+        __syncwarp();
+        if (active)   // compute_3B/4B early-outs on the per-pair outer cutoffs
+            for (int p = 0; p < NP; p++)
+                if (geo[(4 * p + 3) * G + grp] >= R->rout[p]) active = false;
+        if (active)
+            for (int p = gl; p < NP; p += TPC) {
+                CT fc, fcd;
+                pair_setup<CT>(*P, *R, p, geo[(4 * p + 3) * G + grp], Tt + p * rs * G + grp, Dt + p * rs * G + grp,
+                               G, Rp, fc, fcd, B.flags);
+                fcs[p * G + grp] = double(fc);
+                fcds[p * G + grp] = double(fcd);
+            }
+        __syncwarp();
+        // column-side products Y_J (and row-side X_I for 4-body); the mixed-radix
+        // digits of the running index advance by TPC with carries (no division)
+        {
+            constexpr int C = NP - K;
+            int ny = 1;
+            for (int p = K; p < NP; p++) ny *= Rp;
+            int q[C];
+#pragma unroll
+            for (int p = 0; p < C; p++) q[p] = 0;
+            q[C - 1] = gl;
+            for (int j = gl; j < ny; j += TPC) {
+#pragma unroll
+                for (int p = C - 1; p > 0; p--)
+                    while (q[p] >= Rp) { q[p] -= Rp; q[p - 1]++; }
+                CT y = CT(1);
+#pragma unroll
+                for (int p = 0; p < C; p++) y *= Tt[((K + p) * rs + q[p]) * G + grp];
+                Y[j * G + grp] = y;
+                q[C - 1] += TPC;
+            }
+            if constexpr (K > 1) {
+                int nx = 1;
+                for (int p = 0; p < K; p++) nx *= Rp;
+                int v[K];
+#pragma unroll
+                for (int p = 0; p < K; p++) v[p] = 0;
+                v[K - 1] = gl;
+                for (int i = gl; i < nx; i += TPC) {
+#pragma unroll
+                    for (int p = K - 1; p > 0; p--)
+                        while (v[p] >= Rp) { v[p] -= Rp; v[p - 1]++; }
+                    CT x = CT(1);
+#pragma unroll
+                    for (int p = 0; p < K; p++) x *= Tt[(p * rs + v[p]) * G + grp];
+                    X[i * G + grp] = x;
+                    v[K - 1] += TPC;
+                }
+            }
+        }
+        __syncwarp();
+
+        const CT* fe = fact_coef<CT, NB>(*P);
+        const uint16_t* fi = NB == 3 ? P->fe3i : P->fe4i;
+        const FactRow* rows = (NB == 3 ? P->fr3 : P->fr4) + R->f_row;
+        const int nrow = R->f_nrow, ncol = R->f_ncol;
+        CT S = CT(0), Gp[NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++) Gp[p] = CT(0);
+        int e = R->f_ent;
+        // row pass: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K)
+        for (int r = 0; r < nrow; r++) {
+            const FactRow rw = rows[r];
+            CT z = CT(0);
+#pragma unroll 4
+            for (int k = e + gl; k < rw.end; k += TPC) z += fe[k] * Y[fi[k] * G + grp];
+            e = rw.end;
+            CT t[K], d[K];
+#pragma unroll
+            for (int p = 0; p < K; p++) {
+                const int q = (rw.pows >> (kPowBits * p)) & 31;
+                t[p] = Tt[(p * rs + q) * G + grp];
+                d[p] = Dt[(p * rs + q) * G + grp];
+            }
+            if constexpr (K == 1) {
+                S += t[0] * z;
+                Gp[0] += d[0] * z;
+            } else {
+                const CT t12 = t[1] * t[2], t01 = t[0] * t[1];
+                S += (t[0] * t12) * z;
+                Gp[0] += (d[0] * t12) * z;
+                Gp[1] += (t[0] * t[2] * d[1]) * z;
+                Gp[K - 1] += (t01 * d[K - 1]) * z;
+            }
+        }
+        // column pass: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K)
+        for (int cc = 0; cc < ncol; cc++) {
+            const FactRow cl = rows[nrow + cc];
+            CT w = CT(0);
+#pragma unroll 4
+            for (int k = e + gl; k < cl.end; k += TPC) w += fe[k] * Xv[fi[k] * G + grp];
+            e = cl.end;
+            constexpr int C = NP - K;
+            CT t[C], d[C];
+#pragma unroll
+            for (int p = 0; p < C; p++) {
+                const int q = (cl.pows >> (kPowBits * p)) & 31;
+                t[p] = Tt[((K + p) * rs + q) * G + grp];
+                d[p] = Dt[((K + p) * rs + q) * G + grp];
+            }
+            if constexpr (C == 2) {
+                Gp[K] += (d[0] * t[1]) * w;
+                Gp[K + 1] += (t[0] * d[1]) * w;
+            } else {
+                const CT t12 = t[1] * t[C - 1];
+                Gp[K] += (d[0] * t12) * w;
+                Gp[K + 1] += (t[0] * d[1] * t[C - 1]) * w;
+                Gp[K + C - 1] += (t[0] * t[1] * d[C - 1]) * w;
+            }
+        }
+        // combine the TPC partial sums of each cluster
+#pragma unroll
+        for (int off = TPC / 2; off > 0; off >>= 1) {
+            S += __shfl_xor_sync(kFull, S, off);
+#pragma unroll
+            for (int p = 0; p < NP; p++) Gp[p] += __shfl_xor_sync(kFull, Gp[p], off);
+        }
+        if (active && gl == 0) {
+            double dr[NP][4], fc[NP], fcd[NP], Gd[NP];
+            for (int p = 0; p < NP; p++) {
+                for (int k = 0; k < 4; k++) dr[p][k] = geo[(4 * p + k) * G + grp];
+                fc[p] = fcs[p * G + grp];
+                fcd[p] = fcds[p * G + grp];
+                Gd[p] = double(Gp[p]);
+            }
+            cluster_epilogue<NB>(B, id, s, dr, fc, fcd, double(S), Gd, acc);
+        }
+        __syncwarp();
+    }
+    acc.flush_warp(B);
+}
+
+template <int NB, typename CT>
+size_t smem_bytes(int tpc, int rs) {
+    constexpr int NP = Topo<NB>::NP;
+    constexpr int K = Split<NB>::K;
+    const int G = 32 / tpc;
+    long long ys = 1, xs = 1;
+    for (int p = K; p < NP; p++) ys *= rs;
+    for (int p = 0; p < K; p++) xs *= rs;
+    if (K == 1) xs = 0;
+    return sizeof(double) * (size_t)NP * 6 * G + sizeof(CT) * (size_t)(2 * NP * rs + ys + xs) * G;
+}
+
+template <int NB, typename CT>
+void launch_f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    constexpr int NP = Topo<NB>::NP;
+    constexpr int K = Split<NB>::K;
+    const int tpc = NB == 3 ? L.ftpc3 : L.ftpc4;
+    const int rs = NB == 3 ? L.rf3 : L.rf4;
+    const long long pcap = NB == 3 ? B.perm3_cap : B.perm4_cap;
+    const int nbk = NB == 3 ? B.nbk3 : B.nbk4;
+    if (pcap <= 0 || nbk <= 0 || rs <= 0) return;
+    int ys = 1, xs = 1;
+    for (int p = K; p < NP; p++) ys *= rs;
+    for (int p = 0; p < K; p++) xs *= rs;
+    if (K == 1) xs = 0;
+    const size_t smem = smem_bytes<NB, CT>(tpc, rs);
+    const long long* pn = B.bk_start + (NB == 3 ? 0 : B.nbk3 + 1) + nbk;
+    const int* clusters = NB == 3 ? B.c3 : B.c4;
+    const int* perm = NB == 3 ? B.perm3 : B.perm4;
+    const int want_bps = NB == 3 ? L.fbps3 : L.fbps4;
+#define CK_LAUNCH_F(T_)                                                                                  \
+    do {                                                                                                 \
+        auto kern = k_forcef<NB, CT, T_>;                                                                \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);              \
+        int occ = 0;                                                                                     \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, smem);                             \
+        if (occ < 1) occ = 1;                                                                            \
+        const long long steps = (pcap + (32 / T_) - 1) / (32 / T_);                                      \
+        long long want = (long long)sm_count() * (want_bps < occ ? want_bps : occ);                       \
+        const unsigned grid = (unsigned)(want < steps ? want : steps);                                   \
+        count_launch(), kern<<<grid, 32, smem, st>>>(B, clusters, perm, pn, pcap, rs, ys, xs);            \
+    } while (0)
+    switch (tpc) {
+        case 1: CK_LAUNCH_F(1); break;
+        case 2: CK_LAUNCH_F(2); break;
+        default: CK_LAUNCH_F(4); break;
+    }
+#undef CK_LAUNCH_F
+}
+
+template <int NB>
+void launch_bucket_n(const BatchView& B, cudaStream_t st) {
+    const int nbk = NB == 3 ? B.nbk3 : B.nbk4;
+    const long long cap = NB == 3 ? B.n3_cap : B.n4_cap;
+    if (nbk <= 0 || cap <= 0) return;
+    const long long* n_ptr = (NB == 3 ? B.e_off3 : B.e_off4) + B.n2_cap;
+    const int* clusters = NB == 3 ? B.c3 : B.c4;
+    long long want = (long long)sm_count() * 8;
+    long long need = (cap + 255) / 256;
+    const unsigned grid = (unsigned)(want < need ? want : need);
+    count_launch(), k_bucket_count<NB><<<grid, 256, 0, st>>>(B, clusters, n_ptr, cap);
+    count_launch(), k_bucket_scan<<<1, 1024, 0, st>>>(B, NB);
+    count_launch(), k_bucket_scatter<NB><<<grid, 256, 0, st>>>(B, clusters, n_ptr, cap);
+}
+
+}  // namespace
+
+size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs) {
+    if (nbody == 3)
+        return precision == kMixed ? smem_bytes<3, float>(tpc, rs) : smem_bytes<3, double>(tpc, rs);
+    return precision == kMixed ? smem_bytes<4, float>(tpc, rs) : smem_bytes<4, double>(tpc, rs);
+}
+
+void launch_bucket(const BatchView& B, int nbody, cudaStream_t st) {
+    if (nbody == 3) launch_bucket_n<3>(B, st);
+    else launch_bucket_n<4>(B, st);
+}
+
+void launch_force3f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    if (L.precision == kMixed) launch_f<3, float>(B, L, st);
+    else launch_f<3, double>(B, L, st);
+}
+
+void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    if (L.precision == kMixed) launch_f<4, float>(B, L, st);
+    else launch_f<4, double>(B, L, st);
+}
+
+}  // namespace ck

@@ -29,77 +29,12 @@
 
 #include "ck_common.h"
 #include "ck_kernels.h"
+#include "ck_force_common.cuh"
 #include "ck_math.cuh"
 
 namespace ck {
 
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
-__device__ __forceinline__ void pair_geom(const BatchView& B, const double* h, int ga, int gb, double* dr, double& r) {
-    const double* fa = &B.ghost_fs[3 * (long long)ga];
-    const double* fb = &B.ghost_fs[3 * (long long)gb];
-    const double dx = fb[0] - fa[0], dy = fb[1] - fa[1], dz = fb[2] - fa[2];
-    dr[0] = h[0] * dx + h[1] * dy + h[2] * dz;
-    dr[1] = h[3] * dx + h[4] * dy + h[5] * dz;
-    dr[2] = h[6] * dx + h[7] * dy + h[8] * dz;
-    r = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
-}
-
-__device__ __forceinline__ void add_force(const BatchView& B, int ghost, double fx, double fy, double fz) {
-    const int o = B.atom_orig[B.ghost_parent[ghost]];
-    atomicAdd(&B.force[3 * (long long)o + 0], fx);
-    atomicAdd(&B.force[3 * (long long)o + 1], fy);
-    atomicAdd(&B.force[3 * (long long)o + 2], fz);
-}
-
-// Per-lane energy/virial accumulator for one system at a time.
-struct EVAcc {
-    int s = -1;
-    double v[7] = {0, 0, 0, 0, 0, 0, 0};
-    __device__ void flush(const BatchView& B) {
-        if (s >= 0)
-            for (int k = 0; k < 7; k++) atomicAdd(&B.ev[8 * s + k], v[k]);
-        s = -1;
-        for (int k = 0; k < 7; k++) v[k] = 0;
-    }
-    __device__ void add(const BatchView& B, int sys, double e, const double* vir) {
-        if (sys != s) { flush(B); s = sys; }
-        v[0] += e;
-        for (int k = 0; k < 6; k++) v[1 + k] += vir[k];
-    }
-    // end of kernel: one set of atomics per warp when the warp holds one system
-    __device__ void flush_warp(const BatchView& B) {
-        const int lane = threadIdx.x & 31;
-        int key = s;
-        int s0 = -1;
-        for (int l = 0; l < 32; l++) {
-            int t = __shfl_sync(kFull, key, l);
-            if (t >= 0) { s0 = t; break; }
-        }
-        const bool uniform = __all_sync(kFull, s < 0 || s == s0);
-        if (uniform) {
-            for (int k = 0; k < 7; k++) {
-                double x = v[k];
-                for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(kFull, x, off);
-                v[k] = x;
-            }
-            if (lane == 0 && s0 >= 0)
-                for (int k = 0; k < 7; k++) atomicAdd(&B.ev[8 * s0 + k], v[k]);
-        } else {
-            flush(B);
-        }
-    }
-};
-
-__device__ __forceinline__ void virial_add(double* vir, double f, const double* d) {
-    vir[0] -= f * d[0] * d[0];
-    vir[1] -= f * d[0] * d[1];
-    vir[2] -= f * d[0] * d[2];
-    vir[3] -= f * d[1] * d[1];
-    vir[4] -= f * d[1] * d[2];
-    vir[5] -= f * d[2] * d[2];
-}
 
 // ---------------------------------------------------------------------------
 // 1-body + 2-body: one thread per neighbour-list entry (and per atom for 1B).

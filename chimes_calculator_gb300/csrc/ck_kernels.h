@@ -37,6 +37,13 @@ struct ForceLaunch {
     int blocks_per_sm = 4;
     int stride3 = 0;       // polynomial table stride (max 3B order + 1 over the batch's sets)
     int stride4 = 0;
+    // factored contraction (ck_factored.cu), used per body order when every
+    // parameter set of the batch has its tables
+    int fact3 = 0, fact4 = 0;
+    int want_fact3 = 1, want_fact4 = 1;   // preference (autotuner); fact = want && tables present
+    int rf3 = 0, rf4 = 0;  // powers per pair (max over the batch's sets)
+    int ftpc3 = 1, ftpc4 = 1;      // threads per cluster: 1, 2 or 4
+    int fbps3 = 8, fbps4 = 8;      // resident one-warp blocks per SM (capped by occupancy)
 };
 
 // Cluster counts are read on the device (l2_off[n_atoms], e_off3/4[n2_cap]) and
@@ -44,6 +51,15 @@ struct ForceLaunch {
 void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L, cudaStream_t st);
 void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 void launch_force4(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+
+// Factored contraction (ck_factored.cu): bucket the clusters of one body
+// order by (parameter set, type tuple), then contract.  Both read their
+// counts on the device.
+void launch_bucket(const BatchView& B, int nbody, cudaStream_t st);
+void launch_force3f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+// dynamic shared memory of one factored-kernel block (one warp)
+size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 
 // Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
 void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,

@@ -505,6 +505,115 @@ __global__ void k_enum(BatchView B, const int* l2_owner) {
     }
 }
 
+// Warp-per-entry form of the same enumeration.  When the 4-body outer cutoff
+// does not exceed the 3-body one (or a system lacks one of the two), the
+// valid_3mer / valid_4mer flags are restored before every k (the reference's
+// reset branch), so each k -- and each l -- is decided on its own: lanes take
+// consecutive k (then l) of the atom's list and a ballot plus prefix count
+// emits the clusters in the reference's (k, l) order.  Systems with 3- and
+// 4-body terms and rc4 > rc3 keep the sequential carry-over (k_enum).
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner) {
+    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const float4* vec = reinterpret_cast<const float4*>(B.l2_vec);
+    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < B.n2_cap; e += nwarps) {
+        if (e >= n2) {
+            if (!FILL && lane == 0) { B.e_cnt3[e] = 0; B.e_cnt4[e] = 0; }
+            continue;
+        }
+        const int r = l2_owner[e];
+        const SysDesc& d = B.sys[B.atom_sys[r]];
+        const double c3 = d.c3, c4 = d.c4, eps = d.eps;
+        const double dij = B.l2_dist[e];
+        const bool want3 = d.has3 && dij < c3, want4 = d.has4 && dij < c4;
+        long long n3 = 0, n4 = 0;
+        long long o3 = 0, o4 = 0;
+        if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
+        if (want3 || want4) {
+            double hn[9];
+            for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
+            const int gi = B.atom_self[r];
+            const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
+            const int jj = B.l2_ghost[e];
+            const float4 vj = vec[e];
+            const double* fj = &B.ghost_fn[3 * (long long)jj];
+            const int pj = B.ghost_parent[jj];
+            for (long long kb = b0; kb < b1; kb += 32) {
+                const long long k = kb + lane;
+                bool ok3 = false, ok4 = false;
+                int kk = -1, pk = 0;
+                float4 vk = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (k < b1) {
+                    kk = B.l2_ghost[k];
+                    pk = B.ghost_parent[kk];
+                    if (kk != jj && pj <= pk) {
+                        const double dik = B.l2_dist[k];
+                        vk = vec[k];
+                        PairDist jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk), 0.0, false};
+                        ok3 = want3 && dik < c3 && !jk.ge(c3, eps);
+                        ok4 = want4 && dik < c4 && !jk.ge(c4, eps);
+                    }
+                }
+                const unsigned m3 = __ballot_sync(kFull, ok3);
+                if (FILL && ok3) {
+                    const long long q = o3 + n3 + __popc(m3 & lt);
+                    if (q < B.n3_cap) {
+                        int* out = B.c3 + 3 * q;
+                        out[0] = gi; out[1] = jj; out[2] = kk;
+                    }
+                }
+                n3 += __popc(m3);
+                unsigned m4 = __ballot_sync(kFull, ok4);
+                while (m4) {
+                    const int src = __ffs(m4) - 1;
+                    m4 &= m4 - 1;
+                    const int ks = __shfl_sync(kFull, kk, src);
+                    const int pks = __shfl_sync(kFull, pk, src);
+                    float4 vks;
+                    vks.x = __shfl_sync(kFull, vk.x, src);
+                    vks.y = __shfl_sync(kFull, vk.y, src);
+                    vks.z = __shfl_sync(kFull, vk.z, src);
+                    vks.w = 0.f;
+                    const double* fk = &B.ghost_fn[3 * (long long)ks];
+                    for (long long lb = b0; lb < b1; lb += 32) {
+                        const long long l = lb + lane;
+                        bool okl = false;
+                        int ll = -1;
+                        if (l < b1) {
+                            ll = B.l2_ghost[l];
+                            if (ll != jj && ll != ks) {
+                                const int pl = B.ghost_parent[ll];
+                                if (pj <= pl && pks <= pl && B.l2_dist[l] < c4) {
+                                    const float4 vl = vec[l];
+                                    const double* fl = &B.ghost_fn[3 * (long long)ll];
+                                    PairDist jl{hn, fj, fl, vdist(vj, vl), 0.0, false};
+                                    if (!jl.ge(c4, eps)) {
+                                        PairDist kl{hn, fk, fl, vdist(vks, vl), 0.0, false};
+                                        okl = !kl.ge(c4, eps);
+                                    }
+                                }
+                            }
+                        }
+                        const unsigned ml = __ballot_sync(kFull, okl);
+                        if (FILL && okl) {
+                            const long long q = o4 + n4 + __popc(ml & lt);
+                            if (q < B.n4_cap) {
+                                int* out = B.c4 + 4 * q;
+                                out[0] = gi; out[1] = jj; out[2] = ks; out[3] = ll;
+                            }
+                        }
+                        n4 += __popc(ml);
+                    }
+                }
+            }
+        }
+        if (!FILL && lane == 0) { B.e_cnt3[e] = (int)n3; B.e_cnt4[e] = (int)n4; }
+    }
+}
+
 // --- capacity checks and accumulator reset ---------------------------------
 __global__ void k_check(BatchView B) {
     if (B.l2_off[B.n_atoms_total] > B.n2_cap) atomicOr(&B.flags[0], 2);
@@ -627,11 +736,19 @@ void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st) {
 }
 void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n2_cap) return;
-    long long want = (long long)sm_count() * 16;
-    long long need = (B.n2_cap + 127) / 128;
+    if (B.enum_serial) {
+        long long want = (long long)sm_count() * 16;
+        long long need = (B.n2_cap + 127) / 128;
+        const unsigned grid = (unsigned)(want < need ? want : need);
+        if (fill) count_launch(), k_enum<true><<<grid, 128, 0, st>>>(B, l2_owner);
+        else count_launch(), k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
+        return;
+    }
+    long long want = (long long)sm_count() * 8;      // 8 blocks of 8 warps per SM
+    long long need = (B.n2_cap + 7) / 8;             // one warp per list entry
     const unsigned grid = (unsigned)(want < need ? want : need);
-    if (fill) count_launch(), k_enum<true><<<grid, 128, 0, st>>>(B, l2_owner);
-    else count_launch(), k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
+    if (fill) count_launch(), k_enumw<true><<<grid, 256, 0, st>>>(B, l2_owner);
+    else count_launch(), k_enumw<false><<<grid, 256, 0, st>>>(B, l2_owner);
 }
 void launch_check(const BatchView& B, cudaStream_t st) { count_launch(), k_check<<<1, 1, 0, st>>>(B); }
 void launch_reset(const BatchView& B, cudaStream_t st) {

@@ -90,6 +90,39 @@ __device__ __forceinline__ void cheby_table(CT* T, CT* D, double r, double rin, 
     }
 }
 
+// The same table from a precomputed Morse coordinate (x, dx/dr, r below the
+// inner cutoff), entries n = 0..nT-1 only, at T[n*stride], D[n*stride]
+// (interleaved per-cluster tables of the factored contraction).
+template <typename CT>
+__device__ __forceinline__ void cheby_fill_strided(CT* T, CT* D, int stride, int nT, double xd, double dxdr, bool oor,
+                                                   double r, double rin, double inner_smooth, int* flags) {
+    const CT x = CT(xd), tx = CT(2) * x, g = CT(dxdr);
+    CT k = CT(0), dm = CT(1);
+    if (oor) {
+        if (flags) atomicAdd(&flags[4], 1);
+        const double damp = exp((r - rin) / inner_smooth);
+        k = CT(inner_smooth * (damp - 1.0));
+        dm = CT(damp);
+    }
+    // n = 0: T = 1, dT = 0
+    T[0] = CT(1);
+    D[0] = CT(0);
+    CT t0 = CT(1), t1 = x, u0 = CT(1), u1 = tx;
+    if (nT > 1) {
+        const CT d1 = g * u0;
+        T[stride] = oor ? t1 + k * d1 : t1;
+        D[stride] = oor ? d1 * dm : d1;
+    }
+    for (int n = 2; n < nT; n++) {
+        const CT t2 = tx * t1 - t0;
+        const CT u2 = tx * u1 - u0;
+        const CT dn = CT(n) * g * u1;
+        T[n * stride] = oor ? t2 + k * dn : t2;
+        D[n * stride] = oor ? dn * dm : dn;
+        t0 = t1; t1 = t2; u0 = u1; u1 = u2;
+    }
+}
+
 template <int NB>
 struct Topo;
 template <>

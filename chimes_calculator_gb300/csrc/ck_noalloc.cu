@@ -181,6 +181,7 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
 
     BatchView B;
     std::memset(&B, 0, sizeof(B));
+    B.enum_serial = 1;   // one thread per list entry: the enumeration this entry point was validated with
     B.n_sys = 1;
     B.n_in_total = natom;
     B.n_atoms_total = d.n_atoms;

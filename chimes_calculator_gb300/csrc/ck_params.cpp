@@ -542,7 +542,21 @@ ParamImage pack_params(const HostParams& P) {
         std::vector<double> cd;
         std::vector<float> cf;
         std::vector<uint32_t> pw;
-        std::map<std::pair<int, std::vector<int>>, int> shared;  // (type, mapping) -> coef_off
+        // factored tables: R powers per pair; kept when R^K and R^(P-K) fit
+        const int K = nb == 3 ? 1 : 3;
+        int R_pow = 1;
+        for (size_t ti = 0; ti < Bd.pows.size(); ti++)
+            for (int v : Bd.pows[ti]) R_pow = std::max(R_pow, v + 1);
+        long long rk = 1, rc = 1;
+        for (int k = 0; k < K; k++) rk *= R_pow;
+        for (int k = K; k < np; k++) rc *= R_pow;
+        const bool fact = rk <= kFactMaxDim && rc <= kFactMaxDim;
+        std::vector<FactRow> fr;
+        std::vector<double> fed;
+        std::vector<float> fef;
+        std::vector<uint16_t> fei;
+        struct Shared { int coef_off, f_row, f_nrow, f_ncol, f_ent; };
+        std::map<std::pair<int, std::vector<int>>, Shared> shared;  // (type, mapping) -> tables
         for (int u = 0; u < ntup; u++) {
             TupleRec& R = tr[u];
             std::memset(&R, 0, sizeof(R));
@@ -559,36 +573,99 @@ ParamImage pack_params(const HostParams& P) {
                     R.rout[p] = Bd.cut_out[ti][m[p]];
                     R.lam[p] = P.lam[P.pair_map[a[i] * nt + a[j]]];
                     morse_consts(R.rin[p], R.rout[p], R.lam[p], R.xavg[p], R.xdiff[p]);
+                    R.inv_lam[p] = 1.0 / R.lam[p];
+                    R.inv_xdiff[p] = 1.0 / R.xdiff[p];
+                    if (P.tersoff) {
+                        R.fc_th[p] = R.rout[p] - P.fcut_var * R.rout[p];
+                        R.fc_inv[p] = 1.0 / (R.rout[p] - R.fc_th[p]);
+                    } else {
+                        R.fc_th[p] = 0.0;
+                        R.fc_inv[p] = 1.0 / R.rout[p];
+                    }
                 }
             R.ncoef = Bd.ncoef[ti];
             R.valid = R.ncoef > 0 ? 1 : 0;
             auto key = std::make_pair(ti, m);
             auto it = shared.find(key);
             if (it != shared.end()) {
-                R.coef_off = it->second;
+                R.coef_off = it->second.coef_off;
+                R.f_row = it->second.f_row; R.f_nrow = it->second.f_nrow;
+                R.f_ncol = it->second.f_ncol; R.f_ent = it->second.f_ent;
                 continue;
             }
             R.coef_off = (int)cd.size();
-            shared[key] = R.coef_off;
+            const int Rp = R_pow;
+            std::vector<int> rowi(R.ncoef), coli(R.ncoef), rowp(R.ncoef), colp(R.ncoef);
             for (int c = 0; c < R.ncoef; c++) {
                 cd.push_back(Bd.coef[ti][c]);
                 cf.push_back((float)Bd.coef[ti][c]);
                 uint32_t packed = 0;
-                for (int q = 0; q < np; q++)
-                    packed |= uint32_t(Bd.pows[ti][(size_t)c * np + m[q]]) << (kPowBits * q);
+                int I = 0, J = 0, Ip = 0, Jp = 0;
+                for (int q = 0; q < np; q++) {
+                    const int v = Bd.pows[ti][(size_t)c * np + m[q]];
+                    packed |= uint32_t(v) << (kPowBits * q);
+                    if (q < K) { I = I * Rp + v; Ip |= v << (kPowBits * q); }
+                    else { J = J * Rp + v; Jp |= v << (kPowBits * (q - K)); }
+                }
                 pw.push_back(packed);
+                rowi[c] = I;
+                coli[c] = J;
+                rowp[c] = Ip;
+                colp[c] = Jp;
             }
+            if (fact) {
+                R.f_row = (int)fr.size();
+                R.f_ent = (int)fed.size();
+                // rows: entries by (I, J) holding (a, J); then columns: by (J, I) holding (a, I)
+                for (int pass = 0; pass < 2; pass++) {
+                    const std::vector<int>& major = pass == 0 ? rowi : coli;
+                    const std::vector<int>& minor = pass == 0 ? coli : rowi;
+                    const std::vector<int>& mpows = pass == 0 ? rowp : colp;
+                    std::vector<int> ord(R.ncoef);
+                    for (int c = 0; c < R.ncoef; c++) ord[c] = c;
+                    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+                        return major[x] != major[y] ? major[x] < major[y] : minor[x] < minor[y];
+                    });
+                    int nrec = 0;
+                    for (int k = 0; k < R.ncoef; k++) {
+                        const int c = ord[k];
+                        fed.push_back(Bd.coef[ti][c]);
+                        fef.push_back((float)Bd.coef[ti][c]);
+                        fei.push_back((uint16_t)minor[c]);
+                        if (k + 1 == R.ncoef || major[ord[k + 1]] != major[c]) {
+                            fr.push_back(FactRow{mpows[c], (int)fed.size()});
+                            nrec++;
+                        }
+                    }
+                    if (pass == 0) R.f_nrow = nrec; else R.f_ncol = nrec;
+                }
+            }
+            shared[key] = Shared{R.coef_off, R.f_row, R.f_nrow, R.f_ncol, R.f_ent};
         }
         size_t tro = B.add(tr.data(), tr.size());
         size_t cdo = B.add(cd.data(), cd.size());
         size_t cfo = B.add(cf.data(), cf.size());
         size_t pwo = B.add(pw.data(), pw.size());
+        size_t fro = 0, fdo = 0, ffo = 0, fio = 0;
+        if (fact && !fed.empty()) {
+            fro = B.add(fr.data(), fr.size());
+            fdo = B.add(fed.data(), fed.size());
+            ffo = B.add(fef.data(), fef.size());
+            fio = B.add(fei.data(), fei.size());
+        }
+        const int Rf = (fact && !fed.empty()) ? R_pow : 0;
         if (nb == 3) {
             H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
             H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);
+            H.R3 = Rf;
+            H.fr3 = as_off<const FactRow>(fro); H.fe3d = as_off<const double>(fdo);
+            H.fe3f = as_off<const float>(ffo); H.fe3i = as_off<const uint16_t>(fio);
         } else {
             H.t4 = as_off<const TupleRec>(tro); H.c4d = as_off<const double>(cdo);
             H.c4f = as_off<const float>(cfo); H.p4 = as_off<const uint32_t>(pwo);
+            H.R4 = Rf;
+            H.fr4 = as_off<const FactRow>(fro); H.fe4d = as_off<const double>(fdo);
+            H.fe4f = as_off<const float>(ffo); H.fe4i = as_off<const uint16_t>(fio);
         }
     }
     img.header_off = B.add(&H, 1);

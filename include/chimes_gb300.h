@@ -49,14 +49,31 @@ int ck_param_info(void *h, int slot, int *orders, int *ntypes, double *maxcuts);
  * valid[u] (an included type with coefficients), ncoef[u] and rout[u][6], the
  * outer cutoffs in the cluster's own pair order. */
 int ck_tuple_table(void *h, int slot, int nbody, int *valid, int *ncoef, double *rout);
+/* Factored coefficient lists per ordered tuple u (see ck_set_contraction):
+ * nrow[u], ncol[u] row and column records (0 for tuples without coefficients)
+ * and *R, the powers per pair (0 when the set has no factored tables). */
+int ck_tuple_factored(void *h, int slot, int nbody, int *nrow, int *ncol, int *R);
+/* out[9] = tpc3, tpc4, blocks_per_sm (per-coefficient kernels), factored 3B and
+ * 4B in use for the staged batch (0/1), their threads per cluster and one-warp
+ * blocks per SM (ftpc3, ftpc4, fbps3, fbps4) */
+int ck_get_tuning(void *h, int *out);
 /* index of an atom type name in a slot, or -1 */
 int ck_type_index(void *h, int slot, const char *name);
 
 /* 0: FP64 throughout (default); 1: FP32 Chebyshev/cutoff/contraction with FP64
  * distances and FP64 energy/force/virial accumulation. */
 int ck_set_precision(void *h, int precision);
-/* threads per 3-body and 4-body cluster (1,2,4,8,16,32) and resident blocks per SM */
+/* threads per 3-body and 4-body cluster (1,2,4,8,16,32) and resident 4-warp
+ * blocks per SM of the per-coefficient kernels; the factored kernels take
+ * min(tpc, 4) threads per cluster and 4 * blocks_per_sm one-warp blocks
+ * (capped by their shared-memory occupancy). */
 int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
+/* 3-/4-body contraction kernels: 1 (default) = factored (coefficients grouped
+ * by row and column products, two multiply-adds per coefficient) wherever every
+ * parameter set of the batch has factored tables (powers per pair R with R^K and
+ * R^(P-K) <= 128, K = 1 for 3-body and 3 for 4-body), 0 = per-coefficient
+ * kernels everywhere.  Both give the same sums in another rounding order. */
+int ck_set_contraction(void *h, int factored);
 /* Autotuner for the batch staged with ck_stage_batch: times the 3-body and
  * 4-body force kernels (CUDA events) for threads per cluster 1..32 and then
  * 1, 2, 4, 8 resident blocks per SM, keeps the fastest and caches it by the

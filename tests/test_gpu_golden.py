@@ -12,9 +12,10 @@ from conftest import (E_REL_TOL, F_ABS_TOL, MIXED_E_REL_TOL, MIXED_F_ABS_TOL, S_
 pytestmark = pytest.mark.gpu
 
 
-def evaluate(g, precision=0, graph=False, tpc=None):
+def evaluate(g, precision=0, graph=False, tpc=None, factored=True):
     from chimes_calculator_gb300 import Calculator
     c = Calculator(precision=precision, graph=graph)
+    c.set_contraction(factored)
     if tpc:
         c.set_tuning(*tpc)
     c.load_params(g.params)
@@ -22,10 +23,11 @@ def evaluate(g, precision=0, graph=False, tpc=None):
     return c, r
 
 
+@pytest.mark.parametrize("factored", [True, False], ids=["factored", "per_coef"])
 @pytest.mark.parametrize("name", golden_names())
-def test_fp64_matches_reference(golden, native_lib, name):
+def test_fp64_matches_reference(golden, native_lib, name, factored):
     g = golden[name]
-    c, r = evaluate(g)
+    c, r = evaluate(g, factored=factored)
     assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
     assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
     assert np.abs(r["stress"] - g.stress).max() <= S_ABS_TOL
@@ -46,19 +48,21 @@ def test_lists_match_oracle(golden, native_lib, name):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("factored", [True, False], ids=["factored", "per_coef"])
 @pytest.mark.parametrize("name", golden_names())
-def test_mixed_precision_error(golden, native_lib, name):
+def test_mixed_precision_error(golden, native_lib, name, factored):
     g = golden[name]
-    _, r64 = evaluate(g, precision=0)
-    _, r32 = evaluate(g, precision=1)
+    _, r64 = evaluate(g, precision=0, factored=factored)
+    _, r32 = evaluate(g, precision=1, factored=factored)
     assert abs(r32["energy"] - r64["energy"]) <= MIXED_E_REL_TOL * max(1.0, abs(r64["energy"]))
     assert np.abs(r32["force"] - r64["force"]).max() <= MIXED_F_ABS_TOL
 
 
-@pytest.mark.parametrize("tpc", [(1, 1, 2), (2, 4, 4), (8, 16, 4), (32, 32, 2)])
-def test_threads_per_cluster_variants(golden, native_lib, tpc):
+@pytest.mark.parametrize("factored", [True, False], ids=["factored", "per_coef"])
+@pytest.mark.parametrize("tpc", [(1, 1, 2), (2, 4, 4), (8, 16, 4), (32, 32, 2), (4, 2, 1)])
+def test_threads_per_cluster_variants(golden, native_lib, tpc, factored):
     g = golden["c2_small"]
-    _, r = evaluate(g, tpc=tpc)
+    _, r = evaluate(g, tpc=tpc, factored=factored)
     assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
     assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
 

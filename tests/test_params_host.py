@@ -107,3 +107,28 @@ def test_seven_column_pair_lines(lib, tmp_path):
     a = check(lib, p7)
     b = check(lib, p8)
     assert a[0] == 0 and a[1:4] == b[1:4]
+
+
+@pytest.fixture(scope="module")
+def factored_check(tmp_path_factory):
+    """tests/factored_check.cpp built against the product's parameter packer."""
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "chimes_calculator_gb300", "csrc")
+    exe = str(tmp_path_factory.mktemp("fc") / "factored_check")
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-I" + csrc,
+                    os.path.join(here, "factored_check.cpp"), os.path.join(csrc, "ck_params.cpp"), "-o", exe],
+                   check=True)
+    return exe
+
+
+def test_factored_tables_reproduce_the_coefficient_sums(factored_check, golden, tmp_path):
+    import subprocess
+    paths = [g.params for g in golden.values()]
+    for k, spec in enumerate([synth.spec_c3(), synth.spec_c4()] + list(synth.specs_c5())):
+        paths.append(synth.write_param_file(str(tmp_path / ("s%d.txt" % k)), spec))
+    if os.path.isdir(REFFF):
+        paths += [os.path.join(REFFF, f) for f in sorted(os.listdir(REFFF)) if f.endswith(".txt")]
+    for p in paths:
+        out = subprocess.run([factored_check, str(p)], capture_output=True, text=True)
+        assert out.returncode == 0 and out.stdout.startswith("ok"), (p, out.stdout)
