@@ -426,6 +426,25 @@ def serving(args):
     return out
 
 
+def profile_batched(args):
+    """The batched workload alone, for a profiler's launch list."""
+    import torch
+    from chimes_calculator_gb300 import Calculator, synth
+    torch.cuda.set_device(0)
+    tmp = tempfile.mkdtemp(prefix="ckp")
+    p4 = synth.write_param_file(os.path.join(tmp, "c4.params"), synth.spec_c4())
+    cfgs = synth.configs_c4(n_configs=args.batch_configs)
+    atoms = sum(c.n_atoms for c in cfgs)
+    c = Calculator(precision=args.precision, graph=True)
+    c.load_params(p4)
+    c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
+    c.autotune()
+    r = time_steps(c, atoms, 2)
+    r["autotuned"] = c.tuning()
+    r["configs"] = len(cfgs)
+    print(json.dumps(r))
+
+
 def time_steps(c, atoms, steps):
     import torch
     from chimes_calculator_gb300 import _lib
@@ -567,7 +586,13 @@ def main():
     ap.add_argument("--precision", type=int, default=0, help="0 FP64 (headline), 1 mixed")
     ap.add_argument("--profile-run", action="store_true",
                     help="minimal run for a profiler: 3 warm-up + 2 steps, no e2e / CPU legs")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="profiler run of the batched workload (--batch-configs configurations, "
+                         "--precision): autotune, 3 warm-up + 2 launches")
     args = ap.parse_args()
+    if args.profile_batched:
+        profile_batched(args)
+        return
     if args.profile_run:
         args.steps, args.warmup, args.no_cpu, args.extras = 2, 3, True, False
     if args.warmup < 3:

@@ -58,6 +58,8 @@ SIGNATURES = {
     "ck_load_params": (I, [P, S]),
     "ck_select_params": (I, [P, I]),
     "ck_check_params": (I, [S, IP, IP, DP]),
+    "ck_save_params_cache": (I, [P, I, S]),
+    "ck_convert_params": (I, [S, S]),
     "ck_param_info": (I, [P, I, IP, IP, DP]),
     "ck_type_index": (I, [P, I, S]),
     "ck_tuple_table": (I, [P, I, I, IP, IP, DP]),

@@ -68,6 +68,10 @@ class Calculator:
         self._types.append({})
         return slot
 
+    def save_params_cache(self, path: str, slot: int = 0):
+        """Writes the slot's parsed tables as a binary cache that load_params reads without parsing."""
+        self._check(self.lib.ck_save_params_cache(self.h, slot, path.encode()))
+
     def info(self, slot: int = 0):
         orders = (ctypes.c_int * 3)()
         nt = ctypes.c_int()

@@ -249,6 +249,25 @@ int ck_tuple_table(void* h, int slot, int nbody, int* valid, int* ncoef, double*
     return ck::kOk;
 }
 
+int ck_save_params_cache(void* h, int slot, const char* path) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (slot < 0 || slot >= in->eng.n_param_sets()) return report(ck::kErrInput, "no such parameter slot");
+    std::string err;
+    ck::Status st = ck::save_parameter_cache(in->eng.params(slot), path ? path : "", err);
+    if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
+int ck_convert_params(const char* text_path, const char* cache_path) {
+    ck::HostParams P;
+    std::string err;
+    ck::Status st = ck::parse_parameter_file(text_path ? text_path : "", P, err);
+    if (st == ck::kOk) st = ck::save_parameter_cache(P, cache_path ? cache_path : "", err);
+    if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
 int ck_tuple_factored(void* h, int slot, int nbody, int* nrow, int* ncol, int* R) {
     if (int st = check_handle(h)) return st;
     Instance* in = static_cast<Instance*>(h);

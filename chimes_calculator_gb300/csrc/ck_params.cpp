@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <sstream>
 
@@ -443,12 +444,163 @@ int HostParams::type_index(const std::string& name) const {
     return -1;
 }
 
+// ---------------------------------------------------------------------------
+// Binary parameter cache: the parsed tables in a flat little-endian stream
+// ("CKPC" magic, format version, then every HostParams field in declaration
+// order; strings and vectors carry their lengths).  Loading it skips the text
+// parse; packing it gives the same device image as the text file.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr char kCacheMagic[4] = {'C', 'K', 'P', 'C'};
+constexpr int kCacheVersion = 1;
+
+struct Writer {
+    std::string b;
+    void raw(const void* p, size_t n) { b.append(static_cast<const char*>(p), n); }
+    void i(long long v) { raw(&v, sizeof(v)); }
+    void d(double v) { raw(&v, sizeof(v)); }
+    void str(const std::string& v) { i((long long)v.size()); raw(v.data(), v.size()); }
+    void vi(const std::vector<int>& v) { i((long long)v.size()); for (int x : v) i(x); }
+    void vd(const std::vector<double>& v) { i((long long)v.size()); raw(v.data(), v.size() * sizeof(double)); }
+    void vs(const std::vector<std::string>& v) { i((long long)v.size()); for (auto& x : v) str(x); }
+    void vvi(const std::vector<std::vector<int>>& v) { i((long long)v.size()); for (auto& x : v) vi(x); }
+    void vvd(const std::vector<std::vector<double>>& v) { i((long long)v.size()); for (auto& x : v) vd(x); }
+    void vvs(const std::vector<std::vector<std::string>>& v) { i((long long)v.size()); for (auto& x : v) vs(x); }
+};
+
+struct Reader {
+    const std::string& b;
+    size_t pos = 0;
+    explicit Reader(const std::string& s) : b(s) {}
+    void raw(void* p, size_t n) {
+        if (pos + n > b.size()) throw ParseError{"truncated parameter cache"};
+        std::memcpy(p, b.data() + pos, n);
+        pos += n;
+    }
+    long long i() { long long v; raw(&v, sizeof(v)); return v; }
+    double d() { double v; raw(&v, sizeof(v)); return v; }
+    size_t len() {
+        const long long n = i();
+        if (n < 0 || (size_t)n > b.size()) throw ParseError{"corrupt parameter cache"};
+        return (size_t)n;
+    }
+    std::string str() { std::string v(len(), '\0'); raw(&v[0], v.size()); return v; }
+    std::vector<int> vi() { std::vector<int> v(len()); for (auto& x : v) x = (int)i(); return v; }
+    std::vector<double> vd() { std::vector<double> v(len()); raw(v.data(), v.size() * sizeof(double)); return v; }
+    std::vector<std::string> vs() { std::vector<std::string> v(len()); for (auto& x : v) x = str(); return v; }
+    std::vector<std::vector<int>> vvi() { std::vector<std::vector<int>> v(len()); for (auto& x : v) x = vi(); return v; }
+    std::vector<std::vector<double>> vvd() { std::vector<std::vector<double>> v(len()); for (auto& x : v) x = vd(); return v; }
+    std::vector<std::vector<std::string>> vvs() {
+        std::vector<std::vector<std::string>> v(len());
+        for (auto& x : v) x = vs();
+        return v;
+    }
+};
+
+void put_body(Writer& w, const HostParams::Body& B) {
+    w.i(B.nbody); w.i(B.npair); w.i(B.ntyp);
+    w.vi(B.ncoef); w.vvi(B.pows); w.vvd(B.coef); w.vvd(B.cut_in); w.vvd(B.cut_out);
+    w.vvs(B.atoms); w.vvs(B.pairs); w.vi(B.map); w.vvi(B.perm);
+}
+
+void get_body(Reader& r, HostParams::Body& B) {
+    B.nbody = (int)r.i(); B.npair = (int)r.i(); B.ntyp = (int)r.i();
+    B.ncoef = r.vi(); B.pows = r.vvi(); B.coef = r.vvd(); B.cut_in = r.vvd(); B.cut_out = r.vvd();
+    B.atoms = r.vvs(); B.pairs = r.vvs(); B.map = r.vi(); B.perm = r.vvi();
+}
+
+void get_params(Reader& r, HostParams& P) {
+    P.ntypes = (int)r.i(); P.npairs = (int)r.i();
+    P.o2 = (int)r.i(); P.o3 = (int)r.i(); P.o4 = (int)r.i();
+    P.atm = r.vs(); P.mass = r.vd(); P.pa1 = r.vs(); P.pa2 = r.vs();
+    P.rin = r.vd(); P.rout = r.vd(); P.lam = r.vd();
+    P.tersoff = r.i() != 0;
+    P.fcut_var = r.d(); P.pen_dist = r.d(); P.pen_scale = r.d(); P.inner_smooth = r.d();
+    P.eoff = r.vd(); P.pows2 = r.vvi(); P.coef2 = r.vvd();
+    P.pair_map = r.vi(); P.prpr = r.vi(); P.pair_map_file_idx = r.vi();
+    get_body(r, P.b3);
+    get_body(r, P.b4);
+    // the kernels index these tables without further checks
+    const int nt = P.ntypes;
+    if (nt <= 0 || nt > kMaxTypes || P.npairs != nt * (nt + 1) / 2 || (int)P.pair_map.size() != nt * nt ||
+        (int)P.rin.size() != P.npairs || (int)P.coef2.size() != P.npairs || (int)P.eoff.size() != nt ||
+        P.o2 < 0 || P.o2 > kMaxOrder || P.o3 < 0 || P.o3 > kMaxOrder || P.o4 < 0 || P.o4 > kMaxOrder)
+        throw ParseError{"inconsistent parameter cache"};
+    for (int v : P.pair_map)
+        if (v < 0 || v >= P.npairs) throw ParseError{"inconsistent parameter cache"};
+    for (int nb = 3; nb <= 4; nb++) {
+        const HostParams::Body& B = nb == 3 ? P.b3 : P.b4;
+        if ((nb == 3 ? P.o3 : P.o4) == 0) continue;
+        int ntup = 1;
+        for (int k = 0; k < nb; k++) ntup *= nt;
+        if ((int)B.map.size() != ntup || (int)B.perm.size() != ntup) throw ParseError{"inconsistent parameter cache"};
+        for (int u = 0; u < ntup; u++) {
+            const int ti = B.map[u];
+            if (ti < 0) continue;
+            if (ti >= (int)B.ncoef.size() || ti >= (int)B.pows.size() || ti >= (int)B.coef.size() ||
+                ti >= (int)B.cut_in.size() || ti >= (int)B.cut_out.size() || (int)B.perm[u].size() != B.npair ||
+                (long long)B.pows[ti].size() != (long long)B.ncoef[ti] * B.npair ||
+                (int)B.coef[ti].size() != B.ncoef[ti])
+                throw ParseError{"inconsistent parameter cache"};
+            for (int m : B.perm[u])
+                if (m < 0 || m >= B.npair || m >= (int)B.cut_in[ti].size() || m >= (int)B.cut_out[ti].size())
+                    throw ParseError{"inconsistent parameter cache"};
+            for (int v : B.pows[ti])
+                if (v < 0 || v > kMaxOrder) throw ParseError{"inconsistent parameter cache"};
+        }
+    }
+}
+}  // namespace
+
+Status save_parameter_cache(const HostParams& P, const std::string& path, std::string& err) {
+    Writer w;
+    w.raw(kCacheMagic, 4);
+    w.i(kCacheVersion);
+    w.i(P.ntypes); w.i(P.npairs); w.i(P.o2); w.i(P.o3); w.i(P.o4);
+    w.vs(P.atm); w.vd(P.mass); w.vs(P.pa1); w.vs(P.pa2);
+    w.vd(P.rin); w.vd(P.rout); w.vd(P.lam);
+    w.i(P.tersoff ? 1 : 0);
+    w.d(P.fcut_var); w.d(P.pen_dist); w.d(P.pen_scale); w.d(P.inner_smooth);
+    w.vd(P.eoff); w.vvi(P.pows2); w.vvd(P.coef2);
+    w.vi(P.pair_map); w.vi(P.prpr); w.vi(P.pair_map_file_idx);
+    put_body(w, P.b3);
+    put_body(w, P.b4);
+    std::ofstream f(path, std::ios::binary | std::ios::trunc);
+    if (!f.is_open()) {
+        err = "cannot write parameter cache: " + path;
+        return kErrParam;
+    }
+    f.write(w.b.data(), (std::streamsize)w.b.size());
+    if (!f) {
+        err = "error writing parameter cache: " + path;
+        return kErrParam;
+    }
+    return kOk;
+}
+
 Status parse_parameter_file(const std::string& path, HostParams& P, std::string& err) {
-    std::ifstream f(path);
+    std::ifstream f(path, std::ios::binary);
     if (!f.is_open()) {
         err = "cannot open parameter file: " + path;
         return kErrParam;
     }
+    char head[4] = {0, 0, 0, 0};
+    f.read(head, 4);
+    if (f.gcount() == 4 && std::memcmp(head, kCacheMagic, 4) == 0) {
+        std::string all((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        P = HostParams();
+        try {
+            Reader r(all);
+            if (r.i() != kCacheVersion) throw ParseError{"parameter cache of another format version"};
+            get_params(r, P);
+        } catch (const ParseError& e) {
+            err = e.msg + ": " + path;
+            return kErrParam;
+        }
+        return kOk;
+    }
+    f.clear();
+    f.seekg(0);
     Lines L;
     std::string line;
     while (std::getline(f, line)) L.v.push_back(line);

@@ -47,7 +47,10 @@ struct HostParams {
     std::string pair_name(int p) const { return pa1[p] + pa2[p]; }
 };
 
+// Reads a ChIMES parameter file, or a binary parameter cache written by
+// save_parameter_cache (recognised by its magic bytes).
 Status parse_parameter_file(const std::string& path, HostParams& P, std::string& err);
+Status save_parameter_cache(const HostParams& P, const std::string& path, std::string& err);
 
 // Contiguous host image of one DevParamSet: the struct followed by its arrays.
 // Pointers inside `header` are offsets until relocated to a device base.

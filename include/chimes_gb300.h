@@ -44,6 +44,14 @@ int ck_select_params(void *h, int slot);
  * inspection.  Same outputs as ck_param_info. */
 int ck_check_params(const char *path, int *orders, int *ntypes, double *maxcuts);
 /* orders[3] = 2B/3B/4B orders, *ntypes, maxcuts[3] = max outer cutoffs. */
+/* Binary parameter cache (no counterpart in the reference, whose
+ * read_parameters parses the text file, chimesFF.cpp:354-1570, on every start):
+ * the parsed tables of a slot, or of a text file (host only, no device), in a
+ * flat binary file.  ck_load_params / ck_check_params / init_chimes_serial
+ * accept either form (the cache is recognised by its magic bytes) and give the
+ * same device tables; loading the cache skips the text parse. */
+int ck_save_params_cache(void *h, int slot, const char *path);
+int ck_convert_params(const char *text_path, const char *cache_path);
 int ck_param_info(void *h, int slot, int *orders, int *ntypes, double *maxcuts);
 /* Per ordered atom-type tuple u (nbody = 3: nt^3 entries, 4: nt^4) of a slot:
  * valid[u] (an included type with coefficients), ncoef[u] and rout[u][6], the

@@ -2,7 +2,9 @@
 // 3-/4-body tuple of a parameter file, random Chebyshev tables T_p, dT_p give
 // the same S = sum a prod T and G_p = sum a dT_p prod_{q!=p} T through the
 // per-coefficient packed powers and through the row/column factored lists.
-// Usage: factored_check <params>; prints "ok <tuples checked>" or a mismatch.
+// With a second argument (a binary parameter cache of the same file) it also
+// checks that the cache packs into the same device image as the text file.
+// Usage: factored_check <params> [cache]; prints "ok <tuples checked>" or a mismatch.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -28,6 +30,18 @@ int main(int argc, char** argv) {
     }
     ParamImage img = pack_params(P);
     const DevParamSet& H = img.header;
+    if (argc > 2) {
+        HostParams Q;
+        if (parse_parameter_file(argv[2], Q, err) != kOk) {
+            std::printf("cache parse error: %s\n", err.c_str());
+            return 1;
+        }
+        ParamImage img2 = pack_params(Q);
+        if (img2.bytes != img.bytes || img2.header_off != img.header_off) {
+            std::printf("cache packs differently\n");
+            return 1;
+        }
+    }
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> U(-1.0, 1.0);
     int checked = 0;

@@ -132,3 +132,30 @@ def test_factored_tables_reproduce_the_coefficient_sums(factored_check, golden, 
     for p in paths:
         out = subprocess.run([factored_check, str(p)], capture_output=True, text=True)
         assert out.returncode == 0 and out.stdout.startswith("ok"), (p, out.stdout)
+
+
+def test_parameter_cache_round_trip(lib, factored_check, golden, tmp_path):
+    """A binary cache parses to the same tables (same device image) as its text file."""
+    import subprocess
+    paths = [g.params for g in golden.values()]
+    if os.path.isdir(REFFF):
+        paths += [os.path.join(REFFF, f) for f in sorted(os.listdir(REFFF)) if f.endswith(".txt")]
+    for k, p in enumerate(paths):
+        cache = str(tmp_path / ("c%d.ckpc" % k))
+        assert lib.ck_convert_params(str(p).encode(), cache.encode()) == 0, lib.ck_last_error()
+        a, b = check(lib, p), check(lib, cache)
+        assert a[:4] == b[:4] and a[0] == 0
+        out = subprocess.run([factored_check, str(p), cache], capture_output=True, text=True)
+        assert out.returncode == 0 and out.stdout.startswith("ok"), (p, out.stdout)
+
+
+def test_parameter_cache_rejects_corruption(lib, golden, tmp_path):
+    g = golden["c2"]
+    cache = tmp_path / "c2.ckpc"
+    assert lib.ck_convert_params(str(g.params).encode(), str(cache).encode()) == 0
+    data = cache.read_bytes()
+    for cut in (6, len(data) // 2, len(data) - 3):
+        bad = tmp_path / ("cut%d.ckpc" % cut)
+        bad.write_bytes(data[:cut])
+        rc, *_, msg = check(lib, bad)
+        assert rc == -1 and "cache" in msg
