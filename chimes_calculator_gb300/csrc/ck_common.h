@@ -84,6 +84,18 @@ struct FactRow {
 };
 constexpr int kFactMaxDim = 128;   // largest R^K and R^(P-K) kept in shared memory per cluster
 
+// One factored-list entry: coefficient and the other side's linear index, in
+// one 16-byte (FP64) or 8-byte (FP32) load.
+struct __attribute__((aligned(16))) FactEntD {
+    double a;
+    int idx;
+    int pad;
+};
+struct __attribute__((aligned(8))) FactEntF {
+    float a;
+    int idx;
+};
+
 struct DevParamSet {
     int ntypes, npairs, o2, o3, o4;
     int tersoff;
@@ -101,8 +113,8 @@ struct DevParamSet {
     // absent (R^K or R^(P-K) above kFactMaxDim)
     int R3, R4;
     int bk3, bk4;              // first cluster bucket of this set (per engine; see BatchView)
-    const FactRow* fr3; const double* fe3d; const float* fe3f; const uint16_t* fe3i;
-    const FactRow* fr4; const double* fe4d; const float* fe4f; const uint16_t* fe4i;
+    const FactRow* fr3; const FactEntD* fe3d; const FactEntF* fe3f;
+    const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
 };
 
 // Per-system geometry, written by the host set-up (cell algebra) and

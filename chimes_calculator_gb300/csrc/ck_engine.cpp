@@ -106,8 +106,8 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.eoff); rel(h.pair_map); rel(h.pairs); rel(h.c2d); rel(h.c2f); rel(h.p2);
     rel(h.t3); rel(h.c3d); rel(h.c3f); rel(h.p3);
     rel(h.t4); rel(h.c4d); rel(h.c4f); rel(h.p4);
-    rel(h.fr3); rel(h.fe3d); rel(h.fe3f); rel(h.fe3i);
-    rel(h.fr4); rel(h.fe4d); rel(h.fe4f); rel(h.fe4i);
+    rel(h.fr3); rel(h.fe3d); rel(h.fe3f);
+    rel(h.fr4); rel(h.fe4d); rel(h.fe4f);
     // this set's cluster buckets follow those of the sets loaded before it
     int nt3 = h.ntypes * h.ntypes * h.ntypes;
     h.bk3 = nbk3_;

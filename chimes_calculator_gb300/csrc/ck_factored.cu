@@ -43,12 +43,46 @@ struct Split<4> {
     static constexpr int K = 3;
 };
 
+template <typename CT>
+struct EntOf;
+template <>
+struct EntOf<double> {
+    using type = FactEntD;
+};
+template <>
+struct EntOf<float> {
+    using type = FactEntF;
+};
+
 template <typename CT, int NB>
-__device__ __forceinline__ const CT* fact_coef(const DevParamSet& P);
-template <> __device__ __forceinline__ const double* fact_coef<double, 3>(const DevParamSet& P) { return P.fe3d; }
-template <> __device__ __forceinline__ const float* fact_coef<float, 3>(const DevParamSet& P) { return P.fe3f; }
-template <> __device__ __forceinline__ const double* fact_coef<double, 4>(const DevParamSet& P) { return P.fe4d; }
-template <> __device__ __forceinline__ const float* fact_coef<float, 4>(const DevParamSet& P) { return P.fe4f; }
+__device__ __forceinline__ const typename EntOf<CT>::type* fact_ent(const DevParamSet& P);
+template <> __device__ __forceinline__ const FactEntD* fact_ent<double, 3>(const DevParamSet& P) { return P.fe3d; }
+template <> __device__ __forceinline__ const FactEntF* fact_ent<float, 3>(const DevParamSet& P) { return P.fe3f; }
+template <> __device__ __forceinline__ const FactEntD* fact_ent<double, 4>(const DevParamSet& P) { return P.fe4d; }
+template <> __device__ __forceinline__ const FactEntF* fact_ent<float, 4>(const DevParamSet& P) { return P.fe4f; }
+
+// sum over entries [e0, e1) taken by lane gl of TPC: a * V[idx]; eight
+// entries per round in two partial sums, so their loads overlap
+template <typename CT, int TPC, int G, typename E>
+__device__ __forceinline__ CT entry_sum(const E* __restrict__ ent, int e0, int e1, int gl, const CT* V, int grp) {
+    CT z0 = CT(0), z1 = CT(0);
+    int k = e0 + gl;
+    for (; k + 7 * TPC < e1; k += 8 * TPC) {
+        E q[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) q[u] = ent[k + u * TPC];
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+            z0 += CT(q[u].a) * V[q[u].idx * G + grp];
+            z1 += CT(q[u + 1].a) * V[q[u + 1].idx * G + grp];
+        }
+    }
+    for (; k < e1; k += TPC) {
+        const E q = ent[k];
+        z0 += CT(q.a) * V[q.idx * G + grp];
+    }
+    return z0 + z1;
+}
 
 // Ordered type tuple of cluster c: its ghost slots, system, parameter set and tuple index.
 template <int NB>
@@ -303,8 +337,7 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         }
         __syncwarp();
 
-        const CT* fe = fact_coef<CT, NB>(*P);
-        const uint16_t* fi = NB == 3 ? P->fe3i : P->fe4i;
+        const auto* ent = fact_ent<CT, NB>(*P);
         const FactRow* rows = (NB == 3 ? P->fr3 : P->fr4) + R->f_row;
         const int nrow = R->f_nrow, ncol = R->f_ncol;
         CT S = CT(0), Gp[NP];
@@ -314,9 +347,7 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         // row pass: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K)
         for (int r = 0; r < nrow; r++) {
             const FactRow rw = rows[r];
-            CT z = CT(0);
-#pragma unroll 4
-            for (int k = e + gl; k < rw.end; k += TPC) z += fe[k] * Y[fi[k] * G + grp];
+            const CT z = entry_sum<CT, TPC, G>(ent, e, rw.end, gl, Y, grp);
             e = rw.end;
             CT t[K], d[K];
 #pragma unroll
@@ -339,9 +370,7 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         // column pass: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K)
         for (int cc = 0; cc < ncol; cc++) {
             const FactRow cl = rows[nrow + cc];
-            CT w = CT(0);
-#pragma unroll 4
-            for (int k = e + gl; k < cl.end; k += TPC) w += fe[k] * Xv[fi[k] * G + grp];
+            const CT w = entry_sum<CT, TPC, G>(ent, e, cl.end, gl, Xv, grp);
             e = cl.end;
             constexpr int C = NP - K;
             CT t[C], d[C];

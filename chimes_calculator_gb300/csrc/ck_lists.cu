@@ -343,47 +343,68 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     const long long total = (long long)d.nb[0] * d.nb[1] * d.nb[2];
     long long base = FILL ? B.l2_off[r] : 0;
     int count = 0;
-    for (int i = bx - 1; i <= bx + 1; i++)
-        for (int j = by - 1; j <= by + 1; j++)
-            for (int k = bz - 1; k <= bz + 1; k++) {
-                const long long ib = i + (long long)j * d.nb[0] + (long long)k * d.nb[0] * d.nb[1];
-                if (ib >= total) {
-                    if (lane == 0) atomicExch(&B.flags[1], 4);
-                    continue;
-                }
-                const long long b = d.bin_off + ib;
-                const long long st = bin_start[b];
-                const int nb = B.bin_count[b];
-                for (int q0 = 0; q0 < nb; q0 += 32) {
-                    const int qq = q0 + lane;
-                    bool pred = false;
-                    int ajj = -1;
-                    double dd = 0.0, rv[3] = {0, 0, 0};
-                    if (qq < nb) {
-                        ajj = B.bin_items[st + qq];
-                        if (ajj != gi && r <= B.ghost_parent[ajj]) {
-                            const float* xj = &B.ghost_xf[3 * (long long)ajj];
-                            const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
-                            if (ex * ex + ey * ey + ez * ez < far2) {   // else certainly >= sd
-                                dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj], rv);
-                                pred = dd < sd;
-                            }
-                        }
-                    }
-                    const unsigned bal = __ballot_sync(kFull, pred);
-                    if (FILL && pred) {
-                        const long long pos = base + count + __popc(bal & ((1u << lane) - 1u));
-                        if (pos < B.n2_cap) {
-                            B.l2_ghost[pos] = ajj;
-                            B.l2_dist[pos] = dd;
-                            l2_owner[pos] = (int)r;
-                            float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], (float)dd);
-                            reinterpret_cast<float4*>(B.l2_vec)[pos] = v;
-                        }
-                    }
-                    count += __popc(bal);
+    // Lane b < 27 owns neighbour bin b in the reference's loop order (x bins
+    // outermost, z innermost); the candidates of all 27 bins are numbered
+    // bin by bin and the warp walks them 32 at a time, so the emitted order
+    // is the reference's and short bins leave no lanes idle.
+    long long bst = 0;
+    int nbin = 0;
+    if (lane < 27) {
+        const int i = bx - 1 + lane / 9, j = by - 1 + (lane / 3) % 3, k = bz - 1 + lane % 3;
+        const long long ib = i + (long long)j * d.nb[0] + (long long)k * d.nb[0] * d.nb[1];
+        if (ib >= total) {
+            atomicExch(&B.flags[1], 4);
+        } else {
+            const long long b = d.bin_off + ib;
+            bst = bin_start[b];
+            nbin = B.bin_count[b];
+        }
+    }
+    int incl = nbin;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int excl = incl - nbin;
+    const int ncand = __shfl_sync(kFull, incl, 31);
+    for (int t0 = 0; t0 < ncand; t0 += 32) {
+        const int t = t0 + lane;
+        // bin of candidate t: the last bin whose first candidate is <= t
+        int lo = 0;
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int cand = lo + step;
+            const int ex = __shfl_sync(kFull, excl, cand & 31);
+            if (cand < 27 && ex <= t) lo = cand;
+        }
+        const long long st = __shfl_sync(kFull, bst, lo);
+        const int first = __shfl_sync(kFull, excl, lo);
+        bool pred = false;
+        int ajj = -1;
+        double dd = 0.0, rv[3] = {0, 0, 0};
+        if (t < ncand) {
+            ajj = B.bin_items[st + (t - first)];
+            if (ajj != gi && r <= B.ghost_parent[ajj]) {
+                const float* xj = &B.ghost_xf[3 * (long long)ajj];
+                const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
+                if (ex * ex + ey * ey + ez * ez < far2) {   // else certainly >= sd
+                    dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj], rv);
+                    pred = dd < sd;
                 }
             }
+        }
+        const unsigned bal = __ballot_sync(kFull, pred);
+        if (FILL && pred) {
+            const long long pos = base + count + __popc(bal & ((1u << lane) - 1u));
+            if (pos < B.n2_cap) {
+                B.l2_ghost[pos] = ajj;
+                B.l2_dist[pos] = dd;
+                l2_owner[pos] = (int)r;
+                float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], (float)dd);
+                reinterpret_cast<float4*>(B.l2_vec)[pos] = v;
+            }
+        }
+        count += __popc(bal);
+    }
     if (!FILL && lane == 0) B.l2_count[r] = count;
 }
 

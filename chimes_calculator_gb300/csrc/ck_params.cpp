@@ -704,9 +704,8 @@ ParamImage pack_params(const HostParams& P) {
         for (int k = K; k < np; k++) rc *= R_pow;
         const bool fact = rk <= kFactMaxDim && rc <= kFactMaxDim;
         std::vector<FactRow> fr;
-        std::vector<double> fed;
-        std::vector<float> fef;
-        std::vector<uint16_t> fei;
+        std::vector<FactEntD> fed;
+        std::vector<FactEntF> fef;
         struct Shared { int coef_off, f_row, f_nrow, f_ncol, f_ent; };
         std::map<std::pair<int, std::vector<int>>, Shared> shared;  // (type, mapping) -> tables
         for (int u = 0; u < ntup; u++) {
@@ -781,9 +780,8 @@ ParamImage pack_params(const HostParams& P) {
                     int nrec = 0;
                     for (int k = 0; k < R.ncoef; k++) {
                         const int c = ord[k];
-                        fed.push_back(Bd.coef[ti][c]);
-                        fef.push_back((float)Bd.coef[ti][c]);
-                        fei.push_back((uint16_t)minor[c]);
+                        fed.push_back(FactEntD{Bd.coef[ti][c], minor[c], 0});
+                        fef.push_back(FactEntF{(float)Bd.coef[ti][c], minor[c]});
                         if (k + 1 == R.ncoef || major[ord[k + 1]] != major[c]) {
                             fr.push_back(FactRow{mpows[c], (int)fed.size()});
                             nrec++;
@@ -798,26 +796,25 @@ ParamImage pack_params(const HostParams& P) {
         size_t cdo = B.add(cd.data(), cd.size());
         size_t cfo = B.add(cf.data(), cf.size());
         size_t pwo = B.add(pw.data(), pw.size());
-        size_t fro = 0, fdo = 0, ffo = 0, fio = 0;
+        size_t fro = 0, fdo = 0, ffo = 0;
         if (fact && !fed.empty()) {
             fro = B.add(fr.data(), fr.size());
             fdo = B.add(fed.data(), fed.size());
             ffo = B.add(fef.data(), fef.size());
-            fio = B.add(fei.data(), fei.size());
         }
         const int Rf = (fact && !fed.empty()) ? R_pow : 0;
         if (nb == 3) {
             H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
             H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);
             H.R3 = Rf;
-            H.fr3 = as_off<const FactRow>(fro); H.fe3d = as_off<const double>(fdo);
-            H.fe3f = as_off<const float>(ffo); H.fe3i = as_off<const uint16_t>(fio);
+            H.fr3 = as_off<const FactRow>(fro); H.fe3d = as_off<const FactEntD>(fdo);
+            H.fe3f = as_off<const FactEntF>(ffo);
         } else {
             H.t4 = as_off<const TupleRec>(tro); H.c4d = as_off<const double>(cdo);
             H.c4f = as_off<const float>(cfo); H.p4 = as_off<const uint32_t>(pwo);
             H.R4 = Rf;
-            H.fr4 = as_off<const FactRow>(fro); H.fe4d = as_off<const double>(fdo);
-            H.fe4f = as_off<const float>(ffo); H.fe4i = as_off<const uint16_t>(fio);
+            H.fr4 = as_off<const FactRow>(fro); H.fe4d = as_off<const FactEntD>(fdo);
+            H.fe4f = as_off<const FactEntF>(ffo);
         }
     }
     img.header_off = B.add(&H, 1);

@@ -60,8 +60,8 @@ int main(int argc, char** argv) {
         const double* cd = at(img.bytes, nb == 3 ? H.c3d : H.c4d);
         const uint32_t* pw = at(img.bytes, nb == 3 ? H.p3 : H.p4);
         const FactRow* fr = at(img.bytes, nb == 3 ? H.fr3 : H.fr4);
-        const double* fe = at(img.bytes, nb == 3 ? H.fe3d : H.fe4d);
-        const uint16_t* fi = at(img.bytes, nb == 3 ? H.fe3i : H.fe4i);
+        const FactEntD* fe = at(img.bytes, nb == 3 ? H.fe3d : H.fe4d);
+        const FactEntF* ff = at(img.bytes, nb == 3 ? H.fe3f : H.fe4f);
         for (int u = 0; u < ntup; u++) {
             const TupleRec& R = tr[u];
             if (!R.valid) continue;
@@ -116,8 +116,11 @@ int main(int argc, char** argv) {
                 const FactRow rw = fr[R.f_row + r];
                 double z = 0;
                 for (int k = e; k < rw.end; k++) {
-                    if (fi[k] >= ny) { std::printf("column index out of range\n"); return 1; }
-                    z += fe[k] * prod_of(fi[k], K, np, -1);
+                    if (fe[k].idx < 0 || fe[k].idx >= ny || ff[k].idx != fe[k].idx || ff[k].a != (float)fe[k].a) {
+                        std::printf("bad row entry\n");
+                        return 1;
+                    }
+                    z += fe[k].a * prod_of(fe[k].idx, K, np, -1);
                 }
                 e = rw.end;
                 S1 += prod_packed(rw.pows, 0, K, -1) * z;
@@ -128,8 +131,11 @@ int main(int argc, char** argv) {
                 const FactRow cl = fr[R.f_row + R.f_nrow + c];
                 double w = 0;
                 for (int k = e; k < cl.end; k++) {
-                    if (fi[k] >= nx) { std::printf("row index out of range\n"); return 1; }
-                    w += fe[k] * prod_of(fi[k], 0, K, -1);
+                    if (fe[k].idx < 0 || fe[k].idx >= nx || ff[k].idx != fe[k].idx) {
+                        std::printf("bad column entry\n");
+                        return 1;
+                    }
+                    w += fe[k].a * prod_of(fe[k].idx, 0, K, -1);
                 }
                 e = cl.end;
                 for (int p = K; p < np; p++) G1[p] += prod_packed(cl.pows, K, np, p) * w;
