@@ -69,6 +69,7 @@ SIGNATURES = {
     "ck_set_tuning": (I, [P, I, I, I]),
     "ck_set_contraction": (I, [P, I]),
     "ck_use_graph": (I, [P, I]),
+    "ck_autotune_repeats": (I, [P, I]),
     "ck_autotune": (I, [P, IP]),
     "ck_calculate_batch": (I, [P, I, IP, DP, IP, DP, IP, IP, DP, DP, DP]),
     "ck_stage_batch": (I, [P, I, IP, DP, IP, DP, IP, IP]),
@@ -83,6 +84,8 @@ SIGNATURES = {
     "ck_export_lists": (I, [P, IP, IP, IP]),
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
     "ck_calculate_noalloc": (I, [P, I, P, P, DP, I, P, P, P, P]),
+    "ck_nl_compute": (I, [P, I, DP, IP, LLP, I, IP, IP, IP, D, I, DP, DP, DP]),
+    "ck_nl_lists": (I, [P, LLP, IP, IP]),
     "ck_server_open": (P, [I, D, LL, I]),
     "ck_server_close": (None, [P]),
     "ck_server_load_params": (I, [P, S]),

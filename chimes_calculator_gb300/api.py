@@ -130,6 +130,32 @@ class Calculator:
     def set_tuning(self, tpc3: int = 4, tpc4: int = 8, blocks_per_sm: int = 4):
         self._check(self.lib.ck_set_tuning(self.h, tpc3, tpc4, blocks_per_sm))
 
+    def nl_compute(self, nl, skin: float, rebuild: bool = True):
+        """LAMMPS pair-style evaluation on a neighbour list `nl` (fields x, type,
+        tag, ilist, numneigh, neigh as synth.NeighborData): forces on local and
+        ghost atoms, energy and virial (xx yy zz xy xz yz), all from zero."""
+        x = np.ascontiguousarray(nl.x, dtype=np.float64)
+        nall = x.shape[0]
+        f = np.zeros((nall, 3))
+        e = ctypes.c_double(0.0)
+        vir = np.zeros(6)
+        tag = np.ascontiguousarray(nl.tag, dtype=np.int64)
+        self._check(self.lib.ck_nl_compute(
+            self.h, nall, _dp(x), _ip(np.ascontiguousarray(nl.type, dtype=np.int32)),
+            tag.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), len(nl.ilist),
+            _ip(np.ascontiguousarray(nl.ilist, dtype=np.int32)), _ip(np.ascontiguousarray(nl.numneigh, dtype=np.int32)),
+            _ip(np.ascontiguousarray(nl.neigh, dtype=np.int32)), float(skin), int(bool(rebuild)), _dp(f),
+            ctypes.byref(e), _dp(vir)))
+        return {"energy": e.value, "force": f, "virial": vir}
+
+    def nl_lists(self):
+        cnt = (ctypes.c_longlong * 2)()
+        self._check(self.lib.ck_nl_lists(self.h, cnt, None, None))
+        l3 = np.zeros((cnt[0], 3), dtype=np.int32)
+        l4 = np.zeros((cnt[1], 4), dtype=np.int32)
+        self._check(self.lib.ck_nl_lists(self.h, cnt, _ip(l3), _ip(l4)))
+        return l3, l4
+
     def set_contraction(self, factored: bool = True):
         """Factored (default) or per-coefficient 3-/4-body contraction kernels."""
         self._check(self.lib.ck_set_contraction(self.h, int(bool(factored))))

@@ -15,17 +15,26 @@
 #include <cstring>
 #include <iostream>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "ck_engine.h"
+#include "ck_nl.h"
 
 namespace {
 
 struct Instance {
     ck::Engine eng;
+    std::unique_ptr<ck::NeighCompute> nl;   // pair-style path, made on first use
     int slot = -1;
     bool small = true;   // serial_chimes_interface(bool small = true)
+    // Repeated single-configuration calls (an MD loop) replay one CUDA graph,
+    // and the launch shape is autotuned once on the third consecutive call
+    // with the same atom count (the tuning is cached by shape).
+    int last_natom = -1, same_shape_calls = 0;
+    bool autotune_repeats = true;
+    Instance() { eng.use_graph = true; }
 };
 
 Instance* g_static = nullptr;               // the instance of set_chimes_serial
@@ -85,6 +94,17 @@ int calculate_one(Instance* in, int natom, const double* xc, const double* yc, c
     std::string err;
     ck::Status st = in->eng.run({s}, force.data(), res, err);
     if (st != ck::kOk) return report(st, err);
+    if (natom == in->last_natom) {
+        in->same_shape_calls++;
+    } else {
+        in->last_natom = natom;
+        in->same_shape_calls = 1;
+    }
+    if (in->autotune_repeats && in->same_shape_calls == 3) {
+        // tunes on the batch just evaluated; a failure leaves the previous tuning
+        std::string terr;
+        in->eng.autotune(nullptr, terr);
+    }
     const ck::SystemResult& r = res[0];
     // serial_chimes_interface::calculate: energy accumulates into the caller's
     // value and the sum is divided by (n_rep+1)^3; forces accumulate; stress
@@ -335,6 +355,44 @@ int ck_autotune(void* h, int* chosen) {
     std::string err;
     ck::Status st = static_cast<Instance*>(h)->eng.autotune(chosen, err);
     if (st != ck::kOk) return report(st, err);
+    return ck::kOk;
+}
+
+int ck_nl_compute(void* h, int nall, const double* x, const int* type, const long long* tag, int inum,
+                  const int* ilist, const int* numneigh, const int* neigh, double skin, int rebuild, double* f,
+                  double* energy, double* virial) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    if (!f) return report(ck::kErrInput, "force array is null");
+    if (!in->nl) in->nl.reset(new ck::NeighCompute(in->eng));
+    std::string err;
+    ck::Status st = in->nl->compute(in->slot, nall, x, type, tag, inum, ilist, numneigh, neigh, skin, rebuild != 0,
+                                    f, energy, virial, err);
+    if (st != ck::kOk) return report(st, err);
+    g_err.clear();
+    return ck::kOk;
+}
+
+int ck_nl_lists(void* h, long long* counts, int* l3, int* l4) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (!in->nl) return report(ck::kErrState, "no neighbour-list evaluation yet");
+    counts[0] = in->nl->n3();
+    counts[1] = in->nl->n4();
+    if (!l3 && !l4) return ck::kOk;
+    std::vector<int> a, b;
+    std::string err;
+    ck::Status st = in->nl->lists(a, b, err);
+    if (st != ck::kOk) return report(st, err);
+    if (l3) std::memcpy(l3, a.data(), sizeof(int) * a.size());
+    if (l4) std::memcpy(l4, b.data(), sizeof(int) * b.size());
+    return ck::kOk;
+}
+
+int ck_autotune_repeats(void* h, int on) {
+    if (int st = check_handle(h)) return st;
+    static_cast<Instance*>(h)->autotune_repeats = on != 0;
     return ck::kOk;
 }
 

@@ -17,6 +17,7 @@ struct chimesFF::Impl {
     ck::Engine eng;
     int slot = -1;
     int badness = 0;
+    Impl() { eng.use_graph = true; }   // repeated calculate() calls replay one CUDA graph
 };
 
 namespace {

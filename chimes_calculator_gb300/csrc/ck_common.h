@@ -201,4 +201,18 @@ struct BatchView {
     long long perm3_cap, perm4_cap;
 };
 
+// A caller's full neighbour list with ghost atoms (LAMMPS layout), for the
+// pair-style path (ck_neigh.cu): local atoms ilist[inum], entries of atom
+// ilist[ii] at neigh[off[ii] .. off[ii+1]), owner[e] = ii.
+struct NeighView {
+    long long inum, nent;
+    const int* ilist;
+    const long long* off;
+    const int* neigh;
+    int* owner;
+    const long long* tag;
+    double c3p, c4p;               // max 3-/4-body outer cutoffs + skin (0 + skin for an absent order)
+    int has3, has4;
+};
+
 }  // namespace ck

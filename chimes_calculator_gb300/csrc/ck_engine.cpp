@@ -416,6 +416,13 @@ Status Engine::launch(std::string& err) {
                           (const void*)V_.bk_start})
         key.push_back((long long)(uintptr_t)p);
     if (key != graph_key_) {
+        // capture only when the same shape launches twice in a row: a batch
+        // seen once (a one-off call, or sizes that change every call) runs
+        // stream-ordered without paying for a capture
+        if (key != seen_key_) {
+            seen_key_ = key;
+            return enqueue(err);
+        }
         drop_graph();
         CK_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         Status st = enqueue(err);
@@ -537,6 +544,7 @@ Status Engine::autotune(int* chosen, std::string& err) {
             return kOk;
         }
     const bool save_profile = profile, save_graph = use_graph;
+    const ForceLaunch save_tuning = tuning;
     profile = true;
     use_graph = false;
     std::vector<SystemResult> res;
@@ -635,7 +643,10 @@ Status Engine::autotune(int* chosen, std::string& err) {
     use_graph = save_graph;
     for (double& v : stage_ms) v = 0.0;
     stage_launches = 0;
-    if (st != kOk) return st;
+    if (st != kOk) {
+        tuning = save_tuning;
+        return st;
+    }
     tune_cache_.push_back({key, tuning});
     report();
     return kOk;

@@ -91,6 +91,7 @@ public:
     int n_param_sets() const { return (int)sets_.size(); }
     const DevParamSet* device_params() const { return dsets_.p; }   // device array, by slot
     const DevParamSet& param_view(int slot) const { return sets_[slot].view; }
+    int n_buckets(int nbody) const { return nbody == 3 ? nbk3_ : nbk4_; }
     const std::vector<TupleRec>& tuples(int slot, int nbody) const {
         return nbody == 3 ? sets_[slot].t3 : sets_[slot].t4;
     }
@@ -200,6 +201,7 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     std::vector<long long> graph_key_;
+    std::vector<long long> seen_key_;   // shape of the last launch (a graph is captured on a repeat)
     cudaEvent_t ev_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     bool ev_recorded_ = false;
 

@@ -66,44 +66,8 @@ __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner
         double dr[3], dist;
         pair_geom(B, d.h, gi, gj, dr, dist);
         if (dist >= pr.rout) continue;
-        double xd, dxdr;
-        bool oor;
-        morse_x(dist, pr.rin, pr.lam, pr.xavg, pr.xdiff, xd, dxdr, oor);
-        const CT* a = coef2<CT>(P) + pr.coef_off;   // dense a_n, n = 0..o2
-        const CT x = CT(xd), tx = CT(2) * x;
-        CT t0c = CT(1), t1c = x, u0 = CT(1), u1 = tx;
-        CT S = a[0] * t0c + a[1] * t1c;
-        CT GD = a[1] * u0;                     // sum a_n n U_{n-1}
-        for (int n = 2; n <= P.o2; n++) {
-            const CT t2 = tx * t1c - t0c;
-            const CT u2 = tx * u1 - u0;
-            S += a[n] * t2;
-            GD += a[n] * CT(n) * u1;
-            t0c = t1c; t1c = t2; u0 = u1; u1 = u2;
-        }
-        double Sd = double(S), Gd = double(GD) * dxdr;
-        if (oor) {
-            atomicAdd(&B.flags[4], 1);
-            const double damp = exp((dist - pr.rin) / P.inner_smooth);
-            Sd += P.inner_smooth * (damp - 1.0) * Gd;
-            Gd *= damp;
-        }
-        CT fcc, fcdc;
-        fcut_eval<CT>(P, dist, pr.rout, fcc, fcdc);
-        const double fc = double(fcc), fcd = double(fcdc);
-        double E = fc * Sd;
-        const double dx_inv = dist > 0.0 ? 1.0 / dist : 1e20;
-        double fs = (fc * Gd + fcd * Sd) * dx_inv;
-        // get_penalty (chimesFF.h:388-419)
-        if (dist - P.pen_dist < pr.rin) {
-            const double rp = pr.rin + P.pen_dist - dist;
-            atomicMax(&B.flags[2], dist < pr.rin ? 2 : 1);
-            if (rp > 0.0) {
-                atomicAdd(&B.flags[3], 1);
-                E += rp * rp * rp * P.pen_scale;
-                fs += (-3.0 * rp * rp * P.pen_scale) / dist;
-            }
-        }
+        double E, fs;
+        pair_2b<CT>(P, pr, dist, B.flags, E, fs);
         add_force(B, gi, fs * dr[0], fs * dr[1], fs * dr[2]);
         add_force(B, gj, -fs * dr[0], -fs * dr[1], -fs * dr[2]);
         virial_add(vir, fs, dr);

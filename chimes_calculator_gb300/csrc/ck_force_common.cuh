@@ -76,6 +76,53 @@ __device__ __forceinline__ void virial_add(double* vir, double f, const double* 
     vir[5] -= f * d[2] * d[2];
 }
 
+// compute_2B (chimesFF.cpp:1644-1775) of one pair below its outer cutoff:
+// energy E (Chebyshev sum with T_{pow+1}, cutoff, penalty) and the force
+// scalar fs (F_i += fs dr, F_j -= fs dr, virial -= fs dr (x) dr).  flags:
+// device diagnostics (badness max, penalty hits, below-rin count).
+template <typename CT>
+__device__ __forceinline__ void pair_2b(const DevParamSet& P, const PairRec& pr, double dist, int* flags, double& E,
+                                        double& fs) {
+    double xd, dxdr;
+    bool oor;
+    morse_x(dist, pr.rin, pr.lam, pr.xavg, pr.xdiff, xd, dxdr, oor);
+    const CT* a = coef2<CT>(P) + pr.coef_off;   // dense a_n, n = 0..o2
+    const CT x = CT(xd), tx = CT(2) * x;
+    CT t0c = CT(1), t1c = x, u0 = CT(1), u1 = tx;
+    CT S = a[0] * t0c + a[1] * t1c;
+    CT GD = a[1] * u0;                     // sum a_n n U_{n-1}
+    for (int n = 2; n <= P.o2; n++) {
+        const CT t2 = tx * t1c - t0c;
+        const CT u2 = tx * u1 - u0;
+        S += a[n] * t2;
+        GD += a[n] * CT(n) * u1;
+        t0c = t1c; t1c = t2; u0 = u1; u1 = u2;
+    }
+    double Sd = double(S), Gd = double(GD) * dxdr;
+    if (oor) {
+        atomicAdd(&flags[4], 1);
+        const double damp = exp((dist - pr.rin) / P.inner_smooth);
+        Sd += P.inner_smooth * (damp - 1.0) * Gd;
+        Gd *= damp;
+    }
+    CT fcc, fcdc;
+    fcut_eval<CT>(P, dist, pr.rout, fcc, fcdc);
+    const double fc = double(fcc), fcd = double(fcdc);
+    E = fc * Sd;
+    const double dx_inv = dist > 0.0 ? 1.0 / dist : 1e20;
+    fs = (fc * Gd + fcd * Sd) * dx_inv;
+    // get_penalty (chimesFF.h:388-419)
+    if (dist - P.pen_dist < pr.rin) {
+        const double rp = pr.rin + P.pen_dist - dist;
+        atomicMax(&flags[2], dist < pr.rin ? 2 : 1);
+        if (rp > 0.0) {
+            atomicAdd(&flags[3], 1);
+            E += rp * rp * rp * P.pen_scale;
+            fs += (-3.0 * rp * rp * P.pen_scale) / dist;
+        }
+    }
+}
+
 // Forces, virial and energy of one 3- or 4-body cluster from its contraction
 // sums (compute_3B/4B, chimesFF.cpp:2068-2169 and the 4-body counterpart):
 //   f_p = (prod_{q!=p} fc_q / r_p) (fc_p G_p + fc'_p S),  E = prod fc * S.

@@ -61,6 +61,12 @@ void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // dynamic shared memory of one factored-kernel block (one warp)
 size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 
+// Pair-style path on a caller's neighbour list (ck_neigh.cu): list-entry
+// owners and the identity atom/slot mapping; cluster counting / filling; 1B+2B.
+void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st);
+void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st);
+void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st);
+
 // Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
 void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
                    double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st);

@@ -1,0 +1,199 @@
+// LAMMPS pair-style path: ChIMES on a caller's full neighbour list with ghost
+// atoms, as pair_style chimesFF computes it (etc/lmp/src/pair_chimes.cpp).
+//
+//   * 1-body for every atom of ilist, 2-body for every listed (i, j) with
+//     tag[j] > tag[i] (compute, :572-655);
+//   * 3-/4-body clusters built from the list of i only (build_mb_neighlists,
+//     :321-478): j, k, l with tags not below the earlier members', every
+//     distance below the padded cutoff max_cutoff_nB + skin; the clusters are
+//     rebuilt only when the caller says so (LAMMPS: neighbor->ago == 0) and
+//     evaluated every call with the current positions by the batch force
+//     kernels, which apply the per-tuple cutoffs of compute_3B/4B.
+//
+// The batch kernels see the atoms through an identity mapping: atom index =
+// ghost slot = force slot, positions as "fractional" coordinates of a unit
+// cell, so their pair geometry is x_b - x_a (PairCHIMES::get_dist, :303-312).
+// Distances that decide list membership are taken in FP64 with separate
+// roundings (no fused multiply-add), as the reference computes them.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ck_common.h"
+#include "ck_force_common.cuh"
+#include "ck_kernels.h"
+#include "ck_math.cuh"
+
+namespace ck {
+
+namespace {
+
+__device__ __forceinline__ double nl_dist(const double* x, int i, int j, double* dr) {
+    const double d0 = __dsub_rn(x[3 * (long long)j + 0], x[3 * (long long)i + 0]);
+    const double d1 = __dsub_rn(x[3 * (long long)j + 1], x[3 * (long long)i + 1]);
+    const double d2 = __dsub_rn(x[3 * (long long)j + 2], x[3 * (long long)i + 2]);
+    if (dr) { dr[0] = d0; dr[1] = d1; dr[2] = d2; }
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+}
+
+// list entry -> position of its atom in ilist
+__global__ void k_nl_owner(NeighView N) {
+    const long long ii = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ii >= N.inum) return;
+    for (long long e = N.off[ii]; e < N.off[ii + 1]; e++) N.owner[e] = (int)ii;
+}
+
+// identity atom <-> slot mapping of the batch kernels
+__global__ void k_nl_identity(BatchView B) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= B.n_atoms_total) return;
+    B.atom_sys[q] = 0;
+    B.atom_orig[q] = (int)q;
+    B.ghost_parent[q] = (int)q;
+}
+
+// 1-body over ilist and 2-body over the list entries (compute, :572-655)
+template <typename CT>
+__global__ void __launch_bounds__(256) k_nl_pairs(BatchView B, NeighView N) {
+    const DevParamSet& P = B.psets[B.sys[0].pset];
+    const double* x = B.ghost_fs;
+    EVAcc acc;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long ntot = N.nent > N.inum ? N.nent : N.inum;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ntot; e += stride) {
+        double vir[6] = {0, 0, 0, 0, 0, 0};
+        if (e < N.inum) acc.add(B, 0, P.eoff[B.atom_type[N.ilist[e]]], vir);
+        if (e >= N.nent) continue;
+        const int i = N.ilist[N.owner[e]];
+        const int j = N.neigh[e];
+        if (N.tag[j] <= N.tag[i]) continue;
+        double dr[3];
+        const double dist = nl_dist(x, i, j, dr);
+        const PairRec pr = P.pairs[P.pair_map[B.atom_type[i] * P.ntypes + B.atom_type[j]]];
+        if (dist >= pr.rout) continue;
+        double E, fs;
+        pair_2b<CT>(P, pr, dist, B.flags, E, fs);
+        add_force(B, i, fs * dr[0], fs * dr[1], fs * dr[2]);
+        add_force(B, j, -fs * dr[0], -fs * dr[1], -fs * dr[2]);
+        virial_add(vir, fs, dr);
+        acc.add(B, 0, E, vir);
+    }
+    acc.flush_warp(B);
+}
+
+// Cluster lists (build_mb_neighlists, :321-478): one warp per list entry
+// (i, j); lanes take consecutive k of i's list, a ballot and prefix count
+// emit triplets in list order; for each k that can start a quadruplet, lanes
+// take consecutive l.  Count pass (FILL = false) and fill pass.
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const double* x = B.ghost_fs;
+    const double c3p = N.c3p, c4p = N.c4p;
+    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < N.nent; e += nwarps) {
+        long long n3 = 0, n4 = 0, o3 = 0, o4 = 0;
+        if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
+        const int ii = N.owner[e];
+        const int i = N.ilist[ii];
+        const int j = N.neigh[e];
+        const long long ti = N.tag[i], tj = N.tag[j];
+        bool go = j != i && tj >= ti;
+        double dij = 0.0;
+        if (go) {
+            dij = nl_dist(x, i, j, nullptr);
+            go = !(dij >= c3p && dij >= c4p);
+        }
+        if (go) {
+            const long long b0 = N.off[ii], b1 = N.off[ii + 1];
+            for (long long kb = b0; kb < b1; kb += 32) {
+                const long long kk = kb + lane;
+                bool ok3 = false, ok4 = false;
+                int k = -1;
+                long long tk = 0;
+                if (kk < b1) {
+                    k = N.neigh[kk];
+                    tk = N.tag[k];
+                    if (k != i && k != j && tk >= ti && tk >= tj) {
+                        const double dik = nl_dist(x, i, k, nullptr);
+                        if (!(dik >= c3p && dik >= c4p)) {
+                            const double djk = nl_dist(x, j, k, nullptr);
+                            ok3 = N.has3 && dij < c3p && dik < c3p && djk < c3p;
+                            ok4 = N.has4 && dij < c4p && dik < c4p && djk < c4p;
+                        }
+                    }
+                }
+                const unsigned m3 = __ballot_sync(kFull, ok3);
+                if (FILL && ok3) {
+                    const long long q = o3 + n3 + __popc(m3 & lt);
+                    if (q < B.n3_cap) {
+                        int* out = B.c3 + 3 * q;
+                        out[0] = i; out[1] = j; out[2] = k;
+                    }
+                }
+                n3 += __popc(m3);
+                unsigned m4 = __ballot_sync(kFull, ok4);
+                while (m4) {
+                    const int src = __ffs(m4) - 1;
+                    m4 &= m4 - 1;
+                    const int ks = __shfl_sync(kFull, k, src);
+                    const long long tks = __shfl_sync(kFull, tk, src);
+                    for (long long lb = b0; lb < b1; lb += 32) {
+                        const long long ll = lb + lane;
+                        bool okl = false;
+                        int l = -1;
+                        if (ll < b1) {
+                            l = N.neigh[ll];
+                            const long long tl = N.tag[l];
+                            if (l != i && l != j && l != ks && tl >= ti && tl >= tj && tl >= tks)
+                                okl = nl_dist(x, i, l, nullptr) < c4p && nl_dist(x, j, l, nullptr) < c4p &&
+                                      nl_dist(x, ks, l, nullptr) < c4p;
+                        }
+                        const unsigned ml = __ballot_sync(kFull, okl);
+                        if (FILL && okl) {
+                            const long long q = o4 + n4 + __popc(ml & lt);
+                            if (q < B.n4_cap) {
+                                int* out = B.c4 + 4 * q;
+                                out[0] = i; out[1] = j; out[2] = ks; out[3] = l;
+                            }
+                        }
+                        n4 += __popc(ml);
+                    }
+                }
+            }
+        }
+        if (!FILL && lane == 0) { B.e_cnt3[e] = (int)n3; B.e_cnt4[e] = (int)n4; }
+    }
+}
+
+unsigned grid_of(long long n, int block, long long cap_blocks) {
+    long long need = (n + block - 1) / block;
+    if (need < 1) need = 1;
+    return (unsigned)(need < cap_blocks ? need : cap_blocks);
+}
+
+}  // namespace
+
+void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st) {
+    if (N.inum > 0) count_launch(), k_nl_owner<<<grid_of(N.inum, 128, 1LL << 30), 128, 0, st>>>(N);
+    if (B.n_atoms_total > 0)
+        count_launch(), k_nl_identity<<<grid_of(B.n_atoms_total, 256, 1LL << 30), 256, 0, st>>>(B);
+}
+
+void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st) {
+    if (N.nent <= 0) return;
+    const unsigned grid = grid_of(N.nent * 32, 256, (long long)sm_count() * 8);
+    if (fill) count_launch(), k_nl_enum<true><<<grid, 256, 0, st>>>(B, N);
+    else count_launch(), k_nl_enum<false><<<grid, 256, 0, st>>>(B, N);
+}
+
+void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st) {
+    const long long ntot = N.nent > N.inum ? N.nent : N.inum;
+    if (ntot <= 0) return;
+    const unsigned grid = grid_of(ntot, 256, (long long)sm_count() * 8);
+    if (precision == kMixed) count_launch(), k_nl_pairs<float><<<grid, 256, 0, st>>>(B, N);
+    else count_launch(), k_nl_pairs<double><<<grid, 256, 0, st>>>(B, N);
+}
+
+}  // namespace ck

@@ -453,3 +453,66 @@ def specs_c5() -> List[ParamSpec]:
     return [spec_c2(elements=("C",), orders=(12, 8, 4), seed=1051),
             spec_c2(elements=("C", "N"), orders=(12, 10, 4), seed=1052),
             spec_c2(elements=("C", "N", "O"), orders=(12, 8, 4), seed=1053)]
+
+
+# ----------------------------------------------------------------------------
+# LAMMPS-style inputs: local atoms, ghost images and full neighbour lists
+# ----------------------------------------------------------------------------
+@dataclasses.dataclass
+class NeighborData:
+    """What a LAMMPS pair style sees on one rank: nall = local + ghost atoms
+    (positions x, ChIMES type indices, global tags; ghosts carry their owner's
+    tag), and full neighbour lists of the local atoms (ilist order), with
+    neighbours concatenated in `neigh`."""
+    x: np.ndarray            # (nall, 3)
+    type: np.ndarray         # (nall,) int32
+    tag: np.ndarray          # (nall,) int64
+    nlocal: int
+    ilist: np.ndarray        # (inum,) int32
+    numneigh: np.ndarray     # (inum,) int32
+    neigh: np.ndarray        # (sum numneigh,) int32
+    owner: np.ndarray        # (nall,) local atom each atom images
+
+
+def lammps_neighbors(cfg: Config, type_idx: np.ndarray, cutoff: float, seed: Optional[int] = None) -> NeighborData:
+    """Ghost atoms: every periodic image of a local atom within `cutoff` of the
+    cell (fractional margin cutoff / perpendicular height on each axis), as
+    LAMMPS's communication builds them; neighbour lists: every other atom
+    (local or ghost) within `cutoff` of each local atom.  `seed` shuffles each
+    list (LAMMPS lists come in bin order, not sorted)."""
+    cell = np.asarray(cfg.cell, dtype=np.float64)
+    inv = np.linalg.inv(cell)
+    frac = cfg.pos @ inv
+    frac -= np.floor(frac)
+    n = cfg.n_atoms
+    vol = abs(np.linalg.det(cell))
+    heights = [vol / np.linalg.norm(np.cross(cell[(k + 1) % 3], cell[(k + 2) % 3])) for k in range(3)]
+    margin = np.array([cutoff / h for h in heights])
+    reach = [int(math.ceil(m)) for m in margin]
+    xs, owners = [frac @ cell], [np.arange(n)]
+    for sa in range(-reach[0], reach[0] + 1):
+        for sb in range(-reach[1], reach[1] + 1):
+            for sc in range(-reach[2], reach[2] + 1):
+                if sa == 0 and sb == 0 and sc == 0:
+                    continue
+                fs = frac + np.array([sa, sb, sc], dtype=np.float64)
+                keep = np.all((fs >= -margin) & (fs < 1.0 + margin), axis=1)
+                if keep.any():
+                    xs.append(fs[keep] @ cell)
+                    owners.append(np.nonzero(keep)[0])
+    x = np.concatenate(xs)
+    owner = np.concatenate(owners)
+    rng = np.random.default_rng(seed) if seed is not None else None
+    numneigh, neigh = [], []
+    for i in range(n):
+        d = np.linalg.norm(x - x[i], axis=1)
+        nb = np.nonzero(d < cutoff)[0]
+        nb = nb[nb != i]
+        if rng is not None:
+            nb = rng.permutation(nb)
+        numneigh.append(len(nb))
+        neigh.append(nb)
+    return NeighborData(x=np.ascontiguousarray(x), type=np.ascontiguousarray(np.asarray(type_idx)[owner], dtype=np.int32),
+                        tag=(owner + 1).astype(np.int64), nlocal=n, ilist=np.arange(n, dtype=np.int32),
+                        numneigh=np.array(numneigh, dtype=np.int32),
+                        neigh=np.ascontiguousarray(np.concatenate(neigh).astype(np.int32)), owner=owner)

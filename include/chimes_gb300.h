@@ -88,8 +88,13 @@ int ck_set_contraction(void *h, int factored);
  * batch's shape (precision, parameter orders, atom and configuration counts
  * rounded to powers of two).  chosen[3] = tpc3, tpc4, blocks_per_sm. */
 int ck_autotune(void *h, int *chosen);
-/* replay the whole list-build + force sequence as one CUDA graph (1) or launch it stream-ordered (0) */
+/* replay the whole list-build + force sequence as one CUDA graph (1) or launch
+ * it stream-ordered (0).  Instances of the serial interface start with 1. */
 int ck_use_graph(void *h, int on);
+/* Serial-interface instances (calculate_chimes*) autotune once on the third
+ * consecutive call with the same atom count (on = 1, the default); 0 keeps the
+ * default launch shape. */
+int ck_autotune_repeats(void *h, int on);
 
 /* Evaluates nsys configurations in one set of launches.  small[s] (or NULL for
  * all 0) allows replication of small cells, pset[s] (or NULL for the current
@@ -178,6 +183,29 @@ int ck_server_take(void *server, long long id, int wait, double timeout_s, doubl
                    double *stress, double *latency_s);
 /* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
 int ck_server_stats(void *server, long long *out);
+
+/* Pair-style evaluation on a caller's full neighbour list with ghost atoms:
+ * the GPU form of LAMMPS pair_style chimesFF (etc/lmp/src/pair_chimes.cpp:
+ * build_mb_neighlists :321-478, compute :480-884), newton on.  Arrays are the
+ * caller's host arrays: x[nall][3] (local then ghost atoms), type[nall] (type
+ * indices of the handle's current parameter set, i.e. chimes_type[type-1]),
+ * tag[nall] (global atom ids; a ghost carries its owner's id); ilist[inum]
+ * (atoms with lists), numneigh[inum] and neigh[] (each list's neighbour
+ * indices with the NEIGHMASK bits stripped, concatenated in ilist order).
+ * 1-body for ilist atoms and 2-body for listed pairs with tag[j] > tag[i] use
+ * this call's list; 3-/4-body clusters are built from it when rebuild != 0
+ * (LAMMPS: neighbor->ago == 0; also on the first call and whenever nall, inum
+ * or the entry count change) with the cutoffs max_cutoff_3B/4B + skin, and
+ * evaluated every call with the current positions.  Accumulates f[nall][3]
+ * (forces on ghosts included, for the reverse communication), *energy and
+ * virial[6] (xx yy zz xy xz yz, as Pair::ev_tally_mb).  Per-atom energy and
+ * virial are not produced. */
+int ck_nl_compute(void *h, int nall, const double *x, const int *type, const long long *tag, int inum,
+                  const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
+                  double *energy, double *virial);
+/* counts[2] = triplets, quadruplets of the last cluster build; l3[n3][3] and
+ * l4[n4][4] (atom indices, may be NULL) */
+int ck_nl_lists(void *h, long long *counts, int *l3, int *l4);
 
 /* Batched per-cluster evaluation (chimesFF::compute_nB semantics, FP64) with
  * the handle's current parameter set: n clusters of nbody = 2, 3 or 4 atoms,

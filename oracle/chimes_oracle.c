@@ -70,6 +70,10 @@ typedef struct {
     /* last calculate() cluster lists (neigh/sys ghost indices) */
     long n2, n3, n4;
     int *l2, *l3, *l4;
+    /* cluster lists of the LAMMPS pair-style restatement (atom indices) */
+    int *lmp_l3, *lmp_l4;
+    long lmp_n3, lmp_n4, lmp_c3, lmp_c4;
+    int lmp_built;
     long cap2, cap3, cap4;
 } ora_handle;
 
@@ -896,6 +900,7 @@ void *ora_load(const char *path, char *err, int errlen) {
 void ora_free(void *vh) {
     ora_handle *h = vh; if (!h) return;
     free(h->l2); free(h->l3); free(h->l4);
+    free(h->lmp_l3); free(h->lmp_l4);
     free(h);  /* parameter tables are left to process exit: test-only object */
 }
 
@@ -992,4 +997,150 @@ void ora_get_lists(void *vh, int *l2, int *l3, int *l4) {
     if (l2) memcpy(l2, h->l2, h->n2 * 2 * sizeof(int));
     if (l3) memcpy(l3, h->l3, h->n3 * 3 * sizeof(int));
     if (l4) memcpy(l4, h->l4, h->n4 * 4 * sizeof(int));
+}
+
+/* ------------------------------------------------------------------------
+ * LAMMPS pair style (etc/lmp/src/pair_chimes.cpp): build_mb_neighlists
+ * (:321-478) and compute (:480-884) over a full neighbour list with ghost
+ * atoms, newton on (forces on ghosts are kept for the reverse communication).
+ * x[nall*3], typ[nall] (ChIMES type index), tag[nall]; ilist[inum];
+ * numneigh[inum] and the concatenated lists neigh[] in ilist order.
+ * Accumulates f[nall*3], *energy and virial[6] (LAMMPS order xx yy zz xy xz
+ * yz, the stensor mapping of Pair::ev_tally_mb, etc/lmp/etc/pair.cpp).
+ * rebuild = 0 reuses the previous cluster lists (the reference rebuilds them
+ * only when neighbor->ago == 0).
+ * ---------------------------------------------------------------------- */
+static double lmp_dist(const double *x, int i, int j, double *dr) {   /* PairCHIMES::get_dist, :303-312 */
+    double d[3];
+    d[0] = x[3 * j + 0] - x[3 * i + 0];
+    d[1] = x[3 * j + 1] - x[3 * i + 1];
+    d[2] = x[3 * j + 2] - x[3 * i + 2];
+    if (dr) { dr[0] = d[0]; dr[1] = d[1]; dr[2] = d[2]; }
+    return sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
+static int push_cluster(int **buf, long *n, long *cap, const int *v, int k) {
+    if (*n >= *cap) {
+        long nc = *cap ? 2 * *cap : 1024;
+        int *nb = realloc(*buf, (size_t)nc * k * sizeof(int));
+        if (!nb) return -1;
+        *buf = nb; *cap = nc;
+    }
+    memcpy(*buf + (*n) * k, v, k * sizeof(int));
+    (*n)++;
+    return 0;
+}
+
+int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, const long long *tag, int inum,
+                       const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
+                       double *energy, double *virial) {
+    ora_handle *h = vh;
+    ora_ff *ff = &h->ff;
+    (void)nall;
+    long *off = malloc((size_t)(inum + 1) * sizeof(long));
+    if (!off) FAIL(h, "out of memory");
+    off[0] = 0;
+    for (int ii = 0; ii < inum; ii++) off[ii + 1] = off[ii] + numneigh[ii];
+    double c3 = 0.0, c4 = 0.0;   /* chimesFF::max_cutoff_3B/4B: 0 when the order is 0 */
+    if (ff->o3 > 0) c3 = max_cutn(ff, 3);
+    if (ff->o4 > 0) c4 = max_cutn(ff, 4);
+    const double c3p = c3 + skin, c4p = c4 + skin;   /* maxcut_nb + neighbor->skin */
+    if (rebuild || !h->lmp_built) {
+        h->lmp_n3 = h->lmp_n4 = 0;
+        h->lmp_built = 1;
+        if (ff->o3 > 0 || ff->o4 > 0)
+            for (int ii = 0; ii < inum; ii++) {
+                const int i = ilist[ii];
+                for (long jj = off[ii]; jj < off[ii + 1]; jj++) {
+                    const int j = neigh[jj];
+                    if (j == i || tag[j] < tag[i]) continue;
+                    const double dij = lmp_dist(x, i, j, NULL);
+                    if (dij >= c3p && dij >= c4p) continue;
+                    for (long kk = off[ii]; kk < off[ii + 1]; kk++) {
+                        const int k = neigh[kk];
+                        if (k == i || k == j) continue;
+                        if (tag[k] < tag[i] || tag[k] < tag[j]) continue;
+                        const double dik = lmp_dist(x, i, k, NULL);
+                        if (dik >= c3p && dik >= c4p) continue;
+                        const double djk = lmp_dist(x, j, k, NULL);
+                        if (ff->o3 > 0 && dij < c3p && dik < c3p && djk < c3p) {
+                            const int v[3] = {i, j, k};
+                            if (push_cluster(&h->lmp_l3, &h->lmp_n3, &h->lmp_c3, v, 3)) { free(off); FAIL(h, "out of memory"); }
+                        }
+                        if (dij >= c4p || dik >= c4p || djk >= c4p) continue;
+                        if (ff->o4 == 0) continue;
+                        for (long ll = off[ii]; ll < off[ii + 1]; ll++) {
+                            const int l = neigh[ll];
+                            if (l == i || l == j || l == k) continue;
+                            if (tag[l] < tag[i] || tag[l] < tag[j] || tag[l] < tag[k]) continue;
+                            if (lmp_dist(x, i, l, NULL) >= c4p) continue;
+                            if (lmp_dist(x, j, l, NULL) >= c4p) continue;
+                            if (lmp_dist(x, k, l, NULL) >= c4p) continue;
+                            const int v[4] = {i, j, k, l};
+                            if (push_cluster(&h->lmp_l4, &h->lmp_n4, &h->lmp_c4, v, 4)) { free(off); FAIL(h, "out of memory"); }
+                        }
+                    }
+                }
+            }
+    }
+    double st[6], f2[6], f3[9], f4[12], dr[18], dx[6];
+    /* 1- and 2-body over the current neighbour list (:572-655) */
+    for (int ii = 0; ii < inum; ii++) {
+        const int i = ilist[ii];
+        double e = 0.0;
+        ora_compute_1b(h, typ[i], &e);
+        *energy += e;
+        for (long jj = off[ii]; jj < off[ii + 1]; jj++) {
+            const int j = neigh[jj];
+            if (tag[j] <= tag[i]) continue;
+            const double d = lmp_dist(x, i, j, dr);
+            memset(f2, 0, sizeof(f2)); memset(st, 0, sizeof(st));
+            e = 0.0;
+            ora_compute_2b(h, d, dr, typ[i], typ[j], f2, st, &e);
+            for (int c = 0; c < 3; c++) { f[3 * i + c] += f2[c]; f[3 * j + c] += f2[3 + c]; }
+            *energy += e;
+            virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
+            virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
+        }
+    }
+    static const int A[6] = {0, 0, 0, 1, 1, 2}, B[6] = {1, 2, 3, 2, 3, 3};
+    if (ff->o3 > 0)   /* :660-735 */
+        for (long q = 0; q < h->lmp_n3; q++) {
+            const int *id = &h->lmp_l3[3 * q];
+            static const int A3[3] = {0, 0, 1}, B3[3] = {1, 2, 2};   /* ij, ik, jk */
+            for (int p = 0; p < 3; p++) dx[p] = lmp_dist(x, id[A3[p]], id[B3[p]], &dr[3 * p]);
+            const int t[3] = {typ[id[0]], typ[id[1]], typ[id[2]]};
+            memset(f3, 0, sizeof(f3)); memset(st, 0, sizeof(st));
+            double e = 0.0;
+            ora_compute_3b(h, dx, dr, t, f3, st, &e);
+            for (int a = 0; a < 3; a++)
+                for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f3[3 * a + c];
+            *energy += e;
+            virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
+            virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
+        }
+    if (ff->o4 > 0)   /* :740-820 */
+        for (long q = 0; q < h->lmp_n4; q++) {
+            const int *id = &h->lmp_l4[4 * q];
+            for (int p = 0; p < 6; p++) dx[p] = lmp_dist(x, id[A[p]], id[B[p]], &dr[3 * p]);
+            const int t[4] = {typ[id[0]], typ[id[1]], typ[id[2]], typ[id[3]]};
+            memset(f4, 0, sizeof(f4)); memset(st, 0, sizeof(st));
+            double e = 0.0;
+            ora_compute_4b(h, dx, dr, t, f4, st, &e);
+            for (int a = 0; a < 4; a++)
+                for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f4[3 * a + c];
+            *energy += e;
+            virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
+            virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
+        }
+    free(off);
+    return 0;
+}
+
+void ora_lammps_sizes(void *vh, long *n3, long *n4) { ora_handle *h = vh; *n3 = h->lmp_n3; *n4 = h->lmp_n4; }
+
+void ora_lammps_lists(void *vh, int *l3, int *l4) {
+    ora_handle *h = vh;
+    if (l3 && h->lmp_n3) memcpy(l3, h->lmp_l3, h->lmp_n3 * 3 * sizeof(int));
+    if (l4 && h->lmp_n4) memcpy(l4, h->lmp_l4, h->lmp_n4 * 4 * sizeof(int));
 }

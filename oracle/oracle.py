@@ -70,6 +70,11 @@ def _load():
         lib.ora_compute_2b.argtypes = [P, D, dp, I, I, dp, dp, dp]
         lib.ora_compute_3b.argtypes = [P, dp, dp, ip, dp, dp, dp]
         lib.ora_compute_4b.argtypes = [P, dp, dp, ip, dp, dp, dp]
+        llp = ctypes.POINTER(ctypes.c_longlong)
+        lib.ora_lammps_compute.restype = I
+        lib.ora_lammps_compute.argtypes = [P, I, dp, ip, llp, I, ip, ip, ip, D, I, dp, dp, dp]
+        lib.ora_lammps_sizes.argtypes = [P, lp, lp]
+        lib.ora_lammps_lists.argtypes = [P, ip, ip]
         _lib = lib
     return _lib
 
@@ -128,6 +133,34 @@ class Oracle:
             raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
         return {"energy": e.value, "force": np.stack([fx, fy, fz], axis=1), "stress": st,
                 "badness": self.lib.ora_badness(self.h)}
+
+    def lammps_compute(self, nl, skin: float, rebuild: bool = True):
+        """pair_style chimesFF (etc/lmp/src/pair_chimes.cpp) on a LAMMPS-style
+        neighbour list `nl` (synth.NeighborData): forces on local and ghost
+        atoms, energy and virial (xx yy zz xy xz yz), all from zero."""
+        x = np.ascontiguousarray(nl.x, dtype=np.float64)
+        nall = x.shape[0]
+        f = np.zeros((nall, 3))
+        e = ctypes.c_double(0.0)
+        vir = np.zeros(6)
+        tag = np.ascontiguousarray(nl.tag, dtype=np.int64)
+        rc = self.lib.ora_lammps_compute(
+            self.h, nall, _dp(x), _ip(np.ascontiguousarray(nl.type, dtype=np.int32)),
+            tag.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), len(nl.ilist),
+            _ip(np.ascontiguousarray(nl.ilist, dtype=np.int32)), _ip(np.ascontiguousarray(nl.numneigh, dtype=np.int32)),
+            _ip(np.ascontiguousarray(nl.neigh, dtype=np.int32)), float(skin), int(bool(rebuild)), _dp(f),
+            ctypes.byref(e), _dp(vir))
+        if rc != 0:
+            raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
+        return {"energy": e.value, "force": f, "virial": vir}
+
+    def lammps_lists(self):
+        n3, n4 = ctypes.c_long(), ctypes.c_long()
+        self.lib.ora_lammps_sizes(self.h, ctypes.byref(n3), ctypes.byref(n4))
+        l3 = np.zeros((n3.value, 3), dtype=np.int32)
+        l4 = np.zeros((n4.value, 4), dtype=np.int32)
+        self.lib.ora_lammps_lists(self.h, _ip(l3), _ip(l4))
+        return l3, l4
 
     def lists(self):
         n2, n3, n4 = ctypes.c_long(), ctypes.c_long(), ctypes.c_long()

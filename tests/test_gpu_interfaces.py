@@ -31,6 +31,33 @@ def test_serial_wrapper_accumulates(golden, native_lib):
     assert np.abs(np.array(st[:]) - g.stress).max() <= S_ABS_TOL   # stress is overwritten
 
 
+def test_repeated_calls_replay_and_autotune(golden, native_lib):
+    """An MD-style loop through the serial C ABI: graph replay from the second
+    call and an autotune on the third; every call returns the reference result."""
+    lib = native_lib
+    lib.ck_set_error_mode(1)
+    g = golden["c2_small"]
+    h = lib.chimes_open_instance()
+    try:
+        lib.set_chimes_serial_instance(h, 0)
+        lib.init_chimes_serial_instance(h, g.params.encode(), 0)
+        n = g.cfg.n_atoms
+        arr = lambda v: (ctypes.c_double * len(v))(*v)
+        x, y, z = (arr(g.cfg.pos[:, k]) for k in range(3))
+        ty = (ctypes.c_char_p * n)(*[t.encode() for t in g.cfg.types])
+        ca, cb, cc = (arr(g.cfg.cell[k]) for k in range(3))
+        for call in range(5):
+            fx, fy, fz, st = arr([0.0] * n), arr([0.0] * n), arr([0.0] * n), arr([0.0] * 9)
+            e = ctypes.c_double(0.0)
+            lib.calculate_chimes_instance(h, n, x, y, z, ty, ca, cb, cc, ctypes.byref(e), fx, fy, fz, st)
+            assert lib.ck_last_error() == b"", lib.ck_last_error()
+            assert abs(e.value - g.energy) <= E_REL_TOL * abs(g.energy), call
+            F = np.stack([np.array(fx[:]), np.array(fy[:]), np.array(fz[:])], axis=1)
+            assert np.abs(F - g.force).max() <= F_ABS_TOL, call
+    finally:
+        lib.chimes_close_instance(h)
+
+
 def test_instances_and_replication(golden, native_lib):
     lib = native_lib
     lib.ck_set_error_mode(1)
