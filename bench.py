@@ -214,8 +214,14 @@ def run_ours(args):
     calc = Calculator(precision=args.precision, graph=True)
     calc.load_params(params)
     packed = calc.pack([(cfg.pos, cfg.types, cfg.cell)])
-    calc.stage(packed)
-    tuning = calc.autotune()
+    if args.contraction == "auto":
+        calc.stage(packed)
+        calc.autotune()
+    else:   # a fixed launch shape (profiler runs): no autotuning
+        calc.set_contraction(args.contraction == "factored")
+        if args.tuning:
+            calc.set_tuning(*[int(v) for v in args.tuning.split(",")])
+        calc.stage(packed)
     stream = torch.cuda.ExternalStream(calc.stream_ptr(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -465,8 +471,10 @@ def profile_batched(args):
     c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
     if args.contraction == "auto":
         c.autotune()
-    else:   # one contraction form at the default launch shape, no autotuning
+    else:   # one contraction form at a fixed launch shape, no autotuning
         c.set_contraction(args.contraction == "factored")
+        if args.tuning:
+            c.set_tuning(*[int(v) for v in args.tuning.split(",")])
         c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
     r = time_steps(c, atoms, 2)
     r["autotuned"] = c.tuning()
@@ -621,7 +629,9 @@ def main():
                     help="profiler run of the batched workload (--batch-configs configurations, "
                          "--precision): autotune, 3 warm-up + 2 launches")
     ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "percoef"],
-                    help="--profile-batched: autotune (auto) or force one 3-/4-body contraction form")
+                    help="autotune (auto) or one fixed 3-/4-body contraction form (profiler runs)")
+    ap.add_argument("--tuning", default="",
+                    help="with a fixed --contraction: tpc3,tpc4,blocks_per_sm (ck_set_tuning)")
     args = ap.parse_args()
     if args.profile_batched:
         profile_batched(args)

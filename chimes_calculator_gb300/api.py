@@ -130,23 +130,29 @@ class Calculator:
     def set_tuning(self, tpc3: int = 4, tpc4: int = 8, blocks_per_sm: int = 4):
         self._check(self.lib.ck_set_tuning(self.h, tpc3, tpc4, blocks_per_sm))
 
-    def nl_compute(self, nl, skin: float, rebuild: bool = True):
+    def nl_compute(self, nl, skin: float, rebuild: bool = True, per_atom: bool = False):
         """LAMMPS pair-style evaluation on a neighbour list `nl` (fields x, type,
         tag, ilist, numneigh, neigh as synth.NeighborData): forces on local and
-        ghost atoms, energy and virial (xx yy zz xy xz yz), all from zero."""
+        ghost atoms, energy and virial (xx yy zz xy xz yz), all from zero, and
+        with per_atom the per-atom energy and virial."""
         x = np.ascontiguousarray(nl.x, dtype=np.float64)
         nall = x.shape[0]
         f = np.zeros((nall, 3))
         e = ctypes.c_double(0.0)
         vir = np.zeros(6)
+        eatom = np.zeros(nall) if per_atom else None
+        vatom = np.zeros((nall, 6)) if per_atom else None
         tag = np.ascontiguousarray(nl.tag, dtype=np.int64)
         self._check(self.lib.ck_nl_compute(
             self.h, nall, _dp(x), _ip(np.ascontiguousarray(nl.type, dtype=np.int32)),
             tag.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), len(nl.ilist),
             _ip(np.ascontiguousarray(nl.ilist, dtype=np.int32)), _ip(np.ascontiguousarray(nl.numneigh, dtype=np.int32)),
             _ip(np.ascontiguousarray(nl.neigh, dtype=np.int32)), float(skin), int(bool(rebuild)), _dp(f),
-            ctypes.byref(e), _dp(vir)))
-        return {"energy": e.value, "force": f, "virial": vir}
+            ctypes.byref(e), _dp(vir), _dp(eatom) if per_atom else None, _dp(vatom) if per_atom else None))
+        out = {"energy": e.value, "force": f, "virial": vir}
+        if per_atom:
+            out["eatom"], out["vatom"] = eatom, vatom
+        return out
 
     def nl_lists(self):
         cnt = (ctypes.c_longlong * 2)()

@@ -360,7 +360,7 @@ int ck_autotune(void* h, int* chosen) {
 
 int ck_nl_compute(void* h, int nall, const double* x, const int* type, const long long* tag, int inum,
                   const int* ilist, const int* numneigh, const int* neigh, double skin, int rebuild, double* f,
-                  double* energy, double* virial) {
+                  double* energy, double* virial, double* eatom, double* vatom) {
     if (int st = check_handle(h)) return st;
     Instance* in = static_cast<Instance*>(h);
     if (int st = ensure_params(in)) return st;
@@ -368,7 +368,7 @@ int ck_nl_compute(void* h, int nall, const double* x, const int* type, const lon
     if (!in->nl) in->nl.reset(new ck::NeighCompute(in->eng));
     std::string err;
     ck::Status st = in->nl->compute(in->slot, nall, x, type, tag, inum, ilist, numneigh, neigh, skin, rebuild != 0,
-                                    f, energy, virial, err);
+                                    f, energy, virial, eatom, vatom, err);
     if (st != ck::kOk) return report(st, err);
     g_err.clear();
     return ck::kOk;

@@ -186,6 +186,8 @@ struct BatchView {
     int enum_serial;               // 1: some system has 3B and 4B terms with rc4 > rc3 (sequential enumeration)
     // results
     double* force;                 // [n_in_total][3]
+    double* eatom;                 // [n_in_total] per-atom energy or null (pair-style path)
+    double* vatom;                 // [n_in_total][6] per-atom virial (xx yy zz xy xz yz) or null
     double* ev;                    // [n_sys][8]: energy, virial xx xy xz yy yz zz, spare
     int* flags;                    // [8] device error flags: 0 capacity, 1 geometry, 2 badness max,
                                    //     3 penalty count, 4 below-rin count, 5 timeout

@@ -43,6 +43,9 @@ Engine::~Engine() {
         if (e) cudaEventDestroy(e);
     for (auto& s : sets_)
         if (s.dev) cudaFree(s.dev);
+    if (fork_) cudaEventDestroy(fork_);
+    if (join_) cudaEventDestroy(join_);
+    if (stream2_) cudaStreamDestroy(stream2_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -63,6 +66,9 @@ Status Engine::init_device(std::string& err) {
         return kErrCuda;
     }
     CK_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    CK_TRY(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
+    CK_TRY(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    CK_TRY(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     CK_TRY(h_flags_.reserve(8));
     CK_TRY(h_counts_.reserve(4));
     CK_TRY(d_flags_.reserve(8));
@@ -348,28 +354,45 @@ Status Engine::enqueue(std::string& err) {
     if (profile) CK_TRY(record_stage_event(ev_[1], st));
     ForceLaunch L = tuning;
     L.precision = precision;
-    launch_force2(B, d_l2_owner_.p, L, st);
-    if (profile) CK_TRY(record_stage_event(ev_[2], st));
     if ((L.stride3 > 0 && L.fact3) || (L.stride4 > 0 && L.fact4)) {
         CK_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
         CK_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
     }
-    if (L.stride3 > 0) {
+    auto body3 = [&](cudaStream_t q) {
+        if (L.stride3 <= 0) return;
         if (L.fact3) {
-            launch_bucket(B, 3, st);
-            launch_force3f(B, L, st);
+            launch_bucket(B, 3, q);
+            launch_force3f(B, L, q);
         } else {
-            launch_force3(B, L, st);
+            launch_force3(B, L, q);
         }
-    }
-    if (profile) CK_TRY(record_stage_event(ev_[3], st));
-    if (L.stride4 > 0) {
+    };
+    auto body4 = [&](cudaStream_t q) {
+        if (L.stride4 <= 0) return;
         if (L.fact4) {
-            launch_bucket(B, 4, st);
-            launch_force4f(B, L, st);
+            launch_bucket(B, 4, q);
+            launch_force4f(B, L, q);
         } else {
-            launch_force4(B, L, st);
+            launch_force4(B, L, q);
         }
+    };
+    if (!profile && concurrent && L.stride4 > 0) {
+        // the 4-body branch runs beside 1B+2B and 3-body on a second stream
+        // (separate work queues; forces and energies meet in atomics), joined
+        // before the results are copied out; captured as parallel graph branches
+        CK_TRY(cudaEventRecord(fork_, st));
+        CK_TRY(cudaStreamWaitEvent(stream2_, fork_, 0));
+        body4(stream2_);
+        CK_TRY(cudaEventRecord(join_, stream2_));
+        launch_force2(B, d_l2_owner_.p, L, st);
+        body3(st);
+        CK_TRY(cudaStreamWaitEvent(st, join_, 0));
+    } else {
+        launch_force2(B, d_l2_owner_.p, L, st);
+        if (profile) CK_TRY(record_stage_event(ev_[2], st));
+        body3(st);
+        if (profile) CK_TRY(record_stage_event(ev_[3], st));
+        body4(st);
     }
     if (profile) CK_TRY(record_stage_event(ev_[4], st));
     ev_recorded_ = profile;
@@ -406,7 +429,7 @@ Status Engine::launch(std::string& err) {
                                   V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
                                   tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0,
                                   tuning.fact3, tuning.fact4, tuning.rf3, tuning.rf4, tuning.ftpc3, tuning.ftpc4,
-                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_};
+                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,

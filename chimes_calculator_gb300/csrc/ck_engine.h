@@ -111,6 +111,8 @@ public:
     // 3-/4-body contraction: true = factored kernels wherever every parameter
     // set of the batch has factored tables, false = per-coefficient kernels
     bool factored = true;
+    // run the 4-body branch on a second stream beside 1B+2B and 3-body (not while profiling)
+    bool concurrent = true;
     int precision = kFP64;
     bool use_graph = false;
     RunStats last;
@@ -153,6 +155,8 @@ private:
     std::vector<PSet> sets_;
     DevBuf<DevParamSet> dsets_;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t stream2_ = nullptr;              // the 4-body branch
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
     bool ready_ = false;
 
     // batch layout of the staged batch

@@ -28,6 +28,27 @@ __device__ __forceinline__ void add_force(const BatchView& B, int ghost, double 
     atomicAdd(&B.force[3 * (long long)o + 2], fz);
 }
 
+// Per-atom energy and virial of one n-atom interaction, shared equally by its
+// atoms (Pair::ev_tally_mb, etc/lmp/etc/pair.cpp); vir in the order
+// xx xy xz yy yz zz, stored as xx yy zz xy xz yz.  Only when requested.
+__device__ __forceinline__ void tally_atoms(const BatchView& B, const int* ghosts, int n, double e, const double* vir) {
+    if (!B.eatom && !B.vatom) return;
+    const double w = 1.0 / n;
+    for (int k = 0; k < n; k++) {
+        const long long o = B.atom_orig[B.ghost_parent[ghosts[k]]];
+        if (B.eatom) atomicAdd(&B.eatom[o], e * w);
+        if (B.vatom) {
+            double* v = &B.vatom[6 * o];
+            atomicAdd(&v[0], vir[0] * w);
+            atomicAdd(&v[1], vir[3] * w);
+            atomicAdd(&v[2], vir[5] * w);
+            atomicAdd(&v[3], vir[1] * w);
+            atomicAdd(&v[4], vir[2] * w);
+            atomicAdd(&v[5], vir[4] * w);
+        }
+    }
+}
+
 // Per-lane energy/virial accumulator for one system at a time.
 struct EVAcc {
     int s = -1;
@@ -150,6 +171,7 @@ __device__ __forceinline__ void cluster_epilogue(const BatchView& B, const int* 
     }
     for (int k = 0; k < NB; k++) add_force(B, id[k], f[k][0], f[k][1], f[k][2]);
     acc.add(B, sys, pre[NP] * S, vir);
+    tally_atoms(B, id, NB, pre[NP] * S, vir);
 }
 
 }  // namespace

@@ -62,7 +62,11 @@ __global__ void __launch_bounds__(256) k_nl_pairs(BatchView B, NeighView N) {
     const long long ntot = N.nent > N.inum ? N.nent : N.inum;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ntot; e += stride) {
         double vir[6] = {0, 0, 0, 0, 0, 0};
-        if (e < N.inum) acc.add(B, 0, P.eoff[B.atom_type[N.ilist[e]]], vir);
+        if (e < N.inum) {
+            const int a = N.ilist[e];
+            acc.add(B, 0, P.eoff[B.atom_type[a]], vir);
+            tally_atoms(B, &a, 1, P.eoff[B.atom_type[a]], vir);
+        }
         if (e >= N.nent) continue;
         const int i = N.ilist[N.owner[e]];
         const int j = N.neigh[e];
@@ -77,6 +81,8 @@ __global__ void __launch_bounds__(256) k_nl_pairs(BatchView B, NeighView N) {
         add_force(B, j, -fs * dr[0], -fs * dr[1], -fs * dr[2]);
         virial_add(vir, fs, dr);
         acc.add(B, 0, E, vir);
+        const int pair[2] = {i, j};
+        tally_atoms(B, pair, 2, E, vir);
     }
     acc.flush_warp(B);
 }

@@ -20,7 +20,8 @@ namespace ck {
 
 Status NeighCompute::compute(int slot, int nall, const double* x, const int* type, const long long* tag, int inum,
                              const int* ilist, const int* numneigh, const int* neigh, double skin, bool rebuild,
-                             double* f, double* energy, double* virial, std::string& err) {
+                             double* f, double* energy, double* virial, double* eatom, double* vatom,
+                             std::string& err) {
     Status st = eng_.init_device(err);
     if (st != kOk) return st;
     if (slot < 0 || slot >= eng_.n_param_sets()) {
@@ -204,6 +205,16 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     }
 
     // evaluation with the current positions
+    if (eatom) {
+        NL_TRY(d_eatom_.reserve(nall));
+        NL_TRY(cudaMemsetAsync(d_eatom_.p, 0, sizeof(double) * nall, s));
+        B.eatom = d_eatom_.p;
+    }
+    if (vatom) {
+        NL_TRY(d_vatom_.reserve(6 * (long long)nall));
+        NL_TRY(cudaMemsetAsync(d_vatom_.p, 0, sizeof(double) * 6 * nall, s));
+        B.vatom = d_vatom_.p;
+    }
     launch_reset(B, s);
     launch_nl_pairs(B, N, L.precision, s);
     if (L.stride3 > 0 && n3_ > 0) {
@@ -219,8 +230,20 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     double ev[8];
     NL_TRY(cudaMemcpyAsync(h_force_.data(), d_force_.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s));
     NL_TRY(cudaMemcpyAsync(ev, d_ev_.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
+    if (eatom) {
+        h_eatom_.resize(nall);
+        NL_TRY(cudaMemcpyAsync(h_eatom_.data(), d_eatom_.p, sizeof(double) * nall, cudaMemcpyDeviceToHost, s));
+    }
+    if (vatom) {
+        h_vatom_.resize(6 * (size_t)nall);
+        NL_TRY(cudaMemcpyAsync(h_vatom_.data(), d_vatom_.p, sizeof(double) * 6 * nall, cudaMemcpyDeviceToHost, s));
+    }
     NL_TRY(cudaStreamSynchronize(s));
     for (size_t k = 0; k < h_force_.size(); k++) f[k] += h_force_[k];
+    if (eatom)
+        for (int a = 0; a < nall; a++) eatom[a] += h_eatom_[a];
+    if (vatom)
+        for (size_t k = 0; k < h_vatom_.size(); k++) vatom[k] += h_vatom_[k];
     if (energy) *energy += ev[0];
     if (virial) {   // Pair::ev_tally_mb order: xx yy zz xy xz yz
         virial[0] += ev[1];

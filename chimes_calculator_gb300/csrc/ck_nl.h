@@ -19,9 +19,11 @@ public:
     // list (also done on the first call and whenever nall, inum or the entry
     // count change); 0 reuses them with the new positions.  Accumulates
     // f[nall][3], *energy and virial[6] (xx yy zz xy xz yz).
+    // eatom[nall] / vatom[nall][6] (may be null): per-atom energy and virial,
+    // each interaction shared equally by its atoms, accumulated.
     Status compute(int slot, int nall, const double* x, const int* type, const long long* tag, int inum,
                    const int* ilist, const int* numneigh, const int* neigh, double skin, bool rebuild, double* f,
-                   double* energy, double* virial, std::string& err);
+                   double* energy, double* virial, double* eatom, double* vatom, std::string& err);
 
     long long n3() const { return n3_; }
     long long n4() const { return n4_; }
@@ -38,7 +40,7 @@ private:
     BatchView B_{};
     NeighView N_{};
     DevBuf<SysDesc> d_sys_;
-    DevBuf<double> d_x_, d_force_, d_ev_;
+    DevBuf<double> d_x_, d_force_, d_ev_, d_eatom_, d_vatom_;
     DevBuf<int> d_type_, d_atom_sys_, d_atom_orig_, d_parent_, d_ilist_, d_neigh_, d_owner_;
     DevBuf<long long> d_tag_, d_off_;
     DevBuf<int> d_e_cnt3_, d_e_cnt4_, d_c3_, d_c4_;
@@ -47,7 +49,7 @@ private:
     DevBuf<long long> d_bk_start_;
     DevBuf<unsigned long long> d_queue_, d_minmax_;
     DevBuf<unsigned char> d_scan_tmp_;
-    std::vector<double> h_force_;
+    std::vector<double> h_force_, h_eatom_, h_vatom_;
 };
 
 }  // namespace ck

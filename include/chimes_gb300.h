@@ -198,11 +198,13 @@ int ck_server_stats(void *server, long long *out);
  * or the entry count change) with the cutoffs max_cutoff_3B/4B + skin, and
  * evaluated every call with the current positions.  Accumulates f[nall][3]
  * (forces on ghosts included, for the reverse communication), *energy and
- * virial[6] (xx yy zz xy xz yz, as Pair::ev_tally_mb).  Per-atom energy and
- * virial are not produced. */
+ * virial[6] (xx yy zz xy xz yz, as Pair::ev_tally_mb) and, when not NULL,
+ * per-atom eatom[nall] and vatom[nall][6] (each interaction's energy and
+ * virial shared equally by its atoms, as ev_tally_mb's eflag_atom and
+ * vflag_atom branches). */
 int ck_nl_compute(void *h, int nall, const double *x, const int *type, const long long *tag, int inum,
                   const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
-                  double *energy, double *virial);
+                  double *energy, double *virial, double *eatom, double *vatom);
 /* counts[2] = triplets, quadruplets of the last cluster build; l3[n3][3] and
  * l4[n4][4] (atom indices, may be NULL) */
 int ck_nl_lists(void *h, long long *counts, int *l3, int *l4);

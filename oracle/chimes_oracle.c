@@ -1031,9 +1031,22 @@ static int push_cluster(int **buf, long *n, long *cap, const int *v, int k) {
     return 0;
 }
 
+/* Pair::ev_tally_mb (etc/lmp/etc/pair.cpp): an n-atom interaction's energy and
+ * stress shared equally by its atoms (eatom, vatom in LAMMPS order) */
+static void lmp_tally(const int *atoms, int n, double e, const double *st, double *eatom, double *vatom) {
+    for (int a = 0; a < n; a++) {
+        if (eatom) eatom[atoms[a]] += e / n;
+        if (vatom && n > 1) {
+            double *v = &vatom[6 * atoms[a]];
+            v[0] += st[0] / n; v[1] += st[3] / n; v[2] += st[5] / n;
+            v[3] += st[1] / n; v[4] += st[2] / n; v[5] += st[4] / n;
+        }
+    }
+}
+
 int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, const long long *tag, int inum,
                        const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
-                       double *energy, double *virial) {
+                       double *energy, double *virial, double *eatom, double *vatom) {
     ora_handle *h = vh;
     ora_ff *ff = &h->ff;
     (void)nall;
@@ -1090,6 +1103,7 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
         double e = 0.0;
         ora_compute_1b(h, typ[i], &e);
         *energy += e;
+        lmp_tally(&i, 1, e, NULL, eatom, vatom);
         for (long jj = off[ii]; jj < off[ii + 1]; jj++) {
             const int j = neigh[jj];
             if (tag[j] <= tag[i]) continue;
@@ -1099,6 +1113,8 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             ora_compute_2b(h, d, dr, typ[i], typ[j], f2, st, &e);
             for (int c = 0; c < 3; c++) { f[3 * i + c] += f2[c]; f[3 * j + c] += f2[3 + c]; }
             *energy += e;
+            const int pr[2] = {i, j};
+            lmp_tally(pr, 2, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
             virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
         }
@@ -1116,6 +1132,7 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             for (int a = 0; a < 3; a++)
                 for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f3[3 * a + c];
             *energy += e;
+            lmp_tally(id, 3, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
             virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
         }
@@ -1130,6 +1147,7 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             for (int a = 0; a < 4; a++)
                 for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f4[3 * a + c];
             *energy += e;
+            lmp_tally(id, 4, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
             virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
         }

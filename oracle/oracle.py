@@ -72,7 +72,7 @@ def _load():
         lib.ora_compute_4b.argtypes = [P, dp, dp, ip, dp, dp, dp]
         llp = ctypes.POINTER(ctypes.c_longlong)
         lib.ora_lammps_compute.restype = I
-        lib.ora_lammps_compute.argtypes = [P, I, dp, ip, llp, I, ip, ip, ip, D, I, dp, dp, dp]
+        lib.ora_lammps_compute.argtypes = [P, I, dp, ip, llp, I, ip, ip, ip, D, I, dp, dp, dp, dp, dp]
         lib.ora_lammps_sizes.argtypes = [P, lp, lp]
         lib.ora_lammps_lists.argtypes = [P, ip, ip]
         _lib = lib
@@ -143,16 +143,17 @@ class Oracle:
         f = np.zeros((nall, 3))
         e = ctypes.c_double(0.0)
         vir = np.zeros(6)
+        eatom, vatom = np.zeros(nall), np.zeros((nall, 6))
         tag = np.ascontiguousarray(nl.tag, dtype=np.int64)
         rc = self.lib.ora_lammps_compute(
             self.h, nall, _dp(x), _ip(np.ascontiguousarray(nl.type, dtype=np.int32)),
             tag.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), len(nl.ilist),
             _ip(np.ascontiguousarray(nl.ilist, dtype=np.int32)), _ip(np.ascontiguousarray(nl.numneigh, dtype=np.int32)),
             _ip(np.ascontiguousarray(nl.neigh, dtype=np.int32)), float(skin), int(bool(rebuild)), _dp(f),
-            ctypes.byref(e), _dp(vir))
+            ctypes.byref(e), _dp(vir), _dp(eatom), _dp(vatom))
         if rc != 0:
             raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
-        return {"energy": e.value, "force": f, "virial": vir}
+        return {"energy": e.value, "force": f, "virial": vir, "eatom": eatom, "vatom": vatom}
 
     def lammps_lists(self):
         n3, n4 = ctypes.c_long(), ctypes.c_long()

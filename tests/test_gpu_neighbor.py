@@ -50,6 +50,17 @@ def test_matches_pair_style_oracle(golden, native_lib, name, factored):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["c2_small", "smallbox"])
+def test_per_atom_energy_and_virial(golden, native_lib, name):
+    g = golden[name]
+    o, nl = _setup(g)
+    ref = o.lammps_compute(nl, SKIN)
+    r = _calc(g).nl_compute(nl, SKIN, per_atom=True)
+    _close(r, ref, E_REL_TOL, F_ABS_TOL)
+    assert np.abs(r["eatom"] - ref["eatom"]).max() <= 1e-9
+    assert np.abs(r["vatom"] - ref["vatom"]).max() <= 1e-9 * max(1.0, np.abs(ref["vatom"]).max())
+
+
 def test_lists_reused_until_rebuild(golden, native_lib):
     g = golden["c2_small"]
     o, nl = _setup(g, seed=3)

@@ -28,6 +28,9 @@ def test_pair_style_restatement_matches_serial(golden, name):
     assert abs(r["energy"] - ref["energy"]) <= 1e-11 * abs(ref["energy"])
     assert np.abs(F - ref["force"]).max() <= 1e-10
     assert np.abs(r["virial"] - vir).max() <= 1e-9 * max(1.0, np.abs(vir).max())
+    # per-atom shares add up to the totals
+    assert abs(r["eatom"].sum() - r["energy"]) <= 1e-10 * max(1.0, abs(r["energy"]))
+    assert np.abs(r["vatom"].sum(axis=0) - r["virial"]).max() <= 1e-9 * max(1.0, np.abs(r["virial"]).max())
 
 
 def test_pair_style_lists_are_reused_until_rebuild(golden):
