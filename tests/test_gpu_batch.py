@@ -60,3 +60,31 @@ def test_batch_reuse_and_growth(golden, native_lib):
         for g, r in zip(cfgs, res):
             assert abs(r["energy"] - g.energy) <= E_REL_TOL * abs(g.energy)
             assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+
+
+def test_sparse_and_tiny_configurations(golden, native_lib):
+    """Edge cases in one batch: a single atom (1-body only), two atoms beyond
+    every cutoff, a pair without triplets, beside a normal configuration --
+    each equals the oracle, alone and batched."""
+    from chimes_calculator_gb300 import Calculator, synth
+    from oracle.oracle import Oracle
+    g = golden["c2_small"]
+    o = Oracle(g.params)
+    el = sorted(set(g.cfg.types))
+    box = np.diag([13.0, 13.0, 13.0])
+    cases = [
+        synth.Config(types=[el[0]], pos=np.array([[1.0, 2.0, 3.0]]), cell=box),
+        synth.Config(types=[el[0], el[-1]], pos=np.array([[1.0, 1.0, 1.0], [7.5, 7.5, 7.5]]), cell=box),
+        synth.Config(types=[el[0], el[-1]], pos=np.array([[1.0, 1.0, 1.0], [3.5, 1.0, 1.0]]), cell=box),
+        g.cfg,
+    ]
+    ref = [o.calculate(cf.pos, cf.types, cf.cell) for cf in cases]
+    c = Calculator()
+    c.load_params(g.params)
+    batched = c.evaluate_batch([(cf.pos, cf.types, cf.cell) for cf in cases])
+    alone = [c.evaluate(cf.pos, cf.types, cf.cell) for cf in cases]
+    for cf, e, rb, ra in zip(cases, ref, batched, alone):
+        for r in (rb, ra):
+            assert abs(r["energy"] - e["energy"]) <= E_REL_TOL * max(1.0, abs(e["energy"]))
+            assert np.abs(r["force"] - e["force"]).max() <= F_ABS_TOL
+            assert np.abs(r["stress"] - e["stress"]).max() <= S_ABS_TOL
