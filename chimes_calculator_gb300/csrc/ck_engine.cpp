@@ -347,8 +347,7 @@ Status Engine::enqueue(std::string& err) {
     exclusive_scan(B.l2_count, B.l2_off, B.n_atoms_total, d_scan_tmp_.p, st);
     launch_l2(B, d_l2_owner_.p, true, st);
     launch_enum(B, d_l2_owner_.p, false, st);
-    exclusive_scan(B.e_cnt3, B.e_off3, B.n2_cap, d_scan_tmp_.p, st);
-    exclusive_scan(B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
+    exclusive_scan2(B.e_cnt3, B.e_off3, B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
     launch_enum(B, d_l2_owner_.p, true, st);
     launch_check(B, st);
     if (profile) CK_TRY(record_stage_event(ev_[1], st));

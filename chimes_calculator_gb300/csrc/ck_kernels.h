@@ -25,6 +25,9 @@ void launch_reset(const BatchView& B, cudaStream_t st);
 // scan_tmp_bytes(n) bytes.
 size_t scan_tmp_bytes(long long n);
 void exclusive_scan(const int* in, long long* out, long long n, void* tmp, cudaStream_t st);
+// two scans of the same length in the same launches (tmp as for one)
+void exclusive_scan2(const int* in_a, long long* out_a, const int* in_b, long long* out_b, long long n, void* tmp,
+                     cudaStream_t st);
 
 // ---- forces (ck_force.cu) ------------------------------------------------
 enum Precision : int { kFP64 = 0, kMixed = 1 };

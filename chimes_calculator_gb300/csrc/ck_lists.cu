@@ -302,19 +302,39 @@ __global__ void k_bin_scatter(BatchView B, const long long* bin_start) {
 }
 
 // each bin's members in ascending ghost id (the reference pushes ghosts into
-// bins in index order)
-__global__ void k_bin_sort(BatchView B, const long long* bin_start) {
-    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B.n_bins_total) return;
+// bins in index order): one warp per bin; a member's place is the number of
+// members with a smaller id (ids are unique), counted over the warp's
+// registers; bins above 64 members fall back to an insertion sort by one lane
+__global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* bin_start) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= B.n_bins_total) return;   // whole warp
     const long long s0 = bin_start[b];
     const int n = B.bin_count[b];
     int* v = B.bin_items + s0;
-    for (int i = 1; i < n; i++) {
-        const int key = v[i], kid = B.ghost_id[key];
-        int j = i - 1;
-        while (j >= 0 && B.ghost_id[v[j]] > kid) { v[j + 1] = v[j]; j--; }
-        v[j + 1] = key;
+    if (n <= 1) return;
+    if (n > 64) {
+        if (lane == 0)
+            for (int i = 1; i < n; i++) {
+                const int key = v[i], kid = B.ghost_id[key];
+                int j = i - 1;
+                while (j >= 0 && B.ghost_id[v[j]] > kid) { v[j + 1] = v[j]; j--; }
+                v[j + 1] = key;
+            }
+        return;
     }
+    const int big = 0x7fffffff;
+    const int q0 = lane < n ? v[lane] : -1, q1 = lane + 32 < n ? v[lane + 32] : -1;
+    const int k0 = q0 >= 0 ? B.ghost_id[q0] : big, k1 = q1 >= 0 ? B.ghost_id[q1] : big;
+    int r0 = 0, r1 = 0;
+    for (int src = 0; src < 32; src++) {
+        const int o0 = __shfl_sync(kFull, k0, src), o1 = __shfl_sync(kFull, k1, src);
+        r0 += (o0 < k0) + (o1 < k0);
+        r1 += (o0 < k1) + (o1 < k1);
+    }
+    __syncwarp();
+    if (q0 >= 0) v[r0] = q0;
+    if (q1 >= 0) v[r1] = q1;
 }
 
 // --- 5. 2B neighbour lists (:680-731): one warp per atom --------------------
@@ -726,9 +746,94 @@ size_t scan_tmp_bytes(long long n) {
     return (total + 16) * sizeof(long long);
 }
 
+namespace {
+
+// Up to two scans side by side (blockIdx.y): tiles of kScanBlock scanned in
+// place with the tile sums recorded; a single tile also writes the total.
+struct ScanPair {
+    const int* in[2];
+    long long* out[2];
+    long long* sums[2];
+};
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_tiles(ScanPair a, long long n) {
+    const int y = blockIdx.y;
+    __shared__ long long wsum[32];
+    const long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    const long long v = i < n ? (long long)a.in[y][i] : 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        const long long t = __shfl_up_sync(kFull, x, off);
+        if (lane >= off) x += t;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        long long t = wsum[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            const long long u = __shfl_up_sync(kFull, t, off);
+            if (lane >= off) t += u;
+        }
+        wsum[lane] = t;
+    }
+    __syncthreads();
+    const long long incl = x + (w ? wsum[w - 1] : 0);
+    if (i < n) a.out[y][i] = incl - v;
+    if (threadIdx.x == kScanBlock - 1) {
+        a.sums[y][blockIdx.x] = incl;
+        if (gridDim.x == 1) a.out[y][n] = incl;
+    }
+}
+
+// tile b adds the sum of tiles 0..b-1 (reduced by the block itself, at most
+// kScanBlock tiles); the last tile writes the total at out[n]
+__global__ void __launch_bounds__(kScanBlock) k_scan_offsets(ScanPair a, long long n) {
+    const int y = blockIdx.y;
+    const int b = blockIdx.x;
+    __shared__ long long wsum[32];
+    long long v = threadIdx.x < b ? a.sums[y][threadIdx.x] : 0;
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    long long offs = 0;
+    for (int k = 0; k < kScanBlock / 32; k++) offs += wsum[k];
+    const long long i = (long long)b * kScanBlock + threadIdx.x;
+    if (i < n) a.out[y][i] += offs;
+    if (b == (int)gridDim.x - 1 && threadIdx.x == 0) a.out[y][n] = offs + a.sums[y][b];
+}
+
+// nb <= kScanBlock tiles: two launches for one or two arrays
+void scan_small(int m, const int* ia, long long* oa, const int* ib, long long* ob, long long n, long long* tmp,
+                cudaStream_t st) {
+    const long long nb = (n + kScanBlock - 1) / kScanBlock;
+    ScanPair a;
+    a.in[0] = ia; a.out[0] = oa; a.sums[0] = tmp;
+    a.in[1] = ib; a.out[1] = ob; a.sums[1] = tmp + nb;
+    const dim3 grid((unsigned)nb, (unsigned)m);
+    count_launch(), k_scan_tiles<<<grid, kScanBlock, 0, st>>>(a, n);
+    if (nb > 1) count_launch(), k_scan_offsets<<<grid, kScanBlock, 0, st>>>(a, n);
+}
+
+}  // namespace
+
 void exclusive_scan(const int* in, long long* out, long long n, void* tmp, cudaStream_t st) {
+    if (n > 0 && n <= (long long)kScanBlock * kScanBlock) {
+        scan_small(1, in, out, in, out, n, (long long*)tmp, st);
+        return;
+    }
     scan_rec(in, nullptr, out, n, (long long*)tmp, st);
     count_launch(), k_scan_total<<<1, 1, 0, st>>>(out, n, in, nullptr);
+}
+
+void exclusive_scan2(const int* in_a, long long* out_a, const int* in_b, long long* out_b, long long n, void* tmp,
+                     cudaStream_t st) {
+    if (n > 0 && n <= (long long)kScanBlock * kScanBlock) {
+        scan_small(2, in_a, out_a, in_b, out_b, n, (long long*)tmp, st);
+        return;
+    }
+    exclusive_scan(in_a, out_a, n, tmp, st);
+    exclusive_scan(in_b, out_b, n, tmp, st);
 }
 
 void launch_atoms(const BatchView& B, cudaStream_t st) {
@@ -747,7 +852,7 @@ void launch_bin_scatter(const BatchView& B, cudaStream_t st) {
     if (B.n_ghost_total) count_launch(), k_bin_scatter<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B, B.bin_start);
 }
 void launch_bin_sort(const BatchView& B, cudaStream_t st) {
-    if (B.n_bins_total) count_launch(), k_bin_sort<<<grid_for(B.n_bins_total, 128), 128, 0, st>>>(B, B.bin_start);
+    if (B.n_bins_total) count_launch(), k_bin_rank<<<grid_for(B.n_bins_total * 32, 256), 256, 0, st>>>(B, B.bin_start);
 }
 void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n_atoms_total) return;

@@ -158,8 +158,7 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
         long long tot[2] = {0, 0};
         if (nent > 0) {
             launch_nl_enum(B, N, false, s);
-            exclusive_scan(d_e_cnt3_.p, d_e_off3_.p, nent, d_scan_tmp_.p, s);
-            exclusive_scan(d_e_cnt4_.p, d_e_off4_.p, nent, d_scan_tmp_.p, s);
+            exclusive_scan2(d_e_cnt3_.p, d_e_off3_.p, d_e_cnt4_.p, d_e_off4_.p, nent, d_scan_tmp_.p, s);
             NL_TRY(cudaMemcpyAsync(&tot[0], d_e_off3_.p + nent, sizeof(long long), cudaMemcpyDeviceToHost, s));
             NL_TRY(cudaMemcpyAsync(&tot[1], d_e_off4_.p + nent, sizeof(long long), cudaMemcpyDeviceToHost, s));
             NL_TRY(cudaStreamSynchronize(s));
