@@ -117,6 +117,16 @@ class ClockSampler:
 # ----------------------------------------------------------------------------
 # algorithmic work of one evaluation (flop model of the force kernels)
 # ----------------------------------------------------------------------------
+# DRAM bytes (read + write) per launch of the force kernels on this workload,
+# from one ncu capture each (profiles/k_forcef_c2_fp64.md, k_forcen_c2_fp64.md)
+PROFILED_TRAFFIC = {
+    "k_forcef<3,double,1>": 1109248,
+    "k_forcef<4,double,4>": 926720,
+    "k_forcen<3,double,4>": 842000,
+    "k_forcen<4,double,8>": 522000,
+}
+
+
 def algorithmic_flops(calc, cfg, params_path):
     """Per-launch algorithmic FLOPs of the 3B and 4B force kernels:
         flops(cluster) = P*(6*o + 15) + n_c*(5*P + 1) + P*21
@@ -218,7 +228,7 @@ def run_ours(args):
         calc.stage(packed)
         calc.autotune()
     else:   # a fixed launch shape (profiler runs): no autotuning
-        calc.set_contraction(args.contraction == "factored")
+        calc.set_contraction({"factored": 1, "nocache": 2, "percoef": 0}[args.contraction])
         if args.tuning:
             calc.set_tuning(*[int(v) for v in args.tuning.split(",")])
         calc.stage(packed)
@@ -294,7 +304,10 @@ def run_ours(args):
         executed = (work[nb][2] if fact else work[nb][1]) / (stage[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": kname, "achieved": achieved,
                 "peak": peak64.value, "unit": "TFLOP/s", "frac": achieved / peak64.value,
-                "traffic": None, "peak_source": "measured in-run FP64 FMA probe (ck_fma_peak); "
+                "traffic": PROFILED_TRAFFIC.get(kname),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on this "
+                                  "workload (profiles/)" if kname in PROFILED_TRAFFIC else None,
+                "peak_source": "measured in-run FP64 FMA probe (ck_fma_peak); "
                 "MEASURED_PEAKS.json has no CUDA-core FP64 figure",
                 "flops_per_launch": work[nb][1], "clusters_evaluated": work[nb][0],
                 "executed_flops_per_launch": work[nb][2] if fact else work[nb][1],
@@ -472,7 +485,7 @@ def profile_batched(args):
     if args.contraction == "auto":
         c.autotune()
     else:   # one contraction form at a fixed launch shape, no autotuning
-        c.set_contraction(args.contraction == "factored")
+        c.set_contraction({"factored": 1, "nocache": 2, "percoef": 0}[args.contraction])
         if args.tuning:
             c.set_tuning(*[int(v) for v in args.tuning.split(",")])
         c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
@@ -628,7 +641,7 @@ def main():
     ap.add_argument("--profile-batched", action="store_true",
                     help="profiler run of the batched workload (--batch-configs configurations, "
                          "--precision): autotune, 3 warm-up + 2 launches")
-    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "percoef"],
+    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "nocache", "percoef"],
                     help="autotune (auto) or one fixed 3-/4-body contraction form (profiler runs)")
     ap.add_argument("--tuning", default="",
                     help="with a fixed --contraction: tpc3,tpc4,blocks_per_sm (ck_set_tuning)")

@@ -162,9 +162,10 @@ class Calculator:
         self._check(self.lib.ck_nl_lists(self.h, cnt, _ip(l3), _ip(l4)))
         return l3, l4
 
-    def set_contraction(self, factored: bool = True):
-        """Factored (default) or per-coefficient 3-/4-body contraction kernels."""
-        self._check(self.lib.ck_set_contraction(self.h, int(bool(factored))))
+    def set_contraction(self, factored=True):
+        """3-/4-body contraction kernels: True/1 factored (default), False/0
+        per-coefficient, 2 factored without the per-entry pair-table cache."""
+        self._check(self.lib.ck_set_contraction(self.h, int(factored)))
 
     def autotune(self, packed=None):
         """Picks threads per cluster and resident blocks for the staged batch

@@ -346,7 +346,10 @@ int ck_set_tuning(void* h, int tpc3, int tpc4, int blocks_per_sm) {
 
 int ck_set_contraction(void* h, int factored) {
     if (int st = check_handle(h)) return st;
-    static_cast<Instance*>(h)->eng.factored = factored != 0;
+    if (factored < 0 || factored > 2) return report(ck::kErrInput, "contraction mode must be 0, 1 or 2");
+    ck::Engine& e = static_cast<Instance*>(h)->eng;
+    e.factored = factored != 0;
+    e.pair_cache = factored == 1;
     return ck::kOk;
 }
 

@@ -84,6 +84,14 @@ struct FactRow {
 };
 constexpr int kFactMaxDim = 128;   // largest R^K and R^(P-K) kept in shared memory per cluster
 
+// Per-pair-type constants of a body order's Chebyshev stage, when every tuple
+// uses the same inner/outer cutoff for a given pair type (then a pair's
+// tables depend only on its distance and type and can be computed once per
+// neighbour-list entry instead of once per cluster).
+struct PairTab {
+    double rin, rout, xavg, xdiff, inv_lam, inv_xdiff, fc_th, fc_inv;
+};
+
 // One factored-list entry: coefficient and the other side's linear index, in
 // one 16-byte (FP64) or 8-byte (FP32) load.
 struct __attribute__((aligned(16))) FactEntD {
@@ -115,6 +123,8 @@ struct DevParamSet {
     int bk3, bk4;              // first cluster bucket of this set (per engine; see BatchView)
     const FactRow* fr3; const FactEntD* fe3d; const FactEntF* fe3f;
     const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
+    // per-pair-type tables [npairs] (null when some tuple's cutoffs differ by tuple)
+    const PairTab* pt3; const PairTab* pt4;
 };
 
 // Per-system geometry, written by the host set-up (cell algebra) and
@@ -184,6 +194,15 @@ struct BatchView {
     int* c4;                       // [n4][4]
     long long n3_cap, n4_cap;
     int enum_serial;               // 1: some system has 3B and 4B terms with rc4 > rc3 (sequential enumeration)
+    // Pair-table cache of the factored kernels: the list entries (i, j) of a
+    // cluster's first atom, c3e[n3][2] = entries of ij, ik and c4e[n4][3] =
+    // ij, ik, il (written by the enumeration when not null), and per entry
+    // the Chebyshev tables of body order 3 / 4 (pcd: dr[3], r, fc, fcd as
+    // doubles; pct: T[R], dT/dr[R] in the compute type)
+    int* c3e; int* c4e;
+    int use_pc3, use_pc4;
+    double* pcd3; double* pcd4;    // [n2_cap][6]
+    void* pct3; void* pct4;        // [n2_cap][2R]
     // results
     double* force;                 // [n_in_total][3]
     double* eatom;                 // [n_in_total] per-atom energy or null (pair-style path)

@@ -114,6 +114,7 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.t4); rel(h.c4d); rel(h.c4f); rel(h.p4);
     rel(h.fr3); rel(h.fe3d); rel(h.fe3f);
     rel(h.fr4); rel(h.fe4d); rel(h.fe4f);
+    rel(h.pt3); rel(h.pt4);
     // this set's cluster buckets follow those of the sets loaded before it
     int nt3 = h.ntypes * h.ntypes * h.ntypes;
     h.bk3 = nbk3_;
@@ -148,6 +149,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     long long in_off = 0, atom_off = 0, ghost_off = 0, bin_off = 0;
     int stride3 = 0, stride4 = 0;
     bool fact3 = factored, fact4 = factored;
+    bool pc3 = pair_cache, pc4 = pair_cache;
     int rf3 = 0, rf4 = 0;
     bool enum_serial = false;
     double n2_est = 0.0, n3_est = 0.0, n4_est = 0.0;
@@ -188,8 +190,8 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
         stride3 = std::max(stride3, P.o3 > 0 ? P.o3 + 1 : 0);
         stride4 = std::max(stride4, P.o4 > 0 ? P.o4 + 1 : 0);
         const DevParamSet& V = sets_[in.pset].view;
-        if (P.o3 > 0) { fact3 = fact3 && V.R3 > 0; rf3 = std::max(rf3, V.R3); }
-        if (P.o4 > 0) { fact4 = fact4 && V.R4 > 0; rf4 = std::max(rf4, V.R4); }
+        if (P.o3 > 0) { fact3 = fact3 && V.R3 > 0; rf3 = std::max(rf3, V.R3); pc3 = pc3 && V.pt3; }
+        if (P.o4 > 0) { fact4 = fact4 && V.R4 > 0; rf4 = std::max(rf4, V.R4); pc4 = pc4 && V.pt4; }
         // list-size estimates for the first capacity guess
         const double rho = d.n_atoms / (vols_[s] > 0 ? vols_[s] : 1.0);
         const double m = rho * 4.18879 * d.search * d.search * d.search;
@@ -207,6 +209,9 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     tuning.fact4 = fact4 && rf4 > 0 && tuning.want_fact4 ? 1 : 0;
     avail_fact3_ = fact3 && rf3 > 0;
     avail_fact4_ = fact4 && rf4 > 0;
+    // the pair-table cache needs the enumeration that records entry indices
+    avail_pc3_ = avail_fact3_ && pc3 && !enum_serial;
+    avail_pc4_ = avail_fact4_ && pc4 && !enum_serial;
     tuning.rf3 = rf3;
     tuning.rf4 = rf4;
     V_ = BatchView();
@@ -281,6 +286,16 @@ Status Engine::ensure_lists(std::string& err) {
     CK_TRY(d_bk_count_.reserve(nbk3_ + nbk4_ + 1));
     CK_TRY(d_bk_fill_.reserve(nbk3_ + nbk4_ + 1));
     CK_TRY(d_bk_start_.reserve(nbk3_ + nbk4_ + 2));
+    if (avail_pc3_) {
+        CK_TRY(d_c3e_.reserve(2 * n3_cap_));
+        CK_TRY(d_pcd3_.reserve(8 * n2_cap_));
+        CK_TRY(d_pct3_.reserve((long long)sizeof(double) * 2 * tuning.rf3 * n2_cap_));
+    }
+    if (avail_pc4_) {
+        CK_TRY(d_c4e_.reserve(3 * n4_cap_));
+        CK_TRY(d_pcd4_.reserve(8 * n2_cap_));
+        CK_TRY(d_pct4_.reserve((long long)sizeof(double) * 2 * tuning.rf4 * n2_cap_));
+    }
     long long scan_n = std::max(std::max(V_.n_bins_total, V_.n_atoms_total), n2_cap_);
     CK_TRY(d_scan_tmp_.reserve(scan_tmp_bytes(scan_n)));
     BatchView& B = V_;
@@ -306,6 +321,11 @@ Status Engine::ensure_lists(std::string& err) {
     B.n3_cap = n3_cap_; B.n4_cap = n4_cap_;
     B.force = d_force_.p; B.ev = d_ev_.p; B.flags = d_flags_.p; B.queue = d_queue_.p;
     B.enum_serial = enum_serial_ ? 1 : 0;
+    B.c3e = avail_pc3_ ? d_c3e_.p : nullptr;
+    B.c4e = avail_pc4_ ? d_c4e_.p : nullptr;
+    B.pcd3 = d_pcd3_.p; B.pcd4 = d_pcd4_.p;
+    B.pct3 = d_pct3_.p; B.pct4 = d_pct4_.p;
+    B.use_pc3 = B.use_pc4 = 0;   // set per launch from the contraction form
     B.nbk3 = nbk3_; B.nbk4 = nbk4_;
     B.bk_count = d_bk_count_.p; B.bk_fill = d_bk_fill_.p; B.bk_start = d_bk_start_.p;
     B.perm3 = d_perm3_.p; B.perm4 = d_perm4_.p;
@@ -325,7 +345,9 @@ static cudaError_t record_stage_event(cudaEvent_t ev, cudaStream_t st) {
 }
 
 Status Engine::enqueue(std::string& err) {
-    const BatchView& B = V_;
+    BatchView B = V_;
+    B.use_pc3 = avail_pc3_ && tuning.fact3 ? 1 : 0;
+    B.use_pc4 = avail_pc4_ && tuning.fact4 ? 1 : 0;
     cudaStream_t st = stream_;
     const long long k0 = launch_counter();
     if (profile) {
@@ -360,6 +382,7 @@ Status Engine::enqueue(std::string& err) {
     auto body3 = [&](cudaStream_t q) {
         if (L.stride3 <= 0) return;
         if (L.fact3) {
+            launch_pair_tables(B, d_l2_owner_.p, 3, L, q);
             launch_bucket(B, 3, q);
             launch_force3f(B, L, q);
         } else {
@@ -369,6 +392,7 @@ Status Engine::enqueue(std::string& err) {
     auto body4 = [&](cudaStream_t q) {
         if (L.stride4 <= 0) return;
         if (L.fact4) {
+            launch_pair_tables(B, d_l2_owner_.p, 4, L, q);
             launch_bucket(B, 4, q);
             launch_force4f(B, L, q);
         } else {
@@ -435,7 +459,8 @@ Status Engine::launch(std::string& err) {
                           (const void*)h_force_.p, (const void*)h_ev_.p, (const void*)V_.bin_count,
                           (const void*)V_.e_off3, (const void*)V_.psets, (const void*)V_.perm3,
                           (const void*)V_.perm4, (const void*)V_.bk_count, (const void*)V_.bk_fill,
-                          (const void*)V_.bk_start})
+                          (const void*)V_.bk_start, (const void*)V_.c3e, (const void*)V_.c4e,
+                          (const void*)V_.pcd3, (const void*)V_.pcd4, (const void*)V_.pct3, (const void*)V_.pct4})
         key.push_back((long long)(uintptr_t)p);
     if (key != graph_key_) {
         // capture only when the same shape launches twice in a row: a batch

@@ -113,6 +113,8 @@ public:
     bool factored = true;
     // run the 4-body branch on a second stream beside 1B+2B and 3-body (not while profiling)
     bool concurrent = true;
+    // factored kernels take the pairs of a cluster's first atom from a per-entry table cache
+    bool pair_cache = true;
     int precision = kFP64;
     bool use_graph = false;
     RunStats last;
@@ -186,6 +188,10 @@ private:
     int nbk3_ = 0, nbk4_ = 0;     // cluster buckets over all loaded parameter sets
     bool avail_fact3_ = false, avail_fact4_ = false;   // staged batch has factored tables
     bool enum_serial_ = false;                         // staged batch needs the sequential enumeration
+    bool avail_pc3_ = false, avail_pc4_ = false;       // pair-table cache usable for the staged batch
+    DevBuf<int> d_c3e_, d_c4e_;
+    DevBuf<double> d_pcd3_, d_pcd4_;
+    DevBuf<unsigned char> d_pct3_, d_pct4_;
     DevBuf<int> d_bk_count_, d_bk_fill_, d_perm3_, d_perm4_;
     DevBuf<long long> d_bk_start_;
     DevBuf<double> d_force_, d_ev_;

@@ -99,25 +99,29 @@ __device__ __forceinline__ const TupleRec* cluster_tuple(const BatchView& B, con
 // Chebyshev tables and cutoff of pair p of a tuple (set_cheby_polys,
 // chimesFF.h:542-628; get_fcut, chimesFF.h:347-386) with the tuple's
 // precomputed reciprocals in place of the divisions.
+__device__ __forceinline__ PairTab tuple_pair(const TupleRec& R, int p) {
+    return PairTab{R.rin[p], R.rout[p], R.xavg[p], R.xdiff[p], R.inv_lam[p], R.inv_xdiff[p], R.fc_th[p], R.fc_inv[p]};
+}
+
 template <typename CT>
-__device__ __forceinline__ void pair_setup(const DevParamSet& P, const TupleRec& R, int p, double r, CT* T, CT* D,
+__device__ __forceinline__ void pair_setup(const DevParamSet& P, const PairTab& Q, double r, CT* T, CT* D,
                                            int stride, int nT, CT& fc, CT& fcd, int* flags) {
-    const double rin = R.rin[p];
+    const double rin = Q.rin;
     const bool oor = r < rin;
     const double rr = oor ? rin : r;
-    const double e = exp(-rr * R.inv_lam[p]);
-    const double xd = (e - R.xavg[p]) * R.inv_xdiff[p];
-    const double dxdr = -e * R.inv_lam[p] * R.inv_xdiff[p];
+    const double e = exp(-rr * Q.inv_lam);
+    const double xd = (e - Q.xavg) * Q.inv_xdiff;
+    const double dxdr = -e * Q.inv_lam * Q.inv_xdiff;
     cheby_fill_strided<CT>(T, D, stride, nT, xd, dxdr, oor, r, rin, P.inner_smooth, flags);
-    const double finv = R.fc_inv[p];
+    const double finv = Q.fc_inv;
     if (!P.tersoff) {
         const CT f0 = CT(1.0) - CT(r) * CT(finv);
         fc = f0 * f0 * f0;
         fcd = f0 * f0 * (CT(-3.0) * CT(finv));
     } else {
-        const double th = R.fc_th[p];
+        const double th = Q.fc_th;
         if (r < th) { fc = CT(1); fcd = CT(0); }
-        else if (r > R.rout[p]) { fc = CT(0); fcd = CT(0); }
+        else if (r > Q.rout) { fc = CT(0); fcd = CT(0); }
         else {
             const CT f0 = CT(r - th) * CT(finv) * CT(kPi) + CT(kPi / 2.0);
             CT sn, cs;
@@ -225,6 +229,37 @@ __global__ void __launch_bounds__(256) k_bucket_scatter(BatchView B, const int* 
     }
 }
 
+// Pair-table cache: for every list entry (i, j) closer than the body order's
+// largest outer cutoff, the pair's geometry (dr, r), cutoff (fc, fc') and
+// Chebyshev tables T, dT/dr with the pair type's constants -- the same values
+// the cluster kernel would compute for a cluster pair ij, ik (or il), once per
+// entry instead of once per cluster.  pcd[e][8] = dr0 dr1 dr2 r fc fc' oor -;
+// pct[e][2*rs] = T[0..R), then dT/dr at offset rs.
+template <int NB, typename CT>
+__global__ void __launch_bounds__(256) k_pair_tables(BatchView B, const int* l2_owner, int rs) {
+    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
+    double* pcd = NB == 3 ? B.pcd3 : B.pcd4;
+    CT* pct = reinterpret_cast<CT*>(NB == 3 ? B.pct3 : B.pct4);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n2; e += stride) {
+        const int r = l2_owner[e];
+        const SysDesc& d = B.sys[B.atom_sys[r]];
+        if (!(NB == 3 ? d.has3 : d.has4) || B.l2_dist[e] >= (NB == 3 ? d.c3 : d.c4)) continue;
+        const DevParamSet& P = B.psets[d.pset];
+        const int gi = B.atom_self[r], gj = B.l2_ghost[e];
+        double dr[3], rr;
+        pair_geom(B, d.h, gi, gj, dr, rr);
+        const int pt = P.pair_map[B.atom_type[r] * P.ntypes + B.atom_type[B.ghost_parent[gj]]];
+        const PairTab& Q = (NB == 3 ? P.pt3 : P.pt4)[pt];
+        CT fc, fcd;
+        CT* T = pct + (size_t)e * 2 * rs;
+        pair_setup<CT>(P, Q, rr, T, T + rs, 1, NB == 3 ? P.R3 : P.R4, fc, fcd, nullptr);
+        double* g = pcd + 8 * e;
+        g[0] = dr[0]; g[1] = dr[1]; g[2] = dr[2]; g[3] = rr;
+        g[4] = double(fc); g[5] = double(fcd); g[6] = rr < Q.rin ? 1.0 : 0.0; g[7] = 0.0;
+    }
+}
+
 // Shared-memory layout of one warp (one block), G = 32/TPC clusters,
 // interleaved [entry][cluster]:
 //   double geo[NP*4][G] (dr, r), fc[NP][G], fcd[NP][G]
@@ -270,13 +305,25 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         bool active = c >= 0;
         int id[NB];
         int s = 0;
+        // pairs 0 .. KC-1 (ij, ik[, il]) are list entries of the first atom:
+        // with the pair-table cache their geometry and tables are loaded
+        constexpr int KC = NB - 1;
+        const bool use_pc = NB == 3 ? B.use_pc3 : B.use_pc4;
+        const int* ce = NB == 3 ? B.c3e : B.c4e;
+        const double* pcd = NB == 3 ? B.pcd3 : B.pcd4;
+        const CT* pct = reinterpret_cast<const CT*>(NB == 3 ? B.pct3 : B.pct4);
         if (active) {
             for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
             s = B.atom_sys[B.ghost_parent[id[0]]];
             const double* h = B.sys[s].h;
             for (int p = gl; p < NP; p += TPC) {
                 double dr[3], r;
-                pair_geom(B, h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+                if (use_pc && p < KC) {
+                    const double* g = pcd + 8 * (long long)ce[(long long)KC * c + p];
+                    dr[0] = g[0]; dr[1] = g[1]; dr[2] = g[2]; r = g[3];
+                } else {
+                    pair_geom(B, h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+                }
                 geo[(4 * p + 0) * G + grp] = dr[0];
                 geo[(4 * p + 1) * G + grp] = dr[1];
                 geo[(4 * p + 2) * G + grp] = dr[2];
@@ -289,11 +336,24 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
                 if (geo[(4 * p + 3) * G + grp] >= R->rout[p]) active = false;
         if (active)
             for (int p = gl; p < NP; p += TPC) {
-                CT fc, fcd;
-                pair_setup<CT>(*P, *R, p, geo[(4 * p + 3) * G + grp], Tt + p * rs * G + grp, Dt + p * rs * G + grp,
-                               G, Rp, fc, fcd, B.flags);
-                fcs[p * G + grp] = double(fc);
-                fcds[p * G + grp] = double(fcd);
+                if (use_pc && p < KC) {
+                    const long long ent = ce[(long long)KC * c + p];
+                    const double* g = pcd + 8 * ent;
+                    const CT* tab = pct + ent * 2 * rs;
+                    for (int n = 0; n < Rp; n++) {
+                        Tt[(p * rs + n) * G + grp] = tab[n];
+                        Dt[(p * rs + n) * G + grp] = tab[rs + n];
+                    }
+                    fcs[p * G + grp] = g[4];
+                    fcds[p * G + grp] = g[5];
+                    if (g[6] != 0.0) atomicAdd(&B.flags[4], 1);
+                } else {
+                    CT fc, fcd;
+                    pair_setup<CT>(*P, tuple_pair(*R, p), geo[(4 * p + 3) * G + grp], Tt + p * rs * G + grp,
+                                   Dt + p * rs * G + grp, G, Rp, fc, fcd, B.flags);
+                    fcs[p * G + grp] = double(fc);
+                    fcds[p * G + grp] = double(fcd);
+                }
             }
         __syncwarp();
         // column-side products Y_J (and row-side X_I for 4-body); the mixed-radix
@@ -488,6 +548,21 @@ size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs) {
 void launch_bucket(const BatchView& B, int nbody, cudaStream_t st) {
     if (nbody == 3) launch_bucket_n<3>(B, st);
     else launch_bucket_n<4>(B, st);
+}
+
+void launch_pair_tables(const BatchView& B, const int* l2_owner, int nbody, const ForceLaunch& L, cudaStream_t st) {
+    if (!(nbody == 3 ? B.use_pc3 : B.use_pc4) || B.n2_cap <= 0) return;
+    const int rs = nbody == 3 ? L.rf3 : L.rf4;
+    long long want = (long long)sm_count() * 8;
+    long long need = (B.n2_cap + 255) / 256;
+    const unsigned grid = (unsigned)(want < need ? want : need);
+    if (nbody == 3) {
+        if (L.precision == kMixed) count_launch(), k_pair_tables<3, float><<<grid, 256, 0, st>>>(B, l2_owner, rs);
+        else count_launch(), k_pair_tables<3, double><<<grid, 256, 0, st>>>(B, l2_owner, rs);
+    } else {
+        if (L.precision == kMixed) count_launch(), k_pair_tables<4, float><<<grid, 256, 0, st>>>(B, l2_owner, rs);
+        else count_launch(), k_pair_tables<4, double><<<grid, 256, 0, st>>>(B, l2_owner, rs);
+    }
 }
 
 void launch_force3f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {

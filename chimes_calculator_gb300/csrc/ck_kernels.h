@@ -59,6 +59,8 @@ void launch_force4(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // order by (parameter set, type tuple), then contract.  Both read their
 // counts on the device.
 void launch_bucket(const BatchView& B, int nbody, cudaStream_t st);
+// Pair-table cache of body order nbody (when B.use_pc3 / use_pc4): one pass over the list entries.
+void launch_pair_tables(const BatchView& B, const int* l2_owner, int nbody, const ForceLaunch& L, cudaStream_t st);
 void launch_force3f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // dynamic shared memory of one factored-kernel block (one warp)

@@ -604,6 +604,7 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                     if (q < B.n3_cap) {
                         int* out = B.c3 + 3 * q;
                         out[0] = gi; out[1] = jj; out[2] = kk;
+                        if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)k; }
                     }
                 }
                 n3 += __popc(m3);
@@ -644,6 +645,11 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                             if (q < B.n4_cap) {
                                 int* out = B.c4 + 4 * q;
                                 out[0] = gi; out[1] = jj; out[2] = ks; out[3] = ll;
+                                if (B.c4e) {
+                                    B.c4e[3 * q] = (int)e;
+                                    B.c4e[3 * q + 1] = (int)(kb + src);
+                                    B.c4e[3 * q + 2] = (int)l;
+                                }
                             }
                         }
                         n4 += __popc(ml);

@@ -792,6 +792,26 @@ ParamImage pack_params(const HostParams& P) {
             }
             shared[key] = Shared{R.coef_off, R.f_row, R.f_nrow, R.f_ncol, R.f_ent};
         }
+        // per-pair-type tables when no tuple overrides a pair type's cutoffs
+        std::vector<PairTab> ptab(P.npairs);
+        std::vector<int> seen(P.npairs, 0);
+        bool uniform = true;
+        for (int u = 0; u < ntup && uniform; u++) {
+            const TupleRec& R = tr[u];
+            if (!R.valid) continue;
+            int a[4], r = u;
+            for (int k = nb - 1; k >= 0; k--) { a[k] = r % nt; r /= nt; }
+            int p = 0;
+            for (int i = 0; i < nb; i++)
+                for (int j = i + 1; j < nb; j++, p++) {
+                    const int pt = P.pair_map[a[i] * nt + a[j]];
+                    PairTab t{R.rin[p], R.rout[p], R.xavg[p], R.xdiff[p], R.inv_lam[p], R.inv_xdiff[p], R.fc_th[p],
+                              R.fc_inv[p]};
+                    if (!seen[pt]) { ptab[pt] = t; seen[pt] = 1; }
+                    else if (std::memcmp(&ptab[pt], &t, sizeof(t)) != 0) uniform = false;
+                }
+        }
+        size_t pto = uniform ? B.add(ptab.data(), ptab.size()) : 0;
         size_t tro = B.add(tr.data(), tr.size());
         size_t cdo = B.add(cd.data(), cd.size());
         size_t cfo = B.add(cf.data(), cf.size());
@@ -807,12 +827,14 @@ ParamImage pack_params(const HostParams& P) {
             H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
             H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);
             H.R3 = Rf;
+            H.pt3 = as_off<const PairTab>(pto);
             H.fr3 = as_off<const FactRow>(fro); H.fe3d = as_off<const FactEntD>(fdo);
             H.fe3f = as_off<const FactEntF>(ffo);
         } else {
             H.t4 = as_off<const TupleRec>(tro); H.c4d = as_off<const double>(cdo);
             H.c4f = as_off<const float>(cfo); H.p4 = as_off<const uint32_t>(pwo);
             H.R4 = Rf;
+            H.pt4 = as_off<const PairTab>(pto);
             H.fr4 = as_off<const FactRow>(fro); H.fe4d = as_off<const FactEntD>(fdo);
             H.fe4f = as_off<const FactEntF>(ffo);
         }

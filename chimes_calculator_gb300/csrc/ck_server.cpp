@@ -193,8 +193,11 @@ private:
         const double n2 = d.n_atoms * (0.55 * m + 4);
         const double n3 = d.has3 ? d.n_atoms * (0.3 * m * m * std::pow(d.c3 / d.search, 6.0) + 4) : 0.0;
         const double n4 = d.has4 ? d.n_atoms * (0.1 * m * m * m * std::pow(d.c4 / d.search, 9.0) + 4) : 0.0;
-        return (double)d.n_atoms * d.gstride * 110.0 + (double)d.bin_cap * 20.0 + n2 * 70.0 + n3 * 12.0 +
-               n4 * 16.0 + d.n_atoms * 120.0;
+        // pair lists ~70 B per pair plus the factored kernels' per-entry table cache
+        // (~350 B per pair in FP64 for the 3- and 4-body orders), cluster lists
+        // with their entry indices
+        return (double)d.n_atoms * d.gstride * 110.0 + (double)d.bin_cap * 20.0 + n2 * 420.0 + n3 * 20.0 +
+               n4 * 28.0 + d.n_atoms * 120.0;
     }
 
     void worker(int w) {

@@ -80,7 +80,11 @@ int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
  * by row and column products, two multiply-adds per coefficient) wherever every
  * parameter set of the batch has factored tables (powers per pair R with R^K and
  * R^(P-K) <= 128, K = 1 for 3-body and 3 for 4-body), 0 = per-coefficient
- * kernels everywhere.  Both give the same sums in another rounding order. */
+ * kernels everywhere; 2 = factored without the per-entry pair-table cache
+ * (the factored kernels otherwise take the Chebyshev tables of a cluster's
+ * pairs ij, ik[, il] from one evaluation per neighbour-list entry, when every
+ * tuple uses the same cutoffs for a given pair type).  All give the same sums
+ * in another rounding order. */
 int ck_set_contraction(void *h, int factored);
 /* Autotuner for the batch staged with ck_stage_batch: times the 3-body and
  * 4-body force kernels (CUDA events) for threads per cluster 1..32 and then
