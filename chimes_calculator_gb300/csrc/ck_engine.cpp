@@ -44,6 +44,7 @@ Engine::~Engine() {
     for (auto& s : sets_)
         if (s.dev) cudaFree(s.dev);
     if (fork_) cudaEventDestroy(fork_);
+    if (fork2_) cudaEventDestroy(fork2_);
     if (join_) cudaEventDestroy(join_);
     if (stream2_) cudaStreamDestroy(stream2_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -68,6 +69,7 @@ Status Engine::init_device(std::string& err) {
     CK_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     CK_TRY(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
     CK_TRY(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+    CK_TRY(cudaEventCreateWithFlags(&fork2_, cudaEventDisableTiming));
     CK_TRY(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
     CK_TRY(h_flags_.reserve(8));
     CK_TRY(h_counts_.reserve(4));
@@ -209,9 +211,13 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     tuning.fact4 = fact4 && rf4 > 0 && tuning.want_fact4 ? 1 : 0;
     avail_fact3_ = fact3 && rf3 > 0;
     avail_fact4_ = fact4 && rf4 > 0;
-    // the pair-table cache needs the enumeration that records entry indices
-    avail_pc3_ = avail_fact3_ && pc3 && !enum_serial;
-    avail_pc4_ = avail_fact4_ && pc4 && !enum_serial;
+    // the pair-table cache needs the enumeration that records entry indices;
+    // it pays for itself while its tables stay near L2 (measured: ~10% on the
+    // 3-body kernel for 25k list entries, nothing for 11M), so large batches
+    // compute every pair in the cluster kernel
+    const bool pc_size = n2_est <= 2.0e6;
+    avail_pc3_ = avail_fact3_ && pc3 && !enum_serial && pc_size;
+    avail_pc4_ = avail_fact4_ && pc4 && !enum_serial && pc_size;
     tuning.rf3 = rf3;
     tuning.rf4 = rf4;
     V_ = BatchView();
@@ -368,13 +374,23 @@ Status Engine::enqueue(std::string& err) {
     launch_l2(B, d_l2_owner_.p, false, st);
     exclusive_scan(B.l2_count, B.l2_off, B.n_atoms_total, d_scan_tmp_.p, st);
     launch_l2(B, d_l2_owner_.p, true, st);
+    ForceLaunch L = tuning;
+    L.precision = precision;
+    // Concurrent form: the second stream takes 1B+2B (it needs only the pair
+    // lists) while the first enumerates the clusters, then the 4-body branch
+    // while the first runs the 3-body one; both join before the copies out.
+    // Not while profiling (the stage events time the stages one after another).
+    const bool conc = !profile && concurrent;
+    if (conc) {
+        CK_TRY(cudaEventRecord(fork_, st));
+        CK_TRY(cudaStreamWaitEvent(stream2_, fork_, 0));
+        launch_force2(B, d_l2_owner_.p, L, stream2_);
+    }
     launch_enum(B, d_l2_owner_.p, false, st);
     exclusive_scan2(B.e_cnt3, B.e_off3, B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
     launch_enum(B, d_l2_owner_.p, true, st);
     launch_check(B, st);
     if (profile) CK_TRY(record_stage_event(ev_[1], st));
-    ForceLaunch L = tuning;
-    L.precision = precision;
     if ((L.stride3 > 0 && L.fact3) || (L.stride4 > 0 && L.fact4)) {
         CK_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
         CK_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
@@ -399,15 +415,13 @@ Status Engine::enqueue(std::string& err) {
             launch_force4(B, L, q);
         }
     };
-    if (!profile && concurrent && L.stride4 > 0) {
-        // the 4-body branch runs beside 1B+2B and 3-body on a second stream
-        // (separate work queues; forces and energies meet in atomics), joined
-        // before the results are copied out; captured as parallel graph branches
-        CK_TRY(cudaEventRecord(fork_, st));
-        CK_TRY(cudaStreamWaitEvent(stream2_, fork_, 0));
+    if (conc) {
+        // separate work queues; forces and energies meet in atomics; captured
+        // as parallel graph branches
+        CK_TRY(cudaEventRecord(fork2_, st));
+        CK_TRY(cudaStreamWaitEvent(stream2_, fork2_, 0));
         body4(stream2_);
         CK_TRY(cudaEventRecord(join_, stream2_));
-        launch_force2(B, d_l2_owner_.p, L, st);
         body3(st);
         CK_TRY(cudaStreamWaitEvent(st, join_, 0));
     } else {

@@ -158,7 +158,7 @@ private:
     DevBuf<DevParamSet> dsets_;
     cudaStream_t stream_ = nullptr;
     cudaStream_t stream2_ = nullptr;              // the 4-body branch
-    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    cudaEvent_t fork_ = nullptr, fork2_ = nullptr, join_ = nullptr;
     bool ready_ = false;
 
     // batch layout of the staged batch

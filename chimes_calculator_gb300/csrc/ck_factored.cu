@@ -17,8 +17,9 @@
 // bucket padded with -1 to a multiple of 32 slots, so every warp works on one
 // tuple: loop bounds and coefficient loads are uniform across the warp (the
 // loads are broadcasts).  TPC lanes share a cluster (TPC = 1, 2 or 4) and
-// split each row's and column's entries; per-cluster tables (T, dT/dr per
-// pair, Y and X) sit in shared memory interleaved by cluster, [entry][cluster].
+// take its rows, then its columns, round robin (each lane sums and flushes
+// whole records); per-cluster tables (T, dT/dr per pair, Y and X) sit in
+// shared memory interleaved by cluster, [entry][cluster].
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -316,7 +317,9 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
             for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
             s = B.atom_sys[B.ghost_parent[id[0]]];
             const double* h = B.sys[s].h;
-            for (int p = gl; p < NP; p += TPC) {
+            for (int sl = gl; sl < NP; sl += TPC) {
+                // with the cache the evaluated pairs come first, spread over the lanes
+                const int p = use_pc ? (sl < NP - KC ? KC + sl : sl - (NP - KC)) : sl;
                 double dr[3], r;
                 if (use_pc && p < KC) {
                     const double* g = pcd + 8 * (long long)ce[(long long)KC * c + p];
@@ -335,7 +338,8 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
             for (int p = 0; p < NP; p++)
                 if (geo[(4 * p + 3) * G + grp] >= R->rout[p]) active = false;
         if (active)
-            for (int p = gl; p < NP; p += TPC) {
+            for (int sl = gl; sl < NP; sl += TPC) {
+                const int p = use_pc ? (sl < NP - KC ? KC + sl : sl - (NP - KC)) : sl;
                 if (use_pc && p < KC) {
                     const long long ent = ce[(long long)KC * c + p];
                     const double* g = pcd + 8 * ent;
@@ -403,51 +407,61 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         CT S = CT(0), Gp[NP];
 #pragma unroll
         for (int p = 0; p < NP; p++) Gp[p] = CT(0);
-        int e = R->f_ent;
+        // The TPC lanes of a cluster take whole rows (and then whole columns)
+        // round robin, each flushing its own rows: the per-row products are
+        // issued once per TPC rows instead of once per row.  A record's
+        // entries start where the previous record's end.
+        const int e_col0 = R->f_ent + R->ncoef;
         // row pass: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K)
-        for (int r = 0; r < nrow; r++) {
-            const FactRow rw = rows[r];
-            const CT z = entry_sum<CT, TPC, G>(ent, e, rw.end, gl, Y, grp);
-            e = rw.end;
-            CT t[K], d[K];
+        for (int r0 = 0; r0 < nrow; r0 += TPC) {
+            const int r = r0 + gl;
+            if (r < nrow) {
+                const FactRow rw = rows[r];
+                const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
+                const CT z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
+                CT t[K], d[K];
 #pragma unroll
-            for (int p = 0; p < K; p++) {
-                const int q = (rw.pows >> (kPowBits * p)) & 31;
-                t[p] = Tt[(p * rs + q) * G + grp];
-                d[p] = Dt[(p * rs + q) * G + grp];
-            }
-            if constexpr (K == 1) {
-                S += t[0] * z;
-                Gp[0] += d[0] * z;
-            } else {
-                const CT t12 = t[1] * t[2], t01 = t[0] * t[1];
-                S += (t[0] * t12) * z;
-                Gp[0] += (d[0] * t12) * z;
-                Gp[1] += (t[0] * t[2] * d[1]) * z;
-                Gp[K - 1] += (t01 * d[K - 1]) * z;
+                for (int p = 0; p < K; p++) {
+                    const int q = (rw.pows >> (kPowBits * p)) & 31;
+                    t[p] = Tt[(p * rs + q) * G + grp];
+                    d[p] = Dt[(p * rs + q) * G + grp];
+                }
+                if constexpr (K == 1) {
+                    S += t[0] * z;
+                    Gp[0] += d[0] * z;
+                } else {
+                    const CT t12 = t[1] * t[2], t01 = t[0] * t[1];
+                    S += (t[0] * t12) * z;
+                    Gp[0] += (d[0] * t12) * z;
+                    Gp[1] += (t[0] * t[2] * d[1]) * z;
+                    Gp[K - 1] += (t01 * d[K - 1]) * z;
+                }
             }
         }
         // column pass: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K)
-        for (int cc = 0; cc < ncol; cc++) {
-            const FactRow cl = rows[nrow + cc];
-            const CT w = entry_sum<CT, TPC, G>(ent, e, cl.end, gl, Xv, grp);
-            e = cl.end;
-            constexpr int C = NP - K;
-            CT t[C], d[C];
+        for (int c0 = 0; c0 < ncol; c0 += TPC) {
+            const int cc = c0 + gl;
+            if (cc < ncol) {
+                const FactRow cl = rows[nrow + cc];
+                const int e0 = cc == 0 ? e_col0 : rows[nrow + cc - 1].end;
+                const CT w = entry_sum<CT, 1, G>(ent, e0, cl.end, 0, Xv, grp);
+                constexpr int C = NP - K;
+                CT t[C], d[C];
 #pragma unroll
-            for (int p = 0; p < C; p++) {
-                const int q = (cl.pows >> (kPowBits * p)) & 31;
-                t[p] = Tt[((K + p) * rs + q) * G + grp];
-                d[p] = Dt[((K + p) * rs + q) * G + grp];
-            }
-            if constexpr (C == 2) {
-                Gp[K] += (d[0] * t[1]) * w;
-                Gp[K + 1] += (t[0] * d[1]) * w;
-            } else {
-                const CT t12 = t[1] * t[C - 1];
-                Gp[K] += (d[0] * t12) * w;
-                Gp[K + 1] += (t[0] * d[1] * t[C - 1]) * w;
-                Gp[K + C - 1] += (t[0] * t[1] * d[C - 1]) * w;
+                for (int p = 0; p < C; p++) {
+                    const int q = (cl.pows >> (kPowBits * p)) & 31;
+                    t[p] = Tt[((K + p) * rs + q) * G + grp];
+                    d[p] = Dt[((K + p) * rs + q) * G + grp];
+                }
+                if constexpr (C == 2) {
+                    Gp[K] += (d[0] * t[1]) * w;
+                    Gp[K + 1] += (t[0] * d[1]) * w;
+                } else {
+                    const CT t12 = t[1] * t[C - 1];
+                    Gp[K] += (d[0] * t12) * w;
+                    Gp[K + 1] += (t[0] * d[1] * t[C - 1]) * w;
+                    Gp[K + C - 1] += (t[0] * t[1] * d[C - 1]) * w;
+                }
             }
         }
         // combine the TPC partial sums of each cluster
@@ -505,7 +519,7 @@ void launch_f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
 #define CK_LAUNCH_F(T_)                                                                                  \
     do {                                                                                                 \
         auto kern = k_forcef<NB, CT, T_>;                                                                \
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);              \
+        allow_max_smem((const void*)kern);                                                              \
         int occ = 0;                                                                                     \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, smem);                             \
         if (occ < 1) occ = 1;                                                                            \

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <set>
 
 #include "ck_common.h"
 #include "ck_kernels.h"
@@ -238,7 +240,7 @@ void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, l
 #define CK_LAUNCH(T_)                                                                          \
     do {                                                                                       \
         auto kern = k_forcen<NB, CT, T_>;                                                      \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (smem > 48 * 1024) allow_max_smem((const void*)kern);                                \
         count_launch(), kern<<<grid, block, smem, st>>>(B, clusters, n_ptr, n, stride);                               \
     } while (0)
     switch (tpc) {
@@ -297,6 +299,19 @@ double fma_peak_tflops(int precision) {
     if (cudaGetLastError() != cudaSuccess) return -1.0;
     const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
     return flops / (best * 1e-3) / 1e12;
+}
+
+cudaError_t allow_max_smem(const void* kernel) {
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> g(mu);
+    if (done.count(kernel)) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess) done.insert(kernel);
+    return e;
 }
 
 int sm_count() {

@@ -8,6 +8,14 @@
 #include "ck_math.cuh"
 
 namespace ck {
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in maximum,
+// once per kernel.  The limit is a per-function attribute shared by every host
+// thread, so it is never lowered: threads launching the same kernel with
+// different shared-memory sizes (request-server workers) cannot race on it.
+// The shared memory a launch actually gets is its own launch argument.
+cudaError_t allow_max_smem(const void* kernel);
+
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
