@@ -434,8 +434,35 @@ def extras(args):
     sa = sum(x.n_atoms for x in sample)
     out["plain_fp64_per_config"] = {"value": sa / wall, "unit": UNIT, "configs": len(sample), "atoms": sa,
                                     "ms_per_config": 1e3 * wall / len(sample)}
+    out["pair_style_c2"] = pair_style(params, cfg)
     out["serving"] = serving(args)
     return out
+
+
+def pair_style(params, cfg, skin=1.0, calls=30):
+    """The LAMMPS pair-style path (ck_nl_compute) on the C2 configuration as
+    a rank sees it: 1024 local atoms plus ghosts, full neighbour lists within
+    cutoff + skin; clusters built once, then evaluated per call with the host
+    positions copied in and forces copied out (as between re-neighbourings)."""
+    from chimes_calculator_gb300 import Calculator, synth
+    c = Calculator()
+    c.load_params(params)
+    info = c.info(0)
+    nl = synth.lammps_neighbors(cfg, c.type_indices(cfg.types, 0), max(info["max_cutoffs"]) + skin, seed=11)
+    c.nl_compute(nl, skin, rebuild=True)
+    t0 = time.perf_counter()
+    c.nl_compute(nl, skin, rebuild=True)
+    build = time.perf_counter() - t0
+    for _ in range(3):
+        c.nl_compute(nl, skin, rebuild=False)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        c.nl_compute(nl, skin, rebuild=False)
+    sec = (time.perf_counter() - t0) / calls
+    l3, l4 = c.nl_lists()
+    return {"value": nl.nlocal / sec, "unit": UNIT, "ms_per_call": 1e3 * sec, "ms_rebuild_call": 1e3 * build,
+            "local_atoms": nl.nlocal, "ghost_atoms": int(len(nl.x) - nl.nlocal), "list_entries": int(len(nl.neigh)),
+            "listed_triplets": int(len(l3)), "listed_quadruplets": int(len(l4)), "skin": skin}
 
 
 def serving(args):

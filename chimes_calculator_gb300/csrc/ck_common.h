@@ -201,6 +201,9 @@ struct BatchView {
     // doubles; pct: T[R], dT/dr[R] in the compute type)
     int* c3e; int* c4e;
     int use_pc3, use_pc4;
+    // 1: bucketing drops clusters with a pair at or beyond its tuple's outer
+    // cutoff (lists built with padded cutoffs; rebucketed every evaluation)
+    int bucket_cut;
     double* pcd3; double* pcd4;    // [n2_cap][6]
     void* pct3; void* pct4;        // [n2_cap][2R]
     // results

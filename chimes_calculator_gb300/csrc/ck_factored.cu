@@ -140,6 +140,14 @@ __device__ __forceinline__ int bucket_key(const BatchView& B, const int* cluster
     const DevParamSet* P;
     const TupleRec* R = cluster_tuple<NB>(B, clusters, c, id, s, P, u);
     if (!R->valid || (NB == 3 ? P->R3 : P->R4) <= 0) return -1;
+    if (B.bucket_cut) {   // compute_3B/4B would return at once: leave the cluster out
+        const double* h = B.sys[s].h;
+        for (int p = 0; p < Topo<NB>::NP; p++) {
+            double dr[3], r;
+            pair_geom(B, h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+            if (r >= R->rout[p]) return -1;
+        }
+    }
     return (NB == 3 ? P->bk3 : P->bk4) + u;
 }
 

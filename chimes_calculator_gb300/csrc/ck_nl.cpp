@@ -185,12 +185,6 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     B.perm4_cap = nbk4 > 0 ? n4_ + 32LL * nbk4 : 0;
     if (build) {
         if (nent > 0) launch_nl_enum(B, N, true, s);
-        if ((L.stride3 > 0 && L.fact3) || (L.stride4 > 0 && L.fact4)) {
-            NL_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (nbk3 + nbk4), s));
-            NL_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (nbk3 + nbk4), s));
-            if (L.stride3 > 0 && L.fact3) launch_bucket(B, 3, s);
-            if (L.stride4 > 0 && L.fact4) launch_bucket(B, 4, s);
-        }
         built_ = true;
         slot_ = slot;
         nall_ = nall;
@@ -215,6 +209,16 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
         B.vatom = d_vatom_.p;
     }
     launch_reset(B, s);
+    // The lists hold every cluster within the padded cutoffs; the factored
+    // kernels get only those within their tuple's cutoffs at the current
+    // positions (rebucketed every call, as atoms move between rebuilds).
+    B.bucket_cut = 1;
+    if ((L.stride3 > 0 && L.fact3 && n3_ > 0) || (L.stride4 > 0 && L.fact4 && n4_ > 0)) {
+        NL_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (nbk3 + nbk4), s));
+        NL_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (nbk3 + nbk4), s));
+        if (L.stride3 > 0 && L.fact3 && n3_ > 0) launch_bucket(B, 3, s);
+        if (L.stride4 > 0 && L.fact4 && n4_ > 0) launch_bucket(B, 4, s);
+    }
     launch_nl_pairs(B, N, L.precision, s);
     if (L.stride3 > 0 && n3_ > 0) {
         if (L.fact3) launch_force3f(B, L, s);
