@@ -399,11 +399,11 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
         const long long st = __shfl_sync(kFull, bst, lo);
         const int first = __shfl_sync(kFull, excl, lo);
         bool pred = false;
-        int ajj = -1;
+        int ajj = -1, par = -1;
         double dd = 0.0, rv[3] = {0, 0, 0};
         if (t < ncand) {
             ajj = B.bin_items[st + (t - first)];
-            if (ajj != gi && r <= B.ghost_parent[ajj]) {
+            if (ajj != gi && r <= (par = B.ghost_parent[ajj])) {
                 const float* xj = &B.ghost_xf[3 * (long long)ajj];
                 const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
                 if (ex * ex + ey * ey + ez * ez < far2) {   // else certainly >= sd
@@ -419,7 +419,10 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
                 B.l2_ghost[pos] = ajj;
                 B.l2_dist[pos] = dd;
                 l2_owner[pos] = (int)r;
-                float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], (float)dd);
+                // x, y, z: FP32 displacement for the enumeration's prefilter;
+                // w: the neighbour's parent atom (int bits), saving the
+                // enumeration a dependent load per candidate
+                float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], __int_as_float(par));
                 reinterpret_cast<float4*>(B.l2_vec)[pos] = v;
             }
         }
@@ -581,7 +584,7 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
             const int jj = B.l2_ghost[e];
             const float4 vj = vec[e];
             const double* fj = &B.ghost_fn[3 * (long long)jj];
-            const int pj = B.ghost_parent[jj];
+            const int pj = __float_as_int(vj.w);
             for (long long kb = b0; kb < b1; kb += 32) {
                 const long long k = kb + lane;
                 bool ok3 = false, ok4 = false;
@@ -589,10 +592,10 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                 float4 vk = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (k < b1) {
                     kk = B.l2_ghost[k];
-                    pk = B.ghost_parent[kk];
+                    vk = vec[k];
+                    pk = __float_as_int(vk.w);
                     if (kk != jj && pj <= pk) {
                         const double dik = B.l2_dist[k];
-                        vk = vec[k];
                         PairDist jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk), 0.0, false};
                         ok3 = want3 && dik < c3 && !jk.ge(c3, eps);
                         ok4 = want4 && dik < c4 && !jk.ge(c4, eps);
@@ -626,10 +629,10 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                         int ll = -1;
                         if (l < b1) {
                             ll = B.l2_ghost[l];
+                            const float4 vl = vec[l];
                             if (ll != jj && ll != ks) {
-                                const int pl = B.ghost_parent[ll];
+                                const int pl = __float_as_int(vl.w);
                                 if (pj <= pl && pks <= pl && B.l2_dist[l] < c4) {
-                                    const float4 vl = vec[l];
                                     const double* fl = &B.ghost_fn[3 * (long long)ll];
                                     PairDist jl{hn, fj, fl, vdist(vj, vl), 0.0, false};
                                     if (!jl.ge(c4, eps)) {
