@@ -120,8 +120,8 @@ class ClockSampler:
 # DRAM bytes (read + write) per launch of the force kernels on this workload,
 # from one ncu capture each (profiles/k_forcef_c2_fp64.md, k_forcen_c2_fp64.md)
 PROFILED_TRAFFIC = {
-    "k_forcef<3,double,1>": 1109248,
-    "k_forcef<4,double,4>": 926720,
+    "k_forcef<3,double,1>": 4272384,
+    "k_forcef<4,double,4>": 2047488,
     "k_forcen<3,double,4>": 842000,
     "k_forcen<4,double,8>": 522000,
 }
