@@ -161,7 +161,7 @@ def algorithmic_flops(calc, cfg, params_path):
     out = {}
     for nb, lst, order in ((3, l3, o3), (4, l4, o4)):
         if lst.shape[0] == 0 or order == 0:
-            out[nb] = (0, 0.0, 0.0)
+            out[nb] = (0, 0.0, 0.0, 0.0)
             continue
         P = nb * (nb - 1) // 2
         pairs = [(i, j) for i in range(nb) for j in range(i + 1, nb)]
@@ -187,7 +187,9 @@ def algorithmic_flops(calc, cfg, params_path):
         ex = ok.sum() * (P * (6 * order + 15) + P * 21 + R ** C * (C - 1) + R ** K * (K - 1)) \
             + (4.0 * nc).sum() + (per_row * nrow[u][ok].astype(np.float64)).sum() \
             + (per_col * ncol[u][ok].astype(np.float64)).sum()
-        out[nb] = (int(ok.sum()), float(flops), float(ex))
+        # without the Y table (3-body): one more multiply per row entry, no table
+        ex_noy = ex + nc.sum() - ok.sum() * (R ** C * (C - 1)) if nb == 3 else ex
+        out[nb] = (int(ok.sum()), float(flops), float(ex), float(ex_noy))
     del maxc
     return out
 
@@ -228,7 +230,7 @@ def run_ours(args):
         calc.stage(packed)
         calc.autotune()
     else:   # a fixed launch shape (profiler runs): no autotuning
-        calc.set_contraction({"factored": 1, "nocache": 2, "percoef": 0}[args.contraction])
+        calc.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0}[args.contraction])
         if args.tuning:
             calc.set_tuning(*[int(v) for v in args.tuning.split(",")])
         calc.stage(packed)
@@ -299,7 +301,11 @@ def run_ours(args):
         nb = 3 if dom == 2 else 4
         fact = tun["fact%d" % nb]
         tpc = tun[("ftpc%d" if fact else "tpc%d") % nb]
+        noy = fact and nb == 3 and tun.get("noy3", 0)
         kname = ("k_forcef<%d,double,%d>" if fact else "k_forcen<%d,double,%d>") % (nb, tpc)
+        if noy:
+            kname = kname[:-1] + ",true>"
+            work[nb] = (work[nb][0], work[nb][1], work[nb][3])
         achieved = work[nb][1] / (stage[dom] * 1e-3) / 1e12
         executed = (work[nb][2] if fact else work[nb][1]) / (stage[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": kname, "achieved": achieved,
@@ -512,7 +518,7 @@ def profile_batched(args):
     if args.contraction == "auto":
         c.autotune()
     else:   # one contraction form at a fixed launch shape, no autotuning
-        c.set_contraction({"factored": 1, "nocache": 2, "percoef": 0}[args.contraction])
+        c.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0}[args.contraction])
         if args.tuning:
             c.set_tuning(*[int(v) for v in args.tuning.split(",")])
         c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
@@ -668,7 +674,7 @@ def main():
     ap.add_argument("--profile-batched", action="store_true",
                     help="profiler run of the batched workload (--batch-configs configurations, "
                          "--precision): autotune, 3 warm-up + 2 launches")
-    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "nocache", "percoef"],
+    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "nocache", "noy", "percoef"],
                     help="autotune (auto) or one fixed 3-/4-body contraction form (profiler runs)")
     ap.add_argument("--tuning", default="",
                     help="with a fixed --contraction: tpc3,tpc4,blocks_per_sm (ck_set_tuning)")

@@ -92,8 +92,9 @@ struct PairTab {
     double rin, rout, xavg, xdiff, inv_lam, inv_xdiff, fc_th, fc_inv;
 };
 
-// One factored-list entry: coefficient and the other side's linear index, in
-// one 16-byte (FP64) or 8-byte (FP32) load.
+// One factored-list entry: coefficient and the other side's record, in one
+// 16-byte (FP64) or 8-byte (FP32) load.  idx = linear index (low 16 bits) |
+// the other side's powers packed kPowBits per pair (high 16 bits).
 struct __attribute__((aligned(16))) FactEntD {
     double a;
     int idx;

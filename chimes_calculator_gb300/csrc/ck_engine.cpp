@@ -466,7 +466,7 @@ Status Engine::launch(std::string& err) {
                                   V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
                                   tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0,
                                   tuning.fact3, tuning.fact4, tuning.rf3, tuning.rf4, tuning.ftpc3, tuning.ftpc4,
-                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0};
+                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0, tuning.noy3};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,
@@ -599,6 +599,7 @@ Status Engine::autotune(int* chosen, std::string& err) {
             tuning.fbps4 = kv.second.fbps4;
             tuning.want_fact3 = kv.second.want_fact3;
             tuning.want_fact4 = kv.second.want_fact4;
+            tuning.noy3 = kv.second.noy3;
             tuning.fact3 = avail_fact3_ && tuning.want_fact3;
             tuning.fact4 = avail_fact4_ && tuning.want_fact4;
             report();
@@ -636,27 +637,32 @@ Status Engine::autotune(int* chosen, std::string& err) {
     const bool do3 = tuning.stride3 > 0, do4 = tuning.stride4 > 0;
     // candidates per body order: factored kernels (1, 2, 4 lanes per cluster)
     // where the tables exist, then the per-coefficient kernels (1..32 lanes)
-    struct Cand { int fact, tpc; };
-    auto cands = [](bool can_fact) {
+    // (3-body factored also without its Y table)
+    struct Cand { int fact, tpc, noy; };
+    auto cands = [](bool can_fact, bool with_noy) {
         std::vector<Cand> v;
         if (can_fact)
-            for (int t : {1, 2, 4}) v.push_back({1, t});
-        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t});
+            for (int t : {1, 2, 4}) {
+                v.push_back({1, t, 0});
+                if (with_noy) v.push_back({1, t, 1});
+            }
+        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0});
         return v;
     };
-    const std::vector<Cand> c3 = cands(avail_fact3_), c4 = cands(avail_fact4_);
+    const std::vector<Cand> c3 = cands(avail_fact3_, true), c4 = cands(avail_fact4_, false);
     auto apply = [&](int nb, const Cand& c) {
         if (nb == 3) {
             tuning.fact3 = c.fact;
             (c.fact ? tuning.ftpc3 : tuning.tpc3) = c.tpc;
+            tuning.noy3 = c.noy;
         } else {
             tuning.fact4 = c.fact;
             (c.fact ? tuning.ftpc4 : tuning.tpc4) = c.tpc;
         }
     };
     double best3 = 1e300, best4 = 1e300;
-    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3};
-    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4};
+    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3};
+    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0};
     const size_t nc = std::max(c3.size(), c4.size());
     for (size_t i = 0; i < nc && st == kOk; i++) {
         const bool need3 = do3 && i < c3.size(), need4 = do4 && i < c4.size();

@@ -74,13 +74,39 @@ __device__ __forceinline__ CT entry_sum(const E* __restrict__ ent, int e0, int e
         for (int u = 0; u < 8; u++) q[u] = ent[k + u * TPC];
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
-            z0 += CT(q[u].a) * V[q[u].idx * G + grp];
-            z1 += CT(q[u + 1].a) * V[q[u + 1].idx * G + grp];
+            z0 += CT(q[u].a) * V[(q[u].idx & 0xffff) * G + grp];
+            z1 += CT(q[u + 1].a) * V[(q[u + 1].idx & 0xffff) * G + grp];
         }
     }
     for (; k < e1; k += TPC) {
         const E q = ent[k];
-        z0 += CT(q.a) * V[q.idx * G + grp];
+        z0 += CT(q.a) * V[(q.idx & 0xffff) * G + grp];
+    }
+    return z0 + z1;
+}
+
+// The 3-body row sum without a Y table: sum over [e0, e1) of a * T1[q1] T2[q2],
+// the column's powers q1, q2 taken from the entry's high bits.
+template <typename CT, int G, typename E>
+__device__ __forceinline__ CT entry_sum_noy(const E* __restrict__ ent, int e0, int e1, const CT* T1, const CT* T2,
+                                            int grp) {
+    CT z0 = CT(0), z1 = CT(0);
+    int k = e0;
+    for (; k + 3 < e1; k += 4) {
+        E q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) q[u] = ent[k + u];
+#pragma unroll
+        for (int u = 0; u < 4; u += 2) {
+            const int c0 = q[u].idx >> 16, c1 = q[u + 1].idx >> 16;
+            z0 += CT(q[u].a) * (T1[(c0 & 31) * G + grp] * T2[((c0 >> kPowBits) & 31) * G + grp]);
+            z1 += CT(q[u + 1].a) * (T1[(c1 & 31) * G + grp] * T2[((c1 >> kPowBits) & 31) * G + grp]);
+        }
+    }
+    for (; k < e1; k++) {
+        const E q = ent[k];
+        const int c = q.idx >> 16;
+        z0 += CT(q.a) * (T1[(c & 31) * G + grp] * T2[((c >> kPowBits) & 31) * G + grp]);
     }
     return z0 + z1;
 }
@@ -273,7 +299,10 @@ __global__ void __launch_bounds__(256) k_pair_tables(BatchView B, const int* l2_
 // interleaved [entry][cluster]:
 //   double geo[NP*4][G] (dr, r), fc[NP][G], fcd[NP][G]
 //   CT     T[NP*rs][G], D[NP*rs][G], Y[ys][G], X[xs][G]
-template <int NB, typename CT, int TPC>
+// NOY (3-body only): no Y table in shared memory; the row sums multiply the
+// two column pairs' Chebyshev values per entry instead (one more multiply per
+// coefficient, half the shared memory, so twice the resident warps).
+template <int NB, typename CT, int TPC, bool NOY = false>
 __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters, const int* perm,
                                                const long long* perm_n, long long perm_cap, int rs, int ys,
                                                int xs) {
@@ -374,6 +403,7 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
             constexpr int C = NP - K;
             int ny = 1;
             for (int p = K; p < NP; p++) ny *= Rp;
+            if (NOY) ny = 0;   // the row sums form the products themselves
             int q[C];
 #pragma unroll
             for (int p = 0; p < C; p++) q[p] = 0;
@@ -426,7 +456,11 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
             if (r < nrow) {
                 const FactRow rw = rows[r];
                 const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
-                const CT z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
+                CT z;
+                if constexpr (NOY && NB == 3)
+                    z = entry_sum_noy<CT, G>(ent, e0, rw.end, Tt + 1 * rs * G, Tt + 2 * rs * G, grp);
+                else
+                    z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
                 CT t[K], d[K];
 #pragma unroll
                 for (int p = 0; p < K; p++) {
@@ -495,7 +529,7 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
 }
 
 template <int NB, typename CT>
-size_t smem_bytes(int tpc, int rs) {
+size_t smem_bytes(int tpc, int rs, bool noy = false) {
     constexpr int NP = Topo<NB>::NP;
     constexpr int K = Split<NB>::K;
     const int G = 32 / tpc;
@@ -503,6 +537,7 @@ size_t smem_bytes(int tpc, int rs) {
     for (int p = K; p < NP; p++) ys *= rs;
     for (int p = 0; p < K; p++) xs *= rs;
     if (K == 1) xs = 0;
+    if (noy) ys = 0;
     return sizeof(double) * (size_t)NP * 6 * G + sizeof(CT) * (size_t)(2 * NP * rs + ys + xs) * G;
 }
 
@@ -515,18 +550,20 @@ void launch_f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
     const long long pcap = NB == 3 ? B.perm3_cap : B.perm4_cap;
     const int nbk = NB == 3 ? B.nbk3 : B.nbk4;
     if (pcap <= 0 || nbk <= 0 || rs <= 0) return;
+    const bool noy = NB == 3 && L.noy3;
     int ys = 1, xs = 1;
     for (int p = K; p < NP; p++) ys *= rs;
     for (int p = 0; p < K; p++) xs *= rs;
     if (K == 1) xs = 0;
-    const size_t smem = smem_bytes<NB, CT>(tpc, rs);
+    if (noy) ys = 0;
+    const size_t smem = smem_bytes<NB, CT>(tpc, rs, noy);
     const long long* pn = B.bk_start + (NB == 3 ? 0 : B.nbk3 + 1) + nbk;
     const int* clusters = NB == 3 ? B.c3 : B.c4;
     const int* perm = NB == 3 ? B.perm3 : B.perm4;
     const int want_bps = NB == 3 ? L.fbps3 : L.fbps4;
-#define CK_LAUNCH_F(T_)                                                                                  \
+#define CK_LAUNCH_F(T_, NOY_)                                                                            \
     do {                                                                                                 \
-        auto kern = k_forcef<NB, CT, T_>;                                                                \
+        auto kern = k_forcef<NB, CT, T_, NOY_>;                                                          \
         allow_max_smem((const void*)kern);                                                              \
         int occ = 0;                                                                                     \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, smem);                             \
@@ -536,10 +573,18 @@ void launch_f(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
         const unsigned grid = (unsigned)(want < steps ? want : steps);                                   \
         count_launch(), kern<<<grid, 32, smem, st>>>(B, clusters, perm, pn, pcap, rs, ys, xs);            \
     } while (0)
-    switch (tpc) {
-        case 1: CK_LAUNCH_F(1); break;
-        case 2: CK_LAUNCH_F(2); break;
-        default: CK_LAUNCH_F(4); break;
+    if (noy) {
+        switch (tpc) {
+            case 1: CK_LAUNCH_F(1, NB == 3); break;
+            case 2: CK_LAUNCH_F(2, NB == 3); break;
+            default: CK_LAUNCH_F(4, NB == 3); break;
+        }
+    } else {
+        switch (tpc) {
+            case 1: CK_LAUNCH_F(1, false); break;
+            case 2: CK_LAUNCH_F(2, false); break;
+            default: CK_LAUNCH_F(4, false); break;
+        }
     }
 #undef CK_LAUNCH_F
 }

@@ -47,6 +47,7 @@ struct ForceLaunch {
     int rf3 = 0, rf4 = 0;  // powers per pair (max over the batch's sets)
     int ftpc3 = 1, ftpc4 = 1;      // threads per cluster: 1, 2 or 4
     int fbps3 = 8, fbps4 = 8;      // resident one-warp blocks per SM (capped by occupancy)
+    int noy3 = 0;                  // factored 3-body without the Y table (products per entry)
 };
 
 // Cluster counts are read on the device (l2_off[n_atoms], e_off3/4[n2_cap]) and

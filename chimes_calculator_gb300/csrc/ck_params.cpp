@@ -772,6 +772,7 @@ ParamImage pack_params(const HostParams& P) {
                     const std::vector<int>& major = pass == 0 ? rowi : coli;
                     const std::vector<int>& minor = pass == 0 ? coli : rowi;
                     const std::vector<int>& mpows = pass == 0 ? rowp : colp;
+                    const std::vector<int>& opows = pass == 0 ? colp : rowp;   // the other side's powers
                     std::vector<int> ord(R.ncoef);
                     for (int c = 0; c < R.ncoef; c++) ord[c] = c;
                     std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
@@ -780,8 +781,9 @@ ParamImage pack_params(const HostParams& P) {
                     int nrec = 0;
                     for (int k = 0; k < R.ncoef; k++) {
                         const int c = ord[k];
-                        fed.push_back(FactEntD{Bd.coef[ti][c], minor[c], 0});
-                        fef.push_back(FactEntF{(float)Bd.coef[ti][c], minor[c]});
+                        const int code = minor[c] | (opows[c] << 16);
+                        fed.push_back(FactEntD{Bd.coef[ti][c], code, 0});
+                        fef.push_back(FactEntF{(float)Bd.coef[ti][c], code});
                         if (k + 1 == R.ncoef || major[ord[k + 1]] != major[c]) {
                             fr.push_back(FactRow{mpows[c], (int)fed.size()});
                             nrec++;

@@ -109,6 +109,12 @@ int main(int argc, char** argv) {
                 }
                 return v;
             };
+            // packed powers of n pairs (first pair lowest) -> linear index (first pair most significant)
+            auto packed_lin = [&](int pows, int n) {
+                int lin = 0;
+                for (int p = 0; p < n; p++) lin = lin * Rp + ((pows >> (kPowBits * p)) & 31);
+                return lin;
+            };
             double S1 = 0, G1[6] = {0, 0, 0, 0, 0, 0};
             int e = R.f_ent;
             if (R.f_nrow <= 0 || R.f_ncol <= 0) { std::printf("tuple %d without rows\n", u); return 1; }
@@ -116,11 +122,13 @@ int main(int argc, char** argv) {
                 const FactRow rw = fr[R.f_row + r];
                 double z = 0;
                 for (int k = e; k < rw.end; k++) {
-                    if (fe[k].idx < 0 || fe[k].idx >= ny || ff[k].idx != fe[k].idx || ff[k].a != (float)fe[k].a) {
+                    const int lin = fe[k].idx & 0xffff;
+                    if (lin >= ny || ff[k].idx != fe[k].idx || ff[k].a != (float)fe[k].a ||
+                        packed_lin(fe[k].idx >> 16, np - K) != lin) {
                         std::printf("bad row entry\n");
                         return 1;
                     }
-                    z += fe[k].a * prod_of(fe[k].idx, K, np, -1);
+                    z += fe[k].a * prod_of(lin, K, np, -1);
                 }
                 e = rw.end;
                 S1 += prod_packed(rw.pows, 0, K, -1) * z;
@@ -131,11 +139,13 @@ int main(int argc, char** argv) {
                 const FactRow cl = fr[R.f_row + R.f_nrow + c];
                 double w = 0;
                 for (int k = e; k < cl.end; k++) {
-                    if (fe[k].idx < 0 || fe[k].idx >= nx || ff[k].idx != fe[k].idx) {
+                    const int lin = fe[k].idx & 0xffff;
+                    if (lin >= nx || ff[k].idx != fe[k].idx ||
+                        packed_lin(fe[k].idx >> 16, K) != lin) {
                         std::printf("bad column entry\n");
                         return 1;
                     }
-                    w += fe[k].a * prod_of(fe[k].idx, 0, K, -1);
+                    w += fe[k].a * prod_of(lin, 0, K, -1);
                 }
                 e = cl.end;
                 for (int p = K; p < np; p++) G1[p] += prod_packed(cl.pows, K, np, p) * w;

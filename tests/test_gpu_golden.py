@@ -23,7 +23,7 @@ def evaluate(g, precision=0, graph=False, tpc=None, factored=True):
     return c, r
 
 
-@pytest.mark.parametrize("factored", [1, 2, 0], ids=["factored", "factored_nocache", "per_coef"])
+@pytest.mark.parametrize("factored", [1, 2, 3, 0], ids=["factored", "factored_nocache", "factored_noy", "per_coef"])
 @pytest.mark.parametrize("name", golden_names())
 def test_fp64_matches_reference(golden, native_lib, name, factored):
     g = golden[name]
@@ -48,7 +48,7 @@ def test_lists_match_oracle(golden, native_lib, name):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("factored", [1, 2, 0], ids=["factored", "factored_nocache", "per_coef"])
+@pytest.mark.parametrize("factored", [1, 2, 3, 0], ids=["factored", "factored_nocache", "factored_noy", "per_coef"])
 @pytest.mark.parametrize("name", golden_names())
 def test_mixed_precision_error(golden, native_lib, name, factored):
     g = golden[name]
