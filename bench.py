@@ -122,8 +122,8 @@ class ClockSampler:
 PROFILED_TRAFFIC = {
     "k_forcef<3,double,1>": 4272384,
     "k_forcef<4,double,4>": 2047488,
-    "k_forcen<3,double,4>": 842000,
-    "k_forcen<4,double,8>": 522000,
+    "k_forcen<3,double,4>": 872704,
+    "k_forcen<4,double,8>": 599552,
 }
 
 

@@ -81,6 +81,20 @@ __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner
 // ---------------------------------------------------------------------------
 // 3-body and 4-body clusters
 // ---------------------------------------------------------------------------
+// Shared memory of one cluster group: its T and dT/dr tables (CT), then the
+// pair geometry and cutoff values (double).  The group stride is an odd
+// number of 8-byte words, so the groups of a warp start on different banks and
+// lanes reading the same table entry of their own cluster do not conflict (a
+// stride that is a multiple of 32 bytes put every fourth group on the same bank).
+__host__ __device__ inline size_t forcen_table_bytes(int np, int stride, size_t ct) {
+    return ((size_t)2 * np * stride * ct + 7) & ~size_t(7);
+}
+__host__ __device__ inline size_t forcen_group_bytes(int np, int stride, size_t ct) {
+    size_t g = forcen_table_bytes(np, stride, ct) + sizeof(double) * np * 6;
+    if (((g / 8) & 1) == 0) g += 8;
+    return g;
+}
+
 template <int NB, typename CT, int TPC>
 __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters, const long long* n_ptr,
                                                 long long cap, int stride) {
@@ -92,8 +106,8 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
     const int warp_in_block = threadIdx.x >> 5;
     const int grp = lane / TPC, gl = lane % TPC;
     // per-group shared layout: T[NP*stride], D[NP*stride] (CT); geo[NP][4], fc[NP], fcd[NP] (double)
-    const size_t tbytes = ((size_t)2 * NP * stride * sizeof(CT) + 15) & ~size_t(15);
-    const size_t gbytes = tbytes + sizeof(double) * NP * 6;
+    const size_t tbytes = forcen_table_bytes(NP, stride, sizeof(CT));
+    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT));
     unsigned char* gbase = smem + ((size_t)warp_in_block * G + grp) * gbytes;
     CT* T = reinterpret_cast<CT*>(gbase);
     CT* D = T + NP * stride;
@@ -229,8 +243,7 @@ void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, l
     if (n <= 0) return;
     constexpr int NP = NB * (NB - 1) / 2;
     const int block = 128;
-    const size_t tbytes = ((size_t)2 * NP * stride * sizeof(CT) + 15) & ~size_t(15);
-    const size_t gbytes = tbytes + sizeof(double) * NP * 6;
+    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT));
     const int G = 32 / tpc;
     const size_t smem = gbytes * G * (block / 32);
     const long long steps = (n + G - 1) / G;
