@@ -83,6 +83,8 @@ SIGNATURES = {
     "ck_last_diagnostics": (I, [P, IP]),
     "ck_export_lists": (I, [P, IP, IP, IP]),
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
+    "ck_compute_cluster_batch_tab": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
+    "ck_tabulated": (I, [P, IP]),
     "ck_calculate_noalloc": (I, [P, I, P, P, DP, I, P, P, P, P]),
     "ck_nl_compute": (I, [P, I, DP, IP, LLP, I, IP, IP, IP, D, I, DP, DP, DP, DP, DP]),
     "ck_nl_lists": (I, [P, LLP, IP, IP]),

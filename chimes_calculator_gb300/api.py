@@ -162,6 +162,29 @@ class Calculator:
         self._check(self.lib.ck_nl_lists(self.h, cnt, _ip(l3), _ip(l4)))
         return l3, l4
 
+    def tabulated(self):
+        """(2-body tabulated, 3-body tabulated) for the current parameter set."""
+        t = np.zeros(2, dtype=np.int32)
+        self._check(self.lib.ck_tabulated(self.h, _ip(t)))
+        return bool(t[0]), bool(t[1])
+
+    def clusters(self, nbody: int, dx, dr, typ, tab: bool = False):
+        """Per-cluster evaluation of n clusters (compute_nB, or compute_2B_tab /
+        compute_3B_tab with tab=True): dx[n][P], dr[n][P][3], typ[n][nbody] ->
+        dict of per-cluster energy[n], force[n][nbody][3], stress[n][6] and the
+        reference's force scalars fscal[n][P]."""
+        P = nbody * (nbody - 1) // 2
+        dx = np.ascontiguousarray(dx, dtype=np.float64).reshape(-1, P)
+        n = dx.shape[0]
+        dr = np.ascontiguousarray(dr, dtype=np.float64).reshape(n, P, 3)
+        typ = np.ascontiguousarray(typ, dtype=np.int32).reshape(n, nbody)
+        force, stress = np.zeros((n, nbody, 3)), np.zeros((n, 6))
+        energy, fscal = np.zeros(n), np.zeros((n, P))
+        fn = self.lib.ck_compute_cluster_batch_tab if tab else self.lib.ck_compute_cluster_batch
+        self._check(fn(self.h, nbody, n, _dp(dx), _dp(dr), _ip(typ), _dp(force), _dp(stress), _dp(energy),
+                       _dp(fscal)))
+        return {"energy": energy, "force": force, "stress": stress, "fscal": fscal}
+
     def set_contraction(self, factored=True):
         """3-/4-body contraction kernels: True/1 factored (default), False/0
         per-coefficient, 2 factored without the per-entry pair-table cache,

@@ -560,6 +560,38 @@ int ck_compute_cluster_batch(void* h, int nbody, int n, const double* dx, const 
     return ck::kOk;
 }
 
+int ck_compute_cluster_batch_tab(void* h, int nbody, int n, const double* dx, const double* dr, const int* typ,
+                                 double* force, double* stress, double* energy, double* fscal) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    if (nbody != 2 && nbody != 3) return report(ck::kErrInput, "tabulated clusters have 2 or 3 atoms");
+    std::vector<int> status(n > 0 ? n : 1, 0);
+    std::vector<double> fs;
+    if (!fscal) fs.resize((size_t)(n > 0 ? n : 1) * 3);
+    std::string err;
+    ck::Status st = in->eng.compute_clusters(in->slot, nbody, n, dx, dr, typ, force, stress, energy,
+                                             fscal ? fscal : fs.data(), status.data(), err, true);
+    if (st != ck::kOk) return report(st, err);
+    for (int c = 0; c < n; c++)
+        if (status[c] & 16)
+            return report(ck::kErrGeometry, nbody == 2 ? "Distance is outside the tabulated range (cluster " +
+                                                             std::to_string(c) + ")"
+                                                       : "3-body distance past the tabulated grid (cluster " +
+                                                             std::to_string(c) + ")");
+    return ck::kOk;
+}
+
+int ck_tabulated(void* h, int* tab) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    const ck::HostParams& P = in->eng.params(in->slot);
+    tab[0] = P.tab2 ? 1 : 0;
+    tab[1] = P.tab3 ? 1 : 0;
+    return ck::kOk;
+}
+
 int ck_export_lists(void* h, int* l2, int* l3, int* l4) {
     if (int st = check_handle(h)) return st;
     std::vector<int> a, b, c;

@@ -34,17 +34,22 @@ const ck::HostParams* params_of(chimesFF::Impl* im) {
 
 // One cluster through the per-cluster kernel; adds into the caller's buffers.
 bool one_cluster(chimesFF::Impl* im, int nbody, const double* dx, const double* dr, const int* typ, double* force,
-                 double* stress, double& energy, double* fscal_out) {
+                 double* stress, double& energy, double* fscal_out, bool tab = false) {
     const int np = nbody * (nbody - 1) / 2;
     double f[12], s[6], e, fs[6];
     int status = 0;
     std::string err;
-    ck::Status st = im->eng.compute_clusters(im->slot, nbody, 1, dx, dr, typ, f, s, &e, fs, &status, err);
+    ck::Status st = im->eng.compute_clusters(im->slot, nbody, 1, dx, dr, typ, f, s, &e, fs, &status, err, tab);
     if (st != ck::kOk) {
         ck::report_error(st, err);
         return false;
     }
     if (!(status & 1)) return true;   // excluded type or beyond a cutoff: nothing added
+    if (status & 16) {   // get_tab_2B prints this and exits; a 3-body grid index past the table
+        ck::report_error(ck::kErrGeometry, nbody == 2 ? "Distance is outside the tabulated range"
+                                                      : "3-body distance past the tabulated grid");
+        return false;
+    }
     for (int k = 0; k < 3 * nbody; k++) force[k] += f[k];
     for (int k = 0; k < 6; k++) stress[k] += s[k];
     energy += e;
@@ -60,7 +65,7 @@ bool one_cluster(chimesFF::Impl* im, int nbody, const double* dx, const double* 
 // ---------------------------------------------------------------------------
 // chimesFF
 // ---------------------------------------------------------------------------
-chimesFF::chimesFF() : rank(0), natmtyps(0), impl_(new Impl()) {}
+chimesFF::chimesFF() : rank(0), natmtyps(0), tabulate_2B(false), tabulate_3B(false), impl_(new Impl()) {}
 chimesFF::~chimesFF() { delete impl_; }
 
 void chimesFF::init(int mpi_rank) { rank = mpi_rank; }
@@ -78,6 +83,8 @@ void chimesFF::read_parameters(std::string paramfile) {
     poly_orders = {P.o2, P.o3, P.o4};
     atmtyps = P.atm;
     masses = P.mass;
+    tabulate_2B = P.tab2;
+    tabulate_3B = P.tab3;
 }
 
 void chimesFF::compute_1B(const int typ_idx, double& energy) {
@@ -118,6 +125,42 @@ void chimesFF::compute_3B(const std::vector<double>& dx, const std::vector<doubl
     if (force_scalar_in.size() < 3) force_scalar_in.resize(3);
     one_cluster(impl_, 3, dx.data(), dr.data(), typ_idxs.data(), force.data(), stress.data(), energy,
                 force_scalar_in.data());
+}
+
+void chimesFF::compute_2B_tab(const double dx, const std::vector<double>& dr, const std::vector<int> typ_idxs,
+                              std::vector<double>& force, std::vector<double>& stress, double& energy,
+                              chimes2BTmp& tmp) {
+    double fs = 0.0;
+    compute_2B_tab(dx, dr, typ_idxs, force, stress, energy, tmp, fs);
+}
+
+void chimesFF::compute_2B_tab(const double dx, const std::vector<double>& dr, const std::vector<int> typ_idxs,
+                              std::vector<double>& force, std::vector<double>& stress, double& energy, chimes2BTmp&,
+                              double& force_scalar_in) {
+    if (!params_of(impl_)) return;
+    if (dr.size() < 3 || typ_idxs.size() < 2 || force.size() < 6 || stress.size() < 6)
+        return die("compute_2B_tab: dr needs 3, typ_idxs 2, force 6 and stress 6 entries");
+    one_cluster(impl_, 2, &dx, dr.data(), typ_idxs.data(), force.data(), stress.data(), energy, &force_scalar_in,
+                true);
+}
+
+void chimesFF::compute_3B_tab(const std::vector<double>& dx, const std::vector<double>& dr,
+                              const std::vector<int>& typ_idxs, std::vector<double>& force,
+                              std::vector<double>& stress, double& energy, chimes3BTmp& tmp) {
+    std::vector<double> fs(3);
+    compute_3B_tab(dx, dr, typ_idxs, force, stress, energy, tmp, fs);
+}
+
+void chimesFF::compute_3B_tab(const std::vector<double>& dx, const std::vector<double>& dr,
+                              const std::vector<int>& typ_idxs, std::vector<double>& force,
+                              std::vector<double>& stress, double& energy, chimes3BTmp&,
+                              std::vector<double>& force_scalar_in) {
+    if (!params_of(impl_)) return;
+    if (dx.size() < 3 || dr.size() < 9 || typ_idxs.size() < 3 || force.size() < 9 || stress.size() < 6)
+        return die("compute_3B_tab: dx needs 3, dr 9, typ_idxs 3, force 9 and stress 6 entries");
+    if (force_scalar_in.size() < 3) force_scalar_in.resize(3);
+    one_cluster(impl_, 3, dx.data(), dr.data(), typ_idxs.data(), force.data(), stress.data(), energy,
+                force_scalar_in.data(), true);
 }
 
 void chimesFF::compute_4B(const std::vector<double>& dx, const std::vector<double>& dr,

@@ -105,6 +105,32 @@ struct __attribute__((aligned(8))) FactEntF {
     int idx;
 };
 
+// Tabulated 2-body term of one pair type (TABULATION build of the reference:
+// read_2B_tab and get_tab_2B, chimesFF/src/chimesFF.cpp:199-255, 1869-1922).
+// Grid r[0..n) ascending at tab2r[off..]; for every interval start i
+// (1 <= i <= n-2) the local cubic a + b*dx + c*dx^2 + d*dx^3 of the energy and
+// of the force scalar at tab2c[8*(off+i) ..] (E a,b,c,d then F a,b,c,d),
+// computed on the host with get_tab_2B's arithmetic.
+struct Tab2Rec {
+    long long off;
+    int n;
+    int pad;
+};
+
+// Tabulated 3-body term of one triplet type (read_3B_tab, interpolateTricubic,
+// chimesFF.cpp:257-351, 2370-2440): nrows rows of (rij, rik, rjk) with rij the
+// slowest and rjk the fastest coordinate, columns at tab3r[3*off ..] (rij
+// column, then rik, then rjk, nrows each) and values (E, F_ij, F_ik, F_jk) at
+// tab3v[4*(off+row) ..].  size = (int)cbrt(nrows); inv = 1 / (grid step),
+// computed as interpolateTricubic does.
+struct Tab3Rec {
+    long long off;
+    long long nrows;
+    int size;
+    int pad;
+    double inv;
+};
+
 struct DevParamSet {
     int ntypes, npairs, o2, o3, o4;
     int tersoff;
@@ -126,6 +152,12 @@ struct DevParamSet {
     const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
     // per-pair-type tables [npairs] (null when some tuple's cutoffs differ by tuple)
     const PairTab* pt3; const PairTab* pt4;
+    // tabulated terms: 2-body tables looked up by pair type index, 3-body
+    // tables by triplet type index (the reference's tab_*[pair_idx / tripidx])
+    int tab2, tab3;            // 1 when the 2B / 3B terms are tabulated
+    int n_tab2, n_tab3;        // tables present
+    const Tab2Rec* t2rec; const double* tab2r; const double* tab2c;
+    const Tab3Rec* t3rec; const double* tab3r; const double* tab3v;
 };
 
 // Per-system geometry, written by the host set-up (cell algebra) and

@@ -10,12 +10,15 @@
 // coefficient of the list, as the reference's loop leaves them.  status bits:
 // 1 = the cluster passed the type and cutoff checks, 2 = penalty region
 // (badness 1), 4 = below the inner cutoff (badness 2), 8 = a many-body pair below
-// its inner cutoff (the reference prints a warning; badness is unchanged).
+// its inner cutoff (the reference prints a warning; badness is unchanged),
+// 16 = a tabulated term's distance outside its table (the reference exits or
+// reads past its table there).
 #include <cuda_runtime.h>
 
 #include "ck_common.h"
 #include "ck_kernels.h"
 #include "ck_math.cuh"
+#include "ck_tab.cuh"
 
 namespace ck {
 
@@ -166,12 +169,104 @@ __global__ void k_directn(const DevParamSet* Pp, int n, const double* dx, const 
     status[c] = st;
 }
 
+// compute_2B_tab (chimesFF.cpp:1782-1867): table energy and force scalar;
+// force_scalar_in is get_penalty's value (1.0, or the penalty slope inside the
+// penalty region), which overwrites the table's scalar at the end.
+__global__ void k_direct2tab(const DevParamSet* Pp, int n, const double* dx, const double* dr, const int* typ,
+                             double* force, double* stress, double* energy, double* fscal, int* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const DevParamSet& P = *Pp;
+    for (int k = 0; k < 6; k++) { force[6 * c + k] = 0.0; stress[6 * c + k] = 0.0; }
+    energy[c] = 0.0;
+    fscal[c] = 0.0;
+    status[c] = 0;
+    const int pt = P.pair_map[typ[2 * c] * P.ntypes + typ[2 * c + 1]];
+    const PairRec pr = P.pairs[pt];
+    const double r = dx[c];
+    const double* d = &dr[3 * c];
+    if (r >= pr.rout) return;
+    int st = 1;
+    double E, fs;
+    if (tab2_lookup(P, pt, r, E, fs) != kTabOk) st |= 16;
+    for (int k = 0; k < 3; k++) {
+        force[6 * c + k] = __dmul_rn(fs, d[k]);
+        force[6 * c + 3 + k] = __dsub_rn(0.0, __dmul_rn(fs, d[k]));
+    }
+    stress[6 * c + 0] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[0]), d[0]));
+    stress[6 * c + 1] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[0]), d[1]));
+    stress[6 * c + 2] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[0]), d[2]));
+    stress[6 * c + 3] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[1]), d[1]));
+    stress[6 * c + 4] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[1]), d[2]));
+    stress[6 * c + 5] = __dsub_rn(0.0, __dmul_rn(__dmul_rn(fs, d[2]), d[2]));
+    double fs_out = 1.0;
+    if (r - P.pen_dist < pr.rin) {
+        st |= r < pr.rin ? 4 : 2;
+        const double rp = pr.rin + P.pen_dist - r;
+        if (rp > 0.0) fs_out = __dmul_rn(__dmul_rn(__dmul_rn(-3.0, rp), rp), P.pen_scale);
+    }
+    energy[c] = E;
+    fscal[c] = fs_out;
+    status[c] = st;
+}
+
+// compute_3B_tab (chimesFF.cpp:2183-2322): the type and per-pair outer-cutoff
+// checks of compute_3B, then the tricubic look-up; force_scalar_in receives the
+// three table force scalars.
+__global__ void k_direct3tab(const DevParamSet* Pp, int n, const double* dx, const double* dr, const int* typ,
+                             double* force, double* stress, double* energy, double* fscal, int* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const DevParamSet& P = *Pp;
+    for (int k = 0; k < 9; k++) force[9 * c + k] = 0.0;
+    for (int k = 0; k < 6; k++) stress[6 * c + k] = 0.0;
+    for (int k = 0; k < 3; k++) fscal[3 * c + k] = 0.0;
+    energy[c] = 0.0;
+    status[c] = 0;
+    const int u = (typ[3 * c] * P.ntypes + typ[3 * c + 1]) * P.ntypes + typ[3 * c + 2];
+    const TupleRec& R = P.t3[u];
+    if (R.type_id < 0) return;
+    const double* r = &dx[3 * c];
+    for (int p = 0; p < 3; p++)
+        if (r[p] >= R.rout[p]) return;
+    double v[4];
+    int st = 1;
+    if (tab3_lookup(P, R.type_id, r[0], r[1], r[2], v) != kTabOk) st |= 16;
+    double f[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vir[6] = {0, 0, 0, 0, 0, 0};
+    for (int p = 0; p < 3; p++) {
+        const double fsp = v[1 + p];
+        const double* d = &dr[9 * c + 3 * p];
+        const int a = Topo<3>::a(p), b = Topo<3>::b(p);
+        for (int k = 0; k < 3; k++) {
+            f[3 * a + k] = __dadd_rn(f[3 * a + k], __dmul_rn(fsp, d[k]));
+            f[3 * b + k] = __dsub_rn(f[3 * b + k], __dmul_rn(fsp, d[k]));
+        }
+        vir[0] = __dsub_rn(vir[0], __dmul_rn(fsp, __dmul_rn(d[0], d[0])));
+        vir[1] = __dsub_rn(vir[1], __dmul_rn(fsp, __dmul_rn(d[0], d[1])));
+        vir[2] = __dsub_rn(vir[2], __dmul_rn(fsp, __dmul_rn(d[0], d[2])));
+        vir[3] = __dsub_rn(vir[3], __dmul_rn(fsp, __dmul_rn(d[1], d[1])));
+        vir[4] = __dsub_rn(vir[4], __dmul_rn(fsp, __dmul_rn(d[1], d[2])));
+        vir[5] = __dsub_rn(vir[5], __dmul_rn(fsp, __dmul_rn(d[2], d[2])));
+    }
+    for (int k = 0; k < 9; k++) force[9 * c + k] = f[k];
+    for (int k = 0; k < 6; k++) stress[6 * c + k] = vir[k];
+    for (int k = 0; k < 3; k++) fscal[3 * c + k] = v[1 + k];
+    energy[c] = v[0];
+    status[c] = st;
+}
+
 }  // namespace
 
 void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
-                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st) {
+                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st,
+                   bool tab) {
     if (n <= 0) return;
     const unsigned grid = (unsigned)((n + 63) / 64);
+    if (tab) {
+        if (nbody == 2) count_launch(), k_direct2tab<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+        else count_launch(), k_direct3tab<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+        return;
+    }
     if (nbody == 2) count_launch(), k_direct2<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
     else if (nbody == 3) count_launch(), k_directn<3><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
     else count_launch(), k_directn<4><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);

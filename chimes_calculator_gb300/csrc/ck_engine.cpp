@@ -117,6 +117,8 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.fr3); rel(h.fe3d); rel(h.fe3f);
     rel(h.fr4); rel(h.fe4d); rel(h.fe4f);
     rel(h.pt3); rel(h.pt4);
+    rel(h.t2rec); rel(h.tab2r); rel(h.tab2c);
+    rel(h.t3rec); rel(h.tab3r); rel(h.tab3v);
     // this set's cluster buckets follow those of the sets loaded before it
     int nt3 = h.ntypes * h.ntypes * h.ntypes;
     h.bk3 = nbk3_;
@@ -162,6 +164,13 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
             return kErrState;
         }
         const HostParams& P = *sets_[in.pset].host;
+        if (P.tab2 || P.tab3) {
+            // the reference evaluates tabulated terms only in its LAMMPS pair
+            // style; its serial interface has no coefficients to expand for them
+            err = "tabulated parameter sets are evaluated on a neighbour list (ck_nl_compute) or per cluster "
+                  "(chimesFF::compute_2B_tab / compute_3B_tab), not by the serial interface";
+            return kErrParam;
+        }
         SysDesc& d = hsys_[s];
         std::memset(&d, 0, sizeof(d));
         std::string gerr;
@@ -721,7 +730,7 @@ Status Engine::autotune(int* chosen, std::string& err) {
 
 Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, const double* dr, const int* typ,
                                 double* force, double* stress, double* energy, double* fscal, int* status,
-                                std::string& err) {
+                                std::string& err, bool tab) {
     Status st = init_device(err);
     if (st != kOk) return st;
     if (slot < 0 || slot >= (int)sets_.size()) {
@@ -736,6 +745,16 @@ Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, co
     const HostParams& P = *sets_[slot].host;
     if ((nbody == 3 && P.o3 <= 0) || (nbody == 4 && P.o4 <= 0)) {
         err = "the parameter set has no " + std::to_string(nbody) + "-body terms";
+        return kErrInput;
+    }
+    const bool tabbed = (nbody == 2 && P.tab2) || (nbody == 3 && P.tab3);
+    if (tab && !tabbed) {
+        err = "the parameter set's " + std::to_string(nbody) + "-body terms are not tabulated";
+        return kErrInput;
+    }
+    if (!tab && tabbed) {
+        err = "the parameter set's " + std::to_string(nbody) + "-body terms are tabulated (use compute_" +
+              std::to_string(nbody) + "B_tab)";
         return kErrInput;
     }
     for (long long i = 0; i < (long long)n * nbody; i++)
@@ -759,7 +778,8 @@ Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, co
     CK_TRY(cudaMemcpyAsync(ddx, dx, sizeof(double) * n * np, cudaMemcpyHostToDevice, stream_));
     CK_TRY(cudaMemcpyAsync(ddr, dr, sizeof(double) * n * np * 3, cudaMemcpyHostToDevice, stream_));
     CK_TRY(cudaMemcpyAsync(dtyp, typ, sizeof(int) * n * nbody, cudaMemcpyHostToDevice, stream_));
-    launch_direct(dsets_.p + slot, nbody, n, ddx, ddr, dtyp, dforce, dstress, denergy, dfscal, dstatus, stream_);
+    launch_direct(dsets_.p + slot, nbody, n, ddx, ddr, dtyp, dforce, dstress, denergy, dfscal, dstatus, stream_,
+                  tab);
     CK_TRY(cudaGetLastError());
     CK_TRY(cudaMemcpyAsync(force, dforce, sizeof(double) * n * 3 * nbody, cudaMemcpyDeviceToHost, stream_));
     CK_TRY(cudaMemcpyAsync(stress, dstress, sizeof(double) * n * 6, cudaMemcpyDeviceToHost, stream_));

@@ -141,7 +141,7 @@ public:
     // force scalars fscal[n][P] and status[n] (see ck_direct.cu).
     Status compute_clusters(int slot, int nbody, int n, const double* dx, const double* dr, const int* typ,
                             double* force, double* stress, double* energy, double* fscal, int* status,
-                            std::string& err);
+                            std::string& err, bool tab = false);
 
     // Cluster lists of the last run in system-local ghost numbering (the
     // reference's sys_parent/ghost indices), for set comparisons.

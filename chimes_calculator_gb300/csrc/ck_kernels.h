@@ -72,10 +72,12 @@ size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st);
 void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st);
 void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st);
+void launch_nl_tab3(const BatchView& B, long long n3, cudaStream_t st);
 
 // Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
 void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
-                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st);
+                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st,
+                   bool tab = false);
 
 int sm_count();
 

@@ -23,6 +23,7 @@
 #include "ck_force_common.cuh"
 #include "ck_kernels.h"
 #include "ck_math.cuh"
+#include "ck_tab.cuh"
 
 namespace ck {
 
@@ -73,10 +74,22 @@ __global__ void __launch_bounds__(256) k_nl_pairs(BatchView B, NeighView N) {
         if (N.tag[j] <= N.tag[i]) continue;
         double dr[3];
         const double dist = nl_dist(x, i, j, dr);
-        const PairRec pr = P.pairs[P.pair_map[B.atom_type[i] * P.ntypes + B.atom_type[j]]];
+        const int pt = P.pair_map[B.atom_type[i] * P.ntypes + B.atom_type[j]];
+        const PairRec pr = P.pairs[pt];
         if (dist >= pr.rout) continue;
         double E, fs;
-        pair_2b<CT>(P, pr, dist, B.flags, E, fs);
+        if (P.tab2) {
+            // compute_2B_tab (chimesFF.cpp:1782-1867): table energy and force
+            // scalar; the penalty only records badness (the table includes it)
+            const int ts = tab2_lookup(P, pt, dist, E, fs);
+            if (ts) atomicOr(&B.flags[5], ts);
+            if (dist - P.pen_dist < pr.rin) {
+                atomicMax(&B.flags[2], dist < pr.rin ? 2 : 1);
+                if (pr.rin + P.pen_dist - dist > 0.0) atomicAdd(&B.flags[3], 1);
+            }
+        } else {
+            pair_2b<CT>(P, pr, dist, B.flags, E, fs);
+        }
         add_force(B, i, fs * dr[0], fs * dr[1], fs * dr[2]);
         add_force(B, j, -fs * dr[0], -fs * dr[1], -fs * dr[2]);
         virial_add(vir, fs, dr);
@@ -173,6 +186,54 @@ __global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
     }
 }
 
+// Tabulated 3-body term (compute_3B_tab, chimesFF.cpp:2183-2322) of every
+// listed triplet: one thread per triplet; the type and per-pair outer-cutoff
+// checks of compute_3B, then the tricubic table look-up.
+__global__ void __launch_bounds__(128) k_nl_tab3(BatchView B, long long n3) {
+    const DevParamSet& P = B.psets[B.sys[0].pset];
+    const double* x = B.ghost_fs;
+    EVAcc acc;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += stride) {
+        const int id[3] = {B.c3[3 * q], B.c3[3 * q + 1], B.c3[3 * q + 2]};
+        const int u = (B.atom_type[id[0]] * P.ntypes + B.atom_type[id[1]]) * P.ntypes + B.atom_type[id[2]];
+        const TupleRec& R = P.t3[u];
+        if (R.type_id < 0) continue;   // excluded triplet type
+        double dr[3][3], r[3];
+        r[0] = nl_dist(x, id[0], id[1], dr[0]);   // ij
+        r[1] = nl_dist(x, id[0], id[2], dr[1]);   // ik
+        r[2] = nl_dist(x, id[1], id[2], dr[2]);   // jk
+        if (r[0] >= R.rout[0] || r[1] >= R.rout[1] || r[2] >= R.rout[2]) continue;
+        double v[4];
+        const int ts = tab3_lookup(P, R.type_id, r[0], r[1], r[2], v);
+        if (ts) atomicOr(&B.flags[5], ts);
+        // forces in the reference's order: ij on (i, j), ik on (i, k), jk on (j, k)
+        double f[3][3];
+        for (int c = 0; c < 3; c++) {
+            const double a = __dmul_rn(v[1], dr[0][c]), b = __dmul_rn(v[2], dr[1][c]), g = __dmul_rn(v[3], dr[2][c]);
+            f[0][c] = __dadd_rn(__dadd_rn(0.0, a), b);
+            f[1][c] = __dadd_rn(__dsub_rn(0.0, a), g);
+            f[2][c] = __dsub_rn(__dsub_rn(0.0, b), g);
+        }
+        // stress -= fs_p * (dr_p (x) dr_p), pair by pair (distance-tensor form)
+        double vir[6] = {0, 0, 0, 0, 0, 0};
+        for (int p = 0; p < 3; p++) {
+            const double* d = dr[p];
+            const double fsp = v[1 + p];
+            vir[0] = __dsub_rn(vir[0], __dmul_rn(fsp, __dmul_rn(d[0], d[0])));
+            vir[1] = __dsub_rn(vir[1], __dmul_rn(fsp, __dmul_rn(d[0], d[1])));
+            vir[2] = __dsub_rn(vir[2], __dmul_rn(fsp, __dmul_rn(d[0], d[2])));
+            vir[3] = __dsub_rn(vir[3], __dmul_rn(fsp, __dmul_rn(d[1], d[1])));
+            vir[4] = __dsub_rn(vir[4], __dmul_rn(fsp, __dmul_rn(d[1], d[2])));
+            vir[5] = __dsub_rn(vir[5], __dmul_rn(fsp, __dmul_rn(d[2], d[2])));
+        }
+        for (int a = 0; a < 3; a++) add_force(B, id[a], f[a][0], f[a][1], f[a][2]);
+        acc.add(B, 0, v[0], vir);
+        tally_atoms(B, id, 3, v[0], vir);
+    }
+    acc.flush_warp(B);
+}
+
 unsigned grid_of(long long n, int block, long long cap_blocks) {
     long long need = (n + block - 1) / block;
     if (need < 1) need = 1;
@@ -200,6 +261,12 @@ void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cuda
     const unsigned grid = grid_of(ntot, 256, (long long)sm_count() * 8);
     if (precision == kMixed) count_launch(), k_nl_pairs<float><<<grid, 256, 0, st>>>(B, N);
     else count_launch(), k_nl_pairs<double><<<grid, 256, 0, st>>>(B, N);
+}
+
+void launch_nl_tab3(const BatchView& B, long long n3, cudaStream_t st) {
+    if (n3 <= 0) return;
+    const unsigned grid = grid_of(n3, 128, (long long)sm_count() * 16);
+    count_launch(), k_nl_tab3<<<grid, 128, 0, st>>>(B, n3);
 }
 
 }  // namespace ck

@@ -213,15 +213,19 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     // kernels get only those within their tuple's cutoffs at the current
     // positions (rebucketed every call, as atoms move between rebuilds).
     B.bucket_cut = 1;
-    if ((L.stride3 > 0 && L.fact3 && n3_ > 0) || (L.stride4 > 0 && L.fact4 && n4_ > 0)) {
+    // a tabulated 3-body term is looked up per listed triplet (no buckets)
+    const bool tab3 = P.tab3 && L.stride3 > 0;
+    const bool bk3 = L.stride3 > 0 && L.fact3 && n3_ > 0 && !tab3;
+    if (bk3 || (L.stride4 > 0 && L.fact4 && n4_ > 0)) {
         NL_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (nbk3 + nbk4), s));
         NL_TRY(cudaMemsetAsync(B.bk_fill, 0, sizeof(int) * (nbk3 + nbk4), s));
-        if (L.stride3 > 0 && L.fact3 && n3_ > 0) launch_bucket(B, 3, s);
+        if (bk3) launch_bucket(B, 3, s);
         if (L.stride4 > 0 && L.fact4 && n4_ > 0) launch_bucket(B, 4, s);
     }
     launch_nl_pairs(B, N, L.precision, s);
     if (L.stride3 > 0 && n3_ > 0) {
-        if (L.fact3) launch_force3f(B, L, s);
+        if (tab3) launch_nl_tab3(B, n3_, s);
+        else if (L.fact3) launch_force3f(B, L, s);
         else launch_force3(B, L, s);
     }
     if (L.stride4 > 0 && n4_ > 0) {
@@ -231,8 +235,10 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     NL_TRY(cudaGetLastError());
     h_force_.resize(3 * (size_t)nall);
     double ev[8];
+    int flags[8];
     NL_TRY(cudaMemcpyAsync(h_force_.data(), d_force_.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s));
     NL_TRY(cudaMemcpyAsync(ev, d_ev_.p, sizeof(double) * 8, cudaMemcpyDeviceToHost, s));
+    NL_TRY(cudaMemcpyAsync(flags, d_flags_.p, sizeof(int) * 8, cudaMemcpyDeviceToHost, s));
     if (eatom) {
         h_eatom_.resize(nall);
         NL_TRY(cudaMemcpyAsync(h_eatom_.data(), d_eatom_.p, sizeof(double) * nall, cudaMemcpyDeviceToHost, s));
@@ -242,6 +248,16 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
         NL_TRY(cudaMemcpyAsync(h_vatom_.data(), d_vatom_.p, sizeof(double) * 6 * nall, cudaMemcpyDeviceToHost, s));
     }
     NL_TRY(cudaStreamSynchronize(s));
+    badness_ = flags[2];
+    if (flags[5] & 1) {   // get_tab_2B prints and exits here
+        err = "Distance is outside the tabulated range (a 2-body distance at or below the table's first usable "
+              "grid point)";
+        return kErrGeometry;
+    }
+    if (flags[5] & 2) {
+        err = "a 3-body distance lies past the tabulated grid (the table does not cover the 3-body cutoffs)";
+        return kErrGeometry;
+    }
     for (size_t k = 0; k < h_force_.size(); k++) f[k] += h_force_[k];
     if (eatom)
         for (int a = 0; a < nall; a++) eatom[a] += h_eatom_[a];

@@ -26,13 +26,15 @@ public:
                    double* energy, double* virial, double* eatom, double* vatom, std::string& err);
 
     long long n3() const { return n3_; }
+    // worst 2-body penalty region entered by the last call (chimesFF badness: 0, 1, 2)
+    int badness() const { return badness_; }
     long long n4() const { return n4_; }
     // cluster lists of the last build (atom indices), for checks
     Status lists(std::vector<int>& l3, std::vector<int>& l4, std::string& err);
 
 private:
     Engine& eng_;
-    int slot_ = -1, nall_ = -1, inum_ = -1;
+    int slot_ = -1, nall_ = -1, inum_ = -1, badness_ = 0;
     long long nent_ = -1, n3_ = 0, n4_ = 0, cap3_ = 0, cap4_ = 0;
     double skin_ = -1.0;
     bool built_ = false;

@@ -159,6 +159,10 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
         return kErrInput;
     }
     const HostParams& P = eng.params(slot);
+    if (P.tab2 || P.tab3) {
+        err = "ck_calculate_noalloc: tabulated parameter sets are evaluated on a neighbour list only";
+        return kErrParam;
+    }
     SysDesc d;
     std::memset(&d, 0, sizeof(d));
     double vol = 0.0;

@@ -80,6 +80,70 @@ const std::string& tok(const std::vector<std::string>& t, size_t k, const char* 
 }
 
 // get_proper_pair (chimesFF.cpp:69-84)
+// Tabulated-term files (read_2B_tab / read_3B_tab, chimesFF.cpp:199-351):
+// <name>.energy and <name>.force, a row count on the first line, then rows of
+// "r value" (2-body) or "rij rik rjk value[s]" (3-body).  The reference
+// concatenates the parameter file's directory and the table name without a
+// separator; here the name is taken relative to the parameter file's directory
+// (identical when the parameter file is named without a directory).
+std::vector<std::vector<double>> read_table_rows(const std::string& path, const char* what,
+                                                 const std::vector<size_t>& widths) {
+    std::ifstream f(path);
+    if (!f.is_open()) fail("could not open file: " + path);
+    std::string line;
+    if (!std::getline(f, line)) fail("error reading line in " + path);
+    auto t = tokens(line);
+    const long long n = to_int(t, 0, what);
+    if (n < 0) fail(std::string("negative row count in ") + path);
+    std::vector<std::vector<double>> rows;
+    rows.reserve((size_t)n);
+    for (long long i = 0; i < n; i++) {
+        if (!std::getline(f, line)) fail("error reading line in " + path + " (fewer rows than announced)");
+        auto u = tokens(line);
+        if (std::find(widths.begin(), widths.end(), u.size()) == widths.end())
+            fail(std::string("unexpected number of items in ") + what + " row: " + line);
+        std::vector<double> v(u.size());
+        for (size_t k = 0; k < u.size(); k++) v[k] = to_dbl(u, k, what);
+        rows.push_back(std::move(v));
+    }
+    return rows;
+}
+
+void read_tab2(const std::string& dir, const std::string& name, HostParams& P) {
+    auto e = read_table_rows(dir + name + ".energy", "2-body energy table", {2});
+    auto f = read_table_rows(dir + name + ".force", "2-body force table", {2});
+    if (e.size() != f.size()) fail("2-body energy and force tables of " + name + " differ in length");
+    HostParams::Tab2 T;
+    for (size_t i = 0; i < e.size(); i++) {
+        T.r.push_back(e[i][0]);
+        T.e.push_back(e[i][1]);
+        T.f.push_back(f[i][1]);
+        // the interval search (std::lower_bound in get_tab_2B) needs ascending distances
+        if (i > 0 && !(T.r[i] > T.r[i - 1])) fail("2-body table " + name + ": distances must be strictly ascending");
+    }
+    P.t2tab.push_back(std::move(T));
+}
+
+void read_tab3(const std::string& dir, const std::string& name, HostParams& P) {
+    auto e = read_table_rows(dir + name + ".energy", "3-body energy table", {4, 6});
+    auto f = read_table_rows(dir + name + ".force", "3-body force table", {6});
+    if (e.size() != f.size()) fail("3-body energy and force tables of " + name + " differ in length");
+    HostParams::Tab3 T;
+    for (size_t i = 0; i < e.size(); i++) {
+        T.rij.push_back(e[i][0]);
+        T.rik.push_back(e[i][1]);
+        T.rjk.push_back(e[i][2]);
+        T.e.push_back(e[i][3]);
+        T.fij.push_back(f[i][3]);
+        T.fik.push_back(f[i][4]);
+        T.fjk.push_back(f[i][5]);
+    }
+    // interpolateTricubic reads the rjk column at row size^2 + size + 1 for the grid step
+    const int size = (int)std::cbrt((double)T.rik.size());
+    if (size < 2) fail("3-body table " + name + " needs at least 2 grid points per distance (8 rows)");
+    P.t3tab.push_back(std::move(T));
+}
+
 int proper_pair(const HostParams& P, const std::string& a, const std::string& b) {
     for (int i = 0; i < P.npairs; i++) {
         if (a == P.pa1[i] && b == P.pa2[i]) return i;
@@ -120,7 +184,7 @@ void atom_pair_mapper(const HostParams& P, int natoms, const int* typ,
                 mapped[j] = i;
 }
 
-void parse_lines(Lines& L, HostParams& P) {
+void parse_lines(Lines& L, HostParams& P, const std::string& dir) {
     std::string line;
     // pass 1: PAIRTYP: CHEBYSHEV o2 [o3 [o4]]  (chimesFF.cpp:390-437)
     bool found = false;
@@ -220,11 +284,24 @@ void parse_lines(Lines& L, HostParams& P) {
     P.pows2.assign(P.npairs, {});
     P.coef2.assign(P.npairs, {});
     bool have_pmap = false;
+    int n_plain2 = 0;
     while (true) {
         if (!L.next(line)) fail("error reading line: missing ENDFILE");
         if (has(line, "ENDFILE")) break;
         if (has(line, "PAIRTYPE PARAMS:")) {
             auto t = tokens(line);
+            if (t.size() == 7) {   // PAIRTYPE PARAMS: <i> <a> <b> TABULATED <table> (chimesFF.cpp:719-735)
+                if (n_plain2 > 0)
+                    fail("All parameters of a given bodiedness must either be tabulated or not tabulated, but not "
+                         "a mixture of each");
+                read_tab2(dir, t[6], P);
+                P.tab2 = true;
+                continue;
+            }
+            if (P.tab2)
+                fail("All parameters of a given bodiedness must either be tabulated or not tabulated, but not a "
+                     "mixture of each");
+            n_plain2++;
             int p = to_int(t, 2, "PAIRTYPE PARAMS");
             if (p < 0 || p >= P.npairs) fail("PAIRTYPE PARAMS index out of range");
             if (!L.next(line)) fail("error reading line");
@@ -265,8 +342,13 @@ void parse_lines(Lines& L, HostParams& P) {
         }
     }
     if (!have_pmap) fail("missing PAIRMAPS block");
-    for (int p = 0; p < P.npairs; p++)
-        if ((int)P.coef2[p].size() != P.o2) fail("missing PAIRTYPE PARAMS block for a pair type");
+    if (P.tab2) {
+        // get_tab_2B indexes the tables by pair type
+        if ((int)P.t2tab.size() < P.npairs) fail("fewer tabulated 2-body tables than pair types");
+    } else {
+        for (int p = 0; p < P.npairs; p++)
+            if ((int)P.coef2[p].size() != P.o2) fail("missing PAIRTYPE PARAMS block for a pair type");
+    }
 
     // passes 4-7: 3B and 4B blocks (chimesFF.cpp:834-1567)
     for (int nb = 3; nb <= 4; nb++) {
@@ -306,11 +388,16 @@ void parse_lines(Lines& L, HostParams& P) {
                 if (ti < 0 || ti >= B.ntyp) fail("cluster type index out of range");
                 B.atoms[ti].clear();
                 for (int a = 0; a < nb; a++) B.atoms[ti].push_back(tok(t, 3 + a, h_type));
+                if (nb == 3 && t.size() == 8) {   // INDEX: i ATOMS: a b c TABULATED <table> (:882-896)
+                    read_tab3(dir, t[7], P);
+                    P.tab3 = true;
+                }
                 if (!L.next(line)) fail("error reading line");
                 auto u = tokens(line);
                 B.pairs[ti].clear();
                 for (int p = 0; p < np; p++) B.pairs[ti].push_back(tok(u, 1 + p, "PAIRS line"));
-                if (tok(u, 1 + np, "PAIRS line") != "EXCLUDED:") {
+                // once a triplet is tabulated no later triplet's coefficients are read (:912-918)
+                if (tok(u, 1 + np, "PAIRS line") != "EXCLUDED:" && !(nb == 3 && P.tab3)) {
                     int nc = to_int(u, nb == 3 ? 7 : 10, "PAIRS line (TOTAL)");
                     if (nc < 0) fail("negative coefficient count");
                     B.ncoef[ti] = nc;
@@ -354,6 +441,9 @@ void parse_lines(Lines& L, HostParams& P) {
             }
         }
         if (!have_map) fail(std::string("missing ") + h_maps + " block");
+        if (nb == 3 && P.tab3)   // get_tab_3B indexes the tables by triplet type
+            for (int v : B.map)
+                if (v >= (int)P.t3tab.size()) fail("no tabulated 3-body table for triplet type " + std::to_string(v));
         for (int ti = 0; ti < B.ntyp; ti++)
             if ((int)B.atoms[ti].size() != nb || (int)B.pairs[ti].size() != np) fail("missing cluster type block");
         // default cutoffs from the 2B pair types of the type's atoms (chimesFF.cpp:947-980, 1280-1325)
@@ -452,7 +542,7 @@ int HostParams::type_index(const std::string& name) const {
 // ---------------------------------------------------------------------------
 namespace {
 constexpr char kCacheMagic[4] = {'C', 'K', 'P', 'C'};
-constexpr int kCacheVersion = 1;
+constexpr int kCacheVersion = 2;
 
 struct Writer {
     std::string b;
@@ -520,6 +610,15 @@ void get_params(Reader& r, HostParams& P) {
     P.pair_map = r.vi(); P.prpr = r.vi(); P.pair_map_file_idx = r.vi();
     get_body(r, P.b3);
     get_body(r, P.b4);
+    P.tab2 = r.i() != 0;
+    P.t2tab.resize(r.len());
+    for (auto& T : P.t2tab) { T.r = r.vd(); T.e = r.vd(); T.f = r.vd(); }
+    P.tab3 = r.i() != 0;
+    P.t3tab.resize(r.len());
+    for (auto& T : P.t3tab) {
+        T.rij = r.vd(); T.rik = r.vd(); T.rjk = r.vd();
+        T.e = r.vd(); T.fij = r.vd(); T.fik = r.vd(); T.fjk = r.vd();
+    }
     // the kernels index these tables without further checks
     const int nt = P.ntypes;
     if (nt <= 0 || nt > kMaxTypes || P.npairs != nt * (nt + 1) / 2 || (int)P.pair_map.size() != nt * nt ||
@@ -528,6 +627,21 @@ void get_params(Reader& r, HostParams& P) {
         throw ParseError{"inconsistent parameter cache"};
     for (int v : P.pair_map)
         if (v < 0 || v >= P.npairs) throw ParseError{"inconsistent parameter cache"};
+    if (P.tab2 && (int)P.t2tab.size() < P.npairs) throw ParseError{"inconsistent parameter cache"};
+    for (auto& T : P.t2tab) {
+        if (T.e.size() != T.r.size() || T.f.size() != T.r.size()) throw ParseError{"inconsistent parameter cache"};
+        for (size_t i = 1; i < T.r.size(); i++)
+            if (!(T.r[i] > T.r[i - 1])) throw ParseError{"inconsistent parameter cache"};
+    }
+    for (auto& T : P.t3tab) {
+        const size_t n = T.rij.size();
+        if (T.rik.size() != n || T.rjk.size() != n || T.e.size() != n || T.fij.size() != n || T.fik.size() != n ||
+            T.fjk.size() != n || (int)std::cbrt((double)n) < 2)
+            throw ParseError{"inconsistent parameter cache"};
+    }
+    if (P.tab3 && P.o3 > 0)
+        for (int v : P.b3.map)
+            if (v >= (int)P.t3tab.size()) throw ParseError{"inconsistent parameter cache"};
     for (int nb = 3; nb <= 4; nb++) {
         const HostParams::Body& B = nb == 3 ? P.b3 : P.b4;
         if ((nb == 3 ? P.o3 : P.o4) == 0) continue;
@@ -565,6 +679,15 @@ Status save_parameter_cache(const HostParams& P, const std::string& path, std::s
     w.vi(P.pair_map); w.vi(P.prpr); w.vi(P.pair_map_file_idx);
     put_body(w, P.b3);
     put_body(w, P.b4);
+    w.i(P.tab2 ? 1 : 0);
+    w.i((long long)P.t2tab.size());
+    for (auto& T : P.t2tab) { w.vd(T.r); w.vd(T.e); w.vd(T.f); }
+    w.i(P.tab3 ? 1 : 0);
+    w.i((long long)P.t3tab.size());
+    for (auto& T : P.t3tab) {
+        w.vd(T.rij); w.vd(T.rik); w.vd(T.rjk);
+        w.vd(T.e); w.vd(T.fij); w.vd(T.fik); w.vd(T.fjk);
+    }
     std::ofstream f(path, std::ios::binary | std::ios::trunc);
     if (!f.is_open()) {
         err = "cannot write parameter cache: " + path;
@@ -605,8 +728,10 @@ Status parse_parameter_file(const std::string& path, HostParams& P, std::string&
     std::string line;
     while (std::getline(f, line)) L.v.push_back(line);
     P = HostParams();
+    const size_t slash = path.find_last_of("/\\");
+    const std::string dir = slash == std::string::npos ? std::string() : path.substr(0, slash + 1);
     try {
-        parse_lines(L, P);
+        parse_lines(L, P, dir);
     } catch (const ParseError& e) {
         err = e.msg;
         return kErrParam;
@@ -639,6 +764,25 @@ void morse_consts(double rin, double rout, double lam, double& xavg, double& xdi
     xdiff = 0.5 * (x_max - x_min);
     xdiff *= -1.0;
 }
+// Local cubic of get_tab_2B (chimesFF.cpp:1898-1916) on the interval that
+// starts at grid point i (1 <= i <= n-2), for table y: q = {a, b, c, d}.
+// The expressions keep the reference's operation order (the host code is
+// compiled without contraction), so the coefficients are bit-identical.
+void tab2_interval(const std::vector<double>& r, const std::vector<double>& y, int i, double* q) {
+    const double h = r[i + 1] - r[i];
+    const double alpha = (3 * (y[i + 1] - y[i]) / h) - (3 * (y[i] - y[i - 1]) / (r[i] - r[i - 1]));
+    const double l = 2 * (r[i + 1] - r[i - 1]) - h;
+    const double mu = h / l;
+    const double z = alpha / l;
+    const double c_prev = 0.0;   // natural-spline end condition of the reference
+    const double c = z - mu * c_prev;
+    const double b = (y[i + 1] - y[i]) / h - h * (c + 2 * c_prev) / 3.0;
+    const double d = (c - c_prev) / (3.0 * h);
+    q[0] = y[i];
+    q[1] = b;
+    q[2] = c;
+    q[3] = d;
+}
 }  // namespace
 
 ParamImage pack_params(const HostParams& P) {
@@ -669,7 +813,7 @@ ParamImage pack_params(const HostParams& P) {
         pr[p].ncoef = P.o2 + 1;
         pr[p].coef_off = (int)c2d.size();
         std::vector<double> dense(P.o2 + 1, 0.0);
-        for (int c = 0; c < P.o2; c++) {
+        for (int c = 0; c < (int)P.coef2[p].size(); c++) {   // none when the 2-body term is tabulated
             dense[P.pows2[p][c] + 1] += P.coef2[p][c];
             p2.push_back(P.pows2[p][c]);
         }
@@ -840,6 +984,58 @@ ParamImage pack_params(const HostParams& P) {
             H.fr4 = as_off<const FactRow>(fro); H.fe4d = as_off<const FactEntD>(fdo);
             H.fe4f = as_off<const FactEntF>(ffo);
         }
+    }
+    // tabulated terms
+    H.tab2 = P.tab2 ? 1 : 0;
+    H.tab3 = P.tab3 ? 1 : 0;
+    if (!P.t2tab.empty()) {
+        std::vector<Tab2Rec> rec;
+        std::vector<double> r, cf;
+        for (const auto& T : P.t2tab) {
+            const int n = (int)T.r.size();
+            rec.push_back(Tab2Rec{(long long)r.size(), n, 0});
+            r.insert(r.end(), T.r.begin(), T.r.end());
+            for (int i = 0; i < n; i++) {
+                double q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                if (i >= 1 && i <= n - 2)
+                    for (int w = 0; w < 2; w++) tab2_interval(T.r, w == 0 ? T.e : T.f, i, &q[4 * w]);
+                cf.insert(cf.end(), q, q + 8);
+            }
+        }
+        H.n_tab2 = (int)rec.size();
+        H.t2rec = as_off<const Tab2Rec>(B.add(rec.data(), rec.size()));
+        H.tab2r = as_off<const double>(B.add(r.data(), r.size()));
+        H.tab2c = as_off<const double>(B.add(cf.data(), cf.size()));
+    }
+    if (!P.t3tab.empty()) {
+        std::vector<Tab3Rec> rec;
+        std::vector<double> cols, vals;
+        long long off = 0;
+        for (const auto& T : P.t3tab) {
+            const long long n = (long long)T.rij.size();
+            Tab3Rec R{};
+            R.off = off;
+            R.nrows = n;
+            // interpolateTricubic (chimesFF.cpp:2386-2389): rows per rij value, grid step
+            R.size = (int)std::cbrt((double)T.rik.size());
+            const long long sij = (long long)R.size * R.size;
+            R.inv = 1 / (T.rjk[sij + R.size + 1] - T.rjk[0]);
+            rec.push_back(R);
+            cols.insert(cols.end(), T.rij.begin(), T.rij.end());
+            cols.insert(cols.end(), T.rik.begin(), T.rik.end());
+            cols.insert(cols.end(), T.rjk.begin(), T.rjk.end());
+            for (long long k = 0; k < n; k++) {
+                vals.push_back(T.e[k]);
+                vals.push_back(T.fij[k]);
+                vals.push_back(T.fik[k]);
+                vals.push_back(T.fjk[k]);
+            }
+            off += n;
+        }
+        H.n_tab3 = (int)rec.size();
+        H.t3rec = as_off<const Tab3Rec>(B.add(rec.data(), rec.size()));
+        H.tab3r = as_off<const double>(B.add(cols.data(), cols.size()));
+        H.tab3v = as_off<const double>(B.add(vals.data(), vals.size()));
     }
     img.header_off = B.add(&H, 1);
     img.bytes = std::move(B.b);

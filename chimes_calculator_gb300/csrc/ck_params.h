@@ -40,6 +40,16 @@ struct HostParams {
     };
     Body b3, b4;
 
+    // Tabulated 2-/3-body terms (a PAIRTYPE PARAMS line with a table name, or
+    // an INDEX line of a triplet with one: chimesFF.cpp:719-769, 882-934):
+    // the tables in the order the file names them; the 2-body ones are looked
+    // up by pair type index, the 3-body ones by triplet type index.
+    struct Tab2 { std::vector<double> r, e, f; };
+    struct Tab3 { std::vector<double> rij, rik, rjk, e, fij, fik, fjk; };
+    bool tab2 = false, tab3 = false;
+    std::vector<Tab2> t2tab;
+    std::vector<Tab3> t3tab;
+
     double max_cut2() const;
     double max_cut3() const;
     double max_cut4() const;

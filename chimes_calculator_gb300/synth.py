@@ -456,6 +456,108 @@ def specs_c5() -> List[ParamSpec]:
 
 
 # ----------------------------------------------------------------------------
+# Tabulated parameter sets (the reference's TABULATION option)
+# ----------------------------------------------------------------------------
+def _tab_g(r, rc, lam):
+    """Smooth decaying radial factor exp(-r/lam) (1 - r/rc)^3 and its derivative (0 past rc)."""
+    r = np.asarray(r, dtype=np.float64)
+    inside = r < rc
+    u = np.where(inside, 1.0 - r / rc, 0.0)
+    ex = np.exp(-r / lam)
+    g = ex * u ** 3
+    dg = -ex / lam * u ** 3 - 3.0 * ex * u ** 2 / rc
+    return g, np.where(inside, dg, 0.0)
+
+
+def _write_rows(path: str, rows: np.ndarray) -> None:
+    with open(path, "w") as f:
+        f.write("%d\n" % len(rows))
+        f.write("\n".join(" ".join(repr(float(v)) for v in row) for row in rows))
+        f.write("\n")
+
+
+def write_tabulated_param_file(path: str, spec: ParamSpec, tab2: bool = True, tab3: bool = True,
+                               r0_2: float = 0.5, step2: float = 0.005, r0_3: float = 0.8,
+                               step3: float = 0.1, seed: int = 7) -> str:
+    """Writes ``spec``'s parameter file with its 2-body and/or 3-body terms
+    tabulated, as the reference's TABULATION build reads them
+    (chimesFF.cpp:199-351, 719-769, 882-934): ``PAIRTYPE PARAMS: k A B TABULATED
+    <name>`` and ``INDEX: t ATOMS: a b c TABULATED <name>`` lines (the
+    coefficient rows stay and are ignored), and beside the file, for each
+    table, ``<name>.energy`` and ``<name>.force``.
+
+    The tabulated energies are seeded smooth functions, not a Chebyshev fit:
+    2-body E(r) = A_k g(r), 3-body E = B_t g(r_ij) g(r_ik) g(r_jk) with
+    g(r) = exp(-r/1.4) (1 - r/rc)^3, and the force columns are (dE/dr_p)/r_p,
+    the scalar that multiplies the pair vector r_j - r_i in compute_2B_tab /
+    compute_3B_tab.  2-body grids run from ``r0_2`` in steps of ``step2`` to
+    past the pair's outer cutoff; 3-body grids are n x n x n points from
+    ``r0_3`` in steps of ``step3`` (rij slowest, rjk fastest) covering the
+    largest 3-body cutoff."""
+    import os
+    text = build_param_text(spec)
+    rng = np.random.default_rng(seed)
+    base = os.path.splitext(os.path.basename(path))[0]
+    out_dir = os.path.dirname(os.path.abspath(path))
+    lines = text.split("\n")
+    # pair cutoffs and the largest 3-body outer cutoff, from the file itself
+    rout = {}
+    in_pairs = False
+    s3_all = None
+    for ln in lines:
+        t = ln.split()
+        if ln.startswith("# PAIRIDX #"):
+            in_pairs = True
+            continue
+        if in_pairs:
+            if len(t) == 8:
+                rout[int(t[0])] = float(t[4])
+                continue
+            in_pairs = False
+        if ln.startswith("SPECIAL 3B S_MAXIM: ALL"):
+            s3_all = float(t[4])
+    rc3 = s3_all if s3_all is not None else max(rout.values())
+    if isinstance(spec.s3max, dict):
+        rc3 = max([rc3] + [max(v) for v in spec.s3max.values()])
+    out = []
+    after_trip_header = False
+    for ln in lines:
+        t = ln.split()
+        if tab2 and ln.startswith("PAIRTYPE PARAMS:"):
+            k = int(t[2])
+            name = "%s_2b.type_%d.dat" % (base, k)
+            n = int(math.ceil((rout[k] + 2 * step2 - r0_2) / step2)) + 1
+            r = r0_2 + step2 * np.arange(n)
+            g, dg = _tab_g(r, rout[k], 1.4)
+            amp = float(rng.uniform(5.0, 20.0))
+            _write_rows(os.path.join(out_dir, name + ".energy"), np.stack([r, amp * g], axis=1))
+            _write_rows(os.path.join(out_dir, name + ".force"), np.stack([r, amp * dg / r], axis=1))
+            ln = ln + " TABULATED " + name
+        if tab3 and after_trip_header and ln.strip().startswith("INDEX:"):
+            ti = int(t[1])
+            name = "%s_3b.type_%d.dat" % (base, ti)
+            n = int(math.ceil((rc3 + 2 * step3 - r0_3) / step3)) + 1
+            ax = r0_3 + step3 * np.arange(n)
+            rij, rik, rjk = (a.ravel() for a in np.meshgrid(ax, ax, ax, indexing="ij"))
+            gij, dij = _tab_g(rij, rc3, 1.4)
+            gik, dik = _tab_g(rik, rc3, 1.4)
+            gjk, djk = _tab_g(rjk, rc3, 1.4)
+            amp = float(rng.uniform(1.0, 4.0))
+            e = amp * gij * gik * gjk
+            fij = amp * dij * gik * gjk / rij
+            fik = amp * gij * dik * gjk / rik
+            fjk = amp * gij * gik * djk / rjk
+            _write_rows(os.path.join(out_dir, name + ".energy"), np.stack([rij, rik, rjk, e], axis=1))
+            _write_rows(os.path.join(out_dir, name + ".force"), np.stack([rij, rik, rjk, fij, fik, fjk], axis=1))
+            ln = ln + " TABULATED " + name
+        after_trip_header = ln.startswith("TRIPLETTYPE PARAMS:")
+        out.append(ln)
+    with open(path, "w") as f:
+        f.write("\n".join(out))
+    return path
+
+
+# ----------------------------------------------------------------------------
 # LAMMPS-style inputs: local atoms, ghost images and full neighbour lists
 # ----------------------------------------------------------------------------
 @dataclasses.dataclass

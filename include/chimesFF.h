@@ -75,6 +75,12 @@ public:
     std::vector<int> poly_orders;      /* [2B order, 3B order, 4B order] */
     std::vector<std::string> atmtyps;  /* atom type names in parameter-file order */
     std::vector<double> masses;
+    /* Tabulated 2-/3-body terms (chimesFF.h:196-227; the reference declares
+     * these only when built with TABULATION, as its LAMMPS pair style is).
+     * Set by read_parameters when the file names tables; declared in every
+     * build here so that the class layout does not depend on the option. */
+    bool tabulate_2B;
+    bool tabulate_3B;
 
     chimesFF();
     virtual ~chimesFF();
@@ -104,6 +110,23 @@ public:
     void compute_4B(const std::vector<double>& dx, const std::vector<double>& dr, const std::vector<int>& typ_idxs,
                     std::vector<double>& force, std::vector<double>& stress, double& energy, chimes4BTmp& tmp,
                     std::vector<double>& force_scalar_in);
+
+    /* chimesFF.h:204-205, 224-225: the tabulated forms (table look-up instead
+     * of the Chebyshev sum; 2-body spline of get_tab_2B, 3-body tricubic
+     * interpolation of interpolateTricubic).  Same argument conventions and
+     * accumulation as compute_2B/3B; force_scalar_in receives get_penalty's
+     * value (2B) or the three table force scalars (3B).  A distance outside
+     * the table prints the reference's message and exits (error mode 0). */
+    void compute_2B_tab(const double dx, const std::vector<double>& dr, const std::vector<int> typ_idxs,
+                        std::vector<double>& force, std::vector<double>& stress, double& energy, chimes2BTmp& tmp);
+    void compute_2B_tab(const double dx, const std::vector<double>& dr, const std::vector<int> typ_idxs,
+                        std::vector<double>& force, std::vector<double>& stress, double& energy, chimes2BTmp& tmp,
+                        double& force_scalar_in);
+    void compute_3B_tab(const std::vector<double>& dx, const std::vector<double>& dr, const std::vector<int>& typ_idxs,
+                        std::vector<double>& force, std::vector<double>& stress, double& energy, chimes3BTmp& tmp);
+    void compute_3B_tab(const std::vector<double>& dx, const std::vector<double>& dr, const std::vector<int>& typ_idxs,
+                        std::vector<double>& force, std::vector<double>& stress, double& energy, chimes3BTmp& tmp,
+                        std::vector<double>& force_scalar_in);
 
     /* Batched per-cluster evaluation: n clusters of nbody atoms in one launch.
      * dx[n][P], dr[n][P][3], typ[n][nbody]; force[n][nbody][3] (accumulated per

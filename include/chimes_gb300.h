@@ -209,7 +209,10 @@ int ck_server_stats(void *server, long long *out);
  * virial[6] (xx yy zz xy xz yz, as Pair::ev_tally_mb) and, when not NULL,
  * per-atom eatom[nall] and vatom[nall][6] (each interaction's energy and
  * virial shared equally by its atoms, as ev_tally_mb's eflag_atom and
- * vflag_atom branches). */
+ * vflag_atom branches).  A parameter set with tabulated 2-/3-body terms (the
+ * reference's TABULATION build, pair_chimes.cpp:620-622, 697-699) is evaluated
+ * with the table look-ups of compute_2B_tab / compute_3B_tab; a distance
+ * outside a table returns an error. */
 int ck_nl_compute(void *h, int nall, const double *x, const int *type, const long long *tag, int inum,
                   const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
                   double *energy, double *virial, double *eatom, double *vatom);
@@ -225,6 +228,16 @@ int ck_nl_lists(void *h, long long *counts, int *l3, int *l4);
  * (may be NULL); clusters of excluded types or beyond a cutoff get zeros. */
 int ck_compute_cluster_batch(void *h, int nbody, int n, const double *dx, const double *dr, const int *typ,
                              double *force, double *stress, double *energy, double *fscal);
+/* The same for tabulated terms (chimesFF::compute_2B_tab / compute_3B_tab,
+ * chimesFF/src/chimesFF.cpp:1776-1867, 2177-2322, the reference's TABULATION
+ * build): nbody = 2 or 3, the set's terms of that order must be tabulated.
+ * fscal[n][P] receives force_scalar_in (2B: get_penalty's value, 3B: the table
+ * force scalars).  A distance outside a table is an error (the reference prints
+ * "Distance is outside the tabulated range" and exits). */
+int ck_compute_cluster_batch_tab(void *h, int nbody, int n, const double *dx, const double *dr, const int *typ,
+                                 double *force, double *stress, double *energy, double *fscal);
+/* tab[2] = 1 when the handle's 2-body / 3-body terms are tabulated */
+int ck_tabulated(void *h, int *tab);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,9 @@
  *                      serial_interface/src/serial_chimes_interface.cpp:85-587
  *   cluster lists .... simulation_system::build_neigh_lists  serial_chimes_interface.cpp:588-864
  *   driver ........... serial_chimes_interface::calculate    serial_chimes_interface.cpp:960-1124
+ *   tabulated terms .. read_2B_tab / read_3B_tab     chimesFF.cpp:199-351 (TABULATION build)
+ *                      compute_2B_tab / get_tab_2B   chimesFF.cpp:1776-1922
+ *                      compute_3B_tab / interpolateTricubic / get_tab_3B  chimesFF.cpp:2177-2463
  *
  * Errors are returned as negative status codes with a message (the reference
  * prints and calls exit(0)); the oracle never terminates its host process.
@@ -54,6 +57,11 @@ typedef struct {
     int *quad_map; int *quad_perm; /* [nt^4], [nt^4][6] */
     int badness;
     long n_penalty, n_below_rin;
+    /* tabulated terms: tables in the order the file names them */
+    int tab2, tab3, n_t2, n_t3;
+    struct { long n; double *r, *e, *f; } *t2;
+    struct { long n; double *rij, *rik, *rjk, *e, *fij, *fik, *fjk; } *t3;
+    int tab_err;             /* 1: 2B distance below the table (the reference exits); 2: 3B grid index past the rows */
 } ora_ff;
 
 typedef struct {
@@ -182,12 +190,67 @@ static void atom_pair_mapper(ora_ff *ff, int natoms, const int *typ, char (*clu_
 /* ------------------------------------------------------------------ */
 /* read_parameters, chimesFF.cpp:354-1570                              */
 /* ------------------------------------------------------------------ */
+/* read_2B_tab / read_3B_tab (chimesFF.cpp:199-351): "<name>.energy" and
+ * "<name>.force", a row count, then rows of 2 (2B) or 4 / 6 (3B) numbers.  The
+ * name is taken relative to the parameter file's directory. */
+static long read_rows(const char *path, int *widths, int nw, double **cols, int ncols) {
+    ora_text T;
+    if (load_text(path, &T)) return -1;
+    char tok[MAXTOK][MAXTOK];
+    if (T.n < 1 || split(T.lines[0], tok, MAXTOK) < 1) { free(T.lines); free(T.buf); return -1; }
+    long n = atol(tok[0]);
+    if (n < 0 || n + 1 > T.n) { free(T.lines); free(T.buf); return -1; }
+    for (int c = 0; c < ncols; c++) cols[c] = calloc(n + 1, sizeof(double));
+    for (long i = 0; i < n; i++) {
+        int k = split(T.lines[i + 1], tok, MAXTOK), ok = 0;
+        for (int w = 0; w < nw; w++) ok |= k == widths[w];
+        if (!ok || k < ncols) { free(T.lines); free(T.buf); return -1; }
+        for (int c = 0; c < ncols; c++) cols[c][i] = strtod(tok[c], 0);
+    }
+    free(T.lines); free(T.buf);
+    return n;
+}
+
+static int read_tab(ora_handle *h, const char *dir, const char *name, int body) {
+    ora_ff *ff = &h->ff;
+    char pe[1024], pf[1024];
+    snprintf(pe, sizeof(pe), "%s%s.energy", dir, name);
+    snprintf(pf, sizeof(pf), "%s%s.force", dir, name);
+    if (body == 2) {
+        double *e[2], *f[2];
+        int w2[1] = {2};
+        long ne = read_rows(pe, w2, 1, e, 2), nf = read_rows(pf, w2, 1, f, 2);
+        if (ne < 0 || nf < 0 || ne != nf) FAIL(h, "cannot read 2-body table %s", name);
+        ff->t2 = realloc(ff->t2, (size_t)(ff->n_t2 + 1) * sizeof(*ff->t2));
+        ff->t2[ff->n_t2].n = ne; ff->t2[ff->n_t2].r = e[0]; ff->t2[ff->n_t2].e = e[1]; ff->t2[ff->n_t2].f = f[1];
+        free(f[0]);
+        ff->n_t2++;
+    } else {
+        double *e[4], *f[6];
+        int w3[2] = {4, 6}, w6[1] = {6};
+        long ne = read_rows(pe, w3, 2, e, 4), nf = read_rows(pf, w6, 1, f, 6);
+        if (ne < 0 || nf < 0 || ne != nf) FAIL(h, "cannot read 3-body table %s", name);
+        if ((int)cbrt((double)ne) < 2) FAIL(h, "3-body table %s has fewer than 8 rows", name);
+        ff->t3 = realloc(ff->t3, (size_t)(ff->n_t3 + 1) * sizeof(*ff->t3));
+        ff->t3[ff->n_t3].n = ne;
+        ff->t3[ff->n_t3].rij = e[0]; ff->t3[ff->n_t3].rik = e[1]; ff->t3[ff->n_t3].rjk = e[2]; ff->t3[ff->n_t3].e = e[3];
+        ff->t3[ff->n_t3].fij = f[3]; ff->t3[ff->n_t3].fik = f[4]; ff->t3[ff->n_t3].fjk = f[5];
+        free(f[0]); free(f[1]); free(f[2]);
+        ff->n_t3++;
+    }
+    return 0;
+}
+
 static int parse(ora_handle *h, const char *path) {
     ora_ff *ff = &h->ff;
     ora_text T;
     if (load_text(path, &T)) FAIL(h, "cannot open parameter file: %s", path);
     char tok[MAXTOK][MAXTOK];
     int L;
+    char dir[1024] = "";
+    const char *slash = strrchr(path, '/');
+    if (slash && (size_t)(slash - path + 1) < sizeof(dir)) { memcpy(dir, path, slash - path + 1); dir[slash - path + 1] = 0; }
+    int n_plain2 = 0;
     ff->pen_dist = 0.01; ff->pen_scale = 1.0e4; ff->inner_smooth = 0.01; /* chimesFF.cpp:104-116 */
     ff->fcut_tersoff = 0;
     /* pass 1: orders */
@@ -268,7 +331,16 @@ static int parse(ora_handle *h, const char *path) {
         const char *ln = T.lines[L];
         if (strstr(ln, "ENDFILE")) break;
         if (strstr(ln, "PAIRTYPE PARAMS:")) {
-            split(ln, tok, MAXTOK); int p = atoi(tok[2]);
+            int nt7 = split(ln, tok, MAXTOK);
+            if (nt7 == 7) {   /* tabulated 2B (chimesFF.cpp:719-735) */
+                if (n_plain2) FAIL(h, "All parameters of a given bodiedness must either be tabulated or not tabulated");
+                if (read_tab(h, dir, tok[6], 2)) return -1;
+                ff->tab2 = 1;
+                continue;
+            }
+            if (ff->tab2) FAIL(h, "All parameters of a given bodiedness must either be tabulated or not tabulated");
+            n_plain2++;
+            int p = atoi(tok[2]);
             if (p < 0 || p >= ff->npairs) FAIL(h, "pair index out of range");
             L++;
             for (int i = 0; i < ff->o2; i++) {
@@ -298,6 +370,7 @@ static int parse(ora_handle *h, const char *path) {
         }
     }
     if (!have_pmap) FAIL(h, "missing PAIRMAPS");
+    if (ff->tab2 && ff->n_t2 < ff->npairs) FAIL(h, "fewer tabulated 2-body tables than pair types");
     /* passes 4-5: 3B, then 6-7: 4B (same structure) */
     for (int body = 3; body <= 4; body++) {
         int order = body == 3 ? ff->o3 : ff->o4;
@@ -322,14 +395,18 @@ static int parse(ora_handle *h, const char *path) {
             if (strstr(ln, hdr_type)) {
                 if (!ncoef) FAIL(h, "%s before %s", hdr_type, hdr_count);
                 if (++L >= T.n) FAIL(h, "truncated cluster block");
-                split(T.lines[L], tok, MAXTOK);
+                int ntk = split(T.lines[L], tok, MAXTOK);
                 int t = atoi(tok[1]);
                 if (t < 0 || t >= ntyp) FAIL(h, "cluster type index out of range");
                 for (int a = 0; a < body; a++) strncpy(catm[t * body + a], tok[3 + a], 15);
+                if (body == 3 && ntk == 8) {   /* tabulated 3B (chimesFF.cpp:882-896) */
+                    if (read_tab(h, dir, tok[7], 3)) return -1;
+                    ff->tab3 = 1;
+                }
                 if (++L >= T.n) FAIL(h, "truncated cluster block");
                 split(T.lines[L], tok, MAXTOK);
                 for (int p = 0; p < np; p++) strncpy(cpair[t * np + p], tok[1 + p], 39);
-                if (strcmp(tok[1 + np], "EXCLUDED:")) {
+                if (strcmp(tok[1 + np], "EXCLUDED:") && !(body == 3 && ff->tab3)) {   /* :912-918 */
                     int nc = atoi(tok[body == 3 ? 7 : 10]);
                     ncoef[t] = nc; pw[t] = calloc((size_t)nc * np + 1, sizeof(int)); cf[t] = calloc(nc + 1, sizeof(double));
                     L += 2;
@@ -362,6 +439,9 @@ static int parse(ora_handle *h, const char *path) {
             }
         }
         if (!tmap) FAIL(h, "missing %s", hdr_maps);
+        if (body == 3 && ff->tab3)
+            for (int u = 0; u < ntup; u++)
+                if (tmap[u] >= ff->n_t3) FAIL(h, "no tabulated 3-body table for triplet type %d", tmap[u]);
         /* default cutoffs: 2B values of each pair of the type's atoms (chimesFF.cpp:947-980, 1280-1325) */
         for (int t = 0; t < ntyp; t++) {
             int a[4];
@@ -638,6 +718,158 @@ void ora_compute_4b(void *vh, const double *dx, const double *dr, const int *typ
 /* ------------------------------------------------------------------ */
 /* periodic system (serial_chimes_interface.cpp:20-587)                */
 /* ------------------------------------------------------------------ */
+/* ------------------------------------------------------------------ */
+/* tabulated terms (TABULATION build; used by the LAMMPS pair style)    */
+/* ------------------------------------------------------------------ */
+/* get_tab_2B, chimesFF.cpp:1869-1922: the interval from std::lower_bound,
+ * then the local spline coefficients of that interval */
+static double tab2_value(ora_ff *ff, int p, double rij, int for_energy) {
+    long n = ff->t2[p].n;
+    const double *r = ff->t2[p].r;
+    long lo = 0, len = n;   /* lower_bound: first r >= rij */
+    while (len > 0) {
+        long half = len / 2;
+        if (r[lo + half] < rij) { lo += half + 1; len -= half + 1; } else len = half;
+    }
+    long i = lo;
+    if (i == n) return 0.0;
+    if (i == 0) { ff->tab_err |= 1; return 0.0; }
+    if (rij == r[i] && i > 0) i--;
+    const double *y = for_energy ? ff->t2[p].e : ff->t2[p].f;
+    if (i >= n - 1) return 0.0;
+    if (i <= 0) { ff->tab_err |= 1; return 0.0; }
+    double h = r[i + 1] - r[i];
+    double alpha = (3 * (y[i + 1] - y[i]) / h) - (3 * (y[i] - y[i - 1]) / (r[i] - r[i - 1]));
+    double l = 2 * (r[i + 1] - r[i - 1]) - h;
+    double mu = h / l;
+    double z = alpha / l;
+    double c_prev = 0.0;
+    double c = z - mu * c_prev;
+    double b = (y[i + 1] - y[i]) / h - h * (c + 2 * c_prev) / 3.0;
+    double d = (c - c_prev) / (3.0 * h);
+    double a = y[i];
+    double dx = rij - r[i];
+    return a + b * dx + c * dx * dx + d * dx * dx * dx;
+}
+
+double ora_tab2(void *vh, int pair, double r, int for_energy) { return tab2_value(&((ora_handle *)vh)->ff, pair, r, for_energy); }
+
+/* compute_2B_tab, chimesFF.cpp:1782-1867.  fscal receives force_scalar_in:
+ * get_penalty overwrites the table's scalar with 1.0 or the penalty slope. */
+void ora_compute_2b_tab(void *vh, double dx, const double *dr, int t0, int t1, double *force, double *stress, double *E,
+                        double *fscal) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    int p = ff->pair_map[t0 * ff->ntypes + t1];
+    if (dx >= ff->rout[p]) return;
+    *E += tab2_value(ff, p, dx, 1);
+    double fs = tab2_value(ff, p, dx, 0);
+    force[0] += fs * dr[0]; force[1] += fs * dr[1]; force[2] += fs * dr[2];
+    force[3] -= fs * dr[0]; force[4] -= fs * dr[1]; force[5] -= fs * dr[2];
+    stress[0] -= fs * dr[0] * dr[0]; stress[1] -= fs * dr[0] * dr[1]; stress[2] -= fs * dr[0] * dr[2];
+    stress[3] -= fs * dr[1] * dr[1]; stress[4] -= fs * dr[1] * dr[2]; stress[5] -= fs * dr[2] * dr[2];
+    /* get_penalty (chimesFF.h:388-419): badness only, the table carries the penalty */
+    double rpen = 0.0;
+    fs = 1.0;
+    if (dx - ff->pen_dist < ff->rin[p]) {
+        rpen = ff->rin[p] + ff->pen_dist - dx;
+        if (dx < ff->rin[p]) ff->badness = 2;
+        else if (1 > ff->badness) ff->badness = 1;
+    }
+    if (rpen > 0.0) { fs = -3.0 * rpen * rpen * ff->pen_scale; ff->n_penalty++; }
+    if (fscal) *fscal = fs;
+}
+
+/* cubicInterpolate / bicubicInterpolate / tricubicInterpolate, chimesFF.cpp:2339-2366 */
+static double tab_cubic(double p0, double p1, double p2, double p3, double x) {
+    return p1 + 0.5 * x * (p2 - p0 + x * (2 * p0 - 5 * p1 + 4 * p2 - p3 + x * (3 * (p1 - p2) + p3 - p0)));
+}
+static double tab_bicubic(const double *p, double x, double y) {
+    double arr[4];
+    for (int i = 0; i < 4; i++) arr[i] = tab_cubic(p[i * 4 + 0], p[i * 4 + 1], p[i * 4 + 2], p[i * 4 + 3], x);
+    return tab_cubic(arr[0], arr[1], arr[2], arr[3], y);
+}
+static double tab_tricubic(const double *p, double x, double y, double z) {
+    double arr[4];
+    for (int i = 0; i < 4; i++) arr[i] = tab_bicubic(p + i * 16, x, y);
+    return tab_cubic(arr[0], arr[1], arr[2], arr[3], z);
+}
+
+/* interpolateTricubic, chimesFF.cpp:2370-2440: out = {E, F_ij, F_ik, F_jk} */
+static void tab3_value(ora_ff *ff, int t, double rij, double rik, double rjk, double *out) {
+    long nrows = ff->t3[t].n;
+    const double *tij = ff->t3[t].rij, *tik = ff->t3[t].rik, *tjk = ff->t3[t].rjk;
+    const double *ys[4] = {ff->t3[t].e, ff->t3[t].fij, ff->t3[t].fik, ff->t3[t].fjk};
+    int size_ik = (int)cbrt((double)nrows);
+    int size_ij = size_ik * size_ik;
+    double dr = 1 / (tjk[size_ij + size_ik + 1] - tjk[0]);
+    int i = (int)((rij - tij[0]) * dr);
+    int j = (int)((rik - tik[0]) * dr);
+    int k = (int)((rjk - tjk[0]) * dr);
+    if (i < 1) i = 1;
+    if (j < 1) j = 1;
+    if (k < 1) k = 1;
+    long ri = (long)i * size_ij + (long)j * size_ik + k, rj = (long)j * size_ik + k, rk = k;
+    if (ri >= nrows || rj >= nrows || rk >= nrows) {   /* the reference reads past its vectors here */
+        ff->tab_err |= 2;
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return;
+    }
+    double v[4][64];
+    memset(v, 0, sizeof(v));
+    for (int di = -1; di <= 2; ++di)
+        for (int dj = -1; dj <= 2; ++dj)
+            for (int dk = -1; dk <= 2; ++dk) {
+                int ti = i + di, tj = j + dj, tk = k + dk;
+                if (ti < size_ik && tj < size_ik && tk < size_ik) {
+                    long index = (long)size_ij * ti + (long)size_ik * tj + tk;
+                    int idx = (di + 1) * 16 + (dj + 1) * 4 + (dk + 1);
+                    for (int w = 0; w < 4; w++) v[w][idx] = ys[w][index];
+                }
+            }
+    double xi = (rij - tij[ri]) * dr;
+    double yi = (rik - tik[rj]) * dr;
+    double zi = (rjk - tjk[rk]) * dr;
+    for (int w = 0; w < 4; w++) out[w] = tab_tricubic(v[w], zi, yi, xi);
+}
+
+void ora_tab3(void *vh, int t, double rij, double rik, double rjk, double *out) {
+    tab3_value(&((ora_handle *)vh)->ff, t, rij, rik, rjk, out);
+}
+
+/* compute_3B_tab, chimesFF.cpp:2183-2322 (distance-tensor stress form) */
+void ora_compute_3b_tab(void *vh, const double *dx, const double *dr, const int *typ, double *force, double *stress,
+                        double *E, double *fscal) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    int nt = ff->ntypes;
+    int u = typ[0] * nt * nt + typ[1] * nt + typ[2];
+    int t = ff->trip_map[u];
+    if (t < 0) return;
+    const int *m = &ff->trip_perm[u * 3];
+    for (int p = 0; p < 3; p++)
+        if (dx[p] >= ff->cut3[(t * 2 + 1) * 3 + m[p]]) return;
+    double v[4];
+    tab3_value(ff, t, dx[0], dx[1], dx[2], v);
+    *E += v[0];
+    static const int A[3] = {0, 0, 1}, B[3] = {1, 2, 2};
+    for (int p = 0; p < 3; p++) {
+        const double fs = v[1 + p], *d = &dr[3 * p];
+        force[A[p] * 3 + 0] += fs * d[0]; force[A[p] * 3 + 1] += fs * d[1]; force[A[p] * 3 + 2] += fs * d[2];
+        force[B[p] * 3 + 0] -= fs * d[0]; force[B[p] * 3 + 1] -= fs * d[1]; force[B[p] * 3 + 2] -= fs * d[2];
+        stress[0] -= fs * (d[0] * d[0]); stress[1] -= fs * (d[0] * d[1]); stress[2] -= fs * (d[0] * d[2]);
+        stress[3] -= fs * (d[1] * d[1]); stress[4] -= fs * (d[1] * d[2]); stress[5] -= fs * (d[2] * d[2]);
+    }
+    if (fscal) { fscal[0] = v[1]; fscal[1] = v[2]; fscal[2] = v[3]; }
+}
+
+int ora_tab_flags(void *vh, int *tab2, int *tab3) {
+    ora_ff *ff = &((ora_handle *)vh)->ff;
+    if (tab2) *tab2 = ff->tab2;
+    if (tab3) *tab3 = ff->tab3;
+    int e = ff->tab_err;
+    ff->tab_err = 0;
+    return e;
+}
+
 static double mag3(const double *a) { double m = 0; for (int i = 0; i < 3; i++) m += a[i] * a[i]; return sqrt(m); }
 static double dot3(const double *a, const double *b) { double d = 0; for (int i = 0; i < 3; i++) d += a[i] * b[i]; return d; }
 static double angle3(const double *a, const double *b) { double g = dot3(a, b); g /= mag3(a); g /= mag3(b); return acos(g); }
@@ -1110,7 +1342,8 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             const double d = lmp_dist(x, i, j, dr);
             memset(f2, 0, sizeof(f2)); memset(st, 0, sizeof(st));
             e = 0.0;
-            ora_compute_2b(h, d, dr, typ[i], typ[j], f2, st, &e);
+            if (ff->tab2) ora_compute_2b_tab(h, d, dr, typ[i], typ[j], f2, st, &e, NULL);   /* :620-622 */
+            else ora_compute_2b(h, d, dr, typ[i], typ[j], f2, st, &e);
             for (int c = 0; c < 3; c++) { f[3 * i + c] += f2[c]; f[3 * j + c] += f2[3 + c]; }
             *energy += e;
             const int pr[2] = {i, j};
@@ -1128,7 +1361,8 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             const int t[3] = {typ[id[0]], typ[id[1]], typ[id[2]]};
             memset(f3, 0, sizeof(f3)); memset(st, 0, sizeof(st));
             double e = 0.0;
-            ora_compute_3b(h, dx, dr, t, f3, st, &e);
+            if (ff->tab3) ora_compute_3b_tab(h, dx, dr, t, f3, st, &e, NULL);   /* :697-699 */
+            else ora_compute_3b(h, dx, dr, t, f3, st, &e);
             for (int a = 0; a < 3; a++)
                 for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f3[3 * a + c];
             *energy += e;
@@ -1152,6 +1386,11 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
         }
     free(off);
+    if (ff->tab_err) {
+        int e = ff->tab_err;
+        ff->tab_err = 0;
+        FAIL(h, "%s", (e & 1) ? "Distance is outside the tabulated range" : "3-body distance past the tabulated grid");
+    }
     return 0;
 }
 

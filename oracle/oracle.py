@@ -73,6 +73,13 @@ def _load():
         llp = ctypes.POINTER(ctypes.c_longlong)
         lib.ora_lammps_compute.restype = I
         lib.ora_lammps_compute.argtypes = [P, I, dp, ip, llp, I, ip, ip, ip, D, I, dp, dp, dp, dp, dp]
+        lib.ora_tab2.restype = D
+        lib.ora_tab2.argtypes = [P, I, D, I]
+        lib.ora_tab3.argtypes = [P, I, D, D, D, dp]
+        lib.ora_compute_2b_tab.argtypes = [P, D, dp, I, I, dp, dp, dp, dp]
+        lib.ora_compute_3b_tab.argtypes = [P, dp, dp, ip, dp, dp, dp, dp]
+        lib.ora_tab_flags.restype = I
+        lib.ora_tab_flags.argtypes = [P, ip, ip]
         lib.ora_lammps_sizes.argtypes = [P, lp, lp]
         lib.ora_lammps_lists.argtypes = [P, ip, ip]
         _lib = lib
@@ -188,6 +195,32 @@ class Oracle:
         self.lib.ora_compute_3b(self.h, _dp(dx), _dp(dr), _ip(t), _dp(force), _dp(stress), ctypes.byref(e))
         return e.value
 
+    # tabulated terms (TABULATION build of the reference)
+    def tab_flags(self):
+        """(tab2, tab3, error bits since the last call)."""
+        t2, t3 = ctypes.c_int(), ctypes.c_int()
+        e = self.lib.ora_tab_flags(self.h, ctypes.byref(t2), ctypes.byref(t3))
+        return t2.value, t3.value, e
+
+    def compute_2b_tab(self, dx, dr, typ):
+        """compute_2B_tab from zero: (energy, force[6], stress[6], force_scalar_in)."""
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        f, st, fs = np.zeros(6), np.zeros(6), np.zeros(1)
+        e = ctypes.c_double(0.0)
+        self.lib.ora_compute_2b_tab(self.h, float(dx), _dp(dr), int(typ[0]), int(typ[1]), _dp(f), _dp(st),
+                                    ctypes.byref(e), _dp(fs))
+        return e.value, f, st, fs[0]
+
+    def compute_3b_tab(self, dx, dr, typ):
+        """compute_3B_tab from zero: (energy, force[9], stress[6], force_scalar_in[3])."""
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        dr = np.ascontiguousarray(dr, dtype=np.float64)
+        t = np.ascontiguousarray(typ, dtype=np.int32)
+        f, st, fs = np.zeros(9), np.zeros(6), np.zeros(3)
+        e = ctypes.c_double(0.0)
+        self.lib.ora_compute_3b_tab(self.h, _dp(dx), _dp(dr), _ip(t), _dp(f), _dp(st), ctypes.byref(e), _dp(fs))
+        return e.value, f, st, fs
+
     def compute_4b(self, dx, dr, typ, force, stress, energy):
         dx = np.ascontiguousarray(dx, dtype=np.float64)
         dr = np.ascontiguousarray(dr, dtype=np.float64)
@@ -195,6 +228,34 @@ class Oracle:
         e = ctypes.c_double(energy)
         self.lib.ora_compute_4b(self.h, _dp(dx), _dp(dr), _ip(t), _dp(force), _dp(stress), ctypes.byref(e))
         return e.value
+
+
+def build_reference_tab() -> Optional[str]:
+    """Compiles the reference's chimesFF.cpp with -DTABULATION into oracle/_ref
+    (tabulated 2B/3B terms) when the reference sources exist here."""
+    drv = os.path.join(HERE, "_ref", "ref_tab_driver")
+    if not os.path.isdir(REFROOT):
+        return drv if os.path.exists(drv) else None
+    try:
+        subprocess.run(["make", "-s", "-C", HERE, "reftab", "REFROOT=" + REFROOT], check=True,
+                       stdout=subprocess.DEVNULL)
+    except subprocess.CalledProcessError:
+        return None
+    return drv
+
+
+def run_reference_tab(param_file: str, queries: str, out_file: str) -> list:
+    """Runs compute_2B_tab / compute_3B_tab of the reference on a query file
+    (see oracle/ref_tab_driver.cpp); returns one float array per query."""
+    drv = build_reference_tab()
+    if drv is None or not os.path.exists(drv):
+        raise FileNotFoundError("reference tabulation driver not available")
+    # the reference joins the parameter file's directory and a table name with
+    # no separator, so it is run from that directory on the bare file name
+    subprocess.run([drv, os.path.basename(param_file), os.path.abspath(queries), os.path.abspath(out_file)],
+                   check=True, capture_output=True, cwd=os.path.dirname(os.path.abspath(param_file)))
+    with open(out_file) as f:
+        return [np.array([float(v) for v in ln.split()]) for ln in f if ln.strip()]
 
 
 def run_reference(param_file: str, xyz_file: str, small: bool, out_prefix: str, lists: bool = False,
