@@ -441,15 +441,21 @@ def extras(args):
     out["plain_fp64_per_config"] = {"value": sa / wall, "unit": UNIT, "configs": len(sample), "atoms": sa,
                                     "ms_per_config": 1e3 * wall / len(sample)}
     out["pair_style_c2"] = pair_style(params, cfg)
+    # the same with the 2- and 3-body terms tabulated (the reference's
+    # TABULATION option: spline / tricubic look-up instead of the Chebyshev sums)
+    ptab = synth.write_tabulated_param_file(os.path.join(tmp, "c2tab.params"), synth.spec_c2(), step3=0.1)
+    out["pair_style_c2_tabulated"] = pair_style(ptab, cfg, cpu_calls=1)
     out["serving"] = serving(args)
     return out
 
 
-def pair_style(params, cfg, skin=1.0, calls=30):
+def pair_style(params, cfg, skin=1.0, calls=30, cpu_calls=0):
     """The LAMMPS pair-style path (ck_nl_compute) on the C2 configuration as
     a rank sees it: 1024 local atoms plus ghosts, full neighbour lists within
     cutoff + skin; clusters built once, then evaluated per call with the host
-    positions copied in and forces copied out (as between re-neighbourings)."""
+    positions copied in and forces copied out (as between re-neighbourings).
+    cpu_calls > 0 also times the oracle's single-core restatement of the
+    same pair-style call (lists reused) for scale."""
     from chimes_calculator_gb300 import Calculator, synth
     c = Calculator()
     c.load_params(params)
@@ -466,9 +472,19 @@ def pair_style(params, cfg, skin=1.0, calls=30):
         c.nl_compute(nl, skin, rebuild=False)
     sec = (time.perf_counter() - t0) / calls
     l3, l4 = c.nl_lists()
-    return {"value": nl.nlocal / sec, "unit": UNIT, "ms_per_call": 1e3 * sec, "ms_rebuild_call": 1e3 * build,
-            "local_atoms": nl.nlocal, "ghost_atoms": int(len(nl.x) - nl.nlocal), "list_entries": int(len(nl.neigh)),
-            "listed_triplets": int(len(l3)), "listed_quadruplets": int(len(l4)), "skin": skin}
+    out = {"value": nl.nlocal / sec, "unit": UNIT, "ms_per_call": 1e3 * sec, "ms_rebuild_call": 1e3 * build,
+           "local_atoms": nl.nlocal, "ghost_atoms": int(len(nl.x) - nl.nlocal), "list_entries": int(len(nl.neigh)),
+           "listed_triplets": int(len(l3)), "listed_quadruplets": int(len(l4)), "skin": skin,
+           "tabulated": list(c.tabulated())}
+    if cpu_calls > 0:
+        from oracle.oracle import Oracle
+        o = Oracle(params)
+        o.lammps_compute(nl, skin, rebuild=True)
+        t0 = time.perf_counter()
+        for _ in range(cpu_calls):
+            o.lammps_compute(nl, skin, rebuild=False)
+        out["cpu_oracle_1core_ms_per_call"] = 1e3 * (time.perf_counter() - t0) / cpu_calls
+    return out
 
 
 def serving(args):

@@ -82,17 +82,37 @@ __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner
 // 3-body and 4-body clusters
 // ---------------------------------------------------------------------------
 // Shared memory of one cluster group: its T and dT/dr tables (CT), then the
-// pair geometry and cutoff values (double).  The group stride is an odd
-// number of 8-byte words, so the groups of a warp start on different banks and
-// lanes reading the same table entry of their own cluster do not conflict (a
-// stride that is a multiple of 32 bytes put every fourth group on the same bank).
+// pair geometry and cutoff values (double).  Lanes of different groups read
+// the same table offsets of their own clusters at once, so the group stride is
+// padded (in 8-byte steps) to spread the groups' first banks as far apart as
+// possible within one access phase (32 four-byte banks for FP32; 16 lanes of
+// eight-byte words for FP64).  Without it a 416-byte stride put every fourth
+// FP32 group on the same bank.
 __host__ __device__ inline size_t forcen_table_bytes(int np, int stride, size_t ct) {
     return ((size_t)2 * np * stride * ct + 7) & ~size_t(7);
 }
-__host__ __device__ inline size_t forcen_group_bytes(int np, int stride, size_t ct) {
-    size_t g = forcen_table_bytes(np, stride, ct) + sizeof(double) * np * 6;
-    if (((g / 8) & 1) == 0) g += 8;
-    return g;
+__host__ __device__ inline size_t forcen_group_bytes(int np, int stride, size_t ct, int tpc) {
+    const size_t base = forcen_table_bytes(np, stride, ct) + sizeof(double) * np * 6;
+    const int nb = ct == 4 ? 32 : 16;                         // banks per phase, in CT words
+    const int lanes = ct == 4 ? 32 : 16;                      // lanes per phase
+    const int groups = lanes / tpc > 1 ? lanes / tpc : 1;     // groups per phase
+    size_t best = base;
+    int best_d = -1;
+    for (int k = 0; k < 8; k++) {
+        const size_t g = base + 8 * (size_t)k;
+        const int S = (int)((g / ct) % (size_t)nb);
+        int dmin = nb;
+        for (int a = 1; a < groups; a++) {
+            const int o = (a * S) % nb;
+            const int d = o < nb - o ? o : nb - o;
+            if (d < dmin) dmin = d;
+        }
+        if (dmin > best_d) {
+            best_d = dmin;
+            best = g;
+        }
+    }
+    return best;
 }
 
 template <int NB, typename CT, int TPC>
@@ -107,7 +127,7 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
     const int grp = lane / TPC, gl = lane % TPC;
     // per-group shared layout: T[NP*stride], D[NP*stride] (CT); geo[NP][4], fc[NP], fcd[NP] (double)
     const size_t tbytes = forcen_table_bytes(NP, stride, sizeof(CT));
-    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT));
+    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT), TPC);
     unsigned char* gbase = smem + ((size_t)warp_in_block * G + grp) * gbytes;
     CT* T = reinterpret_cast<CT*>(gbase);
     CT* D = T + NP * stride;
@@ -243,7 +263,7 @@ void launch_n(const BatchView& B, const int* clusters, const long long* n_ptr, l
     if (n <= 0) return;
     constexpr int NP = NB * (NB - 1) / 2;
     const int block = 128;
-    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT));
+    const size_t gbytes = forcen_group_bytes(NP, stride, sizeof(CT), tpc);
     const int G = 32 / tpc;
     const size_t smem = gbytes * G * (block / 32);
     const long long steps = (n + G - 1) / G;
