@@ -85,6 +85,8 @@ SIGNATURES = {
     "ck_compute_cluster_batch": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
     "ck_compute_cluster_batch_tab": (I, [P, I, I, DP, DP, IP, DP, DP, DP, DP]),
     "ck_tabulated": (I, [P, IP]),
+    "ck_nl_fingerprint": (I, [P, I, LLP, DP, IP]),
+    "ck_fp_histogram": (I, [P, I, LL, DP, IP, LL, DP, IP, I, I, LLP, LLP]),
     "ck_calculate_noalloc": (I, [P, I, P, P, DP, I, P, P, P, P]),
     "ck_nl_compute": (I, [P, I, DP, IP, LLP, I, IP, IP, IP, D, I, DP, DP, DP, DP, DP]),
     "ck_nl_lists": (I, [P, LLP, IP, IP]),

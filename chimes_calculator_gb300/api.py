@@ -162,6 +162,37 @@ class Calculator:
         self._check(self.lib.ck_nl_lists(self.h, cnt, _ip(l3), _ip(l4)))
         return l3, l4
 
+    def nl_fingerprint(self, nbody: int):
+        """Fingerprint records of the last nl_compute (the pair style's
+        FINGERPRINT output): distances [n][P] and type indices [n][nbody]."""
+        n = ctypes.c_longlong(0)
+        self._check(self.lib.ck_nl_fingerprint(self.h, nbody, ctypes.byref(n), None, None))
+        P = nbody * (nbody - 1) // 2
+        d = np.zeros((n.value, P))
+        t = np.zeros((n.value, nbody), dtype=np.int32)
+        self._check(self.lib.ck_nl_fingerprint(self.h, nbody, ctypes.byref(n), _dp(d), _ip(t)))
+        return d, t
+
+    def fp_histogram(self, nbody: int, d1, t1, d2=None, t2=None, nbin: int = 100):
+        """Cluster-distance histogram of the reference's fingerprint tool on the
+        GPU: (counts[nbin], number of counted pairs).  d2/t2 None compares the
+        first set with itself (pairs j > i)."""
+        P = nbody * (nbody - 1) // 2
+        same = d2 is None
+        d1 = np.ascontiguousarray(d1, dtype=np.float64).reshape(-1, P)
+        t1 = np.ascontiguousarray(t1, dtype=np.int32).reshape(-1, nbody)
+        if same:
+            d2, t2 = d1, t1
+        else:
+            d2 = np.ascontiguousarray(d2, dtype=np.float64).reshape(-1, P)
+            t2 = np.ascontiguousarray(t2, dtype=np.int32).reshape(-1, nbody)
+        counts = np.zeros(nbin, dtype=np.int64)
+        ns = ctypes.c_longlong(0)
+        llp = ctypes.POINTER(ctypes.c_longlong)
+        self._check(self.lib.ck_fp_histogram(self.h, nbody, len(t1), _dp(d1), _ip(t1), len(t2), _dp(d2), _ip(t2),
+                                              int(same), nbin, counts.ctypes.data_as(llp), ctypes.byref(ns)))
+        return counts, ns.value
+
     def tabulated(self):
         """(2-body tabulated, 3-body tabulated) for the current parameter set."""
         t = np.zeros(2, dtype=np.int32)

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "ck_engine.h"
+#include "ck_fingerprint.h"
 #include "ck_nl.h"
 
 namespace {
@@ -34,6 +35,13 @@ struct Instance {
     // with the same atom count (the tuning is cached by shape).
     int last_natom = -1, same_shape_calls = 0;
     bool autotune_repeats = true;
+    // fingerprint records of the last ck_nl_fingerprint call, kept for a
+    // second call that fills the caller's arrays
+    int fp_body = 0;
+    long long fp_calls = -1;
+    std::vector<double> fp_d;
+    std::vector<int> fp_t;
+    long long nl_calls = 0;
     Instance() { eng.use_graph = true; }
 };
 
@@ -373,6 +381,7 @@ int ck_nl_compute(void* h, int nall, const double* x, const int* type, const lon
     std::string err;
     ck::Status st = in->nl->compute(in->slot, nall, x, type, tag, inum, ilist, numneigh, neigh, skin, rebuild != 0,
                                     f, energy, virial, eatom, vatom, err);
+    in->nl_calls++;
     if (st != ck::kOk) return report(st, err);
     g_err.clear();
     return ck::kOk;
@@ -579,6 +588,38 @@ int ck_compute_cluster_batch_tab(void* h, int nbody, int n, const double* dx, co
                                                              std::to_string(c) + ")"
                                                        : "3-body distance past the tabulated grid (cluster " +
                                                              std::to_string(c) + ")");
+    return ck::kOk;
+}
+
+int ck_nl_fingerprint(void* h, int nbody, long long* n, double* dist, int* types) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (!n) return report(ck::kErrInput, "count pointer is null");
+    if (!in->nl) return report(ck::kErrState, "no neighbour-list evaluation yet");
+    if (in->fp_calls != in->nl_calls || in->fp_body != nbody) {
+        std::string err;
+        ck::Status st = in->nl->fp_records(nbody, in->fp_d, in->fp_t, err);
+        if (st != ck::kOk) return report(st, err);
+        in->fp_calls = in->nl_calls;
+        in->fp_body = nbody;
+    }
+    *n = (long long)(in->fp_t.size() / (size_t)nbody);
+    if (dist && !in->fp_d.empty()) std::memcpy(dist, in->fp_d.data(), sizeof(double) * in->fp_d.size());
+    if (types && !in->fp_t.empty()) std::memcpy(types, in->fp_t.data(), sizeof(int) * in->fp_t.size());
+    return ck::kOk;
+}
+
+int ck_fp_histogram(void* h, int nbody, long long n1, const double* d1, const int* t1, long long n2,
+                    const double* d2, const int* t2, int same, int nbin, long long* counts, long long* nsamples) {
+    if (int st = check_handle(h)) return st;
+    Instance* in = static_cast<Instance*>(h);
+    if (int st = ensure_params(in)) return st;
+    if (!counts || !nsamples || (n1 > 0 && (!d1 || !t1)) || (!same && n2 > 0 && (!d2 || !t2)))
+        return report(ck::kErrInput, "fingerprint histogram: null array");
+    std::string err;
+    ck::Status st = ck::fp_histogram(in->eng, in->slot, nbody, n1, d1, t1, n2, d2, t2, same != 0, nbin, counts,
+                                     nsamples, err);
+    if (st != ck::kOk) return report(st, err);
     return ck::kOk;
 }
 

@@ -73,6 +73,11 @@ void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st);
 void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st);
 void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st);
 void launch_nl_tab3(const BatchView& B, long long n3, cudaStream_t st);
+// Fingerprint records of body order nbody over n candidates (list entries for
+// 2-body, listed clusters for 3-/4-body): count pass (flag[n]) or fill pass
+// (records at the scanned offsets off[n]) (ck_fingerprint.cu).
+void launch_nl_fp(const BatchView& B, const NeighView& N, int nbody, long long n, bool fill, int* flag,
+                  const long long* off, double* d, int* t, cudaStream_t st);
 
 // Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
 void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,

@@ -283,4 +283,45 @@ Status NeighCompute::lists(std::vector<int>& l3, std::vector<int>& l4, std::stri
     return kOk;
 }
 
+Status NeighCompute::fp_records(int nbody, std::vector<double>& d, std::vector<int>& t, std::string& err) {
+    d.clear();
+    t.clear();
+    if (!built_) {
+        err = "no neighbour-list evaluation yet";
+        return kErrState;
+    }
+    if (nbody < 2 || nbody > 4) {
+        err = "fingerprint records exist for 2-, 3- and 4-body clusters";
+        return kErrInput;
+    }
+    const HostParams& P = eng_.params(slot_);
+    if ((nbody == 3 && P.o3 <= 0) || (nbody == 4 && P.o4 <= 0)) {
+        err = "the parameter set has no " + std::to_string(nbody) + "-body terms";
+        return kErrInput;
+    }
+    const long long n = nbody == 2 ? nent_ : (nbody == 3 ? n3_ : n4_);
+    if (n <= 0) return kOk;
+    const int np = nbody * (nbody - 1) / 2;
+    const cudaStream_t s = eng_.stream();
+    NL_TRY(d_fp_flag_.reserve(n));
+    NL_TRY(d_fp_off_.reserve(n + 1));
+    NL_TRY(d_fp_tmp_.reserve(scan_tmp_bytes(n)));
+    launch_nl_fp(B_, N_, nbody, n, false, d_fp_flag_.p, nullptr, nullptr, nullptr, s);
+    exclusive_scan(d_fp_flag_.p, d_fp_off_.p, n, d_fp_tmp_.p, s);
+    long long total = 0;
+    NL_TRY(cudaMemcpyAsync(&total, d_fp_off_.p + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    NL_TRY(cudaStreamSynchronize(s));
+    if (total <= 0) return kOk;
+    NL_TRY(d_fp_d_.reserve(total * np));
+    NL_TRY(d_fp_t_.reserve(total * nbody));
+    launch_nl_fp(B_, N_, nbody, n, true, d_fp_flag_.p, d_fp_off_.p, d_fp_d_.p, d_fp_t_.p, s);
+    NL_TRY(cudaGetLastError());
+    d.resize((size_t)total * np);
+    t.resize((size_t)total * nbody);
+    NL_TRY(cudaMemcpyAsync(d.data(), d_fp_d_.p, sizeof(double) * d.size(), cudaMemcpyDeviceToHost, s));
+    NL_TRY(cudaMemcpyAsync(t.data(), d_fp_t_.p, sizeof(int) * t.size(), cudaMemcpyDeviceToHost, s));
+    NL_TRY(cudaStreamSynchronize(s));
+    return kOk;
+}
+
 }  // namespace ck

@@ -31,6 +31,12 @@ public:
     long long n4() const { return n4_; }
     // cluster lists of the last build (atom indices), for checks
     Status lists(std::vector<int>& l3, std::vector<int>& l4, std::string& err);
+    // Fingerprint records of the last compute (FINGERPRINT build of the pair
+    // style): the clusters of body order nbody that compute_nB evaluates and
+    // whose atoms are in recording order (2-body i < j, 3-/4-body strictly
+    // increasing tags), as distances d[n][P] and type indices t[n][nbody], in
+    // the pair style's loop order.
+    Status fp_records(int nbody, std::vector<double>& d, std::vector<int>& t, std::string& err);
 
 private:
     Engine& eng_;
@@ -50,7 +56,10 @@ private:
     DevBuf<int> d_flags_, d_bk_count_, d_bk_fill_, d_perm3_, d_perm4_;
     DevBuf<long long> d_bk_start_;
     DevBuf<unsigned long long> d_queue_, d_minmax_;
-    DevBuf<unsigned char> d_scan_tmp_;
+    DevBuf<unsigned char> d_scan_tmp_, d_fp_tmp_;
+    DevBuf<int> d_fp_flag_, d_fp_t_;
+    DevBuf<long long> d_fp_off_;
+    DevBuf<double> d_fp_d_;
     std::vector<double> h_force_, h_eatom_, h_vatom_;
 };
 

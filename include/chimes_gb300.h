@@ -220,6 +220,31 @@ int ck_nl_compute(void *h, int nall, const double *x, const int *type, const lon
  * l4[n4][4] (atom indices, may be NULL) */
 int ck_nl_lists(void *h, long long *counts, int *l3, int *l4);
 
+/* Cluster fingerprints (the reference's FINGERPRINT build,
+ * etc/lmp/src/pair_chimes.cpp:525-536, 620-662, 700-741, 775-810 and
+ * chimesFF/src/chimesFF.cpp:1694-1702, 2013-2021, 2603-2612): the records the
+ * pair style writes to "<step>.<rank>.<n>b_clusters.txt" for the last
+ * ck_nl_compute call -- the nbody-atom clusters compute_nB evaluated whose
+ * atoms are in recording order (2-body: i < j; 3-/4-body: strictly increasing
+ * tags), in the pair style's loop order.  *n receives the count; dist[n][P]
+ * (distances ij / ij,ik,jk / ij,ik,il,jk,jl,kl) and types[n][nbody] (type
+ * indices) are filled when not NULL (call once with NULLs to size them). */
+int ck_nl_fingerprint(void *h, int nbody, long long *n, double *dist, int *types);
+
+/* Cluster-distance histogram of the reference's fingerprint tool
+ * (chimesFF/src/FP/multi_calc_histogram.cpp, gen_flat_hists with one process)
+ * for records of one body order, with the handle's parameter set: each
+ * record's distances are mapped with the Morse transform of its own cutoffs
+ * and sorted; every pair (i of set 1, j of set 2, or j > i within set 1 when
+ * same != 0) adds its Euclidean distance to counts[nbin] over [0, maxd), maxd
+ * = 3, sqrt(12)+1, sqrt(24)+1 for nbody = 2, 3, 4 (the reference uses nbin =
+ * 100).  *nsamples receives the number of counted pairs; the normalised
+ * histogram is counts / nsamples at bin centres (k + 1/2) * maxd / nbin.  As in
+ * the reference, a first set of fewer than two records counts nothing.  A
+ * distance past the last bin is an error (the reference exits there). */
+int ck_fp_histogram(void *h, int nbody, long long n1, const double *d1, const int *t1, long long n2,
+                    const double *d2, const int *t2, int same, int nbin, long long *counts, long long *nsamples);
+
 /* Batched per-cluster evaluation (chimesFF::compute_nB semantics, FP64) with
  * the handle's current parameter set: n clusters of nbody = 2, 3 or 4 atoms,
  * dx[n][P] distances, dr[n][P][3] vectors (atom2 - atom1, pairs ij / ij,ik,jk /

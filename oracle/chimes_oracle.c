@@ -20,6 +20,9 @@
  *                      serial_interface/src/serial_chimes_interface.cpp:85-587
  *   cluster lists .... simulation_system::build_neigh_lists  serial_chimes_interface.cpp:588-864
  *   driver ........... serial_chimes_interface::calculate    serial_chimes_interface.cpp:960-1124
+ *   fingerprints ..... cluster records of the FINGERPRINT build  etc/lmp/src/pair_chimes.cpp:525-536,
+ *                      620-662, 700-741, 775-810; chimesFF.cpp:1694-1702, 2013-2021, 2603-2612
+ *                      cluster-distance histograms  chimesFF/src/FP/multi_calc_histogram.cpp
  *   tabulated terms .. read_2B_tab / read_3B_tab     chimesFF.cpp:199-351 (TABULATION build)
  *                      compute_2B_tab / get_tab_2B   chimesFF.cpp:1776-1922
  *                      compute_3B_tab / interpolateTricubic / get_tab_3B  chimesFF.cpp:2177-2463
@@ -83,6 +86,10 @@ typedef struct {
     long lmp_n3, lmp_n4, lmp_c3, lmp_c4;
     int lmp_built;
     long cap2, cap3, cap4;
+    /* fingerprint records of the last pair-style call (when lmp_fp is set):
+     * [body-2] -> distances [n][P] and type indices [n][body] */
+    int lmp_fp;
+    double *fp_d[3]; int *fp_t[3]; long fp_n[3], fp_cap[3];
 } ora_handle;
 
 /* ------------------------------------------------------------------ */
@@ -1133,6 +1140,7 @@ void ora_free(void *vh) {
     ora_handle *h = vh; if (!h) return;
     free(h->l2); free(h->l3); free(h->l4);
     free(h->lmp_l3); free(h->lmp_l4);
+    for (int b = 0; b < 3; b++) { free(h->fp_d[b]); free(h->fp_t[b]); }
     free(h);  /* parameter tables are left to process exit: test-only object */
 }
 
@@ -1276,6 +1284,60 @@ static void lmp_tally(const int *atoms, int n, double e, const double *st, doubl
     }
 }
 
+/* one fingerprint record: the cluster's distances and type indices (what
+ * compute_nB appends to clusters_nb in the FINGERPRINT build) */
+static int fp_push(ora_handle *h, int body, const double *d, const int *t) {
+    const int b = body - 2, P = body * (body - 1) / 2;
+    if (h->fp_n[b] >= h->fp_cap[b]) {
+        long nc = h->fp_cap[b] ? 2 * h->fp_cap[b] : 1024;
+        double *nd = realloc(h->fp_d[b], (size_t)nc * P * sizeof(double));
+        if (!nd) return -1;
+        h->fp_d[b] = nd;
+        int *nt = realloc(h->fp_t[b], (size_t)nc * body * sizeof(int));
+        if (!nt) return -1;
+        h->fp_t[b] = nt;
+        h->fp_cap[b] = nc;
+    }
+    memcpy(h->fp_d[b] + h->fp_n[b] * P, d, P * sizeof(double));
+    memcpy(h->fp_t[b] + h->fp_n[b] * body, t, body * sizeof(int));
+    h->fp_n[b]++;
+    return 0;
+}
+
+/* cutoff checks of compute_nB: 1 when the cluster is evaluated (and recorded) */
+static int fp_passes(ora_ff *ff, int body, const double *dx, const int *t) {
+    int nt = ff->ntypes;
+    if (body == 2) return dx[0] < ff->rout[ff->pair_map[t[0] * nt + t[1]]];
+    int u = 0;
+    for (int k = 0; k < body; k++) u = u * nt + t[k];
+    if (body == 3) {
+        int c = ff->trip_map[u];
+        if (c < 0) return 0;
+        for (int p = 0; p < 3; p++) if (dx[p] >= ff->cut3[(c * 2 + 1) * 3 + ff->trip_perm[u * 3 + p]]) return 0;
+        return 1;
+    }
+    int c = ff->quad_map[u];
+    if (c < 0) return 0;
+    for (int p = 0; p < 6; p++) if (dx[p] >= ff->cut4[(c * 2 + 1) * 6 + ff->quad_perm[u * 6 + p]]) return 0;
+    return 1;
+}
+
+void ora_lammps_fp(void *vh, int on) { ((ora_handle *)vh)->lmp_fp = on; }
+
+void ora_lammps_fp_sizes(void *vh, long *n) {
+    ora_handle *h = vh;
+    for (int b = 0; b < 3; b++) n[b] = h->fp_n[b];
+}
+
+void ora_lammps_fp_records(void *vh, int body, double *d, int *t) {
+    ora_handle *h = vh;
+    const int b = body - 2, P = body * (body - 1) / 2;
+    if (h->fp_n[b]) {
+        memcpy(d, h->fp_d[b], (size_t)h->fp_n[b] * P * sizeof(double));
+        memcpy(t, h->fp_t[b], (size_t)h->fp_n[b] * body * sizeof(int));
+    }
+}
+
 int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, const long long *tag, int inum,
                        const int *ilist, const int *numneigh, const int *neigh, double skin, int rebuild, double *f,
                        double *energy, double *virial, double *eatom, double *vatom) {
@@ -1290,6 +1352,7 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
     if (ff->o3 > 0) c3 = max_cutn(ff, 3);
     if (ff->o4 > 0) c4 = max_cutn(ff, 4);
     const double c3p = c3 + skin, c4p = c4 + skin;   /* maxcut_nb + neighbor->skin */
+    h->fp_n[0] = h->fp_n[1] = h->fp_n[2] = 0;
     if (rebuild || !h->lmp_built) {
         h->lmp_n3 = h->lmp_n4 = 0;
         h->lmp_built = 1;
@@ -1347,6 +1410,10 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             for (int c = 0; c < 3; c++) { f[3 * i + c] += f2[c]; f[3 * j + c] += f2[3 + c]; }
             *energy += e;
             const int pr[2] = {i, j};
+            if (h->lmp_fp && i < j) {   /* valid_order = (i < j) (:626) */
+                const int tt[2] = {typ[i], typ[j]};
+                if (fp_passes(ff, 2, &d, tt) && fp_push(h, 2, &d, tt)) { free(off); FAIL(h, "out of memory"); }
+            }
             lmp_tally(pr, 2, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
             virial[3] += st[1]; virial[4] += st[2]; virial[5] += st[4];
@@ -1365,6 +1432,8 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             else ora_compute_3b(h, dx, dr, t, f3, st, &e);
             for (int a = 0; a < 3; a++)
                 for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f3[3 * a + c];
+            if (h->lmp_fp && tag[id[0]] < tag[id[1]] && tag[id[0]] < tag[id[2]] && tag[id[1]] < tag[id[2]] &&
+                fp_passes(ff, 3, dx, t) && fp_push(h, 3, dx, t)) { free(off); FAIL(h, "out of memory"); }
             *energy += e;
             lmp_tally(id, 3, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
@@ -1380,6 +1449,8 @@ int ora_lammps_compute(void *vh, int nall, const double *x, const int *typ, cons
             ora_compute_4b(h, dx, dr, t, f4, st, &e);
             for (int a = 0; a < 4; a++)
                 for (int c = 0; c < 3; c++) f[3 * id[a] + c] += f4[3 * a + c];
+            if (h->lmp_fp && tag[id[0]] < tag[id[1]] && tag[id[1]] < tag[id[2]] && tag[id[2]] < tag[id[3]] &&
+                fp_passes(ff, 4, dx, t) && fp_push(h, 4, dx, t)) { free(off); FAIL(h, "out of memory"); }
             *energy += e;
             lmp_tally(id, 4, e, st, eatom, vatom);
             virial[0] += st[0]; virial[1] += st[3]; virial[2] += st[5];
@@ -1400,4 +1471,94 @@ void ora_lammps_lists(void *vh, int *l3, int *l4) {
     ora_handle *h = vh;
     if (l3 && h->lmp_n3) memcpy(l3, h->lmp_l3, h->lmp_n3 * 3 * sizeof(int));
     if (l4 && h->lmp_n4) memcpy(l4, h->lmp_l4, h->lmp_n4 * 4 * sizeof(int));
+}
+
+/* ------------------------------------------------------------------ */
+/* cluster-distance histograms (chimesFF/src/FP/multi_calc_histogram.cpp,
+ * one process)                                                         */
+/* ------------------------------------------------------------------ */
+/* transform (multi_calc_histogram.cpp:112-123): the Morse map of the cluster's own cutoffs */
+static double fp_transform(double rcin, double rcout, double lambda, double rij) {
+    double x_min = exp(-1 * rcin / lambda);
+    double x_max = exp(-1 * rcout / lambda);
+    double x_avg = 0.5 * (x_max + x_min);
+    double x_diff = 0.5 * (x_max - x_min);
+    x_diff *= -1.0;
+    return (exp(-1 * rij / lambda) - x_avg) / x_diff;
+}
+
+static int cmp_dbl(const void *a, const void *b) {
+    double x = *(const double *)a, y = *(const double *)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* read_flat_clusters (:26-107): transformed edge lengths of each record, ascending */
+static int fp_edges(ora_handle *h, int body, long n, const double *d, const int *t, double *out) {
+    ora_ff *ff = &h->ff;
+    int nt = ff->ntypes, P = body * (body - 1) / 2;
+    static const int A[6] = {0, 0, 0, 1, 1, 2}, B[6] = {1, 2, 3, 2, 3, 3};
+    static const int A3[3] = {0, 0, 1}, B3[3] = {1, 2, 2};
+    for (long c = 0; c < n; c++) {
+        const int *ty = t + c * body;
+        for (int k = 0; k < body; k++)
+            if (ty[k] < 0 || ty[k] >= nt) FAIL(h, "fingerprint record %ld: type index out of range", c);
+        double *e = out + c * P;
+        if (body == 2) {
+            int p = ff->pair_map[ty[0] * nt + ty[1]];
+            e[0] = fp_transform(ff->rin[p], ff->rout[p], ff->lam[p], d[c]);
+        } else {
+            int u = 0;
+            for (int k = 0; k < body; k++) u = u * nt + ty[k];
+            int tt = body == 3 ? ff->trip_map[u] : ff->quad_map[u];
+            if (tt < 0) FAIL(h, "fingerprint record %ld: excluded cluster type", c);
+            const int *m = body == 3 ? &ff->trip_perm[u * 3] : &ff->quad_perm[u * 6];
+            const double *cut = body == 3 ? ff->cut3 : ff->cut4;
+            for (int p = 0; p < P; p++) {
+                int a = body == 3 ? A3[p] : A[p], b = body == 3 ? B3[p] : B[p];
+                double lam = ff->lam[ff->pair_map[ty[a] * nt + ty[b]]];
+                e[p] = fp_transform(cut[(tt * 2 + 0) * P + m[p]], cut[(tt * 2 + 1) * P + m[p]], lam, d[c * P + p]);
+            }
+        }
+        qsort(e, P, sizeof(double), cmp_dbl);
+    }
+    return 0;
+}
+
+/* gen_flat_hists (:240-480) with one process: counts[nbin], *nsamples.  The
+ * composition term is zero there (it reads the zero-filled front of vectors
+ * that were sized before being appended to), so the distance is the Euclidean
+ * distance of the sorted edge vectors.  Returns -1 with a message when a
+ * distance falls past the last bin (the reference exits, or writes past its
+ * histogram when it falls exactly one bin past). */
+int ora_fp_histogram(void *vh, int body, long n1, const double *d1, const int *t1, long n2, const double *d2,
+                     const int *t2, int same, int nbin, long long *counts, long long *nsamples) {
+    ora_handle *h = vh;
+    int P = body * (body - 1) / 2;
+    double maxd = body == 2 ? 3.0 : (body == 3 ? sqrt(12.0) + 1.0 : sqrt(24.0) + 1.0);
+    double binw = maxd / nbin;
+    double *e1 = malloc((size_t)(n1 > 0 ? n1 : 1) * P * sizeof(double));
+    double *e2 = malloc((size_t)(n2 > 0 ? n2 : 1) * P * sizeof(double));
+    if (!e1 || !e2) { free(e1); free(e2); FAIL(h, "out of memory"); }
+    if (fp_edges(h, body, n1, d1, t1, e1) || fp_edges(h, body, n2, d2, t2, e2)) { free(e1); free(e2); return -1; }
+    memset(counts, 0, (size_t)nbin * sizeof(long long));
+    *nsamples = 0;
+    /* divide_task with one process: tasks 0..n1-1, and nothing at all unless
+     * end - start > 0 (a single cluster in the first set counts nothing) */
+    long start = n1 > 0 ? 0 : 1, end = n1 - 1;
+    int bad = 0;
+    if (end - start > 0)
+        for (long i = start; i <= end; i++)
+            for (long j = same ? i + 1 : 0; j < n2; j++) {
+                double ds = 0;
+                for (int k = 0; k < P; k++) ds += pow(e1[i * P + k] - e2[j * P + k], 2.0);
+                double dist = sqrt(ds) + fabs(0.0 - 0.0);
+                int bin = (int)floor(dist / binw);
+                if (dist == maxd) bin = bin - 1;
+                if (bin >= nbin || bin < 0) { bad = 1; continue; }
+                counts[bin] += 1;
+                *nsamples += 1;
+            }
+    free(e1); free(e2);
+    if (bad) FAIL(h, "ERROR: computed bin larger than nbins");
+    return 0;
 }

@@ -80,6 +80,11 @@ def _load():
         lib.ora_compute_3b_tab.argtypes = [P, dp, dp, ip, dp, dp, dp, dp]
         lib.ora_tab_flags.restype = I
         lib.ora_tab_flags.argtypes = [P, ip, ip]
+        lib.ora_lammps_fp.argtypes = [P, I]
+        lib.ora_lammps_fp_sizes.argtypes = [P, lp]
+        lib.ora_lammps_fp_records.argtypes = [P, I, dp, ip]
+        lib.ora_fp_histogram.restype = I
+        lib.ora_fp_histogram.argtypes = [P, I, L, dp, ip, L, dp, ip, I, I, llp, llp]
         lib.ora_lammps_sizes.argtypes = [P, lp, lp]
         lib.ora_lammps_lists.argtypes = [P, ip, ip]
         _lib = lib
@@ -161,6 +166,37 @@ class Oracle:
         if rc != 0:
             raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
         return {"energy": e.value, "force": f, "virial": vir, "eatom": eatom, "vatom": vatom}
+
+    def lammps_fingerprint(self, on: bool = True):
+        """Record the FINGERPRINT build's cluster records on later lammps_compute calls."""
+        self.lib.ora_lammps_fp(self.h, int(bool(on)))
+
+    def lammps_fp_records(self, body: int):
+        """(distances [n][P], types [n][body]) recorded by the last lammps_compute."""
+        n = (ctypes.c_long * 3)()
+        self.lib.ora_lammps_fp_sizes(self.h, n)
+        P = body * (body - 1) // 2
+        d = np.zeros((n[body - 2], P))
+        t = np.zeros((n[body - 2], body), dtype=np.int32)
+        self.lib.ora_lammps_fp_records(self.h, body, _dp(d), _ip(t))
+        return d, t
+
+    def fp_histogram(self, body: int, d1, t1, d2=None, t2=None, nbin: int = 100):
+        """Cluster-distance histogram of multi_calc_histogram.cpp (one process):
+        counts[nbin] and the sample count; d2/t2 None means the same set (pairs j > i)."""
+        same = d2 is None
+        d1 = np.ascontiguousarray(d1, dtype=np.float64)
+        t1 = np.ascontiguousarray(t1, dtype=np.int32)
+        d2 = d1 if same else np.ascontiguousarray(d2, dtype=np.float64)
+        t2 = t1 if same else np.ascontiguousarray(t2, dtype=np.int32)
+        counts = np.zeros(nbin, dtype=np.int64)
+        ns = ctypes.c_longlong(0)
+        llp = ctypes.POINTER(ctypes.c_longlong)
+        rc = self.lib.ora_fp_histogram(self.h, body, len(t1), _dp(d1), _ip(t1), len(t2), _dp(d2), _ip(t2), int(same),
+                                       nbin, counts.ctypes.data_as(llp), ctypes.byref(ns))
+        if rc != 0:
+            raise ValueError("oracle: " + self.lib.ora_error(self.h).decode())
+        return counts, ns.value
 
     def lammps_lists(self):
         n3, n4 = ctypes.c_long(), ctypes.c_long()
