@@ -445,6 +445,7 @@ def extras(args):
     # TABULATION option: spline / tricubic look-up instead of the Chebyshev sums)
     ptab = synth.write_tabulated_param_file(os.path.join(tmp, "c2tab.params"), synth.spec_c2(), step3=0.1)
     out["pair_style_c2_tabulated"] = pair_style(ptab, cfg, cpu_calls=1)
+    out["fingerprint_c2"] = fingerprint(params, cfg)
     out["serving"] = serving(args)
     return out
 
@@ -485,6 +486,61 @@ def pair_style(params, cfg, skin=1.0, calls=30, cpu_calls=0):
             o.lammps_compute(nl, skin, rebuild=False)
         out["cpu_oracle_1core_ms_per_call"] = 1e3 * (time.perf_counter() - t0) / cpu_calls
     return out
+
+
+def fingerprint(params, cfg, skin=1.0, cpu_records=3000):
+    """The FINGERPRINT pipeline on the C2 configuration: the pair style's
+    cluster records of one step (GPU) and the self-histograms of the
+    reference's histogram tool per body order (GPU all-pairs kernel), with
+    the oracle's single-core histogram timed on the first `cpu_records`
+    records of each order for scale."""
+    from chimes_calculator_gb300 import Calculator, synth
+    from oracle.oracle import Oracle
+    c = Calculator()
+    c.load_params(params)
+    nl = synth.lammps_neighbors(cfg, c.type_indices(cfg.types, 0), max(c.info(0)["max_cutoffs"]) + skin, seed=11)
+    c.nl_compute(nl, skin, rebuild=True)
+    o = Oracle(params)
+    out = {}
+    for nb in (2, 3, 4):
+        t0 = time.perf_counter()
+        d, t = c.nl_fingerprint(nb)
+        rec_s = time.perf_counter() - t0
+        c.fp_histogram(nb, d[:64], t[:64])                 # warm-up (module load, allocations)
+        t0 = time.perf_counter()
+        counts, ns = c.fp_histogram(nb, d, t)
+        gpu_s = time.perf_counter() - t0
+        m = min(cpu_records, len(t))
+        t0 = time.perf_counter()
+        _, cns = o.fp_histogram(nb, d[:m], t[:m])
+        cpu_s = time.perf_counter() - t0
+        out["%db" % nb] = {"records": int(len(t)), "pairs": int(ns), "records_ms": 1e3 * rec_s,
+                           "histogram_ms": 1e3 * gpu_s, "pairs_per_s": ns / gpu_s,
+                           "cpu_oracle_1core_pairs_per_s": cns / cpu_s if cpu_s > 0 else None,
+                           "cpu_sample_records": m}
+    return out
+
+
+def profile_pairstyle(args, skin=1.0):
+    """Profiler run of the pair-style path on the C2 configuration."""
+    from chimes_calculator_gb300 import Calculator, synth
+    tmp = tempfile.mkdtemp(prefix="ckp")
+    params, cfg = make_workload(tmp)
+    if args.profile_pairstyle == "tabulated":
+        params = synth.write_tabulated_param_file(os.path.join(tmp, "c2tab.params"), synth.spec_c2(), step3=0.1)
+    c = Calculator()
+    c.load_params(params)
+    nl = synth.lammps_neighbors(cfg, c.type_indices(cfg.types, 0), max(c.info(0)["max_cutoffs"]) + skin, seed=11)
+    c.nl_compute(nl, skin, rebuild=True)
+    if args.profile_pairstyle == "fingerprint":
+        d, t = c.nl_fingerprint(3)
+        counts, ns = c.fp_histogram(3, d, t)
+        print(json.dumps({"records": int(len(t)), "pairs": int(ns)}))
+        return
+    t0 = time.perf_counter()
+    for _ in range(5):
+        c.nl_compute(nl, skin, rebuild=False)
+    print(json.dumps({"mode": args.profile_pairstyle, "ms_per_call": 1e3 * (time.perf_counter() - t0) / 5}))
 
 
 def serving(args):
@@ -694,9 +750,15 @@ def main():
                     help="autotune (auto) or one fixed 3-/4-body contraction form (profiler runs)")
     ap.add_argument("--tuning", default="",
                     help="with a fixed --contraction: tpc3,tpc4,blocks_per_sm (ck_set_tuning)")
+    ap.add_argument("--profile-pairstyle", default="", choices=["", "chebyshev", "tabulated", "fingerprint"],
+                    help="profiler run of the pair-style path on C2 (Chebyshev or tabulated terms: one list "
+                         "build + 5 calls), or of the 3-body fingerprint histogram of its records")
     args = ap.parse_args()
     if args.profile_batched:
         profile_batched(args)
+        return
+    if args.profile_pairstyle:
+        profile_pairstyle(args)
         return
     if args.profile_run:
         args.steps, args.warmup, args.no_cpu, args.extras = 2, 3, True, False

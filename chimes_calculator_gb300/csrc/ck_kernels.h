@@ -45,7 +45,9 @@ struct ForceLaunch {
     int fact3 = 0, fact4 = 0;
     int want_fact3 = 1, want_fact4 = 1;   // preference (autotuner); fact = want && tables present
     int rf3 = 0, rf4 = 0;  // powers per pair (max over the batch's sets)
-    int ftpc3 = 1, ftpc4 = 1;      // threads per cluster: 1, 2 or 4
+    // threads per cluster: 1, 2 or 4 (the 4-body default 4: what the autotuner
+    // picks on the FP64 workloads; untuned paths such as ck_nl_compute use it)
+    int ftpc3 = 1, ftpc4 = 4;
     int fbps3 = 8, fbps4 = 8;      // resident one-warp blocks per SM (capped by occupancy)
     int noy3 = 0;                  // factored 3-body without the Y table (products per entry)
 };
@@ -72,7 +74,10 @@ size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st);
 void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st);
 void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st);
-void launch_nl_tab3(const BatchView& B, long long n3, cudaStream_t st);
+// tabulated 3-body term: selection of the evaluated triplets (sel[n3], selr[3*n3],
+// *count on the device) and their look-ups
+void launch_nl_tab3(const BatchView& B, long long n3, int* sel, double* selr, unsigned long long* count,
+                    cudaStream_t st);
 // Fingerprint records of body order nbody over n candidates (list entries for
 // 2-body, listed clusters for 3-/4-body): count pass (flag[n]) or fill pass
 // (records at the scanned offsets off[n]) (ck_fingerprint.cu).

@@ -186,46 +186,87 @@ __global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
     }
 }
 
-// Tabulated 3-body term (compute_3B_tab, chimesFF.cpp:2183-2322) of every
-// listed triplet: one thread per triplet; the type and per-pair outer-cutoff
-// checks of compute_3B, then the tricubic table look-up.
-__global__ void __launch_bounds__(128) k_nl_tab3(BatchView B, long long n3) {
+// Tabulated 3-body term (compute_3B_tab, chimesFF.cpp:2183-2322) in two
+// passes.  Selection: one thread per listed triplet applies compute_3B's type
+// and per-pair outer-cutoff checks (the lists hold every triplet within the
+// padded cutoffs, most of them outside the table's cutoffs) and appends the
+// evaluated ones with their distances (warp-aggregated atomics).  Evaluation:
+// one thread per selected triplet, so no lane idles in the FP64-bound look-up.
+__global__ void __launch_bounds__(256) k_nl_tab3_sel(BatchView B, long long n3, int* sel, double* selr,
+                                                     unsigned long long* count) {
     const DevParamSet& P = B.psets[B.sys[0].pset];
     const double* x = B.ghost_fs;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n3; base += stride) {
+        const long long q = base + lane;
+        bool pass = false;
+        double r[3] = {0.0, 0.0, 0.0};
+        if (q < n3) {
+            const int id[3] = {B.c3[3 * q], B.c3[3 * q + 1], B.c3[3 * q + 2]};
+            const int u = (B.atom_type[id[0]] * P.ntypes + B.atom_type[id[1]]) * P.ntypes + B.atom_type[id[2]];
+            const TupleRec& R = P.t3[u];
+            if (R.type_id >= 0) {
+                r[0] = nl_dist(x, id[0], id[1], nullptr);
+                r[1] = nl_dist(x, id[0], id[2], nullptr);
+                r[2] = nl_dist(x, id[1], id[2], nullptr);
+                pass = r[0] < R.rout[0] && r[1] < R.rout[1] && r[2] < R.rout[2];
+            }
+        }
+        const unsigned m = __ballot_sync(kFull, pass);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long b0 = 0;
+        if (lane == leader) b0 = atomicAdd(count, (unsigned long long)__popc(m));
+        b0 = __shfl_sync(kFull, b0, leader);
+        if (pass) {
+            const unsigned long long s = b0 + __popc(m & ((1u << lane) - 1u));
+            sel[s] = (int)q;
+            selr[3 * s] = r[0];
+            selr[3 * s + 1] = r[1];
+            selr[3 * s + 2] = r[2];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_nl_tab3(BatchView B, const int* sel, const double* selr,
+                                                 const unsigned long long* count) {
+    const DevParamSet& P = B.psets[B.sys[0].pset];
+    const double* x = B.ghost_fs;
+    const long long n = (long long)*count;
     EVAcc acc;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += stride) {
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += stride) {
+        const long long q = sel[s];
         const int id[3] = {B.c3[3 * q], B.c3[3 * q + 1], B.c3[3 * q + 2]};
         const int u = (B.atom_type[id[0]] * P.ntypes + B.atom_type[id[1]]) * P.ntypes + B.atom_type[id[2]];
-        const TupleRec& R = P.t3[u];
-        if (R.type_id < 0) continue;   // excluded triplet type
-        double dr[3][3], r[3];
-        r[0] = nl_dist(x, id[0], id[1], dr[0]);   // ij
-        r[1] = nl_dist(x, id[0], id[2], dr[1]);   // ik
-        r[2] = nl_dist(x, id[1], id[2], dr[2]);   // jk
-        if (r[0] >= R.rout[0] || r[1] >= R.rout[1] || r[2] >= R.rout[2]) continue;
+        const int type_id = P.t3[u].type_id;
+        double dr[3][3];
+        nl_dist(x, id[0], id[1], dr[0]);   // ij
+        nl_dist(x, id[0], id[2], dr[1]);   // ik
+        nl_dist(x, id[1], id[2], dr[2]);   // jk
         double v[4];
-        const int ts = tab3_lookup(P, R.type_id, r[0], r[1], r[2], v);
+        const int ts = tab3_lookup_sep(P, type_id, selr[3 * s], selr[3 * s + 1], selr[3 * s + 2], v);
         if (ts) atomicOr(&B.flags[5], ts);
         // forces in the reference's order: ij on (i, j), ik on (i, k), jk on (j, k)
         double f[3][3];
         for (int c = 0; c < 3; c++) {
-            const double a = __dmul_rn(v[1], dr[0][c]), b = __dmul_rn(v[2], dr[1][c]), g = __dmul_rn(v[3], dr[2][c]);
-            f[0][c] = __dadd_rn(__dadd_rn(0.0, a), b);
-            f[1][c] = __dadd_rn(__dsub_rn(0.0, a), g);
-            f[2][c] = __dsub_rn(__dsub_rn(0.0, b), g);
+            const double a = v[1] * dr[0][c], b = v[2] * dr[1][c], g = v[3] * dr[2][c];
+            f[0][c] = a + b;
+            f[1][c] = g - a;
+            f[2][c] = -b - g;
         }
         // stress -= fs_p * (dr_p (x) dr_p), pair by pair (distance-tensor form)
         double vir[6] = {0, 0, 0, 0, 0, 0};
         for (int p = 0; p < 3; p++) {
             const double* d = dr[p];
             const double fsp = v[1 + p];
-            vir[0] = __dsub_rn(vir[0], __dmul_rn(fsp, __dmul_rn(d[0], d[0])));
-            vir[1] = __dsub_rn(vir[1], __dmul_rn(fsp, __dmul_rn(d[0], d[1])));
-            vir[2] = __dsub_rn(vir[2], __dmul_rn(fsp, __dmul_rn(d[0], d[2])));
-            vir[3] = __dsub_rn(vir[3], __dmul_rn(fsp, __dmul_rn(d[1], d[1])));
-            vir[4] = __dsub_rn(vir[4], __dmul_rn(fsp, __dmul_rn(d[1], d[2])));
-            vir[5] = __dsub_rn(vir[5], __dmul_rn(fsp, __dmul_rn(d[2], d[2])));
+            vir[0] -= fsp * (d[0] * d[0]);
+            vir[1] -= fsp * (d[0] * d[1]);
+            vir[2] -= fsp * (d[0] * d[2]);
+            vir[3] -= fsp * (d[1] * d[1]);
+            vir[4] -= fsp * (d[1] * d[2]);
+            vir[5] -= fsp * (d[2] * d[2]);
         }
         for (int a = 0; a < 3; a++) add_force(B, id[a], f[a][0], f[a][1], f[a][2]);
         acc.add(B, 0, v[0], vir);
@@ -263,10 +304,14 @@ void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cuda
     else count_launch(), k_nl_pairs<double><<<grid, 256, 0, st>>>(B, N);
 }
 
-void launch_nl_tab3(const BatchView& B, long long n3, cudaStream_t st) {
+void launch_nl_tab3(const BatchView& B, long long n3, int* sel, double* selr, unsigned long long* count,
+                    cudaStream_t st) {
     if (n3 <= 0) return;
-    const unsigned grid = grid_of(n3, 128, (long long)sm_count() * 16);
-    count_launch(), k_nl_tab3<<<grid, 128, 0, st>>>(B, n3);
+    cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+    count_launch(), k_nl_tab3_sel<<<grid_of(n3, 256, (long long)sm_count() * 8), 256, 0, st>>>(B, n3, sel, selr,
+                                                                                                count);
+    // the selected count stays on the device: the grid covers the listed triplets
+    count_launch(), k_nl_tab3<<<grid_of(n3, 128, (long long)sm_count() * 8), 128, 0, st>>>(B, sel, selr, count);
 }
 
 }  // namespace ck

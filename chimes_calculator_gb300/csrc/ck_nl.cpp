@@ -224,7 +224,12 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     }
     launch_nl_pairs(B, N, L.precision, s);
     if (L.stride3 > 0 && n3_ > 0) {
-        if (tab3) launch_nl_tab3(B, n3_, s);
+        if (tab3) {
+            NL_TRY(d_tsel_.reserve(n3_));
+            NL_TRY(d_tselr_.reserve(3 * n3_));
+            NL_TRY(d_tcount_.reserve(1));
+            launch_nl_tab3(B, n3_, d_tsel_.p, d_tselr_.p, d_tcount_.p, s);
+        }
         else if (L.fact3) launch_force3f(B, L, s);
         else launch_force3(B, L, s);
     }

@@ -59,7 +59,9 @@ private:
     DevBuf<unsigned char> d_scan_tmp_, d_fp_tmp_;
     DevBuf<int> d_fp_flag_, d_fp_t_;
     DevBuf<long long> d_fp_off_;
-    DevBuf<double> d_fp_d_;
+    DevBuf<double> d_fp_d_, d_tselr_;
+    DevBuf<int> d_tsel_;
+    DevBuf<unsigned long long> d_tcount_;
     std::vector<double> h_force_, h_eatom_, h_vatom_;
 };
 
