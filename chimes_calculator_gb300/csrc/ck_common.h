@@ -251,6 +251,8 @@ struct BatchView {
     // contraction: bucket key = pset.bk{3,4} + tuple index; each bucket padded
     // to a multiple of 32 slots with -1, so a warp's clusters share one tuple
     int nbk3, nbk4;
+    int* bk_key3;                  // [n3_cap] / [n4_cap] or null: each cluster's bucket key,
+    int* bk_key4;                  //   written by the count pass and read by the scatter pass
     int* bk_count;                 // [nbk3 + nbk4]
     int* bk_fill;                  // [nbk3 + nbk4]
     long long* bk_start;           // [nbk3 + 1] then [nbk4 + 1]; last = slots in use

@@ -182,12 +182,14 @@ __global__ void __launch_bounds__(256) k_bucket_count(BatchView B, const int* cl
                                                       long long cap) {
     const long long n = min(*n_ptr, cap);
     int* count = B.bk_count + (NB == 3 ? 0 : B.nbk3);
+    int* keys = NB == 3 ? B.bk_key3 : B.bk_key4;
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     // base is uniform over the block, so whole warps take part in the match
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long c = base + threadIdx.x;
         const int key = c < n ? bucket_key<NB>(B, clusters, c) : -1;
+        if (keys && c < n) keys[c] = key;
         const unsigned peers = __match_any_sync(kFull, key);
         if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
     }
@@ -247,11 +249,12 @@ __global__ void __launch_bounds__(256) k_bucket_scatter(BatchView B, const int* 
     const long long* start = B.bk_start + (NB == 3 ? 0 : B.nbk3 + 1);
     int* perm = NB == 3 ? B.perm3 : B.perm4;
     const long long pcap = NB == 3 ? B.perm3_cap : B.perm4_cap;
+    const int* keys = NB == 3 ? B.bk_key3 : B.bk_key4;
     const int lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long c = base + threadIdx.x;
-        const int key = c < n ? bucket_key<NB>(B, clusters, c) : -1;
+        const int key = c < n ? (keys ? keys[c] : bucket_key<NB>(B, clusters, c)) : -1;
         const unsigned peers = __match_any_sync(kFull, key);
         const int leader = __ffs(peers) - 1;
         int b = 0;

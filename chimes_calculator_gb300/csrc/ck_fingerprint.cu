@@ -13,9 +13,9 @@
 // cutoffs (read_flat_clusters) and are sorted; every pair of records (i from
 // set 1, j from set 2; j > i when both are the same set) contributes its
 // Euclidean distance to a histogram of nbin bins over [0, maxd).  The pair
-// loop is O(n1*n2) and runs here as tiles of 128 x 256 records: set-2 tiles
-// staged in shared memory (broadcast reads), each thread owning one set-1
-// record and a private histogram column in shared memory (bin-major, so a
+// loop is O(n1*n2) and runs here as tiles of 256 x 256 records: set-2 tiles
+// staged in shared memory (broadcast reads), each thread owning two set-1
+// records and a private histogram column in shared memory (bin-major, so a
 // warp's 32 columns sit on 32 different banks and increments never collide).
 // Distances are computed in FP32 with a rigorous bound on the error of the
 // squared distance; a pair whose bin the bound certifies is counted directly,
@@ -39,6 +39,7 @@ namespace ck {
 namespace {
 
 constexpr int kFpTileJ = 256;   // set-2 records per shared-memory tile
+constexpr int kFpRows = 2;      // set-1 records per thread
 
 template <int P>
 struct __align__(P == 1 ? 8 : 16) FpRec {   // one staged set-2 record: edges and squared norm
@@ -46,6 +47,42 @@ struct __align__(P == 1 ? 8 : 16) FpRec {   // one staged set-2 record: edges an
     float q;
 };
 
+__device__ __forceinline__ float fp_sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Exact FP64 bin of one pair, with the tool's operations (dist_struct +=
+// pow(a - b, 2) in order, sqrt, floor(dist / binw), the dist == maxd rule);
+// -1 when the distance falls past the last bin.
+template <int P>
+__device__ __forceinline__ int fp_exact_bin(const double* a, const double* b, double binw, double maxd, int nbin,
+                                            int cand) {
+    double ds = 0.0;
+    for (int p = 0; p < P; p++) {
+        const double d = __dsub_rn(a[p], b[p]);
+        ds = __dadd_rn(ds, __dmul_rn(d, d));
+    }
+    // the FP32 candidate bin, confirmed in FP64 when ds lies inside its
+    // squared edges by far more than the roundings of sqrt and the division
+    if (cand >= 0 && cand < nbin) {
+        const double lo = cand * binw, hi = lo + binw;
+        if (ds >= lo * lo * (1.0 + 1e-12) && ds <= hi * hi * (1.0 - 1e-12)) return cand;
+    }
+    const double dist = __dadd_rn(__dsqrt_rn(ds), 0.0);
+    int bin = (int)floor(__ddiv_rn(dist, binw));
+    if (dist == maxd) bin = bin - 1;
+    return (bin < 0 || bin >= nbin) ? -1 : bin;
+}
+
+// One thread owns kFpRows set-1 records (i0 + tid + r*T) and loops over the
+// staged set-2 tile.  Per pair: the FP32 squared distance s, its error bound
+// eps, a candidate bin k from an approximate square root (floor by a
+// round-down add at 1.5*2^23: no conversion instructions), and the test
+// (k w)^2 (1+d) <= s - eps, s + eps <= ((k+1) w)^2 (1-d) written as fused
+// multiply-adds; a pair that fails it (near an edge, ~1e-4 of them) takes the
+// exact FP64 path.
 template <int P>
 __global__ void __launch_bounds__(128) k_fp_hist(const float* __restrict__ e1, const float* __restrict__ q1,
                                                  const double* __restrict__ d1, long long n1,
@@ -59,63 +96,63 @@ __global__ void __launch_bounds__(128) k_fp_hist(const float* __restrict__ e1, c
     unsigned int* hist = reinterpret_cast<unsigned int*>(smem);                  // [nbin][T]
     FpRec<P>* tile = reinterpret_cast<FpRec<P>*>(smem + sizeof(unsigned int) * (size_t)nbin * T);
     for (int b = 0; b < nbin; b++) hist[b * T + tid] = 0u;
-    const float wf = (float)binw, inv_wf = (float)(1.0 / binw);
     // |s32 - s| <= (4 + P) u sum_k (|a_k| + |b_k|)^2 <= 2 (4 + P) u (qa + qb), u = 2^-24;
-    // kEps carries a margin of 3x over that bound
+    // the staged norms carry kEps (a margin of 3x over that bound)
     const float kEps = 6.0f * (4 + P) * 5.9604645e-8f;
-    const float kRel = 1.0e-6f;   // covers the FP32 rounding of the bin edges
+    const float inv_wf = (float)(1.0 / binw);
+    const float wlo = (float)(binw * (1.0 + 1.0e-6)), whi = (float)(binw * (1.0 - 1.0e-6));
+    const float kMagic = 12582912.0f;                // 1.5 * 2^23: adding it rounds to an integer
+    const int kMagicBits = 0x4B400000;
+    const int rows = T * kFpRows;
     const long long ntiles = n_itile * n_jtile;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const long long it = t / n_jtile, jt = t % n_jtile;
-        const long long i0 = it * T, j0 = jt * kFpTileJ;
+        const long long i0 = it * rows, j0 = jt * kFpTileJ;
         // a tile whose every j is <= every i holds no pair j > i
         if (same && j0 + kFpTileJ - 1 <= i0) continue;
-        const long long jn = min((long long)kFpTileJ, n2 - j0);
+        const int jn = (int)min((long long)kFpTileJ, n2 - j0);
         __syncthreads();
         for (int k = tid; k < jn; k += T) {
             FpRec<P> r;
             for (int p = 0; p < P; p++) r.e[p] = e2[(j0 + k) * P + p];
-            r.q = q2[j0 + k];
+            r.q = kEps * q2[j0 + k];
             tile[k] = r;
         }
         __syncthreads();
-        const long long i = i0 + tid;
-        if (i >= n1) continue;
-        float a[P];
-        for (int p = 0; p < P; p++) a[p] = e1[i * P + p];
-        const float qa = q1[i];
-        const long long jstart = same ? max(0LL, i + 1 - j0) : 0;
-        for (long long k = jstart; k < jn; k++) {
-            const FpRec<P> r = tile[k];
-            float s = 0.0f;
+        for (int rr = 0; rr < kFpRows; rr++) {
+            const long long i = i0 + tid + (long long)rr * T;
+            if (i >= n1) break;
+            float a[P];
+            for (int p = 0; p < P; p++) a[p] = e1[i * P + p];
+            const float qa = kEps * q1[i];
+            const int jstart = same ? (int)max(0LL, min((long long)jn, i + 1 - j0)) : 0;
+#pragma unroll 2
+            for (int k = jstart; k < jn; k++) {
+                const FpRec<P> r = tile[k];
+                float s = 0.0f;
 #pragma unroll
-            for (int p = 0; p < P; p++) {
-                const float d = a[p] - r.e[p];
-                s = fmaf(d, d, s);
+                for (int p = 0; p < P; p++) {
+                    const float d = a[p] - r.e[p];
+                    s = fmaf(d, d, s);
+                }
+                const float eps = qa + r.q;
+                // rounded down at magnitude 1.5*2^23 (unit spacing): kMagic + floor(sqrt(s) / w)
+                const float mag = __fmaf_rd(fp_sqrt_approx(s), inv_wf, kMagic);
+                const float kf = mag - kMagic;                 // candidate bin, an exact float integer
+                const int bin = __float_as_int(mag) - kMagicBits;
+                const float lo = kf * wlo, hi = fmaf(kf, whi, whi);
+                const bool ok = bin < nbin && fmaf(lo, lo, eps - s) <= 0.0f && fmaf(-hi, hi, s + eps) <= 0.0f;
+                int b = bin;
+                if (!ok) {
+                    const long long j = j0 + k;
+                    b = fp_exact_bin<P>(d1 + i * P, d2 + j * P, binw, maxd, nbin, bin);
+                    if (b < 0) {
+                        atomicOr(&flags[0], 1);
+                        continue;
+                    }
+                }
+                hist[b * T + tid] += 1u;
             }
-            const float eps = kEps * (qa + r.q);
-            const int bin = (int)(sqrtf(s) * inv_wf);
-            const float lo = (float)bin * wf, hi = lo + wf;
-            const bool ok = bin < nbin && s - eps >= lo * lo * (1.0f + kRel) && s + eps <= hi * hi * (1.0f - kRel);
-            if (ok) {
-                hist[bin * T + tid] += 1u;
-                continue;
-            }
-            // exact path: dist_struct += pow(a - b, 2) in order, sqrt, floor(dist / binw)
-            const long long j = j0 + k;
-            double ds = 0.0;
-            for (int p = 0; p < P; p++) {
-                const double d = __dsub_rn(d1[i * P + p], d2[j * P + p]);
-                ds = __dadd_rn(ds, __dmul_rn(d, d));
-            }
-            const double dist = __dadd_rn(__dsqrt_rn(ds), 0.0);
-            int b = (int)floor(__ddiv_rn(dist, binw));
-            if (dist == maxd) b = b - 1;
-            if (b < 0 || b >= nbin) {
-                atomicOr(&flags[0], 1);
-                continue;
-            }
-            hist[b * T + tid] += 1u;
         }
     }
     __syncthreads();
@@ -361,7 +398,8 @@ Status fp_histogram(Engine& eng, int slot, int nbody, long long n1, const double
     FP_TRY(dflags.reserve(1));
     FP_TRY(cudaMemsetAsync(dcounts.p, 0, sizeof(unsigned long long) * nbin, s));
     FP_TRY(cudaMemsetAsync(dflags.p, 0, sizeof(int), s));
-    const long long n_it = (n1 + T - 1) / T, n_jt = (n2 + kFpTileJ - 1) / kFpTileJ;
+    const long long n_it = (n1 + (long long)T * kFpRows - 1) / ((long long)T * kFpRows),
+                    n_jt = (n2 + kFpTileJ - 1) / kFpTileJ;
     const void* kern = nbody == 2 ? (const void*)k_fp_hist<1> : nbody == 3 ? (const void*)k_fp_hist<3>
                                                                            : (const void*)k_fp_hist<6>;
     if (smem > 48 * 1024) allow_max_smem(kern);

@@ -172,6 +172,8 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
         if (n4_ > cap4_ || !d_c4_.p) { NL_TRY(d_c4_.reserve(4 * std::max(1LL, n4_))); cap4_ = std::max(1LL, n4_); }
         NL_TRY(d_perm3_.reserve(std::max(1LL, n3_ + 32LL * nbk3)));
         NL_TRY(d_perm4_.reserve(std::max(1LL, n4_ + 32LL * nbk4)));
+        NL_TRY(d_bk_key3_.reserve(std::max(1LL, n3_)));
+        NL_TRY(d_bk_key4_.reserve(std::max(1LL, n4_)));
         NL_TRY(d_bk_count_.reserve(nbk3 + nbk4 + 1));
         NL_TRY(d_bk_fill_.reserve(nbk3 + nbk4 + 1));
         NL_TRY(d_bk_start_.reserve(nbk3 + nbk4 + 2));
@@ -180,6 +182,8 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     B.n3_cap = cap3_; B.n4_cap = cap4_;
     B.nbk3 = nbk3; B.nbk4 = nbk4;
     B.bk_count = d_bk_count_.p; B.bk_fill = d_bk_fill_.p; B.bk_start = d_bk_start_.p;
+    // the count pass keeps each cluster's key (its cutoff test takes FP64 distances) for the scatter pass
+    B.bk_key3 = d_bk_key3_.p; B.bk_key4 = d_bk_key4_.p;
     B.perm3 = d_perm3_.p; B.perm4 = d_perm4_.p;
     B.perm3_cap = nbk3 > 0 ? n3_ + 32LL * nbk3 : 0;
     B.perm4_cap = nbk4 > 0 ? n4_ + 32LL * nbk4 : 0;

@@ -53,7 +53,7 @@ private:
     DevBuf<long long> d_tag_, d_off_;
     DevBuf<int> d_e_cnt3_, d_e_cnt4_, d_c3_, d_c4_;
     DevBuf<long long> d_e_off3_, d_e_off4_;
-    DevBuf<int> d_flags_, d_bk_count_, d_bk_fill_, d_perm3_, d_perm4_;
+    DevBuf<int> d_flags_, d_bk_count_, d_bk_fill_, d_perm3_, d_perm4_, d_bk_key3_, d_bk_key4_;
     DevBuf<long long> d_bk_start_;
     DevBuf<unsigned long long> d_queue_, d_minmax_;
     DevBuf<unsigned char> d_scan_tmp_, d_fp_tmp_;
