@@ -338,10 +338,24 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
 }
 
 // --- 5. 2B neighbour lists (:680-731): one warp per atom --------------------
+// Lane b < 27 owns neighbour bin b in the reference's loop order (x bins
+// outermost, z innermost); the candidates of all 27 bins are numbered bin by
+// bin and the warp walks them 32 at a time, so the emitted order is the
+// reference's and short bins leave no lanes idle.  The FP32 displacement
+// decides most candidates; the exact FP64 distance (which the list keeps) is
+// taken only for the candidates that survive it, queued in candidate order in
+// shared memory and evaluated 32 at a time, so the FP64 pipe (1/64 of the
+// FP32 rate) runs full warps instead of one or two live lanes per chunk.  The
+// count pass counts the candidates the FP32 test places inside the cutoff by
+// more than the margin without an FP64 distance.
+constexpr int kL2Block = 256;
 template <bool FILL>
-__global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
+__global__ void __launch_bounds__(kL2Block) k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
+    __shared__ int queue[kL2Block / 32][64];
+    __shared__ int qpar[kL2Block / 32][64];
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     if (warp >= B.n_atoms_total) return;
     const long long r = warp;
     const int s = B.atom_sys[r];
@@ -354,6 +368,7 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
     const double sd = d.search;
     const float far2 = (float)((sd + d.eps) * (sd + d.eps));
+    const float near2 = sd > d.eps ? (float)((sd - d.eps) * (sd - d.eps)) : 0.0f;
     int bx, by, bz;
     bin_of(d, &B.ghost_xn[3 * gi], bx, by, bz);
     if (bx < 1 || by < 1 || bz < 1) {
@@ -363,10 +378,6 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     const long long total = (long long)d.nb[0] * d.nb[1] * d.nb[2];
     long long base = FILL ? B.l2_off[r] : 0;
     int count = 0;
-    // Lane b < 27 owns neighbour bin b in the reference's loop order (x bins
-    // outermost, z innermost); the candidates of all 27 bins are numbered
-    // bin by bin and the warp walks them 32 at a time, so the emitted order
-    // is the reference's and short bins leave no lanes idle.
     long long bst = 0;
     int nbin = 0;
     if (lane < 27) {
@@ -387,34 +398,23 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     }
     const int excl = incl - nbin;
     const int ncand = __shfl_sync(kFull, incl, 31);
-    for (int t0 = 0; t0 < ncand; t0 += 32) {
-        const int t = t0 + lane;
-        // bin of candidate t: the last bin whose first candidate is <= t
-        int lo = 0;
-        for (int step = 16; step >= 1; step >>= 1) {
-            const int cand = lo + step;
-            const int ex = __shfl_sync(kFull, excl, cand & 31);
-            if (cand < 27 && ex <= t) lo = cand;
-        }
-        const long long st = __shfl_sync(kFull, bst, lo);
-        const int first = __shfl_sync(kFull, excl, lo);
+    int* q = queue[wib];
+    int* qp = qpar[wib];
+    int qn = 0;   // queued candidates (warp-uniform)
+    // exact distances of the first n queued candidates; members counted / written in order
+    auto drain = [&](int n) {
         bool pred = false;
         int ajj = -1, par = -1;
         double dd = 0.0, rv[3] = {0, 0, 0};
-        if (t < ncand) {
-            ajj = B.bin_items[st + (t - first)];
-            if (ajj != gi && r <= (par = B.ghost_parent[ajj])) {
-                const float* xj = &B.ghost_xf[3 * (long long)ajj];
-                const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
-                if (ex * ex + ey * ey + ez * ez < far2) {   // else certainly >= sd
-                    dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj], rv);
-                    pred = dd < sd;
-                }
-            }
+        if (lane < n) {
+            ajj = q[lane];
+            par = qp[lane];
+            dd = dist_frac(hn, fi, &B.ghost_fn[3 * (long long)ajj], rv);
+            pred = dd < sd;
         }
         const unsigned bal = __ballot_sync(kFull, pred);
         if (FILL && pred) {
-            const long long pos = base + count + __popc(bal & ((1u << lane) - 1u));
+            const long long pos = base + count + __popc(bal & lt);
             if (pos < B.n2_cap) {
                 B.l2_ghost[pos] = ajj;
                 B.l2_dist[pos] = dd;
@@ -427,7 +427,53 @@ __global__ void k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
             }
         }
         count += __popc(bal);
+        // move the rest of the queue to its front
+        __syncwarp();
+        const int rest = qn - n;
+        int mv = -1, mp = -1;
+        if (lane < rest) { mv = q[n + lane]; mp = qp[n + lane]; }
+        __syncwarp();
+        if (lane < rest) { q[lane] = mv; qp[lane] = mp; }
+        __syncwarp();
+        qn = rest;
+    };
+    for (int t0 = 0; t0 < ncand; t0 += 32) {
+        const int t = t0 + lane;
+        // bin of candidate t: the last bin whose first candidate is <= t
+        int lo = 0;
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int cand = lo + step;
+            const int ex = __shfl_sync(kFull, excl, cand & 31);
+            if (cand < 27 && ex <= t) lo = cand;
+        }
+        const long long st = __shfl_sync(kFull, bst, lo);
+        const int first = __shfl_sync(kFull, excl, lo);
+        bool exact = false, sure = false;
+        int ajj = -1, par = -1;
+        if (t < ncand) {
+            ajj = B.bin_items[st + (t - first)];
+            if (ajj != gi && r <= (par = B.ghost_parent[ajj])) {
+                const float* xj = &B.ghost_xf[3 * (long long)ajj];
+                const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
+                const float e2 = ex * ex + ey * ey + ez * ez;
+                if (e2 < far2) {   // else certainly >= sd
+                    if (!FILL && e2 < near2) sure = true;   // certainly < sd
+                    else exact = true;
+                }
+            }
+        }
+        if (!FILL) count += __popc(__ballot_sync(kFull, sure));
+        const unsigned m = __ballot_sync(kFull, exact);
+        if (exact) {
+            const int pos = qn + __popc(m & lt);
+            q[pos] = ajj;
+            qp[pos] = par;
+        }
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) drain(32);
     }
+    if (qn > 0) drain(qn);
     if (!FILL && lane == 0) B.l2_count[r] = count;
 }
 
@@ -846,10 +892,11 @@ void exclusive_scan2(const int* in_a, long long* out_a, const int* in_b, long lo
 }
 
 void launch_atoms(const BatchView& B, cudaStream_t st) {
-    if (B.n_atoms_total) count_launch(), k_atoms<<<grid_for(B.n_atoms_total, 256), 256, 0, st>>>(B);
+    // small blocks: the per-atom cell algebra is FP64 work, spread over as many SMs as possible
+    if (B.n_atoms_total) count_launch(), k_atoms<<<grid_for(B.n_atoms_total, 32), 32, 0, st>>>(B);
 }
 void launch_ghosts(const BatchView& B, cudaStream_t st) {
-    if (B.n_ghost_total) count_launch(), k_ghosts<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B);
+    if (B.n_ghost_total) count_launch(), k_ghosts<<<grid_for(B.n_ghost_total, 64), 64, 0, st>>>(B);
 }
 void launch_bin_setup(const BatchView& B, cudaStream_t st) {
     count_launch(), k_bin_setup<<<grid_for(B.n_sys, 128), 128, 0, st>>>(B);
@@ -865,9 +912,9 @@ void launch_bin_sort(const BatchView& B, cudaStream_t st) {
 }
 void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n_atoms_total) return;
-    const unsigned grid = grid_for(B.n_atoms_total * 32, 256);
-    if (fill) count_launch(), k_l2<true><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
-    else count_launch(), k_l2<false><<<grid, 256, 0, st>>>(B, B.bin_start, l2_owner);
+    const unsigned grid = grid_for(B.n_atoms_total * 32, kL2Block);
+    if (fill) count_launch(), k_l2<true><<<grid, kL2Block, 0, st>>>(B, B.bin_start, l2_owner);
+    else count_launch(), k_l2<false><<<grid, kL2Block, 0, st>>>(B, B.bin_start, l2_owner);
 }
 void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n2_cap) return;
