@@ -349,6 +349,8 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
 // count pass counts the candidates the FP32 test places inside the cutoff by
 // more than the margin without an FP64 distance.
 constexpr int kL2Block = 256;
+// bits of l2_vec.w above the parent atom index (atom indices are below 2^30)
+constexpr unsigned kL2Parent = 0x3FFFFFFFu, kL2In3 = 1u << 30, kL2In4 = 1u << 31;
 template <bool FILL>
 __global__ void __launch_bounds__(kL2Block) k_l2(BatchView B, const long long* bin_start, int* l2_owner) {
     __shared__ int queue[kL2Block / 32][64];
@@ -420,9 +422,12 @@ __global__ void __launch_bounds__(kL2Block) k_l2(BatchView B, const long long* b
                 B.l2_dist[pos] = dd;
                 l2_owner[pos] = (int)r;
                 // x, y, z: FP32 displacement for the enumeration's prefilter;
-                // w: the neighbour's parent atom (int bits), saving the
-                // enumeration a dependent load per candidate
-                float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], __int_as_float(par));
+                // w: the neighbour's parent atom (int bits; saves the
+                // enumeration a dependent load per candidate) with the exact
+                // tests dd < c3 and dd < c4 in bits 30 and 31, so the
+                // enumeration compares no FP64 distances
+                const unsigned w = (unsigned)par | (dd < d.c3 ? kL2In3 : 0u) | (dd < d.c4 ? kL2In4 : 0u);
+                float4 v = make_float4((float)rv[0], (float)rv[1], (float)rv[2], __uint_as_float(w));
                 reinterpret_cast<float4*>(B.l2_vec)[pos] = v;
             }
         }
@@ -491,6 +496,20 @@ struct PairDist {
         if ((double)df >= c + eps) return true;
         if (!have) { exact = dist_frac(hn, fa, fb); have = true; }
         return exact >= c;
+    }
+};
+
+// The same test with the margins as FP32 thresholds (lo <= c - eps, hi >=
+// c + eps, rounded outward), so the decided cases take no FP64 instruction.
+struct PairDistF {
+    const double* hn;
+    const double* fa;
+    const double* fb;
+    float df;
+    __device__ bool ge(double c, float lo, float hi) const {
+        if (df < lo) return false;
+        if (df >= hi) return true;
+        return dist_frac(hn, fa, fb) >= c;
     }
 };
 
@@ -616,21 +635,23 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
         }
         const int r = l2_owner[e];
         const SysDesc& d = B.sys[B.atom_sys[r]];
-        const double c3 = d.c3, c4 = d.c4, eps = d.eps;
-        const double dij = B.l2_dist[e];
-        const bool want3 = d.has3 && dij < c3, want4 = d.has4 && dij < c4;
+        const double c3 = d.c3, c4 = d.c4;
+        const float4 vj = vec[e];
+        const unsigned wj = __float_as_uint(vj.w);
+        const bool want3 = d.has3 && (wj & kL2In3), want4 = d.has4 && (wj & kL2In4);
         long long n3 = 0, n4 = 0;
         long long o3 = 0, o4 = 0;
         if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
         if (want3 || want4) {
             double hn[9];
             for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
+            const float c3lo = __double2float_rd(c3 - d.eps), c3hi = __double2float_ru(c3 + d.eps);
+            const float c4lo = __double2float_rd(c4 - d.eps), c4hi = __double2float_ru(c4 + d.eps);
             const int gi = B.atom_self[r];
             const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
             const int jj = B.l2_ghost[e];
-            const float4 vj = vec[e];
             const double* fj = &B.ghost_fn[3 * (long long)jj];
-            const int pj = __float_as_int(vj.w);
+            const int pj = (int)(wj & kL2Parent);
             for (long long kb = b0; kb < b1; kb += 32) {
                 const long long k = kb + lane;
                 bool ok3 = false, ok4 = false;
@@ -639,12 +660,12 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                 if (k < b1) {
                     kk = B.l2_ghost[k];
                     vk = vec[k];
-                    pk = __float_as_int(vk.w);
+                    const unsigned wk = __float_as_uint(vk.w);
+                    pk = (int)(wk & kL2Parent);
                     if (kk != jj && pj <= pk) {
-                        const double dik = B.l2_dist[k];
-                        PairDist jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk), 0.0, false};
-                        ok3 = want3 && dik < c3 && !jk.ge(c3, eps);
-                        ok4 = want4 && dik < c4 && !jk.ge(c4, eps);
+                        const PairDistF jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk)};
+                        ok3 = want3 && (wk & kL2In3) && !jk.ge(c3, c3lo, c3hi);
+                        ok4 = want4 && (wk & kL2In4) && !jk.ge(c4, c4lo, c4hi);
                     }
                 }
                 const unsigned m3 = __ballot_sync(kFull, ok3);
@@ -677,13 +698,14 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
                             ll = B.l2_ghost[l];
                             const float4 vl = vec[l];
                             if (ll != jj && ll != ks) {
-                                const int pl = __float_as_int(vl.w);
-                                if (pj <= pl && pks <= pl && B.l2_dist[l] < c4) {
+                                const unsigned wl = __float_as_uint(vl.w);
+                                const int pl = (int)(wl & kL2Parent);
+                                if (pj <= pl && pks <= pl && (wl & kL2In4)) {
                                     const double* fl = &B.ghost_fn[3 * (long long)ll];
-                                    PairDist jl{hn, fj, fl, vdist(vj, vl), 0.0, false};
-                                    if (!jl.ge(c4, eps)) {
-                                        PairDist kl{hn, fk, fl, vdist(vks, vl), 0.0, false};
-                                        okl = !kl.ge(c4, eps);
+                                    const PairDistF jl{hn, fj, fl, vdist(vj, vl)};
+                                    if (!jl.ge(c4, c4lo, c4hi)) {
+                                        const PairDistF kl{hn, fk, fl, vdist(vks, vl)};
+                                        okl = !kl.ge(c4, c4lo, c4hi);
                                     }
                                 }
                             }
