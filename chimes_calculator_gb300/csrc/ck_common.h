@@ -179,6 +179,7 @@ struct SysDesc {
     int gstride;               // ghost slots per atom (upper bound of its kept images, itself included)
     double ulo[3], uhi[3];     // kept fractional range per axis of the reoriented cell
     double eps;                // margin of the FP32 distance prefilter (Angstrom)
+    float c3lo, c3hi, c4lo, c4hi;   // c3 -/+ eps and c4 -/+ eps as FP32, rounded outward
     // device-completed
     double minpos[3];
     int nb[3];

@@ -226,6 +226,21 @@ Status system_geometry(const double* ca, const double* cb, const double* cc, int
         return kErrInput;
     }
     d.bin_cap = (int)cap;
+    // FP32 thresholds of the enumeration's pair tests (c -/+ eps), rounded outward
+    auto down = [](double v) {
+        float f = (float)v;
+        if ((double)f > v) f = std::nextafter(f, -INFINITY);
+        return f;
+    };
+    auto up = [](double v) {
+        float f = (float)v;
+        if ((double)f < v) f = std::nextafter(f, INFINITY);
+        return f;
+    };
+    d.c3lo = down(d.c3 - d.eps);
+    d.c3hi = up(d.c3 + d.eps);
+    d.c4lo = down(d.c4 - d.eps);
+    d.c4hi = up(d.c4 + d.eps);
     return kOk;
 }
 

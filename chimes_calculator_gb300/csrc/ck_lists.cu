@@ -645,8 +645,7 @@ __global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner)
         if (want3 || want4) {
             double hn[9];
             for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
-            const float c3lo = __double2float_rd(c3 - d.eps), c3hi = __double2float_ru(c3 + d.eps);
-            const float c4lo = __double2float_rd(c4 - d.eps), c4hi = __double2float_ru(c4 + d.eps);
+            const float c3lo = d.c3lo, c3hi = d.c3hi, c4lo = d.c4lo, c4hi = d.c4hi;
             const int gi = B.atom_self[r];
             const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
             const int jj = B.l2_ghost[e];
