@@ -66,6 +66,7 @@ struct TupleRec {
     // reciprocals for the factored kernels: 1/lam, 1/xdiff, and the cutoff's
     // 1/rc (cubic) or Tersoff threshold rc - f*rc and 1/(rc - threshold)
     double inv_lam[6], inv_xdiff[6], fc_th[6], fc_inv[6];
+    float rout_f[6];       // rout rounded to FP32 (FP32 cutoff tests add a margin for the rounding)
 };
 
 // Factored coefficient lists of one tuple.  The cluster's pairs split into
@@ -238,6 +239,11 @@ struct BatchView {
     // 1: bucketing drops clusters with a pair at or beyond its tuple's outer
     // cutoff (lists built with padded cutoffs; rebucketed every evaluation)
     int bucket_cut;
+    // with bucket_cut on the pair-style path: FP32 copies of the positions and
+    // the margin of an FP32 distance (float_eps); a cutoff test decided by more
+    // than the margin takes no FP64 distance (null: always exact)
+    const float* pos_f;
+    float float_eps;
     double* pcd3; double* pcd4;    // [n2_cap][6]
     void* pct3; void* pct4;        // [n2_cap][2R]
     // results
@@ -273,6 +279,11 @@ struct NeighView {
     const long long* tag;
     double c3p, c4p;               // max 3-/4-body outer cutoffs + skin (0 + skin for an absent order)
     int has3, has4;
+    // FP32 positions and the padded cutoffs -/+ the FP32 distance margin,
+    // rounded outward: a test with the FP32 distance below lo or at or above
+    // hi is decided without the FP64 distance
+    const float* xf;
+    float c3lo, c3hi, c4lo, c4hi;
 };
 
 }  // namespace ck

@@ -169,8 +169,18 @@ __device__ __forceinline__ int bucket_key(const BatchView& B, const int* cluster
     if (B.bucket_cut) {   // compute_3B/4B would return at once: leave the cluster out
         const double* h = B.sys[s].h;
         for (int p = 0; p < Topo<NB>::NP; p++) {
+            const int a = id[Topo<NB>::a(p)], b = id[Topo<NB>::b(p)];
+            if (B.pos_f) {   // decided by the FP32 distance unless within the margin
+                const float* xa = B.pos_f + 3 * (long long)a;
+                const float* xb = B.pos_f + 3 * (long long)b;
+                const float ex = xb[0] - xa[0], ey = xb[1] - xa[1], ez = xb[2] - xa[2];
+                const float df = sqrtf(ex * ex + ey * ey + ez * ez);
+                const float m = B.float_eps + 1e-6f * R->rout_f[p];
+                if (df < R->rout_f[p] - m) continue;
+                if (df >= R->rout_f[p] + m) return -1;
+            }
             double dr[3], r;
-            pair_geom(B, h, id[Topo<NB>::a(p)], id[Topo<NB>::b(p)], dr, r);
+            pair_geom(B, h, a, b, dr, r);
             if (r >= R->rout[p]) return -1;
         }
     }

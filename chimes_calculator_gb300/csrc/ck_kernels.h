@@ -74,6 +74,8 @@ size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 void launch_nl_setup(const BatchView& B, const NeighView& N, cudaStream_t st);
 void launch_nl_enum(const BatchView& B, const NeighView& N, bool fill, cudaStream_t st);
 void launch_nl_pairs(const BatchView& B, const NeighView& N, int precision, cudaStream_t st);
+// FP32 copy of the positions (n = 3 * atoms values) for the cutoff tests
+void launch_nl_xf(const double* x, float* xf, long long n, cudaStream_t st);
 // tabulated 3-body term: selection of the evaluated triplets (sel[n3], selr[3*n3],
 // *count on the device) and their look-ups
 void launch_nl_tab3(const BatchView& B, long long n3, int* sel, double* selr, unsigned long long* count,

@@ -37,6 +37,37 @@ __device__ __forceinline__ double nl_dist(const double* x, int i, int j, double*
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
 }
 
+// Distance of one pair for cutoff tests: the FP32 distance first, the FP64
+// one (as nl_dist computes it) only when the FP32 value is within the margin
+// of the cutoff; the FP64 value is kept for further tests of the same pair.
+struct NlDist {
+    const double* x;
+    int i, j;
+    float df;
+    double exact;
+    bool have;
+    __device__ NlDist(const double* x_, const float* xf, int i_, int j_) : x(x_), i(i_), j(j_), exact(0.0), have(false) {
+        const float* a = xf + 3 * (long long)i;
+        const float* b = xf + 3 * (long long)j;
+        const float ex = b[0] - a[0], ey = b[1] - a[1], ez = b[2] - a[2];
+        df = sqrtf(ex * ex + ey * ey + ez * ez);
+    }
+    __device__ bool lt(double c, float lo, float hi) {
+        if (df < lo) return true;
+        if (df >= hi) return false;
+        if (!have) {
+            exact = nl_dist(x, i, j, nullptr);
+            have = true;
+        }
+        return exact < c;
+    }
+};
+
+__global__ void k_nl_xf(const double* x, float* xf, long long n) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) xf[k] = (float)x[k];
+}
+
 // list entry -> position of its atom in ilist
 __global__ void k_nl_owner(NeighView N) {
     const long long ii = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,10 +150,12 @@ __global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
         const int j = N.neigh[e];
         const long long ti = N.tag[i], tj = N.tag[j];
         bool go = j != i && tj >= ti;
-        double dij = 0.0;
+        bool ij3 = false, ij4 = false;
         if (go) {
-            dij = nl_dist(x, i, j, nullptr);
-            go = !(dij >= c3p && dij >= c4p);
+            NlDist Dij(x, N.xf, i, j);
+            ij3 = Dij.lt(c3p, N.c3lo, N.c3hi);
+            ij4 = Dij.lt(c4p, N.c4lo, N.c4hi);
+            go = ij3 || ij4;
         }
         if (go) {
             const long long b0 = N.off[ii], b1 = N.off[ii + 1];
@@ -135,11 +168,12 @@ __global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
                     k = N.neigh[kk];
                     tk = N.tag[k];
                     if (k != i && k != j && tk >= ti && tk >= tj) {
-                        const double dik = nl_dist(x, i, k, nullptr);
-                        if (!(dik >= c3p && dik >= c4p)) {
-                            const double djk = nl_dist(x, j, k, nullptr);
-                            ok3 = N.has3 && dij < c3p && dik < c3p && djk < c3p;
-                            ok4 = N.has4 && dij < c4p && dik < c4p && djk < c4p;
+                        NlDist Dik(x, N.xf, i, k);
+                        const bool ik3 = Dik.lt(c3p, N.c3lo, N.c3hi), ik4 = Dik.lt(c4p, N.c4lo, N.c4hi);
+                        if (ik3 || ik4) {
+                            NlDist Djk(x, N.xf, j, k);
+                            ok3 = N.has3 && ij3 && ik3 && Djk.lt(c3p, N.c3lo, N.c3hi);
+                            ok4 = N.has4 && ij4 && ik4 && Djk.lt(c4p, N.c4lo, N.c4hi);
                         }
                     }
                 }
@@ -166,8 +200,9 @@ __global__ void __launch_bounds__(256) k_nl_enum(BatchView B, NeighView N) {
                             l = N.neigh[ll];
                             const long long tl = N.tag[l];
                             if (l != i && l != j && l != ks && tl >= ti && tl >= tj && tl >= tks)
-                                okl = nl_dist(x, i, l, nullptr) < c4p && nl_dist(x, j, l, nullptr) < c4p &&
-                                      nl_dist(x, ks, l, nullptr) < c4p;
+                                okl = NlDist(x, N.xf, i, l).lt(c4p, N.c4lo, N.c4hi) &&
+                                      NlDist(x, N.xf, j, l).lt(c4p, N.c4lo, N.c4hi) &&
+                                      NlDist(x, N.xf, ks, l).lt(c4p, N.c4lo, N.c4hi);
                         }
                         const unsigned ml = __ballot_sync(kFull, okl);
                         if (FILL && okl) {
@@ -207,10 +242,14 @@ __global__ void __launch_bounds__(256) k_nl_tab3_sel(BatchView B, long long n3, 
             const int u = (B.atom_type[id[0]] * P.ntypes + B.atom_type[id[1]]) * P.ntypes + B.atom_type[id[2]];
             const TupleRec& R = P.t3[u];
             if (R.type_id >= 0) {
-                r[0] = nl_dist(x, id[0], id[1], nullptr);
-                r[1] = nl_dist(x, id[0], id[2], nullptr);
-                r[2] = nl_dist(x, id[1], id[2], nullptr);
-                pass = r[0] < R.rout[0] && r[1] < R.rout[1] && r[2] < R.rout[2];
+                pass = true;
+                for (int p = 0; p < 3 && pass; p++) {
+                    const int a = id[p == 2 ? 1 : 0], b = id[p == 0 ? 1 : 2];   // ij, ik, jk
+                    NlDist D(x, B.pos_f, a, b);
+                    const float m = B.float_eps + 1e-6f * R.rout_f[p];
+                    pass = D.lt(R.rout[p], R.rout_f[p] - m, R.rout_f[p] + m);
+                    if (pass) r[p] = D.have ? D.exact : nl_dist(x, a, b, nullptr);
+                }
             }
         }
         const unsigned m = __ballot_sync(kFull, pass);
@@ -312,6 +351,11 @@ void launch_nl_tab3(const BatchView& B, long long n3, int* sel, double* selr, un
                                                                                                 count);
     // the selected count stays on the device: the grid covers the listed triplets
     count_launch(), k_nl_tab3<<<grid_of(n3, 128, (long long)sm_count() * 8), 128, 0, st>>>(B, sel, selr, count);
+}
+
+void launch_nl_xf(const double* x, float* xf, long long n, cudaStream_t st) {
+    if (n <= 0) return;
+    count_launch(), k_nl_xf<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, xf, n);
 }
 
 }  // namespace ck

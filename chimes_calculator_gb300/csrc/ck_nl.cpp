@@ -54,7 +54,9 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
             err = "neighbour index out of range at entry " + std::to_string(e) + " (strip the LAMMPS NEIGHMASK bits)";
             return kErrInput;
         }
+    double maxabs = 0.0;
     for (int a = 0; a < nall; a++) {
+        for (int c = 0; c < 3; c++) maxabs = std::max(maxabs, std::fabs(x[3 * a + c]));
         if (type[a] < 0 || type[a] >= P.ntypes) {
             err = "atom type index out of range for the parameter set at atom " + std::to_string(a);
             return kErrInput;
@@ -91,8 +93,13 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     NL_TRY(d_queue_.reserve(2));
     NL_TRY(d_minmax_.reserve(6));
     NL_TRY(d_sys_.reserve(1));
+    NL_TRY(d_xf_.reserve(3 * (long long)nall));
     NL_TRY(cudaMemcpyAsync(d_x_.p, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, s));
     NL_TRY(cudaMemcpyAsync(d_type_.p, type, sizeof(int) * nall, cudaMemcpyHostToDevice, s));
+    launch_nl_xf(d_x_.p, d_xf_.p, 3 * (long long)nall, s);
+    // FP32 distances of coordinates up to maxabs are within 1e-6 * maxabs + 1e-5 of
+    // the FP64 ones (several times the rounding of the coordinates and the arithmetic)
+    const double feps = 1e-5 + 1e-6 * maxabs;
 
     if (build) {
         NL_TRY(d_ilist_.reserve(std::max(1, inum)));
@@ -152,6 +159,23 @@ Status NeighCompute::compute(int slot, int nall, const double* x, const int* typ
     N.c4p = (P.o4 > 0 ? P.max_cut4() : 0.0) + skin;
     N.has3 = P.o3 > 0;
     N.has4 = P.o4 > 0;
+    auto down = [](double v) {
+        float f = (float)v;
+        if ((double)f > v) f = std::nextafter(f, -INFINITY);
+        return f;
+    };
+    auto up = [](double v) {
+        float f = (float)v;
+        if ((double)f < v) f = std::nextafter(f, INFINITY);
+        return f;
+    };
+    N.xf = d_xf_.p;
+    N.c3lo = down(N.c3p - feps);
+    N.c3hi = up(N.c3p + feps);
+    N.c4lo = down(N.c4p - feps);
+    N.c4hi = up(N.c4p + feps);
+    B.pos_f = d_xf_.p;
+    B.float_eps = up(feps);
 
     if (build) {
         launch_nl_setup(B, N, s);

@@ -60,6 +60,7 @@ private:
     DevBuf<int> d_fp_flag_, d_fp_t_;
     DevBuf<long long> d_fp_off_;
     DevBuf<double> d_fp_d_, d_tselr_;
+    DevBuf<float> d_xf_;
     DevBuf<int> d_tsel_;
     DevBuf<unsigned long long> d_tcount_;
     std::vector<double> h_force_, h_eatom_, h_vatom_;

@@ -866,6 +866,7 @@ ParamImage pack_params(const HostParams& P) {
                 for (int j = i + 1; j < nb; j++, p++) {
                     R.rin[p] = Bd.cut_in[ti][m[p]];
                     R.rout[p] = Bd.cut_out[ti][m[p]];
+                    R.rout_f[p] = (float)R.rout[p];
                     R.lam[p] = P.lam[P.pair_map[a[i] * nt + a[j]]];
                     morse_consts(R.rin[p], R.rout[p], R.lam[p], R.xavg[p], R.xdiff[p]);
                     R.inv_lam[p] = 1.0 / R.lam[p];
