@@ -459,63 +459,155 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
 #pragma unroll
         for (int p = 0; p < NP; p++) Gp[p] = CT(0);
         // The TPC lanes of a cluster take whole rows (and then whole columns)
-        // round robin, each flushing its own rows: the per-row products are
-        // issued once per TPC rows instead of once per row.  A record's
-        // entries start where the previous record's end.
+        // round robin (adjacent records, adjacent loads), each flushing its own
+        // rows.  A record's entries start where the previous record's end.
+        // Records are sorted by their powers (first pair most significant), so
+        // the products of a record's pairs are factored out level by level: a
+        // lane sums over its last pair's power within a run of equal leading
+        // powers and multiplies by the leading pairs' values once per run
+        // (nested sums instead of full products per record).  A lane's
+        // round-robin share is a sorted subsequence, so the same flushes apply;
+        // the saving is largest with one lane per cluster, where runs stay whole.
         const int e_col0 = R->f_ent + R->ncoef;
         // row pass: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K)
-        for (int r0 = 0; r0 < nrow; r0 += TPC) {
-            const int r = r0 + gl;
-            if (r < nrow) {
-                const FactRow rw = rows[r];
-                const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
-                CT z;
-                if constexpr (NOY && NB == 3)
-                    z = entry_sum_noy<CT, G>(ent, e0, rw.end, Tt + 1 * rs * G, Tt + 2 * rs * G, grp);
-                else
-                    z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
-                CT t[K], d[K];
-#pragma unroll
-                for (int p = 0; p < K; p++) {
-                    const int q = (rw.pows >> (kPowBits * p)) & 31;
-                    t[p] = Tt[(p * rs + q) * G + grp];
-                    d[p] = Dt[(p * rs + q) * G + grp];
+        if constexpr (K == 1) {
+            for (int r0 = 0; r0 < nrow; r0 += TPC) {
+                const int r = r0 + gl;
+                if (r < nrow) {
+                    const FactRow rw = rows[r];
+                    const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
+                    CT z;
+                    if constexpr (NOY && NB == 3)
+                        z = entry_sum_noy<CT, G>(ent, e0, rw.end, Tt + 1 * rs * G, Tt + 2 * rs * G, grp);
+                    else
+                        z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
+                    const int q = rw.pows & 31;
+                    S += Tt[q * G + grp] * z;
+                    Gp[0] += Dt[q * G + grp] * z;
                 }
-                if constexpr (K == 1) {
-                    S += t[0] * z;
-                    Gp[0] += d[0] * z;
-                } else {
-                    const CT t12 = t[1] * t[2], t01 = t[0] * t[1];
-                    S += (t[0] * t12) * z;
-                    Gp[0] += (d[0] * t12) * z;
-                    Gp[1] += (t[0] * t[2] * d[1]) * z;
-                    Gp[K - 1] += (t01 * d[K - 1]) * z;
+            }
+        } else {
+            // K = 3: I = (q0, q1, q2); inner sums over q2, then q1, then q0
+            int c0 = -1, c1 = -1;
+            CT a = CT(0), b = CT(0), Pq = CT(0), Qq = CT(0), Rq = CT(0);
+            for (int r0 = 0; r0 < nrow; r0 += TPC) {
+                const int r = r0 + gl;
+                if (r < nrow) {
+                    const FactRow rw = rows[r];
+                    const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
+                    const CT z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
+                    const int q0 = rw.pows & 31, q1 = (rw.pows >> kPowBits) & 31, q2 = (rw.pows >> (2 * kPowBits)) & 31;
+                    if (q0 != c0 || q1 != c1) {
+                        if (c1 >= 0) {
+                            const CT t1 = Tt[(1 * rs + c1) * G + grp];
+                            Pq += t1 * a;
+                            Qq += Dt[(1 * rs + c1) * G + grp] * a;
+                            Rq += t1 * b;
+                        }
+                        a = CT(0);
+                        b = CT(0);
+                        if (q0 != c0) {
+                            if (c0 >= 0) {
+                                const CT t0 = Tt[c0 * G + grp];
+                                S += t0 * Pq;
+                                Gp[0] += Dt[c0 * G + grp] * Pq;
+                                Gp[1] += t0 * Qq;
+                                Gp[2] += t0 * Rq;
+                            }
+                            Pq = CT(0);
+                            Qq = CT(0);
+                            Rq = CT(0);
+                            c0 = q0;
+                        }
+                        c1 = q1;
+                    }
+                    a += Tt[(2 * rs + q2) * G + grp] * z;
+                    b += Dt[(2 * rs + q2) * G + grp] * z;
                 }
+            }
+            if (c1 >= 0) {
+                const CT t1 = Tt[(1 * rs + c1) * G + grp];
+                Pq += t1 * a;
+                Qq += Dt[(1 * rs + c1) * G + grp] * a;
+                Rq += t1 * b;
+                const CT t0 = Tt[c0 * G + grp];
+                S += t0 * Pq;
+                Gp[0] += Dt[c0 * G + grp] * Pq;
+                Gp[1] += t0 * Qq;
+                Gp[2] += t0 * Rq;
             }
         }
         // column pass: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K)
-        for (int c0 = 0; c0 < ncol; c0 += TPC) {
-            const int cc = c0 + gl;
-            if (cc < ncol) {
-                const FactRow cl = rows[nrow + cc];
-                const int e0 = cc == 0 ? e_col0 : rows[nrow + cc - 1].end;
-                const CT w = entry_sum<CT, 1, G>(ent, e0, cl.end, 0, Xv, grp);
-                constexpr int C = NP - K;
-                CT t[C], d[C];
-#pragma unroll
-                for (int p = 0; p < C; p++) {
-                    const int q = (cl.pows >> (kPowBits * p)) & 31;
-                    t[p] = Tt[((K + p) * rs + q) * G + grp];
-                    d[p] = Dt[((K + p) * rs + q) * G + grp];
+        {
+            constexpr int C = NP - K;
+            int c0 = -1, c1 = -1;
+            CT a = CT(0), b = CT(0), Pq = CT(0), Qq = CT(0), Rq = CT(0);
+            for (int cb = 0; cb < ncol; cb += TPC) {
+                const int cc = cb + gl;
+                if (cc < ncol) {
+                    const FactRow cl = rows[nrow + cc];
+                    const int e0 = cc == 0 ? e_col0 : rows[nrow + cc - 1].end;
+                    const CT w = entry_sum<CT, 1, G>(ent, e0, cl.end, 0, Xv, grp);
+                    const int q0 = cl.pows & 31, q1 = (cl.pows >> kPowBits) & 31;
+                    if constexpr (C == 2) {
+                        // J = (q0, q1) of pairs K, K+1: sums over q1 within a run of q0
+                        if (q0 != c0) {
+                            if (c0 >= 0) {
+                                Gp[K] += Dt[(K * rs + c0) * G + grp] * a;
+                                Gp[K + 1] += Tt[(K * rs + c0) * G + grp] * b;
+                            }
+                            a = CT(0);
+                            b = CT(0);
+                            c0 = q0;
+                        }
+                        a += Tt[((K + 1) * rs + q1) * G + grp] * w;
+                        b += Dt[((K + 1) * rs + q1) * G + grp] * w;
+                    } else {
+                        // J = (q0, q1, q2) of pairs K .. K+2
+                        const int q2 = (cl.pows >> (2 * kPowBits)) & 31;
+                        if (q0 != c0 || q1 != c1) {
+                            if (c1 >= 0) {
+                                const CT t1 = Tt[((K + 1) * rs + c1) * G + grp];
+                                Pq += t1 * a;
+                                Qq += Dt[((K + 1) * rs + c1) * G + grp] * a;
+                                Rq += t1 * b;
+                            }
+                            a = CT(0);
+                            b = CT(0);
+                            if (q0 != c0) {
+                                if (c0 >= 0) {
+                                    const CT t0 = Tt[(K * rs + c0) * G + grp];
+                                    Gp[K] += Dt[(K * rs + c0) * G + grp] * Pq;
+                                    Gp[K + 1] += t0 * Qq;
+                                    Gp[K + 2] += t0 * Rq;
+                                }
+                                Pq = CT(0);
+                                Qq = CT(0);
+                                Rq = CT(0);
+                                c0 = q0;
+                            }
+                            c1 = q1;
+                        }
+                        a += Tt[((K + 2) * rs + q2) * G + grp] * w;
+                        b += Dt[((K + 2) * rs + q2) * G + grp] * w;
+                    }
                 }
-                if constexpr (C == 2) {
-                    Gp[K] += (d[0] * t[1]) * w;
-                    Gp[K + 1] += (t[0] * d[1]) * w;
-                } else {
-                    const CT t12 = t[1] * t[C - 1];
-                    Gp[K] += (d[0] * t12) * w;
-                    Gp[K + 1] += (t[0] * d[1] * t[C - 1]) * w;
-                    Gp[K + C - 1] += (t[0] * t[1] * d[C - 1]) * w;
+            }
+            if constexpr (C == 2) {
+                if (c0 >= 0) {
+                    Gp[K] += Dt[(K * rs + c0) * G + grp] * a;
+                    Gp[K + 1] += Tt[(K * rs + c0) * G + grp] * b;
+                }
+            } else {
+                if (c1 >= 0) {
+                    const CT t1 = Tt[((K + 1) * rs + c1) * G + grp];
+                    Pq += t1 * a;
+                    Qq += Dt[((K + 1) * rs + c1) * G + grp] * a;
+                    Rq += t1 * b;
+                    const CT t0 = Tt[(K * rs + c0) * G + grp];
+                    Gp[K] += Dt[(K * rs + c0) * G + grp] * Pq;
+                    Gp[K + 1] += t0 * Qq;
+                    Gp[K + 2] += t0 * Rq;
                 }
             }
         }
