@@ -178,12 +178,15 @@ def algorithmic_flops(calc, cfg, params_path):
         flops = ok.sum() * (P * (6 * order + 15) + P * 21) + (nc * (5 * P + 1)).sum()
         # operations the factored kernel performs instead of n_c*(5P+1): two
         # multiply-adds per coefficient per pass, the row/column products and
-        # the per-row and per-column gradient terms
+        # the gradient terms of the nested per-record sums (two multiply-adds
+        # per record, plus three or four per run of equal leading powers; runs
+        # counted as whole, i.e. one lane per cluster)
         nrow, ncol, R = fac[nb]
         K = 1 if nb == 3 else 3
         C = P - K
-        per_row = 4 if K == 1 else 15
-        per_col = 6 if C == 2 else 12
+        Rf = float(max(R, 1))
+        per_row = 4 if K == 1 else 4 + 6 / Rf + 8 / Rf ** 2
+        per_col = 4 + 4 / Rf if C == 2 else 4 + 6 / Rf + 6 / Rf ** 2
         ex = ok.sum() * (P * (6 * order + 15) + P * 21 + R ** C * (C - 1) + R ** K * (K - 1)) \
             + (4.0 * nc).sum() + (per_row * nrow[u][ok].astype(np.float64)).sum() \
             + (per_col * ncol[u][ok].astype(np.float64)).sum()
