@@ -707,7 +707,7 @@ def run_reference_arm(args):
         pool.map(_cpu_worker, [(params, xyz, 1)] * cores)
         one = (time.perf_counter() - t) / 2.0
         steps = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
-        warm = min(args.warmup, 1)
+        warm = min(max(3, args.warmup), 10)   # at least 3 warm-up steps, bounded like the timed ones
         for _ in range(warm):
             pool.map(_cpu_worker, [(params, xyz, 1)] * cores)
         t0 = time.perf_counter()
