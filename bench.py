@@ -443,6 +443,25 @@ def extras(args):
     sa = sum(x.n_atoms for x in sample)
     out["plain_fp64_per_config"] = {"value": sa / wall, "unit": UNIT, "configs": len(sample), "atoms": sa,
                                     "ms_per_config": 1e3 * wall / len(sample)}
+    # one large configuration (32768 atoms, 70 x 70 x 72 A, ChIMES 12/10/4),
+    # FP64 and mixed, with the mixed result's error against FP64
+    p3 = synth.write_param_file(os.path.join(tmp, "c3.params"), synth.spec_c3())
+    cfg3 = synth.config_c3()
+    res = {}
+    for prec, name in ((FP64, "c3_fp64"), (MIXED, "c3_mixed")):
+        c = Calculator(precision=prec, graph=True)
+        c.load_params(p3)
+        c.stage(c.pack([(cfg3.pos, cfg3.types, cfg3.cell)]))
+        c.autotune()
+        r = time_steps(c, cfg3.n_atoms, 10)
+        r["autotuned"] = c.tuning()
+        res[name] = c.evaluate(cfg3.pos, cfg3.types, cfg3.cell)
+        out[name] = r
+    r64, r32 = res["c3_fp64"], res["c3_mixed"]
+    out["c3_mixed"]["error_vs_fp64"] = {
+        "energy_rel": abs(r32["energy"] - r64["energy"]) / abs(r64["energy"]),
+        "force_max_abs": float(np.abs(r32["force"] - r64["force"]).max()),
+        "stress_max_abs": float(np.abs(r32["stress"] - r64["stress"]).max())}
     out["pair_style_c2"] = pair_style(params, cfg)
     # the same with the 2- and 3-body terms tabulated (the reference's
     # TABULATION option: spline / tricubic look-up instead of the Chebyshev sums)
