@@ -94,8 +94,9 @@ struct PairTab {
 };
 
 // One factored-list entry: coefficient and the other side's record, in one
-// 16-byte (FP64) or 8-byte (FP32) load.  idx = linear index (low 16 bits) |
-// the other side's powers packed kPowBits per pair (high 16 bits).
+// 16-byte (FP64) or 8-byte (FP32) load.  idx = linear index (bits 0-15) |
+// the other side's powers packed kPowBits per pair (bits 16-30) | bit 31 set on
+// the last entry of its record (idx < 0).
 struct __attribute__((aligned(16))) FactEntD {
     double a;
     int idx;

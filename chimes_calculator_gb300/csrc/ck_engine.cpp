@@ -646,16 +646,21 @@ Status Engine::autotune(int* chosen, std::string& err) {
     const bool do3 = tuning.stride3 > 0, do4 = tuning.stride4 > 0;
     // candidates per body order: factored kernels (1, 2, 4 lanes per cluster)
     // where the tables exist, then the per-coefficient kernels (1..32 lanes)
-    // (3-body factored also without its Y table)
-    struct Cand { int fact, tpc, noy; };
+    // (3-body factored also without its Y table).  The factored forms differ
+    // in shared memory per cluster, so each is tried at 8 and at up to 16
+    // resident one-warp blocks per SM (capped by its occupancy); the per-SM
+    // count is refined below.
+    struct Cand { int fact, tpc, noy, fbps; };
     auto cands = [](bool can_fact, bool with_noy) {
         std::vector<Cand> v;
         if (can_fact)
-            for (int t : {1, 2, 4}) {
-                v.push_back({1, t, 0});
-                if (with_noy) v.push_back({1, t, 1});
-            }
-        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0});
+            for (int t : {1, 2, 4})
+                for (int nf : {0, 1}) {
+                    if (nf && !with_noy) continue;
+                    v.push_back({1, t, nf, 8});
+                    v.push_back({1, t, nf, 16});
+                }
+        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0, 0});
         return v;
     };
     const std::vector<Cand> c3 = cands(avail_fact3_, true), c4 = cands(avail_fact4_, false);
@@ -664,14 +669,16 @@ Status Engine::autotune(int* chosen, std::string& err) {
             tuning.fact3 = c.fact;
             (c.fact ? tuning.ftpc3 : tuning.tpc3) = c.tpc;
             tuning.noy3 = c.noy;
+            if (c.fbps > 0) tuning.fbps3 = c.fbps;
         } else {
             tuning.fact4 = c.fact;
             (c.fact ? tuning.ftpc4 : tuning.tpc4) = c.tpc;
+            if (c.fbps > 0) tuning.fbps4 = c.fbps;
         }
     };
     double best3 = 1e300, best4 = 1e300;
-    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3};
-    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0};
+    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3, tuning.fbps3};
+    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0, tuning.fbps4};
     const size_t nc = std::max(c3.size(), c4.size());
     for (size_t i = 0; i < nc && st == kOk; i++) {
         const bool need3 = do3 && i < c3.size(), need4 = do4 && i < c4.size();

@@ -85,6 +85,40 @@ __device__ __forceinline__ CT entry_sum(const E* __restrict__ ent, int e0, int e
     return z0 + z1;
 }
 
+// One pass over the entries [e0, e1) of nrec consecutive records (TPC = 1):
+// z += a * V[idx] per entry; at an entry with the record-end bit (idx < 0)
+// flush(record powers, z) and start the next record.  Entries are loaded
+// eight at a time regardless of where records end, so a short record does
+// not pay its own load latency.
+template <typename CT, int G, typename E, typename F>
+__device__ __forceinline__ void flat_pass(const E* __restrict__ ent, int e0, int e1, const FactRow* rec, int nrec,
+                                          const CT* V, int grp, F&& flush) {
+    CT z = CT(0);
+    int r = 0;
+    int pw = nrec > 0 ? rec[0].pows : 0;
+    for (int k = e0; k < e1; k += 8) {
+        E q[8];
+        CT x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k + u < e1) q[u] = ent[k + u];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k + u < e1) x[u] = V[(q[u].idx & 0xffff) * G + grp];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k + u < e1) {
+                z += CT(q[u].a) * x[u];
+                if (q[u].idx < 0) {   // uniform: all lanes read the same entries
+                    flush(pw, z);
+                    z = CT(0);
+                    r++;
+                    pw = r < nrec ? rec[r].pows : 0;
+                }
+            }
+    }
+}
+
 // The 3-body row sum without a Y table: sum over [e0, e1) of a * T1[q1] T2[q2],
 // the column's powers q1, q2 taken from the entry's high bits.
 template <typename CT, int G, typename E>
@@ -458,19 +492,147 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
         CT S = CT(0), Gp[NP];
 #pragma unroll
         for (int p = 0; p < NP; p++) Gp[p] = CT(0);
-        // The TPC lanes of a cluster take whole rows (and then whole columns)
-        // round robin (adjacent records, adjacent loads), each flushing its own
-        // rows.  A record's entries start where the previous record's end.
-        // Records are sorted by their powers (first pair most significant), so
-        // the products of a record's pairs are factored out level by level: a
-        // lane sums over its last pair's power within a run of equal leading
-        // powers and multiplies by the leading pairs' values once per run
-        // (nested sums instead of full products per record).  A lane's
-        // round-robin share is a sorted subsequence, so the same flushes apply;
-        // the saving is largest with one lane per cluster, where runs stay whole.
+        // A record's entries start where the previous record's end; its last
+        // entry carries the record-end bit.  Records are sorted by their powers
+        // (first pair most significant), so the products of a record's pairs
+        // are factored out level by level: the flushes sum over the last pair's
+        // power within a run of equal leading powers and multiply by the
+        // leading pairs' values once per run (nested sums instead of full
+        // products per record); the saving is largest with one lane per
+        // cluster, where runs stay whole.
         const int e_col0 = R->f_ent + R->ncoef;
-        // row pass: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K)
-        if constexpr (K == 1) {
+        // Row records: z_I = sum_J a Y_J; S += X_I z_I, G_p += dX_I/dr_p z_I (p < K).
+        // With K = 3, I = (q0, q1, q2): inner sums over q2, then q1, then q0.
+        int rc0 = -1, rc1 = -1;
+        CT ra = CT(0), rb = CT(0), rP = CT(0), rQ = CT(0), rR = CT(0);
+        auto row_flush = [&](int pows, CT z) {
+            if constexpr (K == 1) {
+                const int q = pows & 31;
+                S += Tt[q * G + grp] * z;
+                Gp[0] += Dt[q * G + grp] * z;
+            } else {
+                const int q0 = pows & 31, q1 = (pows >> kPowBits) & 31, q2 = (pows >> (2 * kPowBits)) & 31;
+                if (q0 != rc0 || q1 != rc1) {
+                    if (rc1 >= 0) {
+                        const CT t1 = Tt[(1 * rs + rc1) * G + grp];
+                        rP += t1 * ra;
+                        rQ += Dt[(1 * rs + rc1) * G + grp] * ra;
+                        rR += t1 * rb;
+                    }
+                    ra = CT(0);
+                    rb = CT(0);
+                    if (q0 != rc0) {
+                        if (rc0 >= 0) {
+                            const CT t0 = Tt[rc0 * G + grp];
+                            S += t0 * rP;
+                            Gp[0] += Dt[rc0 * G + grp] * rP;
+                            Gp[1] += t0 * rQ;
+                            Gp[2] += t0 * rR;
+                        }
+                        rP = CT(0);
+                        rQ = CT(0);
+                        rR = CT(0);
+                        rc0 = q0;
+                    }
+                    rc1 = q1;
+                }
+                ra += Tt[(2 * rs + q2) * G + grp] * z;
+                rb += Dt[(2 * rs + q2) * G + grp] * z;
+            }
+        };
+        auto row_end = [&]() {
+            if constexpr (K == 3) {
+                if (rc1 >= 0) {
+                    const CT t1 = Tt[(1 * rs + rc1) * G + grp];
+                    rP += t1 * ra;
+                    rQ += Dt[(1 * rs + rc1) * G + grp] * ra;
+                    rR += t1 * rb;
+                    const CT t0 = Tt[rc0 * G + grp];
+                    S += t0 * rP;
+                    Gp[0] += Dt[rc0 * G + grp] * rP;
+                    Gp[1] += t0 * rQ;
+                    Gp[2] += t0 * rR;
+                }
+            }
+        };
+        // Column records: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K), summed
+        // over the last column pair within runs of equal leading powers.
+        constexpr int C = NP - K;
+        int cc0 = -1, cc1 = -1;
+        CT ca = CT(0), cb = CT(0), cP = CT(0), cQ = CT(0), cR = CT(0);
+        auto col_flush = [&](int pows, CT w) {
+            const int q0 = pows & 31, q1 = (pows >> kPowBits) & 31;
+            if constexpr (C == 2) {
+                // J = (q0, q1) of pairs K, K+1: sums over q1 within a run of q0
+                if (q0 != cc0) {
+                    if (cc0 >= 0) {
+                        Gp[K] += Dt[(K * rs + cc0) * G + grp] * ca;
+                        Gp[K + 1] += Tt[(K * rs + cc0) * G + grp] * cb;
+                    }
+                    ca = CT(0);
+                    cb = CT(0);
+                    cc0 = q0;
+                }
+                ca += Tt[((K + 1) * rs + q1) * G + grp] * w;
+                cb += Dt[((K + 1) * rs + q1) * G + grp] * w;
+            } else {
+                // J = (q0, q1, q2) of pairs K .. K+2
+                const int q2 = (pows >> (2 * kPowBits)) & 31;
+                if (q0 != cc0 || q1 != cc1) {
+                    if (cc1 >= 0) {
+                        const CT t1 = Tt[((K + 1) * rs + cc1) * G + grp];
+                        cP += t1 * ca;
+                        cQ += Dt[((K + 1) * rs + cc1) * G + grp] * ca;
+                        cR += t1 * cb;
+                    }
+                    ca = CT(0);
+                    cb = CT(0);
+                    if (q0 != cc0) {
+                        if (cc0 >= 0) {
+                            const CT t0 = Tt[(K * rs + cc0) * G + grp];
+                            Gp[K] += Dt[(K * rs + cc0) * G + grp] * cP;
+                            Gp[K + 1] += t0 * cQ;
+                            Gp[K + 2] += t0 * cR;
+                        }
+                        cP = CT(0);
+                        cQ = CT(0);
+                        cR = CT(0);
+                        cc0 = q0;
+                    }
+                    cc1 = q1;
+                }
+                ca += Tt[((K + 2) * rs + q2) * G + grp] * w;
+                cb += Dt[((K + 2) * rs + q2) * G + grp] * w;
+            }
+        };
+        auto col_end = [&]() {
+            if constexpr (C == 2) {
+                if (cc0 >= 0) {
+                    Gp[K] += Dt[(K * rs + cc0) * G + grp] * ca;
+                    Gp[K + 1] += Tt[(K * rs + cc0) * G + grp] * cb;
+                }
+            } else {
+                if (cc1 >= 0) {
+                    const CT t1 = Tt[((K + 1) * rs + cc1) * G + grp];
+                    cP += t1 * ca;
+                    cQ += Dt[((K + 1) * rs + cc1) * G + grp] * ca;
+                    cR += t1 * cb;
+                    const CT t0 = Tt[(K * rs + cc0) * G + grp];
+                    Gp[K] += Dt[(K * rs + cc0) * G + grp] * cP;
+                    Gp[K + 1] += t0 * cQ;
+                    Gp[K + 2] += t0 * cR;
+                }
+            }
+        };
+        if constexpr (TPC == 1 && !NOY) {
+            // one lane per cluster: each pass is one stream of entries across
+            // its records (loads batched across record ends)
+            flat_pass<CT, G>(ent, R->f_ent, e_col0, rows, nrow, Y, grp, row_flush);
+            flat_pass<CT, G>(ent, e_col0, e_col0 + R->ncoef, rows + nrow, ncol, Xv, grp, col_flush);
+        } else {
+            // The TPC lanes of a cluster take whole records round robin
+            // (adjacent records, adjacent loads), each flushing its own.  A
+            // lane's share is a sorted subsequence, so the nested sums apply.
             for (int r0 = 0; r0 < nrow; r0 += TPC) {
                 const int r = r0 + gl;
                 if (r < nrow) {
@@ -481,136 +643,20 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
                         z = entry_sum_noy<CT, G>(ent, e0, rw.end, Tt + 1 * rs * G, Tt + 2 * rs * G, grp);
                     else
                         z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
-                    const int q = rw.pows & 31;
-                    S += Tt[q * G + grp] * z;
-                    Gp[0] += Dt[q * G + grp] * z;
+                    row_flush(rw.pows, z);
                 }
             }
-        } else {
-            // K = 3: I = (q0, q1, q2); inner sums over q2, then q1, then q0
-            int c0 = -1, c1 = -1;
-            CT a = CT(0), b = CT(0), Pq = CT(0), Qq = CT(0), Rq = CT(0);
-            for (int r0 = 0; r0 < nrow; r0 += TPC) {
-                const int r = r0 + gl;
-                if (r < nrow) {
-                    const FactRow rw = rows[r];
-                    const int e0 = r == 0 ? R->f_ent : rows[r - 1].end;
-                    const CT z = entry_sum<CT, 1, G>(ent, e0, rw.end, 0, Y, grp);
-                    const int q0 = rw.pows & 31, q1 = (rw.pows >> kPowBits) & 31, q2 = (rw.pows >> (2 * kPowBits)) & 31;
-                    if (q0 != c0 || q1 != c1) {
-                        if (c1 >= 0) {
-                            const CT t1 = Tt[(1 * rs + c1) * G + grp];
-                            Pq += t1 * a;
-                            Qq += Dt[(1 * rs + c1) * G + grp] * a;
-                            Rq += t1 * b;
-                        }
-                        a = CT(0);
-                        b = CT(0);
-                        if (q0 != c0) {
-                            if (c0 >= 0) {
-                                const CT t0 = Tt[c0 * G + grp];
-                                S += t0 * Pq;
-                                Gp[0] += Dt[c0 * G + grp] * Pq;
-                                Gp[1] += t0 * Qq;
-                                Gp[2] += t0 * Rq;
-                            }
-                            Pq = CT(0);
-                            Qq = CT(0);
-                            Rq = CT(0);
-                            c0 = q0;
-                        }
-                        c1 = q1;
-                    }
-                    a += Tt[(2 * rs + q2) * G + grp] * z;
-                    b += Dt[(2 * rs + q2) * G + grp] * z;
-                }
-            }
-            if (c1 >= 0) {
-                const CT t1 = Tt[(1 * rs + c1) * G + grp];
-                Pq += t1 * a;
-                Qq += Dt[(1 * rs + c1) * G + grp] * a;
-                Rq += t1 * b;
-                const CT t0 = Tt[c0 * G + grp];
-                S += t0 * Pq;
-                Gp[0] += Dt[c0 * G + grp] * Pq;
-                Gp[1] += t0 * Qq;
-                Gp[2] += t0 * Rq;
-            }
-        }
-        // column pass: w_J = sum_I a X_I; G_p += dY_J/dr_p w_J (p >= K)
-        {
-            constexpr int C = NP - K;
-            int c0 = -1, c1 = -1;
-            CT a = CT(0), b = CT(0), Pq = CT(0), Qq = CT(0), Rq = CT(0);
-            for (int cb = 0; cb < ncol; cb += TPC) {
-                const int cc = cb + gl;
+            for (int cb0 = 0; cb0 < ncol; cb0 += TPC) {
+                const int cc = cb0 + gl;
                 if (cc < ncol) {
                     const FactRow cl = rows[nrow + cc];
                     const int e0 = cc == 0 ? e_col0 : rows[nrow + cc - 1].end;
-                    const CT w = entry_sum<CT, 1, G>(ent, e0, cl.end, 0, Xv, grp);
-                    const int q0 = cl.pows & 31, q1 = (cl.pows >> kPowBits) & 31;
-                    if constexpr (C == 2) {
-                        // J = (q0, q1) of pairs K, K+1: sums over q1 within a run of q0
-                        if (q0 != c0) {
-                            if (c0 >= 0) {
-                                Gp[K] += Dt[(K * rs + c0) * G + grp] * a;
-                                Gp[K + 1] += Tt[(K * rs + c0) * G + grp] * b;
-                            }
-                            a = CT(0);
-                            b = CT(0);
-                            c0 = q0;
-                        }
-                        a += Tt[((K + 1) * rs + q1) * G + grp] * w;
-                        b += Dt[((K + 1) * rs + q1) * G + grp] * w;
-                    } else {
-                        // J = (q0, q1, q2) of pairs K .. K+2
-                        const int q2 = (cl.pows >> (2 * kPowBits)) & 31;
-                        if (q0 != c0 || q1 != c1) {
-                            if (c1 >= 0) {
-                                const CT t1 = Tt[((K + 1) * rs + c1) * G + grp];
-                                Pq += t1 * a;
-                                Qq += Dt[((K + 1) * rs + c1) * G + grp] * a;
-                                Rq += t1 * b;
-                            }
-                            a = CT(0);
-                            b = CT(0);
-                            if (q0 != c0) {
-                                if (c0 >= 0) {
-                                    const CT t0 = Tt[(K * rs + c0) * G + grp];
-                                    Gp[K] += Dt[(K * rs + c0) * G + grp] * Pq;
-                                    Gp[K + 1] += t0 * Qq;
-                                    Gp[K + 2] += t0 * Rq;
-                                }
-                                Pq = CT(0);
-                                Qq = CT(0);
-                                Rq = CT(0);
-                                c0 = q0;
-                            }
-                            c1 = q1;
-                        }
-                        a += Tt[((K + 2) * rs + q2) * G + grp] * w;
-                        b += Dt[((K + 2) * rs + q2) * G + grp] * w;
-                    }
-                }
-            }
-            if constexpr (C == 2) {
-                if (c0 >= 0) {
-                    Gp[K] += Dt[(K * rs + c0) * G + grp] * a;
-                    Gp[K + 1] += Tt[(K * rs + c0) * G + grp] * b;
-                }
-            } else {
-                if (c1 >= 0) {
-                    const CT t1 = Tt[((K + 1) * rs + c1) * G + grp];
-                    Pq += t1 * a;
-                    Qq += Dt[((K + 1) * rs + c1) * G + grp] * a;
-                    Rq += t1 * b;
-                    const CT t0 = Tt[(K * rs + c0) * G + grp];
-                    Gp[K] += Dt[(K * rs + c0) * G + grp] * Pq;
-                    Gp[K + 1] += t0 * Qq;
-                    Gp[K + 2] += t0 * Rq;
+                    col_flush(cl.pows, entry_sum<CT, 1, G>(ent, e0, cl.end, 0, Xv, grp));
                 }
             }
         }
+        row_end();
+        col_end();
         // combine the TPC partial sums of each cluster
 #pragma unroll
         for (int off = TPC / 2; off > 0; off >>= 1) {

@@ -926,7 +926,8 @@ ParamImage pack_params(const HostParams& P) {
                     int nrec = 0;
                     for (int k = 0; k < R.ncoef; k++) {
                         const int c = ord[k];
-                        const int code = minor[c] | (opows[c] << 16);
+                        const bool last = k + 1 == R.ncoef || major[ord[k + 1]] != major[c];
+                        const int code = (int)((uint32_t)minor[c] | ((uint32_t)opows[c] << 16) | (last ? 0x80000000u : 0u));
                         fed.push_back(FactEntD{Bd.coef[ti][c], code, 0});
                         fef.push_back(FactEntF{(float)Bd.coef[ti][c], code});
                         if (k + 1 == R.ncoef || major[ord[k + 1]] != major[c]) {

@@ -1,7 +1,8 @@
 // Host check of the factored coefficient tables (pack_params): for every valid
 // 3-/4-body tuple of a parameter file, random Chebyshev tables T_p, dT_p give
 // the same S = sum a prod T and G_p = sum a dT_p prod_{q!=p} T through the
-// per-coefficient packed powers and through the row/column factored lists.
+// per-coefficient packed powers and through the row/column factored lists
+// (whose last entry per record carries the record-end bit).
 // With a second argument (a binary parameter cache of the same file) it also
 // checks that the cache packs into the same device image as the text file.
 // Usage: factored_check <params> [cache]; prints "ok <tuples checked>" or a mismatch.
@@ -124,7 +125,7 @@ int main(int argc, char** argv) {
                 for (int k = e; k < rw.end; k++) {
                     const int lin = fe[k].idx & 0xffff;
                     if (lin >= ny || ff[k].idx != fe[k].idx || ff[k].a != (float)fe[k].a ||
-                        packed_lin(fe[k].idx >> 16, np - K) != lin) {
+                        packed_lin(fe[k].idx >> 16, np - K) != lin || (fe[k].idx < 0) != (k + 1 == rw.end)) {
                         std::printf("bad row entry\n");
                         return 1;
                     }
@@ -141,7 +142,7 @@ int main(int argc, char** argv) {
                 for (int k = e; k < cl.end; k++) {
                     const int lin = fe[k].idx & 0xffff;
                     if (lin >= nx || ff[k].idx != fe[k].idx ||
-                        packed_lin(fe[k].idx >> 16, K) != lin) {
+                        packed_lin(fe[k].idx >> 16, K) != lin || (fe[k].idx < 0) != (k + 1 == cl.end)) {
                         std::printf("bad column entry\n");
                         return 1;
                     }
