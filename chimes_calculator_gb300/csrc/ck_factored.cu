@@ -88,25 +88,38 @@ __device__ __forceinline__ CT entry_sum(const E* __restrict__ ent, int e0, int e
 // One pass over the entries [e0, e1) of nrec consecutive records (TPC = 1):
 // z += a * V[idx] per entry; at an entry with the record-end bit (idx < 0)
 // flush(record powers, z) and start the next record.  Entries are loaded
-// eight at a time regardless of where records end, so a short record does
-// not pay its own load latency.
-template <typename CT, int G, typename E, typename F>
+// eight (NOY: four) at a time regardless of where records end, so a short
+// record does not pay its own load latency.
+// The entry's multiplier is V[idx] (a table), or with NOY the product of the
+// two column pairs' values T1[q1] T2[q2] (powers in the entry's high bits).
+template <typename CT, int G, bool NOY, typename E>
+__device__ __forceinline__ CT entry_value(const E& q, const CT* V, const CT* T2, int grp) {
+    if constexpr (NOY) {
+        const int c = q.idx >> 16;
+        return V[(c & 31) * G + grp] * T2[((c >> kPowBits) & 31) * G + grp];
+    } else {
+        return V[(q.idx & 0xffff) * G + grp];
+    }
+}
+
+template <typename CT, int G, bool NOY = false, typename E, typename F>
 __device__ __forceinline__ void flat_pass(const E* __restrict__ ent, int e0, int e1, const FactRow* rec, int nrec,
-                                          const CT* V, int grp, F&& flush) {
+                                          const CT* V, const CT* T2, int grp, F&& flush) {
+    constexpr int NBAT = NOY ? 4 : 8;   // the NOY form keeps fewer entries in flight (registers)
     CT z = CT(0);
     int r = 0;
     int pw = nrec > 0 ? rec[0].pows : 0;
-    for (int k = e0; k < e1; k += 8) {
-        E q[8];
-        CT x[8];
+    for (int k = e0; k < e1; k += NBAT) {
+        E q[NBAT];
+        CT x[NBAT];
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < NBAT; u++)
             if (k + u < e1) q[u] = ent[k + u];
 #pragma unroll
-        for (int u = 0; u < 8; u++)
-            if (k + u < e1) x[u] = V[(q[u].idx & 0xffff) * G + grp];
+        for (int u = 0; u < NBAT; u++)
+            if (k + u < e1) x[u] = entry_value<CT, G, NOY>(q[u], V, T2, grp);
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < NBAT; u++)
             if (k + u < e1) {
                 z += CT(q[u].a) * x[u];
                 if (q[u].idx < 0) {   // uniform: all lanes read the same entries
@@ -624,11 +637,17 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
                 }
             }
         };
-        if constexpr (TPC == 1 && !NOY) {
+        // (in FP32 the NOY form keeps its per-record loop: the one-stream form's
+        // registers cost it more resident warps than the batched loads save)
+        if constexpr (TPC == 1 && !(NOY && sizeof(CT) == 4)) {
             // one lane per cluster: each pass is one stream of entries across
             // its records (loads batched across record ends)
-            flat_pass<CT, G>(ent, R->f_ent, e_col0, rows, nrow, Y, grp, row_flush);
-            flat_pass<CT, G>(ent, e_col0, e_col0 + R->ncoef, rows + nrow, ncol, Xv, grp, col_flush);
+            if constexpr (NOY && NB == 3)
+                flat_pass<CT, G, true>(ent, R->f_ent, e_col0, rows, nrow, Tt + 1 * rs * G, Tt + 2 * rs * G, grp,
+                                       row_flush);
+            else
+                flat_pass<CT, G>(ent, R->f_ent, e_col0, rows, nrow, Y, nullptr, grp, row_flush);
+            flat_pass<CT, G>(ent, e_col0, e_col0 + R->ncoef, rows + nrow, ncol, Xv, nullptr, grp, col_flush);
         } else {
             // The TPC lanes of a cluster take whole records round robin
             // (adjacent records, adjacent loads), each flushing its own.  A
