@@ -121,6 +121,7 @@ class ClockSampler:
 # from one ncu capture each (profiles/k_forcef_c2_fp64.md, k_forcen_c2_fp64.md)
 PROFILED_TRAFFIC = {
     "k_forcef<3,double,1>": 4272384,
+    "k_forcef<3,double,1,true>": 4273408,
     "k_forcef<4,double,4>": 2047488,
     "k_forcen<3,double,4>": 872704,
     "k_forcen<4,double,8>": 599552,

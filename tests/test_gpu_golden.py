@@ -58,13 +58,19 @@ def test_mixed_precision_error(golden, native_lib, name, factored):
     assert np.abs(r32["force"] - r64["force"]).max() <= MIXED_F_ABS_TOL
 
 
-@pytest.mark.parametrize("factored", [True, False], ids=["factored", "per_coef"])
-@pytest.mark.parametrize("tpc", [(1, 1, 2), (2, 4, 4), (8, 16, 4), (32, 32, 2), (4, 2, 1)])
-def test_threads_per_cluster_variants(golden, native_lib, tpc, factored):
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("factored", [1, 3, 0], ids=["factored", "factored_noy", "per_coef"])
+@pytest.mark.parametrize("tpc", [(1, 1, 2), (2, 4, 4), (8, 16, 4), (32, 32, 2), (4, 2, 1), (1, 2, 4)])
+def test_threads_per_cluster_variants(golden, native_lib, tpc, factored, precision):
+    """Every launch shape of every contraction form (lanes per cluster, one-warp
+    blocks per SM; one lane per cluster takes the one-stream passes) gives the
+    reference's results, FP64 within the FP64 tolerances and mixed within its
+    error budget."""
     g = golden["c2_small"]
-    _, r = evaluate(g, tpc=tpc, factored=factored)
-    assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
-    assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+    _, r = evaluate(g, precision=precision, tpc=tpc, factored=factored)
+    et, ft = (E_REL_TOL, F_ABS_TOL) if precision == 0 else (MIXED_E_REL_TOL, MIXED_F_ABS_TOL)
+    assert abs(r["energy"] - g.energy) <= et * max(1.0, abs(g.energy))
+    assert np.abs(r["force"] - g.force).max() <= ft
 
 
 def test_autotune_keeps_results(golden, native_lib):
