@@ -128,21 +128,14 @@ PROFILED_TRAFFIC = {
 }
 
 
-def algorithmic_flops(calc, cfg, params_path):
-    """Per-launch algorithmic FLOPs of the 3B and 4B force kernels:
-        flops(cluster) = P*(6*o + 15) + n_c*(5*P + 1) + P*21
-    over the clusters that pass the per-type outer cutoffs (exp/sin/cos count
-    as one flop).  Cluster geometry is rebuilt here from the exported lists."""
-    from chimes_calculator_gb300 import synth  # noqa: F401
+def ghost_position_fn(calc, cfg):
+    """Position of a system-local ghost index of the last evaluation (image 0 =
+    the wrapped atoms, then the periodic layers in the library's order)."""
     info = calc.info(0)
-    o2, o3, o4 = info["orders"]
-    l2, l3, l4 = calc.lists()
     cell = np.asarray(cfg.cell, dtype=np.float64)
-    inv = np.linalg.inv(cell)
-    f = cfg.pos @ inv
+    f = cfg.pos @ np.linalg.inv(cell)
     f -= np.floor(f)
     n = cfg.n_atoms
-    maxc = max(info["max_cutoffs"])
     L = np.linalg.norm(cell, axis=1).min()
     nl = int(math.ceil(2 * info["max_cutoffs"][0] / L + 1))
     side = 2 * nl + 1
@@ -156,7 +149,19 @@ def algorithmic_flops(calc, cfg, params_path):
         sh = np.stack([full // (side * side) - nl, (full // side) % side - nl, full % side - nl], axis=-1)
         sh = np.where((img == 0)[..., None], 0, sh)
         return (f[a] + sh) @ cell
+    return ghost_pos
 
+
+def algorithmic_flops(calc, cfg, params_path):
+    """Per-launch algorithmic FLOPs of the 3B and 4B force kernels:
+        flops(cluster) = P*(6*o + 15) + n_c*(5*P + 1) + P*21
+    over the clusters that pass the per-type outer cutoffs (exp/sin/cos count
+    as one flop).  Cluster geometry is rebuilt here from the exported lists."""
+    info = calc.info(0)
+    o2, o3, o4 = info["orders"]
+    l2, l3, l4 = calc.lists()
+    n = cfg.n_atoms
+    ghost_pos = ghost_position_fn(calc, cfg)
     tup = calc.tuple_table(0)
     fac = calc.tuple_factored(0)
     out = {}
@@ -194,7 +199,6 @@ def algorithmic_flops(calc, cfg, params_path):
         # without the Y table (3-body): one more multiply per row entry, no table
         ex_noy = ex + nc.sum() - ok.sum() * (R ** C * (C - 1)) if nb == 3 else ex
         out[nb] = (int(ok.sum()), float(flops), float(ex), float(ex_noy))
-    del maxc
     return out
 
 
@@ -566,6 +570,36 @@ def profile_pairstyle(args, skin=1.0):
     print(json.dumps({"mode": args.profile_pairstyle, "ms_per_call": 1e3 * (time.perf_counter() - t0) / 5}))
 
 
+def profile_direct(args, reps=5):
+    """The per-cluster entry points (chimesFF::compute_2B/3B/4B through
+    ck_compute_cluster_batch) on every cluster the C2 configuration lists:
+    distances, displacements (second atom minus first) and type indices built
+    on the host from the exported lists, one batched call per body order,
+    timed on the host with the copies in and out."""
+    from chimes_calculator_gb300 import Calculator
+    tmp = tempfile.mkdtemp(prefix="ckd")
+    params, cfg = make_workload(tmp)
+    c = Calculator()
+    c.load_params(params)
+    c.evaluate(cfg.pos, cfg.types, cfg.cell)
+    lists = c.lists()
+    gp = ghost_position_fn(c, cfg)
+    ti = c.type_indices(cfg.types)
+    out = {}
+    for nb, lst in zip((2, 3, 4), lists):
+        pos = gp(lst)
+        dr = np.stack([pos[:, b] - pos[:, a] for a in range(nb) for b in range(a + 1, nb)], axis=1)
+        dx = np.linalg.norm(dr, axis=2)
+        typ = ti[lst % cfg.n_atoms]
+        c.clusters(nb, dx, dr, typ)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            c.clusters(nb, dx, dr, typ)
+        dt = (time.perf_counter() - t0) / reps
+        out["%db" % nb] = {"clusters": int(len(lst)), "ms_per_call": 1e3 * dt, "clusters_per_s": len(lst) / dt}
+    print(json.dumps(out))
+
+
 def serving(args):
     """Continuous batching of single-point requests (three parameter sets,
     16-4096 atoms log-uniform): Poisson arrivals at multiples of the plain
@@ -776,7 +810,13 @@ def main():
     ap.add_argument("--profile-pairstyle", default="", choices=["", "chebyshev", "tabulated", "fingerprint"],
                     help="profiler run of the pair-style path on C2 (Chebyshev or tabulated terms: one list "
                          "build + 5 calls), or of the 3-body fingerprint histogram of its records")
+    ap.add_argument("--profile-direct", action="store_true",
+                    help="the per-cluster entry points (compute_2B/3B/4B, ck_compute_cluster_batch) on every "
+                         "listed cluster of C2, one batched call per body order")
     args = ap.parse_args()
+    if args.profile_direct:
+        profile_direct(args)
+        return
     if args.profile_batched:
         profile_batched(args)
         return
