@@ -314,13 +314,26 @@ def run_ours(args):
         if noy:
             kname = kname[:-1] + ",true>"
             work[nb] = (work[nb][0], work[nb][1], work[nb][3])
+        # DRAM traffic of the kernel's ncu capture on this workload; a launch
+        # shape without its own capture (lanes per cluster) reads the same
+        # pair tables, coefficient lists and cluster lists as the captured
+        # shape of the same contraction form (4.27 MB for the 3-body table and
+        # no-table forms alike)
+        traffic, traffic_src = PROFILED_TRAFFIC.get(kname), None
+        if traffic is not None:
+            traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on this workload (profiles/)"
+        else:
+            same = [v for k, v in PROFILED_TRAFFIC.items() if k.startswith("k_forcef<%d,double," % nb)] if fact else []
+            if same:
+                traffic = same[0]
+                traffic_src = ("ncu capture of the same factored %d-body kernel at another launch shape on this "
+                               "workload (profiles/)" % nb)
         achieved = work[nb][1] / (stage[dom] * 1e-3) / 1e12
         executed = (work[nb][2] if fact else work[nb][1]) / (stage[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": kname, "achieved": achieved,
                 "peak": peak64.value, "unit": "TFLOP/s", "frac": achieved / peak64.value,
-                "traffic": PROFILED_TRAFFIC.get(kname),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel on this "
-                                  "workload (profiles/)" if kname in PROFILED_TRAFFIC else None,
+                "traffic": traffic,
+                "traffic_source": traffic_src,
                 "peak_source": "measured in-run FP64 FMA probe (ck_fma_peak); "
                 "MEASURED_PEAKS.json has no CUDA-core FP64 figure",
                 "flops_per_launch": work[nb][1], "clusters_evaluated": work[nb][0],

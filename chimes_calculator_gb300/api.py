@@ -113,16 +113,12 @@ class Calculator:
 
     def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
         cache = self._types[slot]
-        out = np.empty(len(types), dtype=np.int32)
-        for i, t in enumerate(types):
-            k = cache.get(t)
-            if k is None:
-                k = self.lib.ck_type_index(self.h, slot, t.encode())
-                if k < 0:
-                    raise ChimesError("atom type %s is not in parameter set %d" % (t, slot))
-                cache[t] = k
-            out[i] = k
-        return out
+        for t in set(types).difference(cache):   # names not looked up before
+            k = self.lib.ck_type_index(self.h, slot, str(t).encode())
+            if k < 0:
+                raise ChimesError("atom type %s is not in parameter set %d" % (t, slot))
+            cache[t] = k
+        return np.fromiter(map(cache.__getitem__, types), dtype=np.int32, count=len(types))
 
     def set_precision(self, precision: int):
         self._check(self.lib.ck_set_precision(self.h, int(precision)))
@@ -263,13 +259,11 @@ class Calculator:
         stress = np.zeros((n, 9))
         self._check(self.lib.ck_calculate_batch(self.h, n, _ip(natoms), _dp(pos), _ip(types), _dp(cells), _ip(sm),
                                                 _ip(ps), _dp(energy), _dp(force), _dp(stress)))
-        out = []
-        off = 0
-        for s in range(n):
-            out.append({"energy": energy[s], "force": force[off:off + natoms[s]].copy(),
-                        "stress": stress[s].copy()})
-            off += natoms[s]
-        return out
+        # per configuration: views into the batch's freshly allocated arrays
+        ends = np.cumsum(natoms).tolist()
+        starts = [0] + ends[:-1]
+        return [{"energy": energy[s], "force": force[a:b], "stress": stress[s]}
+                for s, (a, b) in enumerate(zip(starts, ends))]
 
     def evaluate(self, pos, types, cell, slot: int = 0, small: bool = False):
         return self.evaluate_batch([(pos, types, cell)], slots=[slot], small=[int(small)])[0]
