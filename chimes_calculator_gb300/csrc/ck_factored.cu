@@ -648,6 +648,17 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
             else
                 flat_pass<CT, G>(ent, R->f_ent, e_col0, rows, nrow, Y, nullptr, grp, row_flush);
             flat_pass<CT, G>(ent, e_col0, e_col0 + R->ncoef, rows + nrow, ncol, Xv, nullptr, grp, col_flush);
+        } else if constexpr (TPC == 2 && !NOY && sizeof(CT) == 8) {
+            // two lanes per cluster (FP64): lane 0 streams the row entries, lane
+            // 1 the column entries (as many), each flushing its own records
+            // (4096-configuration batch, 4-body: 34.0 -> 31.7 ms; in FP32 the
+            // extra registers cost more than the whole runs save)
+            const bool colp = gl == 1;
+            flat_pass<CT, G>(ent, colp ? e_col0 : R->f_ent, colp ? e_col0 + R->ncoef : e_col0, colp ? rows + nrow : rows,
+                             colp ? ncol : nrow, colp ? Xv : Y, nullptr, grp, [&](int pw, CT z) {
+                                 if (colp) col_flush(pw, z);
+                                 else row_flush(pw, z);
+                             });
         } else {
             // The TPC lanes of a cluster take whole records round robin
             // (adjacent records, adjacent loads), each flushing its own.  A
