@@ -14,6 +14,7 @@ energy and forces: kcal/mol, kcal/mol/A and the 3x3 stress in kcal/mol/A^3.
 from __future__ import annotations
 
 import ctypes
+import itertools
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -238,14 +239,18 @@ class Calculator:
         natoms = np.array([len(c[0]) for c in configs], dtype=np.int32)
         pos = np.ascontiguousarray(np.concatenate([np.asarray(c[0], dtype=np.float64).reshape(-1, 3)
                                                    for c in configs]))
-        tys = []
-        for c, s in zip(configs, slots):
-            t = c[1]
-            if len(t) and isinstance(t[0], str):
-                tys.append(self.type_indices(t, s))
-            else:
-                tys.append(np.asarray(t, dtype=np.int32))
-        types = np.ascontiguousarray(np.concatenate(tys).astype(np.int32))
+        if len(set(slots)) == 1 and all(len(c[1]) and isinstance(c[1][0], str) for c in configs):
+            # names throughout, one parameter set: one mapping over the whole batch
+            types = self.type_indices(list(itertools.chain.from_iterable(c[1] for c in configs)), slots[0])
+        else:
+            tys = []
+            for c, s in zip(configs, slots):
+                t = c[1]
+                if len(t) and isinstance(t[0], str):
+                    tys.append(self.type_indices(t, s))
+                else:
+                    tys.append(np.asarray(t, dtype=np.int32))
+            types = np.ascontiguousarray(np.concatenate(tys).astype(np.int32))
         cells = np.ascontiguousarray(np.stack([np.asarray(c[2], dtype=np.float64).reshape(3, 3) for c in configs]))
         sm = np.zeros(n, dtype=np.int32) if small is None else np.asarray(small, dtype=np.int32).reshape(n)
         ps = np.asarray(slots, dtype=np.int32)
