@@ -1,8 +1,9 @@
 // Per-cluster kernels: the chimesFF::compute_2B/3B/4B entry points, where the
 // caller owns the cluster loop and passes distances, displacement vectors and
 // type indices (chimesFF/src/chimesFF.cpp:1644-1775, 1931-2176, 2496-2872).
-// One thread per cluster, FP64, any number of clusters per launch; outputs are
-// per-cluster (the host adds them into the caller's accumulators).
+// One thread (3-/4-body: one or more lanes) per cluster, FP64, any number of
+// clusters per launch; outputs are per-cluster (the host adds them into the
+// caller's accumulators).
 //
 // Besides energy, forces and the packed stress, each cluster reports the
 // reference's `force_scalar_in` value: for 2B the penalty force scalar over r
@@ -21,6 +22,8 @@
 #include "ck_tab.cuh"
 
 namespace ck {
+
+cudaError_t allow_max_smem(const void* kernel);   // ck_force.cu
 
 namespace {
 
@@ -88,68 +91,107 @@ __global__ void k_direct2(const DevParamSet* Pp, int n, const double* dx, const 
     status[c] = st;
 }
 
-template <int NB>
-__global__ void k_directn(const DevParamSet* Pp, int n, const double* dx, const double* dr, const int* typ,
-                          double* force, double* stress, double* energy, double* fscal, int* status) {
+// TPC lanes per cluster (a power of two up to 32): the lanes of a cluster
+// fill its Chebyshev tables and cutoffs in shared memory (pair p by lane
+// p mod TPC), each lane sums every TPC-th coefficient, the group reduces S and
+// G with shuffles, and the lane holding the list's last coefficient supplies
+// force_scalar_in.  With few clusters (a 4-body batch of a few thousand) one
+// lane per cluster leaves most SMs idle; the launcher picks TPC from the
+// cluster count.  One-warp blocks; shared memory per cluster
+// NP * (2 * (order + 1) + 2) doubles.
+template <int NB, int TPC>
+__global__ void __launch_bounds__(32) k_directn(const DevParamSet* Pp, int n, const double* dx, const double* dr,
+                                                const int* typ, double* force, double* stress, double* energy,
+                                                double* fscal, int* status) {
     constexpr int NP = Topo<NB>::NP;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
+    constexpr unsigned kAll = 0xffffffffu;
+    extern __shared__ __align__(16) double dsm[];
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (int)(tid / TPC), gl = (int)(tid % TPC);
     const DevParamSet& P = *Pp;
-    for (int k = 0; k < 3 * NB; k++) force[3 * NB * c + k] = 0.0;
-    for (int k = 0; k < 6; k++) stress[6 * c + k] = 0.0;
-    for (int k = 0; k < NP; k++) fscal[NP * c + k] = 0.0;
-    energy[c] = 0.0;
-    status[c] = 0;
-    int u = 0;
-    for (int k = 0; k < NB; k++) u = u * P.ntypes + typ[NB * c + k];
-    const TupleRec* R = (NB == 3 ? P.t3 : P.t4) + u;
-    if (R->type_id < 0) return;   // excluded cluster type
-    const double* r = &dx[NP * c];
-    const double* d = &dr[3 * NP * c];
-    for (int p = 0; p < NP; p++)
-        if (r[p] >= R->rout[p]) return;
     const int order = NB == 3 ? P.o3 : P.o4;
-    double T[NP][kMaxOrder + 1], D[NP][kMaxOrder + 1], fc[NP], fcd[NP];
-    for (int p = 0; p < NP; p++) {
-        cheby_table<double>(T[p], D[p], r[p], R->rin[p], R->lam[p], R->xavg[p], R->xdiff[p], order,
-                            P.inner_smooth, nullptr);
-        fcut_eval<double>(P, r[p], R->rout[p], fc[p], fcd[p]);
+    const int op1 = order + 1;
+    // this cluster's tables: T[p][0..order], D[p][0..order], then fc[p], fcd[p]
+    double* tab = dsm + (long long)(threadIdx.x / TPC) * NP * (2 * op1 + 2);
+    double* fcs = tab + 2 * NP * op1;
+    double* fcds = fcs + NP;
+    bool active = c < n;   // group-uniform; every lane reaches the syncs and shuffles below
+    if (active && gl == 0) {
+        for (int k = 0; k < 3 * NB; k++) force[3 * NB * c + k] = 0.0;
+        for (int k = 0; k < 6; k++) stress[6 * c + k] = 0.0;
+        for (int k = 0; k < NP; k++) fscal[NP * c + k] = 0.0;
+        energy[c] = 0.0;
+        status[c] = 0;
     }
-    int st = 1;
-    for (int p = 0; p < NP; p++)
-        if (r[p] < R->rin[p]) st |= 8;   // below-rin warning only (badness is a 2B notion)
-    double pre[NP + 1], suf[NP + 1];
-    pre[0] = 1.0;
-    for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * fc[p];
-    suf[NP] = 1.0;
-    for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * fc[p];
-    double S = 0.0, G[NP];
-    for (int p = 0; p < NP; p++) G[p] = 0.0;
-    const double* cf = (NB == 3 ? P.c3d : P.c4d) + R->coef_off;
-    const uint32_t* pw = (NB == 3 ? P.p3 : P.p4) + R->coef_off;
-    double last[NP];
-    for (int p = 0; p < NP; p++) last[p] = 0.0;
-    for (int k = 0; k < R->ncoef; k++) {
-        double t[NP], dd[NP];
-        for (int p = 0; p < NP; p++) {
-            const int q = (pw[k] >> (kPowBits * p)) & 31u;
-            t[p] = T[p][q];
-            dd[p] = D[p][q];
-        }
-        double tp[NP + 1], ts[NP + 1];
-        tp[0] = 1.0;
-        for (int p = 0; p < NP; p++) tp[p + 1] = tp[p] * t[p];
-        ts[NP] = 1.0;
-        for (int p = NP - 1; p >= 0; p--) ts[p] = ts[p + 1] * t[p];
-        S += cf[k] * tp[NP];
-        for (int p = 0; p < NP; p++) G[p] += cf[k] * dd[p] * tp[p] * ts[p + 1];
-        if (k == R->ncoef - 1)
+    const TupleRec* R = nullptr;
+    const double* r = nullptr;
+    if (active) {
+        int u = 0;
+        for (int k = 0; k < NB; k++) u = u * P.ntypes + typ[NB * c + k];
+        R = (NB == 3 ? P.t3 : P.t4) + u;
+        r = &dx[NP * c];
+        if (R->type_id < 0) active = false;   // excluded cluster type
+        else
             for (int p = 0; p < NP; p++)
-                last[p] = cf[k] * (fc[p] * dd[p] + fcd[p] * t[p]) * (pre[p] * suf[p + 1] / r[p]) * tp[p] * ts[p + 1];
+                if (r[p] >= R->rout[p]) active = false;
     }
+    if (active)
+        for (int p = gl; p < NP; p += TPC) {
+            cheby_table<double>(tab + 2 * p * op1, tab + (2 * p + 1) * op1, r[p], R->rin[p], R->lam[p], R->xavg[p],
+                                R->xdiff[p], order, P.inner_smooth, nullptr);
+            fcut_eval<double>(P, r[p], R->rout[p], fcs[p], fcds[p]);
+        }
+    __syncwarp();
+    double S = 0.0, G[NP], last[NP], pre[NP + 1], suf[NP + 1];
+    for (int p = 0; p < NP; p++) G[p] = last[p] = 0.0;
+    pre[NP] = 0.0;
+    int st = 1;
+    if (active) {
+        for (int p = 0; p < NP; p++)
+            if (r[p] < R->rin[p]) st |= 8;   // below-rin warning only (badness is a 2B notion)
+        pre[0] = 1.0;
+        for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * fcs[p];
+        suf[NP] = 1.0;
+        for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * fcs[p];
+        const double* cf = (NB == 3 ? P.c3d : P.c4d) + R->coef_off;
+        const uint32_t* pw = (NB == 3 ? P.p3 : P.p4) + R->coef_off;
+        const int kl = R->ncoef - 1;
+        for (int k = gl; k < R->ncoef; k += TPC) {
+            double t[NP], dd[NP];
+            for (int p = 0; p < NP; p++) {
+                const int q = (pw[k] >> (kPowBits * p)) & 31u;
+                t[p] = tab[2 * p * op1 + q];
+                dd[p] = tab[(2 * p + 1) * op1 + q];
+            }
+            double tp[NP + 1], ts[NP + 1];
+            tp[0] = 1.0;
+            for (int p = 0; p < NP; p++) tp[p + 1] = tp[p] * t[p];
+            ts[NP] = 1.0;
+            for (int p = NP - 1; p >= 0; p--) ts[p] = ts[p + 1] * t[p];
+            S += cf[k] * tp[NP];
+            for (int p = 0; p < NP; p++) G[p] += cf[k] * dd[p] * tp[p] * ts[p + 1];
+            if (k == kl)
+                for (int p = 0; p < NP; p++)
+                    last[p] = cf[k] * (fcs[p] * dd[p] + fcds[p] * t[p]) * (pre[p] * suf[p + 1] / r[p]) * tp[p] *
+                              ts[p + 1];
+        }
+    }
+    // combine the group's partial sums; the last coefficient's lane holds
+    // force_scalar_in, the others hold zeros
+#pragma unroll
+    for (int off = TPC / 2; off > 0; off >>= 1) {
+        S += __shfl_xor_sync(kAll, S, off);
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            G[p] += __shfl_xor_sync(kAll, G[p], off);
+            last[p] += __shfl_xor_sync(kAll, last[p], off);
+        }
+    }
+    if (!active || gl != 0) return;
+    const double* d = &dr[3 * NP * c];
     double vir[6] = {0, 0, 0, 0, 0, 0};
     for (int p = 0; p < NP; p++) {
-        const double fsp = pre[p] * suf[p + 1] / r[p] * (fc[p] * G[p] + fcd[p] * S);
+        const double fsp = pre[p] * suf[p + 1] / r[p] * (fcs[p] * G[p] + fcds[p] * S);
         const double* dp = &d[3 * p];
         const int a = Topo<NB>::a(p), b = Topo<NB>::b(p);
         for (int k = 0; k < 3; k++) {
@@ -167,6 +209,33 @@ __global__ void k_directn(const DevParamSet* Pp, int n, const double* dx, const 
     for (int p = 0; p < NP; p++) fscal[NP * c + p] = last[p];
     energy[c] = pre[NP] * S;
     status[c] = st;
+}
+
+template <int NB>
+void launch_directn(const DevParamSet* Pd, int order, int n, const double* dx, const double* dr, const int* typ,
+                    double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st) {
+    constexpr int NP = Topo<NB>::NP;
+    // lanes per cluster: enough threads for about 16 warps on each of ~152 SMs
+    const long long want = 152LL * 16 * 32 / (n > 0 ? n : 1);
+    int tpc = 1;
+    while (tpc < 32 && 2LL * tpc <= want) tpc *= 2;
+    const unsigned grid = (unsigned)(((long long)n * tpc + 31) / 32);
+    const size_t smem = sizeof(double) * (size_t)(32 / tpc) * NP * (2 * (order + 1) + 2);
+#define CK_DIRECTN(T_)                                                                                    \
+    do {                                                                                                  \
+        auto kern = k_directn<NB, T_>;                                                                    \
+        if (smem > 48 * 1024) allow_max_smem((const void*)kern);                                          \
+        count_launch(), kern<<<grid, 32, smem, st>>>(Pd, n, dx, dr, typ, force, stress, energy, fscal, status); \
+    } while (0)
+    switch (tpc) {
+        case 1: CK_DIRECTN(1); break;
+        case 2: CK_DIRECTN(2); break;
+        case 4: CK_DIRECTN(4); break;
+        case 8: CK_DIRECTN(8); break;
+        case 16: CK_DIRECTN(16); break;
+        default: CK_DIRECTN(32); break;
+    }
+#undef CK_DIRECTN
 }
 
 // compute_2B_tab (chimesFF.cpp:1782-1867): table energy and force scalar;
@@ -257,9 +326,9 @@ __global__ void k_direct3tab(const DevParamSet* Pp, int n, const double* dx, con
 
 }  // namespace
 
-void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
-                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st,
-                   bool tab) {
+void launch_direct(const DevParamSet* P, int nbody, int order, int n, const double* dx, const double* dr,
+                   const int* typ, double* force, double* stress, double* energy, double* fscal, int* status,
+                   cudaStream_t st, bool tab) {
     if (n <= 0) return;
     const unsigned grid = (unsigned)((n + 63) / 64);
     if (tab) {
@@ -268,8 +337,8 @@ void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, con
         return;
     }
     if (nbody == 2) count_launch(), k_direct2<<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
-    else if (nbody == 3) count_launch(), k_directn<3><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
-    else count_launch(), k_directn<4><<<grid, 64, 0, st>>>(P, n, dx, dr, typ, force, stress, energy, fscal, status);
+    else if (nbody == 3) launch_directn<3>(P, order, n, dx, dr, typ, force, stress, energy, fscal, status, st);
+    else launch_directn<4>(P, order, n, dx, dr, typ, force, stress, energy, fscal, status, st);
 }
 
 }  // namespace ck

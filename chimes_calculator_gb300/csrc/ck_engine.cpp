@@ -785,8 +785,8 @@ Status Engine::compute_clusters(int slot, int nbody, int n, const double* dx, co
     CK_TRY(cudaMemcpyAsync(ddx, dx, sizeof(double) * n * np, cudaMemcpyHostToDevice, stream_));
     CK_TRY(cudaMemcpyAsync(ddr, dr, sizeof(double) * n * np * 3, cudaMemcpyHostToDevice, stream_));
     CK_TRY(cudaMemcpyAsync(dtyp, typ, sizeof(int) * n * nbody, cudaMemcpyHostToDevice, stream_));
-    launch_direct(dsets_.p + slot, nbody, n, ddx, ddr, dtyp, dforce, dstress, denergy, dfscal, dstatus, stream_,
-                  tab);
+    launch_direct(dsets_.p + slot, nbody, nbody == 2 ? P.o2 : nbody == 3 ? P.o3 : P.o4, n, ddx, ddr, dtyp, dforce,
+                  dstress, denergy, dfscal, dstatus, stream_, tab);
     CK_TRY(cudaGetLastError());
     CK_TRY(cudaMemcpyAsync(force, dforce, sizeof(double) * n * 3 * nbody, cudaMemcpyDeviceToHost, stream_));
     CK_TRY(cudaMemcpyAsync(stress, dstress, sizeof(double) * n * 6, cudaMemcpyDeviceToHost, stream_));

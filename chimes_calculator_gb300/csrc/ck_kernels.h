@@ -86,10 +86,11 @@ void launch_nl_tab3(const BatchView& B, long long n3, int* sel, double* selr, un
 void launch_nl_fp(const BatchView& B, const NeighView& N, int nbody, long long n, bool fill, int* flag,
                   const long long* off, double* d, int* t, cudaStream_t st);
 
-// Per-cluster evaluation (caller-owned cluster loop), FP64, one thread per cluster.
-void launch_direct(const DevParamSet* P, int nbody, int n, const double* dx, const double* dr, const int* typ,
-                   double* force, double* stress, double* energy, double* fscal, int* status, cudaStream_t st,
-                   bool tab = false);
+// Per-cluster evaluation (caller-owned cluster loop), FP64; order = the body
+// order's polynomial order of the set (sizes the 3-/4-body kernels' tables).
+void launch_direct(const DevParamSet* P, int nbody, int order, int n, const double* dx, const double* dr,
+                   const int* typ, double* force, double* stress, double* energy, double* fscal, int* status,
+                   cudaStream_t st, bool tab = false);
 
 int sm_count();
 
