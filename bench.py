@@ -634,7 +634,9 @@ def serving(args):
         srv = Server(workers=args.serve_workers, precision=prec, max_batch_atoms=1 << 15)
         for p in paths:
             srv.load_params(p)
-        poisson_run(srv, reqs[:40], tidx, rate_hz=1e6)     # warm-up (grows workspaces)
+        # warm-up: every request once, back to back, so the workspaces and
+        # list capacities reach their steady-state sizes before the timed sweeps
+        poisson_run(srv, reqs, tidx, rate_hz=1e6)
         runs = []
         for mult in (0.5, 1.0, 2.0, 8.0, 1e3):
             r = poisson_run(srv, reqs, tidx, rate_hz=mult * base["throughput_req_per_s"])
