@@ -257,6 +257,9 @@ class Calculator:
         return natoms, pos, types, cells, sm, ps
 
     def evaluate_batch(self, configs, slots=None, small=None):
+        """Energy, forces and stress of every configuration in one launch
+        sequence; per configuration a dict whose force and stress are views into
+        arrays allocated for this call."""
         natoms, pos, types, cells, sm, ps = self.pack(configs, slots, small)
         n = len(configs)
         energy = np.zeros(n)
