@@ -141,6 +141,32 @@ def test_cluster_batch_matches_oracle(golden, native_lib, nb):
     assert nonzero > 10
 
 
+@pytest.mark.parametrize("nb", [3, 4])
+def test_cluster_batch_lane_split_consistent(golden, native_lib, nb):
+    """The per-cluster kernels split a cluster's coefficient list over 1-32
+    lanes by batch size: 3000 clusters (several lanes each) and the same
+    clusters inside a batch of about 90000 (one lane each) agree, the
+    reference's force_scalar_in values included."""
+    from chimes_calculator_gb300 import Calculator
+    from oracle.oracle import Oracle
+    g = golden["excluded"]
+    cl = _clusters_from(g, nb, 3000, np.random.default_rng(40 + nb))
+    typ_all = Oracle(g.params).type_indices(g.cfg.types)
+    c = Calculator()
+    c.load_params(g.params)
+    npair = nb * (nb - 1) // 2
+    dx = np.array([a for a, _, _ in cl]).reshape(len(cl), npair)
+    dr = np.array([b for _, b, _ in cl]).reshape(len(cl), npair, 3)
+    ty = np.array([typ_all[ids] for _, _, ids in cl], dtype=np.int32)
+    small = c.clusters(nb, dx, dr, ty)
+    rep = 90000 // len(cl) + 1
+    big = c.clusters(nb, np.tile(dx, (rep, 1)), np.tile(dr, (rep, 1, 1)), np.tile(ty, (rep, 1)))
+    for k in ("energy", "force", "stress", "fscal"):
+        a, b = small[k], big[k][:len(cl)]
+        assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(a).max()), k
+    assert np.count_nonzero(small["energy"]) > 100
+
+
 def test_per_cluster_c_interface(golden, native_lib):
     lib = native_lib
     lib.ck_set_error_mode(1)
