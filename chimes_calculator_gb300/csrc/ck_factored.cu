@@ -16,10 +16,11 @@
 // Clusters are first bucketed by (parameter set, ordered type tuple), each
 // bucket padded with -1 to a multiple of 32 slots, so every warp works on one
 // tuple: loop bounds and coefficient loads are uniform across the warp (the
-// loads are broadcasts).  TPC lanes share a cluster (TPC = 1, 2 or 4) and
-// take its rows, then its columns, round robin (each lane sums and flushes
-// whole records); per-cluster tables (T, dT/dr per pair, Y and X) sit in
-// shared memory interleaved by cluster, [entry][cluster].
+// loads are broadcasts).  TPC lanes share a cluster (TPC = 1, 2 or 4): one
+// lane streams both passes' entries; two lanes (FP64) take one pass each;
+// otherwise the lanes take whole records round robin.  Per-cluster tables
+// (T, dT/dr per pair, Y and X) sit in shared memory interleaved by cluster,
+// [entry][cluster].
 #include <cuda_runtime.h>
 
 #include <cstdint>
