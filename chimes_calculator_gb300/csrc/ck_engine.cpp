@@ -66,6 +66,7 @@ Status Engine::init_device(std::string& err) {
         err = std::string("no CUDA device available: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
         return kErrCuda;
     }
+    CK_TRY(cudaGetDevice(&device_));
     CK_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     CK_TRY(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
     CK_TRY(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));

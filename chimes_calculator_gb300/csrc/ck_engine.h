@@ -85,6 +85,8 @@ public:
     Engine& operator=(const Engine&) = delete;
 
     Status init_device(std::string& err);
+    // CUDA device current when the engine was set up (its stream, parameter sets, workspace)
+    int device() const { return device_; }
     // Parses a parameter file into a new device-resident slot; returns the slot (>= 0).
     int load_params(const std::string& path, std::string& err);
     const HostParams& params(int slot) const { return *sets_[slot].host; }
@@ -160,6 +162,7 @@ private:
     cudaStream_t stream2_ = nullptr;              // the 4-body branch
     cudaEvent_t fork_ = nullptr, fork2_ = nullptr, join_ = nullptr;
     bool ready_ = false;
+    int device_ = -1;
 
     // batch layout of the staged batch
     std::vector<SysDesc> hsys_;

@@ -364,8 +364,11 @@ void launch_force2(const BatchView& B, const int* l2_owner, const ForceLaunch& L
     long long want = (long long)sm_count() * 8;
     long long need = (ntot + 255) / 256;
     const unsigned grid = (unsigned)(want < need ? want : need);
-    if (L.precision == kMixed) count_launch(), k_force2<float><<<grid, 256, 0, st>>>(B, l2_owner);
-    else count_launch(), k_force2<double><<<grid, 256, 0, st>>>(B, l2_owner);
+    // The 1-/2-body stage runs in FP64 in both precision forms.  Fitted force
+    // fields' 2-body series alternate in sign with coefficients of 10-10^3
+    // (the CHON and HN3 parameter files), so an FP32 sum cancels away ~1e-6 of
+    // the energy; this stage is a few per cent of an evaluation.
+    count_launch(), k_force2<double><<<grid, 256, 0, st>>>(B, l2_owner);
 }
 
 void launch_force3(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {

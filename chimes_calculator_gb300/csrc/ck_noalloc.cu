@@ -9,7 +9,14 @@
 // images, bin grid, neighbour and cluster lists, scan workspace, accumulators
 // -- lives in one file-scope device array of fixed size (kScratchBytes, about
 // 13.4 MiB), which every GPU that loads the library holds until the process
-// exits.  The kernels are the same ones the allocating entry points run.
+// exits.  The list-build and force kernels are the allocating path's own, in
+// one fixed launch shape: the thread-per-entry cluster enumeration and the
+// per-coefficient contraction (k_forcen) with the handle's tuning, never the
+// bucketed factored contraction, which needs per-batch bucket arrays the
+// static layout does not hold.  Because the inputs are already on the device,
+// their check (type index inside the parameter set, finite coordinates) runs
+// on the device too; a bad value is replaced in the scratch copy before any
+// table is indexed with it and the call returns an input error.
 //
 // The array is shared by all calls on a device and keeps the previous call's
 // contents; everything that must start at zero is cleared by each call.  Two
@@ -19,6 +26,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "ck_engine.h"
@@ -103,15 +111,16 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 unsigned char* g_base[kMaxDevices] = {nullptr};
+std::mutex g_base_mu;
 
-// Once per device, with that device current: the device address of the array.
-Status scratch_base(unsigned char** out, std::string& err) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        err = std::string("no usable CUDA device: ") + cudaGetErrorString(e);
+// Once per device, with that device (`dev`, current) : the device address of the array.
+Status scratch_base(int dev, unsigned char** out, std::string& err) {
+    if (dev < 0 || dev >= kMaxDevices) {
+        err = "no usable CUDA device";
         return kErrCuda;
     }
+    std::lock_guard<std::mutex> lock(g_base_mu);
+    cudaError_t e = cudaSuccess;
     if (!g_base[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -123,6 +132,28 @@ Status scratch_base(unsigned char** out, std::string& err) {
     }
     *out = g_base[dev];
     return kOk;
+}
+
+// Device-side input check (Engine::stage does the same on host arrays): a type
+// index outside [0, ntypes) becomes 0 and a non-finite coordinate 0.0 in the
+// scratch copies, so no later kernel indexes a table with a bad value;
+// flags[6] bit 1 / bit 2 records it and the call reports an input error.
+__global__ void k_noalloc_check_inputs(double* pos, int* type, int n, int ntypes, int* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int bad = 0;
+    const int t = type[i];
+    if (t < 0 || t >= ntypes) {
+        type[i] = 0;
+        bad |= 1;
+    }
+    for (int k = 0; k < 3; k++) {
+        if (!isfinite(pos[3 * i + k])) {
+            pos[3 * i + k] = 0.0;
+            bad |= 2;
+        }
+    }
+    if (bad) atomicOr(&flags[6], bad);
 }
 
 // energy / (n_rep+1)^3, forces copied out, stress = virial / volume
@@ -177,8 +208,14 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
               std::to_string(kNaBins) + ")";
         return kErrInput;
     }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != eng.device()) {
+        err = "ck_calculate_noalloc: the current CUDA device (" + std::to_string(dev) +
+              ") is not the one the handle's parameters were loaded on (" + std::to_string(eng.device()) + ")";
+        return kErrState;
+    }
     unsigned char* base = nullptr;
-    s = scratch_base(&base, err);
+    s = scratch_base(dev, &base, err);
     if (s != kOk) return s;
     d.pset = slot;
     d.in_off = d.atom_off = d.ghost_off = d.bin_off = 0;
@@ -249,6 +286,9 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     NA_TRY(cudaMemsetAsync(B.bin_count, 0, sizeof(int) * B.n_bins_total, st));
     NA_TRY(cudaMemsetAsync(B.bin_fill, 0, sizeof(int) * B.n_bins_total, st));
     launch_reset(B, st);   // bounding box, energy/virial, forces, flags, system error word
+    count_launch(), k_noalloc_check_inputs<<<(natom + 255) / 256, 256, 0, st>>>(
+        reinterpret_cast<double*>(base + kLayout.in_pos), reinterpret_cast<int*>(base + kLayout.in_type), natom,
+        P.ntypes, B.flags);
     launch_atoms(B, st);
     launch_ghosts(B, st);
     launch_bin_setup(B, st);
@@ -283,7 +323,27 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
     NA_TRY(cudaMemcpyAsync(&counts[2], B.e_off4 + B.n2_cap, sizeof(long long), cudaMemcpyDeviceToHost, st));
     NA_TRY(cudaStreamSynchronize(st));
 #undef NA_TRY
-    if (flags[0] || counts[0] > kNaPairs || counts[1] > kNaTrip || counts[2] > kNaQuad) {
+    eng.last.n2 = counts[0];
+    eng.last.n3 = counts[1];
+    eng.last.n4 = counts[2];
+    eng.last.n_atoms = d.n_atoms;
+    eng.last.n_ghost = n_ghost;
+    eng.last.badness = flags[2];
+    eng.last.penalty_hits = flags[3];
+    eng.last.below_rin = flags[4];
+    if (flags[6]) {
+        err = std::string("ck_calculate_noalloc: ") +
+              ((flags[6] & 1) ? "atom type index outside the parameter set" : "") +
+              ((flags[6] & 3) == 3 ? " and " : "") + ((flags[6] & 2) ? "non-finite atom coordinate" : "") +
+              "; the outputs are not valid";
+        return kErrInput;
+    }
+    if (flags[0] & 1) {
+        err = "ck_calculate_noalloc: the bin grid exceeds its capacity (" + std::to_string(kNaBins) +
+              " bins); the outputs are not valid";
+        return kErrCapacity;
+    }
+    if ((flags[0] & ~1) || counts[0] > kNaPairs || counts[1] > kNaTrip || counts[2] > kNaQuad) {
         err = "ck_calculate_noalloc: cluster lists exceed the static maximum (" + std::to_string(counts[0]) +
               " pairs, " + std::to_string(counts[1]) + " triplets, " + std::to_string(counts[2]) +
               " quadruplets; limits " + std::to_string(kNaPairs) + ", " + std::to_string(kNaTrip) + ", " +

@@ -165,6 +165,32 @@ public:
         return st == kOk ? 1 : st;
     }
 
+    // Tunes worker 0's engine on a representative batch (Engine::autotune:
+    // contraction form, lanes per cluster, resident blocks) and gives every
+    // worker the same choices.  Meant for start-up, before requests arrive:
+    // batches running meanwhile on other workers disturb the timings.
+    Status autotune(const std::vector<SystemSpec>& specs, int* chosen, std::string& err) {
+        std::lock_guard<std::mutex> g(load_mu_);
+        ForceLaunch t;
+        {
+            std::lock_guard<std::mutex> ge(*engine_mu_[0]);
+            Engine& e = *engines_[0];
+            Status st = e.stage(specs, err);
+            if (st != kOk) return st;
+            st = e.autotune(chosen, err);
+            if (st != kOk) return st;
+            t = e.tuning;
+        }
+        for (size_t w = 1; w < engines_.size(); w++) {
+            std::lock_guard<std::mutex> ge(*engine_mu_[w]);
+            ForceLaunch& d = engines_[w]->tuning;
+            d.tpc3 = t.tpc3, d.tpc4 = t.tpc4, d.blocks_per_sm = t.blocks_per_sm;
+            d.ftpc3 = t.ftpc3, d.ftpc4 = t.ftpc4, d.fbps3 = t.fbps3, d.fbps4 = t.fbps4;
+            d.want_fact3 = t.want_fact3, d.want_fact4 = t.want_fact4, d.noy3 = t.noy3;
+        }
+        return kOk;
+    }
+
     void stats(long long* out) {
         std::lock_guard<std::mutex> g(mu_);
         out[0] = submitted_;
@@ -351,6 +377,29 @@ int ck_server_take(void* s, long long id, int wait, double timeout_s, double* en
     int st = static_cast<ck::Server*>(s)->take(id, wait != 0, timeout_s, energy, force, stress, latency_s, err);
     if (st < 0) return ck::report_error(st, err);
     return st;
+}
+
+int ck_server_autotune(void* s, int nsys, const int* natoms, const double* pos, const int* types, const double* cells,
+                       const int* small, const int* pset, int* chosen) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    if (nsys <= 0 || !natoms || !pos || !types || !cells) return ck::report_error(ck::kErrInput, "empty batch");
+    std::vector<ck::SystemSpec> specs(nsys);
+    long long off = 0;
+    for (int i = 0; i < nsys; i++) {
+        ck::SystemSpec& q = specs[i];
+        q.n = natoms[i];
+        if (q.n <= 0) return ck::report_error(ck::kErrInput, "natom must be positive");
+        q.pos = pos + 3 * off;
+        q.types = types + off;
+        std::memcpy(q.cell, cells + 9 * (size_t)i, sizeof(q.cell));
+        q.small = small ? small[i] != 0 : false;
+        q.pset = pset ? pset[i] : 0;
+        off += q.n;
+    }
+    std::string err;
+    ck::Status st = static_cast<ck::Server*>(s)->autotune(specs, chosen, err);
+    if (st != ck::kOk) return ck::report_error(st, err);
+    return ck::kOk;
 }
 
 int ck_server_stats(void* s, long long* out) {

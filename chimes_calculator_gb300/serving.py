@@ -87,6 +87,23 @@ class Server:
             raise ChimesError(self.lib.ck_last_error().decode())
         return {"energy": e.value, "force": force, "stress": stress, "latency": lat.value}
 
+    def autotune(self, configs: Sequence[Tuple[object, object, object]], slots: Sequence[int]) -> Tuple[int, int, int]:
+        """Tunes every worker on a representative batch of (pos, type indices,
+        cell) with their parameter slots; returns (lanes per 3-body cluster,
+        lanes per 4-body cluster, blocks per SM)."""
+        natoms = np.array([np.asarray(c[0]).shape[0] for c in configs], dtype=np.int32)
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(c[0], dtype=np.float64).reshape(-1, 3)
+                                                   for c in configs]))
+        types = np.ascontiguousarray(np.concatenate([np.asarray(c[1], dtype=np.int32) for c in configs]))
+        cells = np.ascontiguousarray(np.stack([np.asarray(c[2], dtype=np.float64).reshape(9) for c in configs]))
+        ps = np.ascontiguousarray(np.asarray(slots, dtype=np.int32))
+        chosen = np.zeros(3, dtype=np.int32)
+        rc = self.lib.ck_server_autotune(self.h, len(configs), _ip(natoms), _dp(pos), _ip(types), _dp(cells), None,
+                                         _ip(ps), _ip(chosen))
+        if rc != 0:
+            raise ChimesError(self.lib.ck_last_error().decode())
+        return tuple(int(v) for v in chosen)
+
     def stats(self) -> dict:
         out = (ctypes.c_longlong * 6)()
         self.lib.ck_server_stats(self.h, out)
@@ -94,23 +111,24 @@ class Server:
                 "bytes_in_flight": out[4], "peak_bytes_in_flight": out[5]}
 
 
-def serving_workload(n_requests: int, seed: int = 1105, n_min: int = 16, n_max: int = 4096):
+def serving_workload(n_requests: int, seed: int = 1105, n_min: int = 16, n_max: int = 4096, processes: int = 0):
     """Requests of the serving workload: each draws one of three parameter
     sets (12/8/4 with one element, 12/10/4 with two, 12/8/4 with three); atom
-    counts log-uniform in [n_min, n_max]; density U(0.05, 0.12) per A^3."""
+    counts log-uniform in [n_min, n_max]; density U(0.05, 0.12) per A^3.
+    ``processes`` > 1 generates the configurations in a spawned pool."""
     from . import synth
     rng = np.random.default_rng(seed)
     specs = synth.specs_c5()
-    reqs = []
+    slots, jobs = [], []
     for q in range(n_requests):
         slot = int(rng.integers(len(specs)))
         n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
         rho = rng.uniform(0.05, 0.12)
         L = (n / rho) ** (1.0 / 3.0)
-        els = list(specs[slot].elements)
-        cfg = synth.random_config(n, np.diag([L, L, L]), els, 1.0, seed=int(rng.integers(1 << 31)))
-        reqs.append((slot, cfg))
-    return specs, reqs
+        slots.append(slot)
+        jobs.append((n, L, list(specs[slot].elements), int(rng.integers(1 << 31))))
+    cfgs = synth.generate_configs(jobs, processes)
+    return specs, list(zip(slots, cfgs))
 
 
 def poisson_run(server: Server, requests: Sequence[Tuple[int, object]], type_idx, rate_hz: float,

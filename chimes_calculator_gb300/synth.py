@@ -391,6 +391,81 @@ def random_config(n_atoms: int, cell, elements: Sequence[str], rmin: float, seed
     return Config([elements[i] for i in tidx], pos, cell)
 
 
+def random_config_batched(n_atoms: int, cell, elements: Sequence[str], rmin: float, seed: int,
+                          batch: Optional[int] = None, max_rounds: int = 100000) -> Config:
+    """Random insertion with rejection, vectorised: candidates (uniform
+    fractional coordinates) are drawn ``batch`` at a time; a candidate is kept
+    when its minimum-image distance to every accepted atom and to every earlier
+    candidate of its batch is at least ``rmin``.  Every pair of the result is
+    at least ``rmin`` apart, as with ``random_config``; the random stream
+    differs.  Used for the many few-thousand-atom configurations of the
+    batched and serving workloads, where the one-candidate-at-a-time loop
+    dominates the set-up time.  The default batch, sqrt(2 V / v) with v the
+    volume of an ``rmin`` sphere, keeps conflicts inside a batch to about
+    one."""
+    rng = np.random.default_rng(seed)
+    cell = np.asarray(cell, dtype=np.float64).reshape(3, 3)
+    if batch is None:
+        vol = abs(float(np.linalg.det(cell)))
+        batch = int(min(256, max(4, math.sqrt(2.0 * vol / (4.18879 * rmin ** 3)))))
+    frac = np.zeros((n_atoms, 3))
+    n = 0
+    r2 = rmin * rmin
+    # orthorhombic cells of at least three rmin-sized bins per axis: accepted
+    # atoms are kept in a bin grid (up to K per bin) and a candidate is tested
+    # against the 27 bins around its own; otherwise against every accepted atom
+    lengths = np.diag(cell)
+    ortho = np.allclose(cell - np.diag(lengths), 0.0)
+    m = (lengths // rmin).astype(int) if ortho else np.zeros(3, dtype=int)
+    use_grid = ortho and bool(np.all(m >= 3))
+    K = 4
+    if use_grid:
+        grid = np.full((m[0], m[1], m[2], K, 3), 10.0)       # empty slots sit far outside the cell
+        fill = np.zeros((m[0], m[1], m[2]), dtype=int)
+        offs = np.array([[a, b, c] for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
+    for _ in range(max_rounds):
+        if n >= n_atoms:
+            break
+        cand = rng.random((batch, 3))
+        ok = np.ones(batch, dtype=bool)
+        if use_grid and n:
+            cb = (cand * m).astype(int) % m
+            nb = (cb[:, None, :] + offs[None, :, :]) % m                       # (B, 27, 3)
+            other = grid[nb[..., 0], nb[..., 1], nb[..., 2]]                   # (B, 27, K, 3)
+            df = other - cand[:, None, None, :]
+            df -= np.round(df)
+            ok &= (((df * lengths) ** 2).sum(axis=3) >= r2).all(axis=(1, 2))
+        elif n:
+            for a in range(0, n, 2048):
+                df = cand[:, None, :] - frac[None, a:min(n, a + 2048), :]
+                df -= np.round(df)
+                ok &= (np.einsum("ijk,kl->ijl", df, cell) ** 2).sum(axis=2).min(axis=1) >= r2
+        df = cand[:, None, :] - cand[None, :, :]
+        df -= np.round(df)
+        close = np.triu((np.einsum("ijk,kl->ijl", df, cell) ** 2).sum(axis=2) < r2, k=1)
+        ok &= ~close.any(axis=0)           # no earlier candidate of the batch within rmin
+        c = cand[ok][:n_atoms - n]
+        if use_grid and len(c):
+            cb = (c * m).astype(int) % m
+            lin = (cb[:, 0] * m[1] + cb[:, 1]) * m[2] + cb[:, 2]
+            order = np.argsort(lin, kind="stable")
+            lin, c = lin[order], c[order]
+            first = np.r_[True, lin[1:] != lin[:-1]]
+            rank = np.arange(len(lin)) - np.maximum.accumulate(np.where(first, np.arange(len(lin)), 0))
+            slot = fill.reshape(-1)[lin] + rank
+            keep = slot < K                # a full bin drops the candidate (never at these densities)
+            lin, slot, c = lin[keep], slot[keep], c[keep]
+            grid.reshape(-1, K, 3)[lin, slot] = c
+            np.add.at(fill.reshape(-1), lin, 1)
+        frac[n:n + len(c)] = c
+        n += len(c)
+    if n < n_atoms:
+        raise RuntimeError("random_config_batched: packing too dense")
+    pos = frac @ cell
+    tidx = rng.choice(len(elements), size=n_atoms)
+    return Config([elements[i] for i in tidx], pos, cell)
+
+
 # ----------------------------------------------------------------------------
 # The named workloads (seed = 1000 + workload number)
 # ----------------------------------------------------------------------------
@@ -432,19 +507,34 @@ def spec_c4() -> ParamSpec:
     return spec_c2(elements=("C", "N", "O"), orders=(12, 10, 4), seed=1004)
 
 
-def configs_c4(n_configs=4096, seed=1104, n_min=8, n_max=512) -> List[Config]:
+def _gen_config(args):
+    n, L, elements, seed = args
+    return random_config_batched(n, np.diag([L, L, L]), elements, 1.0, seed=seed)
+
+
+def generate_configs(jobs, processes: int = 0) -> List[Config]:
+    """Configurations for (n_atoms, box side, elements, seed) jobs, in a pool
+    of ``processes`` spawned workers when that is above 1 (each job has its
+    own seed, so the result does not depend on the pool)."""
+    if processes and processes > 1 and len(jobs) > 64:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(processes) as pool:
+            return pool.map(_gen_config, jobs, chunksize=max(1, len(jobs) // (8 * processes)))
+    return [_gen_config(j) for j in jobs]
+
+
+def configs_c4(n_configs=4096, seed=1104, n_min=8, n_max=512, processes: int = 0) -> List[Config]:
     """Atom counts log-uniform in [n_min, n_max], densities U(0.05, 0.12) per
     cubic Angstrom, 1-3 elements per configuration."""
     rng = np.random.default_rng(seed)
-    out = []
+    jobs = []
     for c in range(n_configs):
         n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
         rho = rng.uniform(0.05, 0.12)
         L = (n / rho) ** (1.0 / 3.0)
         ne = int(rng.integers(1, 4))
-        out.append(random_config(n, np.diag([L, L, L]), list(ELEMENTS[:ne]), 1.0,
-                                 seed=int(rng.integers(1 << 31))))
-    return out
+        jobs.append((n, L, list(ELEMENTS[:ne]), int(rng.integers(1 << 31))))
+    return generate_configs(jobs, processes)
 
 
 def specs_c5() -> List[ParamSpec]:

@@ -189,6 +189,14 @@ long long ck_server_submit(void *server, int slot, int natom, const double *pos,
  * status if the request failed (released; message in ck_last_error). */
 int ck_server_take(void *server, long long id, int wait, double timeout_s, double *energy, double *force,
                    double *stress, double *latency_s);
+/* Tunes the contraction kernels of every worker on a representative batch
+ * (arrays as for ck_calculate_batch; small and pset may be NULL): worker 0
+ * times the contraction forms and launch shapes on it and every worker takes
+ * its choices.  Call it after loading the parameter sets and before
+ * submitting requests.  chosen[3] (may be NULL) = lanes per 3-body and
+ * 4-body cluster, resident blocks per SM. */
+int ck_server_autotune(void *server, int nsys, const int *natoms, const double *pos, const int *types,
+                       const double *cells, const int *small, const int *pset, int *chosen);
 /* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
 int ck_server_stats(void *server, long long *out);
 

@@ -22,7 +22,21 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libchimes_oracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
-REFROOT = "/root/reference"
+
+
+def _default_refroot() -> str:
+    """The reference checkout: $CHIMES_REFERENCE_ROOT, else the Makefile's REFROOT default."""
+    env = os.environ.get("CHIMES_REFERENCE_ROOT")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for ln in f:
+            if ln.startswith("REFROOT") and "?=" in ln:
+                return ln.split("?=", 1)[1].strip()
+    return ""
+
+
+REFROOT = _default_refroot()
 
 _lib = None
 

@@ -9,16 +9,34 @@ digits together with the sizes and SHA-256 digests of its cluster lists
 (neighlist_2b/3b/4b in the reference's order).  The GPU tests compare against
 these files; the reference itself is not needed where the tests run.
 
-Run from the repository root where the reference sources are available:
+Besides the small seeded cases it writes:
+  * the 12/10/4 recipe of the large workloads: a cut-down 3072-atom box of the
+    32768-atom two-element configuration at the same density (``c3_cut``), the
+    full 32768-atom configuration (``c3_full``: energy, stress, list digests,
+    every 16th atom's force and force sums; the configuration is regenerated
+    from its seed and checked by digest), four three-element configurations
+    of the batched workload's extremes (8 and 512 atoms at 0.05 and 0.12
+    atoms/A^3) and each of the serving workload's three parameter sets on one
+    configuration;
+  * the reference's own regression inputs (serial_interface/tests: HN3
+    2+3+4-body with SPECIAL cutoffs and energy offsets, CO2400K with
+    replication, the rotated TiO2 cell, CHON), with the reference's parameter
+    files stored gzipped and its configurations verbatim (``ref_*``).
+
+Run from the repository root where the reference sources are available
+(REFROOT, default the reference checkout the oracle's Makefile uses):
     python tests/golden/make_golden.py [case ...]
 """
 
 from __future__ import annotations
 
+import gzip
 import hashlib
 import json
 import os
+import shutil
 import sys
+import tempfile
 
 import numpy as np
 
@@ -119,35 +137,127 @@ def cases():
     return C
 
 
+C3_DENSITY = 32768 / (70.0 * 70.0 * 72.0)
+# atoms kept for the full-size case's force comparison: every FORCE_STRIDE-th
+FORCE_STRIDE = 16
+
+
+def cycled(cfg, elements):
+    """Types assigned cyclically so every element (and most type tuples) occurs."""
+    return synth.Config([elements[i % len(elements)] for i in range(cfg.n_atoms)], cfg.pos, cfg.cell)
+
+
+def recipe_cases():
+    """The 12/10/4 parameter recipe of the full-size, batched and serving
+    workloads: name -> (ParamSpec, Config, small, extra)."""
+    C = {}
+    n = 3072
+    L = (n / C3_DENSITY / (72.0 / 70.0)) ** (1.0 / 3.0)
+    C["c3_cut"] = (synth.spec_c3(), synth.config_c3(n_atoms=n, box=(L, L, L * 72.0 / 70.0), seed=3103), False, {})
+    C["c3_full"] = (synth.spec_c3(), synth.config_c3(), False,
+                    {"large": True, "params_from": "c3_cut", "config_from": "config_c3"})
+    spec4 = synth.spec_c4()
+    for k, (n, rho) in enumerate(((8, 0.05), (8, 0.12), (512, 0.05), (512, 0.12))):
+        L = (n / rho) ** (1.0 / 3.0)
+        cfg = synth.random_config(n, np.diag([L, L, L]), ["C", "N", "O"], 1.0, seed=3400 + k)
+        C["c4_n%d_rho%03d" % (n, int(round(rho * 100)))] = (spec4, cycled(cfg, ["C", "N", "O"]), False, {})
+    for k, spec in enumerate(synth.specs_c5()):
+        n = (96, 300, 240)[k]
+        L = (n / 0.09) ** (1.0 / 3.0)
+        cfg = synth.random_config(n, np.diag([L, L * 1.05, L * 0.95]), spec.elements, 1.0, seed=3500 + k)
+        C["c5_set%d" % k] = (spec, cycled(cfg, list(spec.elements)), False, {})
+    return C
+
+
+# the reference's own regression inputs (serial_interface/tests/test_list.dat)
+REF_FIELDS = {
+    "ref_hn3": ("published_params.HN3.2+3+4b.Tersoff.special.offsets.txt", "HN3.2gcc_3000K.OUTCAR_#000.xyz", False),
+    "ref_co2400k": ("published_params.CO2400K.2+3+4b.Tersoff.special.offsets.txt", "CO.9GPa_2400K.OUTCAR_#000.xyz",
+                    True),
+    "ref_tio2_arbrot": ("validated_params.TiO2.2+3b.Tersoff.txt", "TiO2.unitcell_arbrot_#000.xyz", False),
+    "ref_chon": ("test_params.CHON.txt", "CHON.testfile_#000.xyz", False),
+}
+
+
+def write_expected(d, name, small, res, lst, timing, n_atoms, extra):
+    out = {
+        "case": name,
+        "small": bool(small),
+        "n_atoms": n_atoms,
+        "energy": repr(res["energy"]),
+        "stress": [repr(float(v)) for v in res["stress"]],
+        "lists": lists_digest(*lst),
+        "reference_seconds": timing["best_s"],
+    }
+    F = np.asarray(res["force"])
+    if extra.get("large"):
+        idx = np.arange(0, n_atoms, FORCE_STRIDE)
+        out["force_index"] = {"start": 0, "stride": FORCE_STRIDE}
+        out["force"] = [[repr(float(v)) for v in row] for row in F[idx]]
+        out["force_sum"] = [repr(float(v)) for v in F.sum(axis=0)]
+        out["force_sumsq"] = repr(float((F * F).sum()))
+    else:
+        out["force"] = [[repr(float(v)) for v in row] for row in F]
+    for k in ("large", "params_from", "config_from", "config_sha256", "source"):
+        if k in extra:
+            out[k] = extra[k]
+    with open(os.path.join(d, "expected.json"), "w") as f:
+        json.dump(out, f, indent=0)
+    print(name, n_atoms, "E=%.10f" % res["energy"], {k: v["n"] for k, v in out["lists"].items()},
+          "%.3fs" % timing["best_s"])
+
+
+def gzip_copy(src, dst):
+    """Deterministic gzip (no name, fixed mtime) so regenerating leaves git clean."""
+    with open(src, "rb") as f:
+        data = f.read()
+    with open(dst, "wb") as raw:
+        with gzip.GzipFile(filename="", mode="wb", fileobj=raw, mtime=0, compresslevel=9) as g:
+            g.write(data)
+
+
 def main(names):
     C = cases()
-    names = names or list(C)
+    R = recipe_cases()
+    names = names or (list(C) + list(R) + list(REF_FIELDS))
     if oracle.build_reference() is None:
         raise SystemExit("reference sources unavailable: cannot generate golden fixtures")
-    for name in names:
-        spec, cfg, small = C[name]
-        d = os.path.join(HERE, name)
-        os.makedirs(d, exist_ok=True)
-        pfile = synth.write_param_file(os.path.join(d, "params.txt"), spec)
-        xfile = cfg.write_xyz(os.path.join(d, "config.xyz"))
-        res, lst, timing = oracle.run_reference(pfile, xfile, small, os.path.join(REPO, "_work", "golden_" + name),
-                                                lists=True, time_reps=1)
-        out = {
-            "case": name,
-            "small": bool(small),
-            "n_atoms": cfg.n_atoms,
-            "energy": repr(res["energy"]),
-            "stress": [repr(float(v)) for v in res["stress"]],
-            "force": [[repr(float(v)) for v in row] for row in res["force"]],
-            "lists": lists_digest(*lst),
-            "reference_seconds": timing["best_s"],
-        }
-        with open(os.path.join(d, "expected.json"), "w") as f:
-            json.dump(out, f, indent=0)
-        print(name, cfg.n_atoms, "E=%.10f" % res["energy"], {k: v["n"] for k, v in out["lists"].items()},
-              "%.3fs" % timing["best_s"])
+    with tempfile.TemporaryDirectory() as scratch:
+        for name in names:
+            d = os.path.join(HERE, name)
+            os.makedirs(d, exist_ok=True)
+            extra = {}
+            if name in REF_FIELDS:
+                ff, xyz, small = REF_FIELDS[name]
+                base = os.path.join(oracle.REFROOT, "serial_interface", "tests")
+                pfile = os.path.join(scratch, name + ".params.txt")
+                shutil.copyfile(os.path.join(base, "force_fields", ff), pfile)
+                gzip_copy(pfile, os.path.join(d, "params.txt.gz"))
+                xfile = os.path.join(d, "config.xyz")
+                shutil.copyfile(os.path.join(base, "configurations", xyz), xfile)
+                n_atoms = synth.read_xyz(xfile).n_atoms
+                extra["source"] = "serial_interface/tests: force_fields/%s, configurations/%s" % (ff, xyz)
+            else:
+                spec, cfg, small = C[name] if name in C else R[name][:3]
+                extra = {} if name in C else dict(R[name][3])
+                n_atoms = cfg.n_atoms
+                if "params_from" in extra:
+                    pfile = os.path.join(HERE, extra["params_from"], "params.txt")
+                else:
+                    pfile = synth.write_param_file(os.path.join(d, "params.txt"), spec)
+                if "config_from" in extra:
+                    # too large to commit: regenerated from its seed, pinned by digest
+                    text = cfg.xyz_text()
+                    extra["config_sha256"] = hashlib.sha256(text.encode()).hexdigest()
+                    xfile = os.path.join(scratch, name + ".xyz")
+                    with open(xfile, "w") as f:
+                        f.write(text)
+                else:
+                    xfile = cfg.write_xyz(os.path.join(d, "config.xyz"))
+            res, lst, timing = oracle.run_reference(pfile, xfile, small, os.path.join(scratch, name),
+                                                    lists=True, time_reps=1)
+            write_expected(d, name, small, res, lst, timing, n_atoms, extra)
 
 
 if __name__ == "__main__":
-    os.makedirs(os.path.join(REPO, "_work"), exist_ok=True)
     main(sys.argv[1:])

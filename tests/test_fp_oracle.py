@@ -13,8 +13,9 @@ import pytest
 
 from chimes_calculator_gb300 import fingerprint as fp
 from chimes_calculator_gb300 import synth
+from oracle.oracle import REFROOT
 
-EX = "/root/reference/etc/lmp/tests/example-fingerprint"
+EX = os.path.join(REFROOT, "etc", "lmp", "tests", "example-fingerprint")
 
 
 def read_lammps_data(path):

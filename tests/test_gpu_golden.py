@@ -6,8 +6,8 @@ within its error budget."""
 import numpy as np
 import pytest
 
-from conftest import (E_REL_TOL, F_ABS_TOL, MIXED_E_REL_TOL, MIXED_F_ABS_TOL, S_ABS_TOL, golden_names,
-                      list_digest)
+from conftest import (E_REL_TOL, F_ABS_TOL, MIXED_E_REL_TOL, MIXED_F_ABS_TOL, MIXED_S_ABS_TOL, S_ABS_TOL,
+                      golden_names, list_digest, mixed_force_tol)
 
 pytestmark = pytest.mark.gpu
 
@@ -29,7 +29,7 @@ def test_fp64_matches_reference(golden, native_lib, name, factored):
     g = golden[name]
     c, r = evaluate(g, factored=factored)
     assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
-    assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+    assert g.force_error(r["force"]) <= F_ABS_TOL
     assert np.abs(r["stress"] - g.stress).max() <= S_ABS_TOL
     l2, l3, l4 = c.lists()
     for key, arr in (("l2", l2), ("l3", l3), ("l4", l4)):
@@ -37,7 +37,7 @@ def test_fp64_matches_reference(golden, native_lib, name, factored):
         assert list_digest(arr) == g.lists[key]["sha256"], key
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names(large=False))
 def test_lists_match_oracle(golden, native_lib, name):
     from oracle.oracle import Oracle
     g = golden[name]
@@ -51,11 +51,15 @@ def test_lists_match_oracle(golden, native_lib, name):
 @pytest.mark.parametrize("factored", [1, 2, 3, 0], ids=["factored", "factored_nocache", "factored_noy", "per_coef"])
 @pytest.mark.parametrize("name", golden_names())
 def test_mixed_precision_error(golden, native_lib, name, factored):
+    """The mixed form against the reference's own FP64 results (the values
+    stored in the fixture), not against the GPU's FP64 path: energy 1e-6
+    relative, forces 1e-5 absolute (5e-6 of the largest force for the fitted
+    force fields, whose forces reach hundreds of kcal/mol/A), stress 1e-5."""
     g = golden[name]
-    _, r64 = evaluate(g, precision=0, factored=factored)
     _, r32 = evaluate(g, precision=1, factored=factored)
-    assert abs(r32["energy"] - r64["energy"]) <= MIXED_E_REL_TOL * max(1.0, abs(r64["energy"]))
-    assert np.abs(r32["force"] - r64["force"]).max() <= MIXED_F_ABS_TOL
+    assert abs(r32["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy))
+    assert g.force_error(r32["force"]) <= mixed_force_tol(np.abs(g.force).max())
+    assert np.abs(r32["stress"] - g.stress).max() <= MIXED_S_ABS_TOL
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])

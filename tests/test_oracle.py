@@ -10,12 +10,11 @@ import pytest
 
 from conftest import golden_names, list_digest
 
-from oracle.oracle import Oracle
-
-REFROOT = "/root/reference"
+from oracle.oracle import REFROOT, Oracle
 
 
-@pytest.mark.parametrize("name", golden_names())
+
+@pytest.mark.parametrize("name", golden_names(large=False))
 def test_oracle_matches_reference_golden(golden, name):
     g = golden[name]
     o = Oracle(g.params)

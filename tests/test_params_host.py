@@ -8,8 +8,9 @@ import os
 import pytest
 
 from chimes_calculator_gb300 import synth
+from oracle.oracle import REFROOT
 
-REFFF = "/root/reference/serial_interface/tests/force_fields"
+REFFF = os.path.join(REFROOT, "serial_interface", "tests", "force_fields")
 
 
 def check(lib, path):

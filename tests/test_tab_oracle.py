@@ -15,13 +15,14 @@ import numpy as np
 import pytest
 
 from chimes_calculator_gb300 import synth
+from oracle.oracle import REFROOT
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden", "tabulated")
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_tab_golden as mtg  # noqa: E402
 
-REF_EXAMPLE = "/root/reference/etc/lmp/tests/example-tabulate"
+REF_EXAMPLE = os.path.join(REFROOT, "etc", "lmp", "tests", "example-tabulate")
 
 
 def _queries():
