@@ -160,7 +160,8 @@ def recipe_cases():
     for k, (n, rho) in enumerate(((8, 0.05), (8, 0.12), (512, 0.05), (512, 0.12))):
         L = (n / rho) ** (1.0 / 3.0)
         cfg = synth.random_config(n, np.diag([L, L, L]), ["C", "N", "O"], 1.0, seed=3400 + k)
-        C["c4_n%d_rho%03d" % (n, int(round(rho * 100)))] = (spec4, cycled(cfg, ["C", "N", "O"]), False, {})
+        C["c4_n%d_rho%03d" % (n, int(round(rho * 100)))] = (spec4, cycled(cfg, ["C", "N", "O"]), False,
+                                                             {} if k == 0 else {"params_from": "c4_n8_rho005"})
     for k, spec in enumerate(synth.specs_c5()):
         n = (96, 300, 240)[k]
         L = (n / 0.09) ** (1.0 / 3.0)
