@@ -14,6 +14,12 @@ value : atom-evaluations/s with the inputs resident in HBM, CUDA events on
         before every step;
 e2e   : the same metric through the reference-facing C ABI
         (calculate_chimes_instance) with host arrays, timed on the host.
+the benchmark spec (default, one GPU): the batched mixed-size workload in FP64 and
+        mixed against the plain FP64 path one configuration per call, the
+        serving loop (p50/p99 latency at three offered rates) against the
+        plain path one request at a time, and the mixed form's error against
+        the reference's FP64 results in the committed fixtures; about a
+        minute (--no-north-star skips it).
 Under torchrun each rank runs an independent replica (weak scaling; the path
 has no exchange step, so there is no collective on the data path).
 
@@ -400,14 +406,10 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "check": check,
         }
+        if world == 1 and not args.no_north_star and not args.profile_run:
+            line["north_star"] = north_star(args)
         if args.extras:
-            ex = extras(args)
-            # the benchmark spec target: batched mixed vs the plain FP64 path on the mixed-size workload
-            ex["batched_mixed_over_plain_fp64"] = ex["batched_mixed"]["value"] / ex["plain_fp64_per_config"]["value"]
-            ex["batched_mixed_e2e_over_plain_fp64"] = (ex["batched_mixed"]["e2e_value"] /
-                                                       ex["plain_fp64_per_config"]["value"])
-            ex["batched_mixed_over_c2_plain_fp64"] = ex["batched_mixed"]["value"] / (value / world)
-            line["extras"] = ex
+            line["extras"] = extras(args)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -428,39 +430,6 @@ def extras(args):
         c.autotune()
         out[name] = time_steps(c, N_ATOMS, 50)
         out[name]["autotuned"] = c.tuning()
-    p4 = synth.write_param_file(os.path.join(tmp, "c4.params"), synth.spec_c4())
-    cfgs = synth.configs_c4(n_configs=args.batch_configs)
-    atoms = sum(c.n_atoms for c in cfgs)
-    for prec, name in ((FP64, "batched_fp64"), (MIXED, "batched_mixed")):
-        c = Calculator(precision=prec, graph=True)
-        c.load_params(p4)
-        c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
-        c.autotune()
-        r = time_steps(c, atoms, 3)
-        r["configs"] = len(cfgs)
-        r["autotuned"] = c.tuning()
-        # end to end: pack + host->device + launches + device->host of the whole batch
-        confs = [(x.pos, x.types, x.cell) for x in cfgs]
-        c.evaluate_batch(confs)
-        t0 = time.perf_counter()
-        c.evaluate_batch(confs)
-        r["e2e_value"] = atoms / (time.perf_counter() - t0)
-        out[name] = r
-    # the plain FP64 path on the same mixed-size workload: one configuration per
-    # call (host buffers in and out, graph replay per shape), as a caller without
-    # batching would run it
-    c = Calculator(precision=FP64, graph=True)
-    c.load_params(p4)
-    sample = cfgs[: min(len(cfgs), args.plain_configs)]
-    for x in sample[:8]:
-        c.evaluate(x.pos, x.types, x.cell)
-    t0 = time.perf_counter()
-    for x in sample:
-        c.evaluate(x.pos, x.types, x.cell)
-    wall = time.perf_counter() - t0
-    sa = sum(x.n_atoms for x in sample)
-    out["plain_fp64_per_config"] = {"value": sa / wall, "unit": UNIT, "configs": len(sample), "atoms": sa,
-                                    "ms_per_config": 1e3 * wall / len(sample)}
     # one large configuration (32768 atoms, 70 x 70 x 72 A, ChIMES 12/10/4),
     # FP64 and mixed, with the mixed result's error against FP64
     p3 = synth.write_param_file(os.path.join(tmp, "c3.params"), synth.spec_c3())
@@ -486,7 +455,145 @@ def extras(args):
     ptab = synth.write_tabulated_param_file(os.path.join(tmp, "c2tab.params"), synth.spec_c2(), step3=0.1)
     out["pair_style_c2_tabulated"] = pair_style(ptab, cfg, cpu_calls=1)
     out["fingerprint_c2"] = fingerprint(params, cfg)
+    return out
+
+
+def gen_processes():
+    return max(1, min(8, os.cpu_count() or 1))
+
+
+def north_star(args):
+    """The comparisons the path is built for, on bounded samples of their
+    workloads (seeded synthetic configurations):
+      batched : the 4096-configuration mixed-size workload (8-512 atoms,
+                0.05-0.12 atoms/A^3, 1-3 elements, ChIMES 12/10/4) in one
+                autotuned launch sequence (CUDA graph), FP64 and mixed; device
+                throughput with the inputs resident and end to end through
+                ck_calculate_batch with host arrays;
+      plain   : the plain FP64 path on the same configurations, one per call
+                through the C ABI with host arrays, as a caller without
+                batching runs it;
+      serving : single-point requests of 16-4096 atoms over three parameter
+                sets, Poisson arrivals; the plain FP64 path one request at a
+                time, then the continuous-batching server (mixed; FP64 at
+                saturation) at offered rates of 1x and 4x the plain path's
+                request rate and at saturation, with p50/p99 latency;
+      error   : the mixed form against the reference's FP64 results stored in
+                the fixtures (the full 32768-atom 12/10/4 configuration, the
+                batched workload's extremes, the serving sets and the
+                reference's own force fields)."""
+    from chimes_calculator_gb300 import FP64, MIXED, Calculator, synth
+    out = {}
+    tmp = tempfile.mkdtemp(prefix="ckns")
+    t_all = time.perf_counter()
+    # -- batched vs plain on the mixed-size workload --------------------------
+    p4 = synth.write_param_file(os.path.join(tmp, "c4.params"), synth.spec_c4())
+    cfgs = synth.configs_c4(n_configs=args.batch_configs, processes=gen_processes())
+    atoms = sum(c.n_atoms for c in cfgs)
+    batched = {"workload": "%d configurations, 8-512 atoms log-uniform, 0.05-0.12 atoms/A^3, 1-3 elements, "
+                           "ChIMES 12/10/4 (3 elements)" % len(cfgs), "atoms": atoms}
+    confs = [(x.pos, x.types, x.cell) for x in cfgs]
+    for prec, name in ((FP64, "fp64"), (MIXED, "mixed")):
+        c = Calculator(precision=prec, graph=True)
+        c.load_params(p4)
+        c.stage(c.pack(confs))
+        c.autotune()
+        r = time_steps(c, atoms, 3)
+        r["autotuned"] = c.tuning()
+        c.evaluate_batch(confs)
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            c.evaluate_batch(confs)
+            ts.append(time.perf_counter() - t0)
+        r["e2e"] = {"value": atoms / min(ts), "unit": UNIT, "api": "ck_calculate_batch (host arrays)",
+                    "h2d_bytes": atoms * 28 + len(cfgs) * 100, "d2h_bytes": atoms * 24 + len(cfgs) * 80}
+        batched[name] = r
+        c.close()
+    c = Calculator(precision=FP64, graph=True)
+    c.load_params(p4)
+    sample = cfgs[: min(len(cfgs), args.plain_configs)]
+    for x in sample[:8]:
+        c.evaluate(x.pos, x.types, x.cell)
+    t0 = time.perf_counter()
+    for x in sample:
+        c.evaluate(x.pos, x.types, x.cell)
+    wall = time.perf_counter() - t0
+    sa = sum(x.n_atoms for x in sample)
+    c.close()
+    plain = {"value": sa / wall, "unit": UNIT, "configs": len(sample), "atoms": sa,
+             "ms_per_config": 1e3 * wall / len(sample), "api": "ck_calculate_batch with one configuration per call"}
+    batched["plain_fp64_per_config"] = plain
+    batched["ratio_mixed_over_plain_fp64"] = batched["mixed"]["value"] / plain["value"]
+    batched["ratio_mixed_e2e_over_plain_fp64"] = batched["mixed"]["e2e"]["value"] / plain["value"]
+    batched["ratio_fp64_over_plain_fp64"] = batched["fp64"]["value"] / plain["value"]
+    out["batched"] = batched
+    # -- serving --------------------------------------------------------------
     out["serving"] = serving(args)
+    # -- error of the mixed form against the reference ------------------------
+    out["error_vs_reference"] = mixed_error_vs_fixtures()
+    out["wall_s"] = time.perf_counter() - t_all
+    return out
+
+
+def _golden(name):
+    """(params path, Config, small, expected dict, force row index or None) of a committed fixture."""
+    import gzip
+    import hashlib
+    from chimes_calculator_gb300 import synth
+    d = os.path.join(REPO, "tests", "golden", name)
+    e = json.load(open(os.path.join(d, "expected.json")))
+    if "params_from" in e:
+        params = os.path.join(REPO, "tests", "golden", e["params_from"], "params.txt")
+    elif os.path.exists(os.path.join(d, "params.txt")):
+        params = os.path.join(d, "params.txt")
+    else:
+        params = os.path.join(tempfile.mkdtemp(prefix="ckg"), "params.txt")
+        with gzip.open(os.path.join(d, "params.txt.gz"), "rb") as f, open(params, "wb") as g:
+            g.write(f.read())
+    if "config_from" in e:
+        cfg = getattr(synth, e["config_from"])()
+        if hashlib.sha256(cfg.xyz_text().encode()).hexdigest() != e["config_sha256"]:
+            raise RuntimeError("%s: regenerated configuration differs from the reference's" % name)
+        cfg = synth.read_xyz(cfg.write_xyz(os.path.join(tempfile.mkdtemp(prefix="ckg"), "c.xyz")))
+    else:
+        cfg = synth.read_xyz(os.path.join(d, "config.xyz"))
+    idx = None
+    if "force_index" in e:
+        idx = np.arange(e["force_index"]["start"], cfg.n_atoms, e["force_index"]["stride"])
+    return params, cfg, e["small"], e, idx
+
+
+def mixed_error_vs_fixtures():
+    """Mixed form vs the reference's FP64 values in the committed fixtures:
+    relative energy, max-abs force (over the stored rows) and stress."""
+    from chimes_calculator_gb300 import MIXED, Calculator
+    groups = {"full_size_32768_atoms_12_10_4": ["c3_full"],
+              "batched_workload_extremes_12_10_4": ["c4_n8_rho005", "c4_n8_rho012", "c4_n512_rho005",
+                                                    "c4_n512_rho012"],
+              "serving_parameter_sets": ["c5_set0", "c5_set1", "c5_set2"],
+              "reference_force_fields": ["ref_hn3", "ref_co2400k", "ref_tio2_arbrot", "ref_chon"]}
+    out = {}
+    for gname, names in groups.items():
+        er = {"energy_rel": 0.0, "force_max_abs": 0.0, "force_max_rel_to_largest": 0.0, "stress_max_abs": 0.0,
+              "cases": names}
+        for n in names:
+            params, cfg, small, e, idx = _golden(n)
+            c = Calculator(precision=MIXED)
+            c.load_params(params)
+            r = c.evaluate(cfg.pos, cfg.types, cfg.cell, small=small)
+            c.close()
+            ref_f = np.array([[float(v) for v in row] for row in e["force"]])
+            got_f = r["force"] if idx is None else r["force"][idx]
+            ref_e = float(e["energy"])
+            fe = float(np.abs(got_f - ref_f).max())
+            er["energy_rel"] = max(er["energy_rel"], abs(r["energy"] - ref_e) / max(1.0, abs(ref_e)))
+            er["force_max_abs"] = max(er["force_max_abs"], fe)
+            er["force_max_rel_to_largest"] = max(er["force_max_rel_to_largest"],
+                                                 fe / max(1.0, float(np.abs(ref_f).max())))
+            er["stress_max_abs"] = max(er["stress_max_abs"], float(np.abs(
+                r["stress"] - np.array([float(v) for v in e["stress"]])).max()))
+        out[gname] = er
     return out
 
 
@@ -615,35 +722,51 @@ def profile_direct(args, reps=5):
 
 def serving(args):
     """Continuous batching of single-point requests (three parameter sets,
-    16-4096 atoms log-uniform): Poisson arrivals at multiples of the plain
-    one-at-a-time path's request rate, p50/p99 latency and throughput, beside
-    the plain path itself."""
+    16-4096 atoms log-uniform): the plain FP64 path one request at a time,
+    then the server (tuned once on a sample of the requests) with Poisson
+    arrivals at 1x and 4x the plain path's request rate and at saturation;
+    p50/p99 latency and throughput per rate."""
     from chimes_calculator_gb300 import Calculator, synth
     from chimes_calculator_gb300.serving import Server, poisson_run, serial_run, serving_workload
     tmp = tempfile.mkdtemp(prefix="cks")
-    specs, reqs = serving_workload(args.serve_requests)
+    specs, reqs = serving_workload(args.serve_requests, processes=gen_processes())
     paths = [synth.write_param_file(os.path.join(tmp, "p%d.txt" % k), sp) for k, sp in enumerate(specs)]
     calc = Calculator(graph=False)
     for p in paths:
         calc.load_params(p)
     tidx = lambda slot, cfg: calc.type_indices(cfg.types, slot)
-    serial_run(calc, reqs[:20], tidx)                      # warm-up
+    serial_run(calc, reqs[:50], tidx)                      # warm-up
     base = serial_run(calc, reqs, tidx)
-    out = {"requests": len(reqs), "atoms": int(sum(c.n_atoms for _, c in reqs)), "serial_fp64": base}
-    for prec, name in ((0, "fp64"), (1, "mixed")):
-        srv = Server(workers=args.serve_workers, precision=prec, max_batch_atoms=1 << 15)
+    out = {"workload": "%d requests, 16-4096 atoms log-uniform, 0.05-0.12 atoms/A^3, parameter sets 12/8/4 "
+                       "(1 element), 12/10/4 (2), 12/8/4 (3)" % len(reqs),
+           "requests": len(reqs), "atoms": int(sum(c.n_atoms for _, c in reqs)),
+           "workers": args.serve_workers, "max_batch_atoms": args.serve_batch_atoms,
+           "plain_fp64_per_request": base}
+    for prec, name, mults in ((1, "mixed", (1.0, 4.0, 1e3)), (0, "fp64", (1e3,))):
+        srv = Server(workers=args.serve_workers, precision=prec, max_batch_atoms=args.serve_batch_atoms)
         for p in paths:
             srv.load_params(p)
+        sample, na = [], 0
+        for slot, cf in reqs:
+            if na + cf.n_atoms > args.serve_batch_atoms:
+                break
+            sample.append((slot, cf))
+            na += cf.n_atoms
+        tuned = srv.autotune([(cf.pos, tidx(sl, cf), cf.cell) for sl, cf in sample], [sl for sl, _ in sample])
         # warm-up: every request once, back to back, so the workspaces and
         # list capacities reach their steady-state sizes before the timed sweeps
         poisson_run(srv, reqs, tidx, rate_hz=1e6)
         runs = []
-        for mult in (0.5, 1.0, 2.0, 8.0, 1e3):
+        for mult in mults:
             r = poisson_run(srv, reqs, tidx, rate_hz=mult * base["throughput_req_per_s"])
-            r["offered_over_serial"] = mult
+            r["offered_over_plain"] = mult if mult < 1e3 else "saturation"
             runs.append(r)
         srv.close()
-        out["server_" + name] = runs
+        out["server_" + name] = {"autotuned": tuned, "runs": runs}
+    sat = out["server_mixed"]["runs"][-1]["throughput_atoms_per_s"]
+    out["ratio_server_mixed_over_plain_fp64"] = sat / base["throughput_atoms_per_s"]
+    out["ratio_server_fp64_over_plain_fp64"] = (out["server_fp64"]["runs"][-1]["throughput_atoms_per_s"] /
+                                                base["throughput_atoms_per_s"])
     return out
 
 
@@ -804,11 +927,16 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--extras", action="store_true", help="also time the mixed, batched and serving paths")
-    ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-workers", type=int, default=2)
+    ap.add_argument("--extras", action="store_true",
+                    help="also time the mixed form on C2, the 32768-atom configuration, the pair-style path "
+                         "and the fingerprint pipeline")
+    ap.add_argument("--no-north-star", action="store_true",
+                    help="skip the batched / plain / serving / error block of the default line")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-batch-atoms", type=int, default=16384)
     ap.add_argument("--batch-configs", type=int, default=4096)
-    ap.add_argument("--plain-configs", type=int, default=4096,
+    ap.add_argument("--plain-configs", type=int, default=1024,
                     help="configurations of the mixed-size workload timed one per call (plain FP64)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
