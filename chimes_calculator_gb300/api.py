@@ -107,9 +107,9 @@ class Calculator:
         return out
 
     def tuning(self) -> dict:
-        v = np.zeros(10, dtype=np.int32)
+        v = np.zeros(11, dtype=np.int32)
         self._check(self.lib.ck_get_tuning(self.h, _ip(v)))
-        keys = ["tpc3", "tpc4", "blocks_per_sm", "fact3", "fact4", "ftpc3", "ftpc4", "fbps3", "fbps4", "noy3"]
+        keys = ["tpc3", "tpc4", "blocks_per_sm", "fact3", "fact4", "ftpc3", "ftpc4", "fbps3", "fbps4", "noy3", "tc3"]
         return {k: int(x) for k, x in zip(keys, v)}
 
     def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
@@ -216,7 +216,8 @@ class Calculator:
     def set_contraction(self, factored=True):
         """3-/4-body contraction kernels: True/1 factored (default), False/0
         per-coefficient, 2 factored without the per-entry pair-table cache,
-        3 factored with the 3-body column products formed per coefficient."""
+        3 factored with the 3-body column products formed per coefficient,
+        4 factored with the 3-body contraction on the tensor cores (mixed form)."""
         self._check(self.lib.ck_set_contraction(self.h, int(factored)))
 
     def autotune(self, packed=None):

@@ -27,7 +27,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CXX_SOURCES = ["ck_params.cpp", "ck_geom.cpp", "ck_engine.cpp", "ck_capi.cpp", "ck_chimesff.cpp", "ck_server.cpp", "ck_nl.cpp"]
-CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_factored.cu", "ck_neigh.cu", "ck_direct.cu", "ck_noalloc.cu",
+CU_SOURCES = ["ck_lists.cu", "ck_force.cu", "ck_factored.cu", "ck_tensor.cu", "ck_neigh.cu", "ck_direct.cu",
+              "ck_noalloc.cu",
               "ck_fingerprint.cu"]
 
 

@@ -317,8 +317,9 @@ int ck_tuple_factored(void* h, int slot, int nbody, int* nrow, int* ncol, int* R
 int ck_get_tuning(void* h, int* out) {
     if (int st = check_handle(h)) return st;
     const ck::ForceLaunch& L = static_cast<Instance*>(h)->eng.tuning;
-    const int v[10] = {L.tpc3, L.tpc4, L.blocks_per_sm, L.fact3, L.fact4, L.ftpc3, L.ftpc4, L.fbps3, L.fbps4, L.noy3};
-    for (int k = 0; k < 10; k++) out[k] = v[k];
+    const int v[11] = {L.tpc3,  L.tpc4,  L.blocks_per_sm, L.fact3, L.fact4, L.ftpc3,
+                       L.ftpc4, L.fbps3, L.fbps4,         L.noy3,  L.tc3};
+    for (int k = 0; k < 11; k++) out[k] = v[k];
     return ck::kOk;
 }
 
@@ -354,11 +355,12 @@ int ck_set_tuning(void* h, int tpc3, int tpc4, int blocks_per_sm) {
 
 int ck_set_contraction(void* h, int factored) {
     if (int st = check_handle(h)) return st;
-    if (factored < 0 || factored > 3) return report(ck::kErrInput, "contraction mode must be 0, 1, 2 or 3");
+    if (factored < 0 || factored > 4) return report(ck::kErrInput, "contraction mode must be 0, 1, 2, 3 or 4");
     ck::Engine& e = static_cast<Instance*>(h)->eng;
     e.factored = factored != 0;
     e.pair_cache = factored != 2;
     e.tuning.noy3 = factored == 3 ? 1 : 0;
+    e.tuning.want_tc3 = factored == 4 ? 1 : 0;
     return ck::kOk;
 }
 

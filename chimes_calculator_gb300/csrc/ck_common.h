@@ -25,6 +25,12 @@
 #pragma once
 #include <cstdint>
 
+#if defined(__CUDACC__)
+#define CK_HD __host__ __device__
+#else
+#define CK_HD
+#endif
+
 namespace ck {
 
 constexpr int kMaxOrder = 31;      // powers are packed 5 bits per pair
@@ -62,6 +68,9 @@ struct TupleRec {
     // right after them (f_ncol); row entries at [f_ent, f_ent+ncoef), column
     // entries at [f_ent+ncoef, f_ent+2*ncoef)
     int f_row, f_nrow, f_ncol, f_ent;
+    // tensor-core form (3-body): offset of the tuple's coefficient matrix
+    // images in DevParamSet::tc3 (floats), -1 when absent
+    int tc_off, tc_pad;
     double rin[6], rout[6], lam[6], xavg[6], xdiff[6];
     // reciprocals for the factored kernels: 1/lam, 1/xdiff, and the cutoff's
     // 1/rc (cubic) or Tersoff threshold rc - f*rc and 1/(rc - threshold)
@@ -84,6 +93,19 @@ struct FactRow {
     int end;
 };
 constexpr int kFactMaxDim = 128;   // largest R^K and R^(P-K) kept in shared memory per cluster
+
+// Tensor-core 3-body images (DevParamSet::tc3): with Rw powers per pair the
+// MMA's K is Rw padded to 8 or 16 and N = Rw^2 padded to 16; a tuple stores
+// one image (TF32 high part, then remainder) per Rw from its own R up to
+// kTc3MaxR, consecutively, so the image for Rw starts tc3_offset floats in.
+constexpr int kTc3MaxR = 11;
+CK_HD constexpr int tc3_kpad(int Rw) { return Rw <= 8 ? 8 : 16; }
+CK_HD constexpr int tc3_npad(int Rw) { return ((Rw * Rw + 15) / 16) * 16; }
+CK_HD inline long long tc3_offset(int R, int Rw) {
+    long long o = 0;
+    for (int r = R; r < Rw; r++) o += 2LL * tc3_kpad(r) * tc3_npad(r);
+    return o;
+}
 
 // Per-pair-type constants of a body order's Chebyshev stage, when every tuple
 // uses the same inner/outer cutoff for a given pair type (then a pair's
@@ -150,6 +172,12 @@ struct DevParamSet {
     // absent (R^K or R^(P-K) above kFactMaxDim)
     int R3, R4;
     int bk3, bk4;              // first cluster bucket of this set (per engine; see BatchView)
+    // tensor-core 3-body contraction (mixed form): per tuple, the dense
+    // coefficient matrix A[q_ij][q_ik*Rw + q_jk] as the B operand of a
+    // tcgen05 TF32 MMA, one image per working width Rw >= R3 (see tc3_offset);
+    // tc3_k, tc3_n = K and N at Rw = R3; null when R3 is 0 or above kTc3MaxR
+    int tc3_k, tc3_n;
+    const float* tc3;
     const FactRow* fr3; const FactEntD* fe3d; const FactEntF* fe3f;
     const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
     // per-pair-type tables [npairs] (null when some tuple's cutoffs differ by tuple)
@@ -253,12 +281,15 @@ struct BatchView {
     double* vatom;                 // [n_in_total][6] per-atom virial (xx yy zz xy xz yz) or null
     double* ev;                    // [n_sys][8]: energy, virial xx xy xz yy yz zz, spare
     int* flags;                    // [8] device error flags: 0 capacity, 1 geometry, 2 badness max,
-                                   //     3 penalty count, 4 below-rin count, 5 timeout
+                                   //     3 penalty count, 4 below-rin count, 5 table look-ups,
+                                   //     6 inputs (no-alloc entry), 7 bounded wait expired
     unsigned long long* queue;     // [2] work-queue heads of the 3-body and 4-body force kernels
     // cluster buckets by (parameter set, ordered type tuple), for the factored
     // contraction: bucket key = pset.bk{3,4} + tuple index; each bucket padded
     // to a multiple of 32 slots with -1, so a warp's clusters share one tuple
+    // (3-body: of bk_pad3 slots, 128 for the tensor-core form's 128-cluster tiles)
     int nbk3, nbk4;
+    int bk_pad3;
     int* bk_key3;                  // [n3_cap] / [n4_cap] or null: each cluster's bucket key,
     int* bk_key4;                  //   written by the count pass and read by the scatter pass
     int* bk_count;                 // [nbk3 + nbk4]

@@ -118,6 +118,7 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.fr3); rel(h.fe3d); rel(h.fe3f);
     rel(h.fr4); rel(h.fe4d); rel(h.fe4f);
     rel(h.pt3); rel(h.pt4);
+    rel(h.tc3);
     rel(h.t2rec); rel(h.tab2r); rel(h.tab2c);
     rel(h.t3rec); rel(h.tab3r); rel(h.tab3v);
     // this set's cluster buckets follow those of the sets loaded before it
@@ -156,6 +157,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     bool fact3 = factored, fact4 = factored;
     bool pc3 = pair_cache, pc4 = pair_cache;
     int rf3 = 0, rf4 = 0;
+    bool tc3 = precision == kMixed;
     bool enum_serial = false;
     double n2_est = 0.0, n3_est = 0.0, n4_est = 0.0;
     for (int s = 0; s < S; s++) {
@@ -202,7 +204,12 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
         stride3 = std::max(stride3, P.o3 > 0 ? P.o3 + 1 : 0);
         stride4 = std::max(stride4, P.o4 > 0 ? P.o4 + 1 : 0);
         const DevParamSet& V = sets_[in.pset].view;
-        if (P.o3 > 0) { fact3 = fact3 && V.R3 > 0; rf3 = std::max(rf3, V.R3); pc3 = pc3 && V.pt3; }
+        if (P.o3 > 0) {
+            fact3 = fact3 && V.R3 > 0;
+            rf3 = std::max(rf3, V.R3);
+            pc3 = pc3 && V.pt3;
+            tc3 = tc3 && V.tc3 != nullptr;
+        }
         if (P.o4 > 0) { fact4 = fact4 && V.R4 > 0; rf4 = std::max(rf4, V.R4); pc4 = pc4 && V.pt4; }
         // list-size estimates for the first capacity guess
         const double rho = d.n_atoms / (vols_[s] > 0 ? vols_[s] : 1.0);
@@ -221,6 +228,8 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     tuning.fact4 = fact4 && rf4 > 0 && tuning.want_fact4 ? 1 : 0;
     avail_fact3_ = fact3 && rf3 > 0;
     avail_fact4_ = fact4 && rf4 > 0;
+    avail_tc3_ = avail_fact3_ && tc3 && tc3_supported(rf3);
+    tuning.tc3 = tuning.fact3 && avail_tc3_ && tuning.want_tc3 ? 1 : 0;
     // the pair-table cache needs the enumeration that records entry indices;
     // it pays for itself while its tables stay near L2 (measured: ~10% on the
     // 3-body kernel for 25k list entries, nothing for 11M), so large batches
@@ -294,8 +303,8 @@ Status Engine::ensure_lists(std::string& err) {
     CK_TRY(d_e_off4_.reserve(n2_cap_ + 1));
     CK_TRY(d_c3_.reserve(3 * n3_cap_));
     CK_TRY(d_c4_.reserve(4 * n4_cap_));
-    // buckets pad each (set, tuple) to 32 slots
-    const long long p3cap = nbk3_ > 0 ? n3_cap_ + 32LL * nbk3_ : 0;
+    // buckets pad each (set, tuple) to 32 slots (3-body: 128 for the tensor-core form)
+    const long long p3cap = nbk3_ > 0 ? n3_cap_ + 128LL * nbk3_ : 0;
     const long long p4cap = nbk4_ > 0 ? n4_cap_ + 32LL * nbk4_ : 0;
     CK_TRY(d_perm3_.reserve(std::max(1LL, p3cap)));
     CK_TRY(d_perm4_.reserve(std::max(1LL, p4cap)));
@@ -362,7 +371,8 @@ static cudaError_t record_stage_event(cudaEvent_t ev, cudaStream_t st) {
 
 Status Engine::enqueue(std::string& err) {
     BatchView B = V_;
-    B.use_pc3 = avail_pc3_ && tuning.fact3 ? 1 : 0;
+    B.use_pc3 = avail_pc3_ && tuning.fact3 && !tuning.tc3 ? 1 : 0;
+    B.bk_pad3 = tuning.tc3 ? 128 : 32;
     B.use_pc4 = avail_pc4_ && tuning.fact4 ? 1 : 0;
     cudaStream_t st = stream_;
     const long long k0 = launch_counter();
@@ -407,7 +417,10 @@ Status Engine::enqueue(std::string& err) {
     }
     auto body3 = [&](cudaStream_t q) {
         if (L.stride3 <= 0) return;
-        if (L.fact3) {
+        if (L.fact3 && L.tc3) {
+            launch_bucket(B, 3, q);
+            launch_force3tc(B, L, q);
+        } else if (L.fact3) {
             launch_pair_tables(B, d_l2_owner_.p, 3, L, q);
             launch_bucket(B, 3, q);
             launch_force3f(B, L, q);
@@ -476,7 +489,8 @@ Status Engine::launch(std::string& err) {
                                   V_.n_bins_total, n2_cap_, n3_cap_, n4_cap_, precision, tuning.tpc3, tuning.tpc4,
                                   tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0,
                                   tuning.fact3, tuning.fact4, tuning.rf3, tuning.rf4, tuning.ftpc3, tuning.ftpc4,
-                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0, tuning.noy3};
+                                  tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0, tuning.noy3,
+                                  tuning.tc3};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,
@@ -531,6 +545,10 @@ Status Engine::collect(double* force_out, std::vector<SystemResult>& res, std::s
         }
         err = "list capacity exceeded";
         return kErrCapacity;
+    }
+    if (f[7] & 1) {
+        err = "tensor-core contraction: a bounded wait for the matrix units expired";
+        return kErrTimeout;
     }
     if (f[1]) {
         err = f[1] == 1 ? "negative bin computed (check box lengths and atom coordinates)"
@@ -610,8 +628,10 @@ Status Engine::autotune(int* chosen, std::string& err) {
             tuning.want_fact3 = kv.second.want_fact3;
             tuning.want_fact4 = kv.second.want_fact4;
             tuning.noy3 = kv.second.noy3;
+            tuning.want_tc3 = kv.second.want_tc3;
             tuning.fact3 = avail_fact3_ && tuning.want_fact3;
             tuning.fact4 = avail_fact4_ && tuning.want_fact4;
+            tuning.tc3 = tuning.fact3 && avail_tc3_ && tuning.want_tc3;
             report();
             return kOk;
         }
@@ -651,25 +671,28 @@ Status Engine::autotune(int* chosen, std::string& err) {
     // in shared memory per cluster, so each is tried at 8 and at up to 16
     // resident one-warp blocks per SM (capped by its occupancy); the per-SM
     // count is refined below.
-    struct Cand { int fact, tpc, noy, fbps; };
-    auto cands = [](bool can_fact, bool with_noy) {
+    // (3-body in the mixed form also the tensor-core contraction)
+    struct Cand { int fact, tpc, noy, fbps, tc; };
+    auto cands = [](bool can_fact, bool with_noy, bool with_tc) {
         std::vector<Cand> v;
+        if (with_tc) v.push_back({1, 1, 0, 0, 1});
         if (can_fact)
             for (int t : {1, 2, 4})
                 for (int nf : {0, 1}) {
                     if (nf && !with_noy) continue;
-                    v.push_back({1, t, nf, 8});
-                    v.push_back({1, t, nf, 16});
+                    v.push_back({1, t, nf, 8, 0});
+                    v.push_back({1, t, nf, 16, 0});
                 }
-        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0, 0});
+        for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0, 0, 0});
         return v;
     };
-    const std::vector<Cand> c3 = cands(avail_fact3_, true), c4 = cands(avail_fact4_, false);
+    const std::vector<Cand> c3 = cands(avail_fact3_, true, avail_tc3_), c4 = cands(avail_fact4_, false, false);
     auto apply = [&](int nb, const Cand& c) {
         if (nb == 3) {
             tuning.fact3 = c.fact;
             (c.fact ? tuning.ftpc3 : tuning.tpc3) = c.tpc;
             tuning.noy3 = c.noy;
+            tuning.tc3 = c.tc;
             if (c.fbps > 0) tuning.fbps3 = c.fbps;
         } else {
             tuning.fact4 = c.fact;
@@ -678,8 +701,8 @@ Status Engine::autotune(int* chosen, std::string& err) {
         }
     };
     double best3 = 1e300, best4 = 1e300;
-    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3, tuning.fbps3};
-    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0, tuning.fbps4};
+    Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3, tuning.fbps3, tuning.tc3};
+    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0, tuning.fbps4, 0};
     const size_t nc = std::max(c3.size(), c4.size());
     for (size_t i = 0; i < nc && st == kOk; i++) {
         const bool need3 = do3 && i < c3.size(), need4 = do4 && i < c4.size();
@@ -699,7 +722,9 @@ Status Engine::autotune(int* chosen, std::string& err) {
     apply(4, b4);
     tuning.want_fact3 = b3.fact;
     tuning.want_fact4 = b4.fact;
-    const bool f3 = tuning.fact3 != 0, f4 = tuning.fact4 != 0;
+    tuning.want_tc3 = b3.tc;
+    // (the tensor-core form's occupancy is fixed by its shared memory: two blocks per SM)
+    const bool f3 = tuning.fact3 != 0 && !tuning.tc3, f4 = tuning.fact4 != 0;
     // resident blocks per SM: 4-warp blocks for the per-coefficient kernels,
     // one-warp blocks for the factored ones (capped by their occupancy)
     const int bps[] = {1, 2, 4, 8};

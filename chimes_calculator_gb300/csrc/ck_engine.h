@@ -190,6 +190,7 @@ private:
     DevBuf<int> d_c3_, d_c4_;
     int nbk3_ = 0, nbk4_ = 0;     // cluster buckets over all loaded parameter sets
     bool avail_fact3_ = false, avail_fact4_ = false;   // staged batch has factored tables
+    bool avail_tc3_ = false;                           // ... and tensor-core 3-body images (mixed form)
     bool enum_serial_ = false;                         // staged batch needs the sequential enumeration
     bool avail_pc3_ = false, avail_pc4_ = false;       // pair-table cache usable for the staged batch
     DevBuf<int> d_c3e_, d_c4e_;

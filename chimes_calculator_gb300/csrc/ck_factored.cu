@@ -159,18 +159,6 @@ __device__ __forceinline__ CT entry_sum_noy(const E* __restrict__ ent, int e0, i
     return z0 + z1;
 }
 
-// Ordered type tuple of cluster c: its ghost slots, system, parameter set and tuple index.
-template <int NB>
-__device__ __forceinline__ const TupleRec* cluster_tuple(const BatchView& B, const int* clusters, long long c,
-                                                         int* id, int& s, const DevParamSet*& P, int& u) {
-    for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
-    s = B.atom_sys[B.ghost_parent[id[0]]];
-    P = &B.psets[B.sys[s].pset];
-    u = 0;
-    for (int k = 0; k < NB; k++) u = u * P->ntypes + B.atom_type[B.ghost_parent[id[k]]];
-    return (NB == 3 ? P->t3 : P->t4) + u;
-}
-
 // Chebyshev tables and cutoff of pair p of a tuple (set_cheby_polys,
 // chimesFF.h:542-628; get_fcut, chimesFF.h:347-386) with the tuple's
 // precomputed reciprocals in place of the divisions.
@@ -253,7 +241,7 @@ __global__ void __launch_bounds__(256) k_bucket_count(BatchView B, const int* cl
     }
 }
 
-// Exclusive scan of the bucket sizes rounded up to 32; the total goes to
+// Exclusive scan of the bucket sizes rounded up to 32 (3-body: bk_pad3); the total goes to
 // start[nbk] and the padding slots of every bucket are set to -1.  One block.
 __global__ void __launch_bounds__(1024) k_bucket_scan(BatchView B, int nb) {
     const int nbk = nb == 3 ? B.nbk3 : B.nbk4;
@@ -261,6 +249,7 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(BatchView B, int nb) {
     long long* start = B.bk_start + (nb == 3 ? 0 : B.nbk3 + 1);
     int* perm = nb == 3 ? B.perm3 : B.perm4;
     const long long pcap = nb == 3 ? B.perm3_cap : B.perm4_cap;
+    const int pad = nb == 3 && B.bk_pad3 > 0 ? B.bk_pad3 : 32;   // a power of two
     __shared__ long long wsum[32];
     __shared__ long long carry;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -268,7 +257,7 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(BatchView B, int nb) {
     __syncthreads();
     for (int base = 0; base < nbk; base += blockDim.x) {
         const int k = base + threadIdx.x;
-        const long long v = k < nbk ? (long long)((count[k] + 31) & ~31) : 0;
+        const long long v = k < nbk ? (long long)((count[k] + pad - 1) & ~(pad - 1)) : 0;
         long long x = v;
         for (int o = 1; o < 32; o <<= 1) {
             const long long y = __shfl_up_sync(kFull, x, o);

@@ -29,6 +29,18 @@ __device__ __forceinline__ void pair_geom(const BatchView& B, const double* h, i
     r = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
 }
 
+// Ordered type tuple of cluster c: its ghost slots, system, parameter set and tuple index.
+template <int NB>
+__device__ __forceinline__ const TupleRec* cluster_tuple(const BatchView& B, const int* clusters, long long c,
+                                                         int* id, int& s, const DevParamSet*& P, int& u) {
+    for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
+    s = B.atom_sys[B.ghost_parent[id[0]]];
+    P = &B.psets[B.sys[s].pset];
+    u = 0;
+    for (int k = 0; k < NB; k++) u = u * P->ntypes + B.atom_type[B.ghost_parent[id[k]]];
+    return (NB == 3 ? P->t3 : P->t4) + u;
+}
+
 __device__ __forceinline__ void add_force(const BatchView& B, int ghost, double fx, double fy, double fz) {
     const int o = B.atom_orig[B.ghost_parent[ghost]];
     atomicAdd(&B.force[3 * (long long)o + 0], fx);

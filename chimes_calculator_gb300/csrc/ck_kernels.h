@@ -50,6 +50,9 @@ struct ForceLaunch {
     int ftpc3 = 1, ftpc4 = 4;
     int fbps3 = 8, fbps4 = 8;      // resident one-warp blocks per SM (capped by occupancy)
     int noy3 = 0;                  // factored 3-body without the Y table (products per entry)
+    // tensor-core 3-body contraction (mixed form only; ck_tensor.cu): tc3 = in
+    // use for this launch, want_tc3 = preference (autotuner or forced)
+    int tc3 = 0, want_tc3 = 0;
 };
 
 // Cluster counts are read on the device (l2_off[n_atoms], e_off3/4[n2_cap]) and
@@ -66,6 +69,10 @@ void launch_bucket(const BatchView& B, int nbody, cudaStream_t st);
 void launch_pair_tables(const BatchView& B, const int* l2_owner, int nbody, const ForceLaunch& L, cudaStream_t st);
 void launch_force3f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+// Tensor-core 3-body contraction (ck_tensor.cu): mixed form, R3 powers per
+// pair in [2, kTc3MaxR]; clusters bucketed with 128-slot padding (bk_pad3).
+bool tc3_supported(int rf3);
+void launch_force3tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // dynamic shared memory of one factored-kernel block (one warp)
 size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 

@@ -756,6 +756,43 @@ struct Blob {
 template <class T>
 T* as_off(size_t off) { return reinterpret_cast<T*>(off); }
 
+// TF32 split of a coefficient for the tensor-core contraction: hi = x rounded
+// to TF32 (10 explicit mantissa bits, ties away from zero), lo = the remainder
+// (which the tensor core truncates to TF32 in turn).
+float tf32_hi_host(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u = (u + 0x1000u) & 0xffffe000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+// Tensor-core image of one 3-body tuple's dense coefficient matrix
+// A[q0][q1*Rw + q2] (q0 the ij power, q1 ik, q2 jk; the tuple's R powers per
+// pair, zero above) for a kernel working with Rw >= R powers: the B operand
+// of W = X . A with X = T_ij, stored as N = tc3_npad(Rw) rows (J) of
+// K = tc3_kpad(Rw) values (q0), K-major, no swizzle: the core matrix of rows
+// 8i..8i+7 and k = 4j..4j+3 (8 x 16 bytes) at byte (i * K/4 + j) * 128, row
+// n % 8 at +16 * (n % 8); the TF32 high parts first, then the remainders.
+void tc3_image(const std::vector<double>& dense, int R, int Rw, std::vector<float>& out) {
+    const int kpad = tc3_kpad(Rw), npad = tc3_npad(Rw);
+    const size_t base = out.size();
+    const size_t part = (size_t)kpad * npad;
+    out.resize(base + 2 * part, 0.0f);
+    for (int q1 = 0; q1 < R; q1++)
+        for (int q2 = 0; q2 < R; q2++)
+            for (int k = 0; k < R; k++) {
+                const double a = dense[(size_t)k * R * R + q1 * R + q2];
+                const int n = q1 * Rw + q2;
+                const float hi = tf32_hi_host((float)a);
+                const float lo = (float)(a - (double)hi);
+                const size_t off = ((size_t)(n / 8) * (kpad / 4) + k / 4) * 32 + (n % 8) * 4 + (k % 4);
+                out[base + off] = hi;
+                out[base + part + off] = lo;
+            }
+}
+
 // set_cheby_polys' Morse-map constants (chimesFF.h:553-559)
 void morse_consts(double rin, double rout, double lam, double& xavg, double& xdiff) {
     double x_min = std::exp(-1 * rin / lam);
@@ -850,7 +887,12 @@ ParamImage pack_params(const HostParams& P) {
         std::vector<FactRow> fr;
         std::vector<FactEntD> fed;
         std::vector<FactEntF> fef;
-        struct Shared { int coef_off, f_row, f_nrow, f_ncol, f_ent; };
+        // tensor-core images (3-body, R <= kTc3MaxR: N = R^2 <= 128 TMEM columns
+        // per accumulator), one per working width Rw = R .. kTc3MaxR so that a
+        // batch mixing sets of different orders runs at its largest R
+        const bool tc = nb == 3 && fact && R_pow >= 2 && R_pow <= kTc3MaxR;
+        std::vector<float> tcimg;
+        struct Shared { int coef_off, f_row, f_nrow, f_ncol, f_ent, tc_off; };
         std::map<std::pair<int, std::vector<int>>, Shared> shared;  // (type, mapping) -> tables
         for (int u = 0; u < ntup; u++) {
             TupleRec& R = tr[u];
@@ -881,12 +923,14 @@ ParamImage pack_params(const HostParams& P) {
                 }
             R.ncoef = Bd.ncoef[ti];
             R.valid = R.ncoef > 0 ? 1 : 0;
+            R.tc_off = -1;
             auto key = std::make_pair(ti, m);
             auto it = shared.find(key);
             if (it != shared.end()) {
                 R.coef_off = it->second.coef_off;
                 R.f_row = it->second.f_row; R.f_nrow = it->second.f_nrow;
                 R.f_ncol = it->second.f_ncol; R.f_ent = it->second.f_ent;
+                R.tc_off = it->second.tc_off;
                 continue;
             }
             R.coef_off = (int)cd.size();
@@ -938,7 +982,13 @@ ParamImage pack_params(const HostParams& P) {
                     if (pass == 0) R.f_nrow = nrec; else R.f_ncol = nrec;
                 }
             }
-            shared[key] = Shared{R.coef_off, R.f_row, R.f_nrow, R.f_ncol, R.f_ent};
+            if (tc && R.ncoef > 0) {
+                std::vector<double> dense((size_t)R_pow * R_pow * R_pow, 0.0);
+                for (int c = 0; c < R.ncoef; c++) dense[(size_t)rowi[c] * R_pow * R_pow + coli[c]] += Bd.coef[ti][c];
+                R.tc_off = (int)tcimg.size();
+                for (int Rw = R_pow; Rw <= kTc3MaxR; Rw++) tc3_image(dense, R_pow, Rw, tcimg);
+            }
+            shared[key] = Shared{R.coef_off, R.f_row, R.f_nrow, R.f_ncol, R.f_ent, R.tc_off};
         }
         // per-pair-type tables when no tuple overrides a pair type's cutoffs
         std::vector<PairTab> ptab(P.npairs);
@@ -971,6 +1021,11 @@ ParamImage pack_params(const HostParams& P) {
             ffo = B.add(fef.data(), fef.size());
         }
         const int Rf = (fact && !fed.empty()) ? R_pow : 0;
+        if (nb == 3 && tc && Rf > 0 && !tcimg.empty()) {
+            H.tc3_k = tc3_kpad(R_pow);
+            H.tc3_n = tc3_npad(R_pow);
+            H.tc3 = as_off<const float>(B.add(tcimg.data(), tcimg.size()));
+        }
         if (nb == 3) {
             H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
             H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);

@@ -1,0 +1,387 @@
+// Tensor-core 3-body contraction (mixed form) on the fifth-generation tensor
+// cores: tcgen05.mma with TF32 operands in shared memory and FP32
+// accumulators in tensor memory (TMEM).
+//
+// For the clusters of one ordered type tuple, with R powers per pair and the
+// tuple's coefficients as a dense matrix A[q_ij][J], J = q_ik * R + q_jk
+// (the factored form's row and column indices, ck_common.h FactRow):
+//   W  = X  . A,   X[c][q]  = T_ij(c)[q]        (energy and column gradients)
+//   W' = dX . A,   dX[c][q] = dT_ij/dr(c)[q]    (row gradient)
+// one MMA pair per 128 clusters (M = 128, K = R padded to 8 or 16, N = R^2
+// padded to 16).  Each cluster's thread then reduces its TMEM row:
+//   V[b] = sum_c W[b,c] T_jk[c],  V2[b] = sum_c W[b,c] dT_jk[c],
+//   V'[b] = sum_c W'[b,c] T_jk[c]
+//   S = sum_b V[b] T_ik[b],   G_ij = sum_b V'[b] T_ik[b],
+//   G_ik = sum_b V[b] dT_ik[b],   G_jk = sum_b V2[b] T_ik[b]
+// which are the sums of compute_3B (chimesFF/src/chimesFF.cpp:2068-2169) in
+// another association order; the force and virial epilogue is the other
+// contraction kernels' (cluster_epilogue, FP64).
+//
+// Precision: TF32 keeps 10 mantissa bits, so both operands are split into a
+// TF32 high part and the remainder, and W = Xh.Ah + Xh.Al + Xl.Ah (three MMAs
+// per product; Xl.Al ~ 2^-22 relative is dropped), with FP32 accumulation:
+// about the FP32 contraction's accuracy.  Geometry, the Morse exponential and
+// the epilogue stay in FP64, the Chebyshev recursion and cutoff in FP32, as
+// in the other kernels of the mixed form.
+//
+// Work: persistent CTAs of 128 threads (one cluster per thread) take
+// 128-cluster tiles from an atomic queue over the clusters bucketed by
+// (parameter set, tuple) and padded to 128 slots, so a tile has one tuple.
+// Per tile: the tuple's coefficient image (B operand) is copied to shared
+// memory when the tuple changes; each thread builds its cluster's tables and
+// writes its X / dX rows (K-major, no-swizzle core-matrix layout); one thread
+// issues the MMAs and commits them to an mbarrier; every thread waits on it
+// with a bounded poll, reads its TMEM row in 16-column chunks and finishes the
+// cluster.  At most two CTAs per SM (their shared memory) hold 256 TMEM
+// columns each.  A wait that runs out sets flags[7] and the CTA stops after
+// freeing its TMEM.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ck_common.h"
+#include "ck_force_common.cuh"
+#include "ck_kernels.h"
+#include "ck_math.cuh"
+
+namespace ck {
+
+namespace {
+
+constexpr int kTcTile = 128;              // clusters per tile (MMA M)
+constexpr uint32_t kTcCols = 256;         // TMEM columns per CTA: W at 0, W' at 128
+constexpr int kTcSpin = 1 << 22;          // bounded mbarrier wait: polls (~0.15 s with the back-off)
+constexpr size_t kTcMinSmem = 80 * 1024;  // keeps two CTAs per SM (TMEM: 2 x 256 of 512 columns)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor of tcgen05.mma: start address, leading
+// byte offset (between core matrices adjacent in K), stride byte offset
+// (between core matrices adjacent in M/N), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+}
+
+// Chebyshev tables T[0..R), dT/dr[0..R) and cutoff of one pair, in registers
+// (the arithmetic of pair_setup / cheby_fill_strided, ck_factored.cu and
+// ck_math.cuh, unrolled for a compile-time R).
+template <int R>
+__device__ __forceinline__ void pair_regs(const DevParamSet& P, const TupleRec& Q, int p, double r, float (&T)[R],
+                                          float (&D)[R], float& fc, float& fcd, int* flags) {
+    const double rin = Q.rin[p];
+    const bool oor = r < rin;
+    const double rr = oor ? rin : r;
+    const double e = exp(-rr * Q.inv_lam[p]);
+    const double xd = (e - Q.xavg[p]) * Q.inv_xdiff[p];
+    const double dxdr = -e * Q.inv_lam[p] * Q.inv_xdiff[p];
+    const float x = float(xd), tx = 2.0f * x, g = float(dxdr);
+    float k = 0.0f, dm = 1.0f;
+    if (oor) {
+        atomicAdd(&flags[4], 1);
+        const double damp = exp((r - rin) / P.inner_smooth);
+        k = float(P.inner_smooth * (damp - 1.0));
+        dm = float(damp);
+    }
+    T[0] = 1.0f;
+    D[0] = 0.0f;
+    float t0 = 1.0f, t1 = x, u0 = 1.0f, u1 = tx;
+    if (R > 1) {
+        const float d1 = g * u0;
+        T[1] = oor ? t1 + k * d1 : t1;
+        D[1] = oor ? d1 * dm : d1;
+    }
+#pragma unroll
+    for (int n = 2; n < R; n++) {
+        const float t2 = tx * t1 - t0;
+        const float u2 = tx * u1 - u0;
+        const float dn = float(n) * g * u1;
+        T[n] = oor ? t2 + k * dn : t2;
+        D[n] = oor ? dn * dm : dn;
+        t0 = t1; t1 = t2; u0 = u1; u1 = u2;
+    }
+    const double finv = Q.fc_inv[p];
+    if (!P.tersoff) {
+        const float f0 = 1.0f - float(r) * float(finv);
+        fc = f0 * f0 * f0;
+        fcd = f0 * f0 * (-3.0f * float(finv));
+    } else {
+        const double th = Q.fc_th[p];
+        if (r < th) { fc = 1.0f; fcd = 0.0f; }
+        else if (r > Q.rout[p]) { fc = 0.0f; fcd = 0.0f; }
+        else {
+            const float f0 = float(r - th) * float(finv) * float(kPi) + float(kPi / 2.0);
+            float sn, cs;
+            sincosf(f0, &sn, &cs);
+            fc = 0.5f + 0.5f * sn;
+            fcd = 0.5f * cs * (float(kPi) * float(finv));
+        }
+    }
+}
+
+// One row of an A operand image (K-major, no swizzle): row m's KP values at
+// core-matrix rows; hi and lo parts of v (zero past R, or all zero).
+template <int R, int KP>
+__device__ __forceinline__ void put_row(float* hi, float* lo, int m, const float (&v)[R], bool on) {
+    constexpr int SBOF = KP * 8;   // floats between row blocks (KP/4 core matrices of 32 floats)
+    float* rh = hi + (m >> 3) * SBOF + (m & 7) * 4;
+    float* rl = lo + (m >> 3) * SBOF + (m & 7) * 4;
+#pragma unroll
+    for (int j = 0; j < KP / 4; j++) {
+        float h[4], l[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = 4 * j + q;
+            const float x = (on && k < R) ? v[k < R ? k : 0] : 0.0f;
+            h[q] = tf32_hi(x);
+            l[q] = x - h[q];
+        }
+        *reinterpret_cast<float4*>(rh + j * 32) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(rl + j * 32) = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* clusters, const int* perm,
+                                                  const long long* perm_n, long long perm_cap) {
+    constexpr int KP = tc3_kpad(R);                     // K padded to whole MMA steps (8 for TF32)
+    constexpr int NP = tc3_npad(R);                     // N padded to 16
+    constexpr int AFL = kTcTile * KP;                   // floats per A image
+    constexpr int BFL = NP * KP;                        // floats per B image part
+    constexpr uint32_t LBO = 128, SBO = KP * 32;        // bytes: next core matrix in K; next 8 rows
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float* Xh = reinterpret_cast<float*>(smem);
+    float* Xl = Xh + AFL;
+    float* Dh = Xl + AFL;
+    float* Dl = Dh + AFL;
+    float* Bh = Dl + AFL;
+    float* Bl = Bh + BFL;
+    __shared__ uint32_t s_tmem;
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ long long s_tile;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const long long n = min(*perm_n, perm_cap);
+    const long long ntiles = n / kTcTile;
+    if (tid < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(kTcCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = s_tmem;
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                           ((uint32_t)(kTcTile >> 4) << 24);
+    uint32_t phase = 0;
+    int loaded = -1;                                    // tc_off of the B image in shared memory
+    const DevParamSet* loaded_set = nullptr;
+    EVAcc acc;
+
+    for (;;) {
+        if (tid == 0) s_tile = (long long)atomicAdd(&B.queue[0], 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= ntiles) break;
+        const long long base = tile * kTcTile;
+        const int c0 = perm[base];
+        if (c0 < 0) {               // uniform: a tile never starts in a bucket's padding
+            __syncthreads();
+            continue;
+        }
+        int id0[3], s0, u0;
+        const DevParamSet* P;
+        const TupleRec* Rt = cluster_tuple<3>(B, clusters, c0, id0, s0, P, u0);
+        // the tuple's coefficient image at this kernel's width, when it is not
+        // the one in shared memory
+        if (Rt->tc_off != loaded || P != loaded_set) {
+            const float4* src = reinterpret_cast<const float4*>(P->tc3 + Rt->tc_off + tc3_offset(P->R3, R));
+            float4* dst = reinterpret_cast<float4*>(Bh);
+            for (int q = tid; q < 2 * BFL / 4; q += kTcTile) dst[q] = src[q];
+            loaded = Rt->tc_off;
+            loaded_set = P;
+        }
+        // this thread's cluster: geometry, cutoff early-outs, tables
+        const int c = perm[base + tid];
+        bool active = c >= 0;
+        int id[3] = {0, 0, 0};
+        int s = 0;
+        double dr[3][4];
+        double fcd64[3] = {0, 0, 0}, fc64[3] = {0, 0, 0};
+        float T0[R], D0[R], T1[R], D1[R], T2[R], D2[R];
+#pragma unroll
+        for (int q = 0; q < R; q++) T0[q] = D0[q] = T1[q] = D1[q] = T2[q] = D2[q] = 0.0f;
+        if (active) {
+            for (int k = 0; k < 3; k++) id[k] = clusters[3LL * c + k];
+            s = B.atom_sys[B.ghost_parent[id[0]]];
+            const double* h = B.sys[s].h;
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                double d[3], r;
+                pair_geom(B, h, id[Topo<3>::a(p)], id[Topo<3>::b(p)], d, r);
+                dr[p][0] = d[0]; dr[p][1] = d[1]; dr[p][2] = d[2]; dr[p][3] = r;
+                if (r >= Rt->rout[p]) active = false;   // compute_3B's early-outs
+            }
+        }
+        if (active) {
+            float fc, fcd;
+            pair_regs<R>(*P, *Rt, 0, dr[0][3], T0, D0, fc, fcd, B.flags);
+            fc64[0] = fc; fcd64[0] = fcd;
+            pair_regs<R>(*P, *Rt, 1, dr[1][3], T1, D1, fc, fcd, B.flags);
+            fc64[1] = fc; fcd64[1] = fcd;
+            pair_regs<R>(*P, *Rt, 2, dr[2][3], T2, D2, fc, fcd, B.flags);
+            fc64[2] = fc; fcd64[2] = fcd;
+        }
+        put_row<R, KP>(Xh, Xl, tid, T0, active);
+        put_row<R, KP>(Dh, Dl, tid, D0, active);
+        // generic-proxy writes of the operands -> visible to the tensor core
+        asm volatile("fence.proxy.async.shared::cta;");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t xh = smem_u32(Xh), xl = smem_u32(Xl), dh = smem_u32(Dh), dl = smem_u32(Dl);
+            const uint32_t bh = smem_u32(Bh), bl = smem_u32(Bl);
+#pragma unroll
+            for (int ks = 0; ks < KP / 8; ks++) {
+                const uint32_t o = ks * 256;   // two core matrices along K per step
+                const uint64_t Bhd = umma_desc(bh + o, LBO, SBO), Bld = umma_desc(bl + o, LBO, SBO);
+                mma_tf32(tmem, umma_desc(xh + o, LBO, SBO), Bhd, idesc, ks > 0);
+                mma_tf32(tmem, umma_desc(xh + o, LBO, SBO), Bld, idesc, 1);
+                mma_tf32(tmem, umma_desc(xl + o, LBO, SBO), Bhd, idesc, 1);
+                mma_tf32(tmem + 128, umma_desc(dh + o, LBO, SBO), Bhd, idesc, ks > 0);
+                mma_tf32(tmem + 128, umma_desc(dh + o, LBO, SBO), Bld, idesc, 1);
+                mma_tf32(tmem + 128, umma_desc(dl + o, LBO, SBO), Bhd, idesc, 1);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&s_bar)));
+        }
+        // bounded wait for the MMAs of this tile (non-blocking polls, then a back-off)
+        uint32_t done = 0;
+        for (int it = 0; it < kTcSpin && !done; it++) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                : "=r"(done)
+                : "r"(smem_u32(&s_bar)), "r"(phase));
+            if (!done && it > 256) __nanosleep(32);
+        }
+        phase ^= 1u;
+        if (!__syncthreads_and(done)) {
+            if (tid == 0) atomicOr(&B.flags[7], 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // this thread's TMEM row (lane = tid): W at columns [0, NP), W' at [128, 128 + NP)
+        float V[R], V2[R], Vp[R];
+#pragma unroll
+        for (int b = 0; b < R; b++) V[b] = V2[b] = Vp[b] = 0.0f;
+        const uint32_t row = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int q = 0; q < NP / 16; q++) {
+            float w[16], wp[16];
+            tmem_ld16(row + 16 * q, w);
+            tmem_ld16(row + 128 + 16 * q, wp);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int j = 16 * q + u;
+                if (j < R * R) {
+                    const int b = j / R, cc = j % R;
+                    V[b] += w[u] * T2[cc];
+                    V2[b] += w[u] * D2[cc];
+                    Vp[b] += wp[u] * T2[cc];
+                }
+            }
+        }
+        if (active) {
+            float S = 0.0f, G0 = 0.0f, G1 = 0.0f, G2 = 0.0f;
+#pragma unroll
+            for (int b = 0; b < R; b++) {
+                S += V[b] * T1[b];
+                G0 += Vp[b] * T1[b];
+                G1 += V[b] * D1[b];
+                G2 += V2[b] * T1[b];
+            }
+            const double G[3] = {double(G0), double(G1), double(G2)};
+            cluster_epilogue<3>(B, id, s, dr, fc64, fcd64, double(S), G, acc);
+        }
+        // TMEM and the operand images are rewritten by the next tile
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    }
+    acc.flush_warp(B);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+}
+
+template <int R>
+void launch_tc_r(const BatchView& B, cudaStream_t st) {
+    constexpr int KP = tc3_kpad(R);
+    constexpr int NP = tc3_npad(R);
+    size_t smem = sizeof(float) * (4 * (size_t)kTcTile * KP + 2 * (size_t)NP * KP);
+    if (smem < kTcMinSmem) smem = kTcMinSmem;
+    auto kern = k_forcetc3<R>;
+    // the kernel's own dynamic size (its static shared memory counts against
+    // the opt-in maximum, so the largest value is not accepted here); every
+    // launch of a width asks for the same size, so concurrent callers agree
+    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const long long tiles = B.perm3_cap / kTcTile;
+    long long want = 2LL * sm_count();
+    const unsigned grid = (unsigned)(want < tiles ? want : (tiles > 0 ? tiles : 1));
+    const long long* pn = B.bk_start + B.nbk3;
+    count_launch(), kern<<<grid, kTcTile, smem, st>>>(B, B.c3, B.perm3, pn, B.perm3_cap);
+}
+
+}  // namespace
+
+bool tc3_supported(int rf3) { return rf3 >= 2 && rf3 <= kTc3MaxR; }
+
+void launch_force3tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    if (B.perm3_cap <= 0 || B.nbk3 <= 0) return;
+    switch (L.rf3) {
+        case 2: launch_tc_r<2>(B, st); break;
+        case 3: launch_tc_r<3>(B, st); break;
+        case 4: launch_tc_r<4>(B, st); break;
+        case 5: launch_tc_r<5>(B, st); break;
+        case 6: launch_tc_r<6>(B, st); break;
+        case 7: launch_tc_r<7>(B, st); break;
+        case 8: launch_tc_r<8>(B, st); break;
+        case 9: launch_tc_r<9>(B, st); break;
+        case 10: launch_tc_r<10>(B, st); break;
+        case 11: launch_tc_r<11>(B, st); break;
+        default: break;
+    }
+}
+
+}  // namespace ck

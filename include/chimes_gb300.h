@@ -61,11 +61,12 @@ int ck_tuple_table(void *h, int slot, int nbody, int *valid, int *ncoef, double 
  * nrow[u], ncol[u] row and column records (0 for tuples without coefficients)
  * and *R, the powers per pair (0 when the set has no factored tables). */
 int ck_tuple_factored(void *h, int slot, int nbody, int *nrow, int *ncol, int *R);
-/* out[10] = tpc3, tpc4, blocks_per_sm (per-coefficient kernels), factored 3B and
+/* out[11] = tpc3, tpc4, blocks_per_sm (per-coefficient kernels), factored 3B and
  * 4B in use for the staged batch (0/1), their threads per cluster and one-warp
- * blocks per SM (ftpc3, ftpc4, fbps3, fbps4), and whether the factored 3-body
+ * blocks per SM (ftpc3, ftpc4, fbps3, fbps4), whether the factored 3-body
  * kernel forms its column products per coefficient instead of keeping a table
- * of them (noy3) */
+ * of them (noy3), and whether the 3-body contraction runs on the tensor cores
+ * (tc3, mixed form) */
 int ck_get_tuning(void *h, int *out);
 /* index of an atom type name in a slot, or -1 */
 int ck_type_index(void *h, int slot, const char *name);
@@ -87,8 +88,12 @@ int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
  * pairs ij, ik[, il] from one evaluation per neighbour-list entry, when every
  * tuple uses the same cutoffs for a given pair type); 3 = factored with the
  * 3-body kernel forming its column products per coefficient instead of
- * keeping a table of them (ck_autotune also tries this).  All give the same
- * sums in another rounding order. */
+ * keeping a table of them (ck_autotune also tries this); 4 = factored with
+ * the 3-body contraction on the tensor cores (tcgen05 TF32 MMAs with a
+ * high/remainder split of both operands) in the mixed form, where every
+ * parameter set of the batch has 2-11 powers per pair (ck_autotune also
+ * tries this in the mixed form).  All give the same sums in another rounding
+ * order. */
 int ck_set_contraction(void *h, int factored);
 /* Autotuner for the batch staged with ck_stage_batch: times the 3-body and
  * 4-body force kernels (CUDA events) for threads per cluster 1..32 and then

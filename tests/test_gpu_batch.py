@@ -88,3 +88,30 @@ def test_sparse_and_tiny_configurations(golden, native_lib):
             assert abs(r["energy"] - e["energy"]) <= E_REL_TOL * max(1.0, abs(e["energy"]))
             assert np.abs(r["force"] - e["force"]).max() <= F_ABS_TOL
             assert np.abs(r["stress"] - e["stress"]).max() <= S_ABS_TOL
+
+
+@pytest.mark.parametrize("factored", [1, 4], ids=["factored", "tensor_core"])
+def test_batch_of_parameter_sets_with_different_orders(golden, native_lib, factored):
+    """The serving workload's three parameter sets (3-body orders 8, 10, 8) in
+    one mixed batch, with the 4096-configuration workload's extremes: each
+    configuration within the mixed budget of the reference's values (the
+    tensor-core form runs every set at the batch's largest order, the
+    smaller sets' coefficient matrices padded with zeros)."""
+    from chimes_calculator_gb300 import MIXED, Calculator
+    from conftest import mixed_force_tol
+    names = ["c5_set0", "c5_set1", "c5_set2", "c4_n8_rho012", "c4_n512_rho005"]
+    c = Calculator(precision=MIXED)
+    c.set_contraction(factored)
+    slots = {}
+    for n in names:
+        if golden[n].params not in slots:
+            slots[golden[n].params] = c.load_params(golden[n].params)
+    sl = [slots[golden[n].params] for n in names]
+    confs = [(golden[n].cfg.pos, c.type_indices(golden[n].cfg.types, s), golden[n].cfg.cell) for n, s in zip(names, sl)]
+    res = c.evaluate_batch(confs, slots=sl)
+    if factored == 4:
+        assert c.tuning()["tc3"] == 1
+    for n, r in zip(names, res):
+        g = golden[n]
+        assert abs(r["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy)), n
+        assert g.force_error(r["force"]) <= mixed_force_tol(np.abs(g.force).max()), n

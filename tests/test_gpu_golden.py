@@ -48,7 +48,8 @@ def test_lists_match_oracle(golden, native_lib, name):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("factored", [1, 2, 3, 0], ids=["factored", "factored_nocache", "factored_noy", "per_coef"])
+@pytest.mark.parametrize("factored", [1, 2, 3, 0, 4],
+                         ids=["factored", "factored_nocache", "factored_noy", "per_coef", "tensor_core"])
 @pytest.mark.parametrize("name", golden_names())
 def test_mixed_precision_error(golden, native_lib, name, factored):
     """The mixed form against the reference's own FP64 results (the values
@@ -60,6 +61,21 @@ def test_mixed_precision_error(golden, native_lib, name, factored):
     assert abs(r32["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy))
     assert g.force_error(r32["force"]) <= mixed_force_tol(np.abs(g.force).max())
     assert np.abs(r32["stress"] - g.stress).max() <= MIXED_S_ABS_TOL
+
+
+def test_tensor_core_form_runs(golden, native_lib):
+    """The tensor-core 3-body contraction is the one that runs when asked for
+    in the mixed form (3-body orders 2-11), gives the reference's results
+    within the mixed budget, and leaves the FP64 form on the CUDA cores."""
+    for name in ("c3_cut", "c2_small", "c1", "smallbox"):
+        g = golden[name]
+        c, r = evaluate(g, precision=1, factored=4)
+        assert c.tuning()["tc3"] == 1, name
+        assert abs(r["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy)), name
+        assert g.force_error(r["force"]) <= MIXED_F_ABS_TOL, name
+        c64, r64 = evaluate(g, precision=0, factored=4)
+        assert c64.tuning()["tc3"] == 0
+        assert abs(r64["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
