@@ -96,14 +96,17 @@ constexpr int kFactMaxDim = 128;   // largest R^K and R^(P-K) kept in shared mem
 
 // Tensor-core 3-body images (DevParamSet::tc3): with Rw powers per pair the
 // MMA's K is Rw padded to 8 or 16 and N = Rw^2 padded to 16; a tuple stores
-// one image (TF32 high part, then remainder) per Rw from its own R up to
-// kTc3MaxR, consecutively, so the image for Rw starts tc3_offset floats in.
+// one image per Rw from its own R up to kTc3MaxR, consecutively, so the image
+// for Rw starts tc3_offset floats in.  An image holds kTc3Parts TF32 parts of
+// each coefficient (high, middle, low: each the TF32 rounding of what the
+// previous parts leave), one after another.
 constexpr int kTc3MaxR = 11;
+constexpr int kTc3Parts = 3;
 CK_HD constexpr int tc3_kpad(int Rw) { return Rw <= 8 ? 8 : 16; }
 CK_HD constexpr int tc3_npad(int Rw) { return ((Rw * Rw + 15) / 16) * 16; }
 CK_HD inline long long tc3_offset(int R, int Rw) {
     long long o = 0;
-    for (int r = R; r < Rw; r++) o += 2LL * tc3_kpad(r) * tc3_npad(r);
+    for (int r = R; r < Rw; r++) o += (long long)kTc3Parts * tc3_kpad(r) * tc3_npad(r);
     return o;
 }
 

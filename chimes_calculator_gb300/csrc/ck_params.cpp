@@ -756,9 +756,8 @@ struct Blob {
 template <class T>
 T* as_off(size_t off) { return reinterpret_cast<T*>(off); }
 
-// TF32 split of a coefficient for the tensor-core contraction: hi = x rounded
-// to TF32 (10 explicit mantissa bits, ties away from zero), lo = the remainder
-// (which the tensor core truncates to TF32 in turn).
+// TF32 rounding for the tensor-core contraction's operand split: x rounded to
+// 10 explicit mantissa bits, ties away from zero.
 float tf32_hi_host(float x) {
     uint32_t u;
     std::memcpy(&u, &x, 4);
@@ -774,22 +773,25 @@ float tf32_hi_host(float x) {
 // of W = X . A with X = T_ij, stored as N = tc3_npad(Rw) rows (J) of
 // K = tc3_kpad(Rw) values (q0), K-major, no swizzle: the core matrix of rows
 // 8i..8i+7 and k = 4j..4j+3 (8 x 16 bytes) at byte (i * K/4 + j) * 128, row
-// n % 8 at +16 * (n % 8); the TF32 high parts first, then the remainders.
+// n % 8 at +16 * (n % 8).  kTc3Parts parts follow each other: the TF32
+// rounding of the coefficient, of what it leaves, and so on (the last part
+// is the FP32 remainder, which the tensor core truncates to TF32).
 void tc3_image(const std::vector<double>& dense, int R, int Rw, std::vector<float>& out) {
     const int kpad = tc3_kpad(Rw), npad = tc3_npad(Rw);
     const size_t base = out.size();
     const size_t part = (size_t)kpad * npad;
-    out.resize(base + 2 * part, 0.0f);
+    out.resize(base + kTc3Parts * part, 0.0f);
     for (int q1 = 0; q1 < R; q1++)
         for (int q2 = 0; q2 < R; q2++)
             for (int k = 0; k < R; k++) {
-                const double a = dense[(size_t)k * R * R + q1 * R + q2];
+                double rest = dense[(size_t)k * R * R + q1 * R + q2];
                 const int n = q1 * Rw + q2;
-                const float hi = tf32_hi_host((float)a);
-                const float lo = (float)(a - (double)hi);
                 const size_t off = ((size_t)(n / 8) * (kpad / 4) + k / 4) * 32 + (n % 8) * 4 + (k % 4);
-                out[base + off] = hi;
-                out[base + part + off] = lo;
+                for (int t = 0; t < kTc3Parts; t++) {
+                    const float v = t + 1 < kTc3Parts ? tf32_hi_host((float)rest) : (float)rest;
+                    out[base + t * part + off] = v;
+                    rest -= (double)v;
+                }
             }
 }
 

@@ -17,10 +17,13 @@
 // another association order; the force and virial epilogue is the other
 // contraction kernels' (cluster_epilogue, FP64).
 //
-// Precision: TF32 keeps 10 mantissa bits, so both operands are split into a
-// TF32 high part and the remainder, and W = Xh.Ah + Xh.Al + Xl.Ah (three MMAs
-// per product; Xl.Al ~ 2^-22 relative is dropped), with FP32 accumulation:
-// about the FP32 contraction's accuracy.  Geometry, the Morse exponential and
+// Precision: TF32 keeps 10 mantissa bits, so both operands are split into
+// three TF32 parts (high h, middle m, low l: each the TF32 rounding of what
+// the previous ones leave) and W = Xh.Ah + Xh.Am + Xm.Ah + Xh.Al + Xl.Ah +
+// Xm.Am (six MMAs per product; the dropped terms are ~2^-33 relative), with
+// FP32 accumulation: the FP32 contraction's accuracy.  (With two parts and
+// three MMAs the error is ~2^-21 per product, 3e-6 of the stress of the
+// reference's HN3 force field.)  Geometry, the Morse exponential and
 // the epilogue stay in FP64, the Chebyshev recursion and cutoff in FP32, as
 // in the other kernels of the mixed form.
 //
@@ -144,25 +147,29 @@ __device__ __forceinline__ void pair_regs(const DevParamSet& P, const TupleRec& 
     }
 }
 
-// One row of an A operand image (K-major, no swizzle): row m's KP values at
-// core-matrix rows; hi and lo parts of v (zero past R, or all zero).
+// One row of an A operand's three part images (K-major, no swizzle; part t
+// at img + t * AFL): row m's KP values at core-matrix rows, split into TF32
+// high / middle / low parts (zero past R, or all zero).
 template <int R, int KP>
-__device__ __forceinline__ void put_row(float* hi, float* lo, int m, const float (&v)[R], bool on) {
+__device__ __forceinline__ void put_row(float* img, int m, const float (&v)[R], bool on) {
     constexpr int SBOF = KP * 8;   // floats between row blocks (KP/4 core matrices of 32 floats)
-    float* rh = hi + (m >> 3) * SBOF + (m & 7) * 4;
-    float* rl = lo + (m >> 3) * SBOF + (m & 7) * 4;
+    constexpr int AFL = 128 * KP;  // floats per part image
+    float* r0 = img + (m >> 3) * SBOF + (m & 7) * 4;
 #pragma unroll
     for (int j = 0; j < KP / 4; j++) {
-        float h[4], l[4];
+        float h[4], md[4], l[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int k = 4 * j + q;
             const float x = (on && k < R) ? v[k < R ? k : 0] : 0.0f;
             h[q] = tf32_hi(x);
-            l[q] = x - h[q];
+            const float rest = x - h[q];
+            md[q] = tf32_hi(rest);
+            l[q] = rest - md[q];
         }
-        *reinterpret_cast<float4*>(rh + j * 32) = make_float4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<float4*>(rl + j * 32) = make_float4(l[0], l[1], l[2], l[3]);
+        *reinterpret_cast<float4*>(r0 + j * 32) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(r0 + AFL + j * 32) = make_float4(md[0], md[1], md[2], md[3]);
+        *reinterpret_cast<float4*>(r0 + 2 * AFL + j * 32) = make_float4(l[0], l[1], l[2], l[3]);
     }
 }
 
@@ -171,16 +178,14 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
                                                   const long long* perm_n, long long perm_cap) {
     constexpr int KP = tc3_kpad(R);                     // K padded to whole MMA steps (8 for TF32)
     constexpr int NP = tc3_npad(R);                     // N padded to 16
-    constexpr int AFL = kTcTile * KP;                   // floats per A image
-    constexpr int BFL = NP * KP;                        // floats per B image part
+    constexpr int AFL = kTcTile * KP;                   // floats per A part image
+    constexpr int BFL = NP * KP;                        // floats per B part image
     constexpr uint32_t LBO = 128, SBO = KP * 32;        // bytes: next core matrix in K; next 8 rows
+    static_assert(kTc3Parts == 3, "the MMA sequence below pairs three parts");
     extern __shared__ __align__(1024) unsigned char smem[];
-    float* Xh = reinterpret_cast<float*>(smem);
-    float* Xl = Xh + AFL;
-    float* Dh = Xl + AFL;
-    float* Dl = Dh + AFL;
-    float* Bh = Dl + AFL;
-    float* Bl = Bh + BFL;
+    float* Xs = reinterpret_cast<float*>(smem);         // T_ij parts h, m, l
+    float* Ds = Xs + 3 * AFL;                           // dT_ij/dr parts
+    float* Bs = Ds + 3 * AFL;                           // coefficient parts
     __shared__ uint32_t s_tmem;
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ long long s_tile;
@@ -226,8 +231,8 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
         // the one in shared memory
         if (Rt->tc_off != loaded || P != loaded_set) {
             const float4* src = reinterpret_cast<const float4*>(P->tc3 + Rt->tc_off + tc3_offset(P->R3, R));
-            float4* dst = reinterpret_cast<float4*>(Bh);
-            for (int q = tid; q < 2 * BFL / 4; q += kTcTile) dst[q] = src[q];
+            float4* dst = reinterpret_cast<float4*>(Bs);
+            for (int q = tid; q < kTc3Parts * BFL / 4; q += kTcTile) dst[q] = src[q];
             loaded = Rt->tc_off;
             loaded_set = P;
         }
@@ -262,25 +267,30 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
             pair_regs<R>(*P, *Rt, 2, dr[2][3], T2, D2, fc, fcd, B.flags);
             fc64[2] = fc; fcd64[2] = fcd;
         }
-        put_row<R, KP>(Xh, Xl, tid, T0, active);
-        put_row<R, KP>(Dh, Dl, tid, D0, active);
+        put_row<R, KP>(Xs, tid, T0, active);
+        put_row<R, KP>(Ds, tid, D0, active);
         // generic-proxy writes of the operands -> visible to the tensor core
         asm volatile("fence.proxy.async.shared::cta;");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t xh = smem_u32(Xh), xl = smem_u32(Xl), dh = smem_u32(Dh), dl = smem_u32(Dl);
-            const uint32_t bh = smem_u32(Bh), bl = smem_u32(Bl);
+            const uint32_t xs = smem_u32(Xs), ds = smem_u32(Ds), bs = smem_u32(Bs);
+            constexpr uint32_t AB = AFL * 4, BB = BFL * 4;   // bytes per part image
+            // part pairs (operand part, coefficient part), smallest first so
+            // that the accumulator is small while the small terms go in (the
+            // tensor core's accumulation rounds each addition at the
+            // accumulator's magnitude): m.m, h.l, l.h, h.m, m.h, then h.h
+            constexpr int pa[6] = {1, 0, 2, 0, 1, 0}, pb[6] = {1, 2, 0, 1, 0, 0};
 #pragma unroll
-            for (int ks = 0; ks < KP / 8; ks++) {
-                const uint32_t o = ks * 256;   // two core matrices along K per step
-                const uint64_t Bhd = umma_desc(bh + o, LBO, SBO), Bld = umma_desc(bl + o, LBO, SBO);
-                mma_tf32(tmem, umma_desc(xh + o, LBO, SBO), Bhd, idesc, ks > 0);
-                mma_tf32(tmem, umma_desc(xh + o, LBO, SBO), Bld, idesc, 1);
-                mma_tf32(tmem, umma_desc(xl + o, LBO, SBO), Bhd, idesc, 1);
-                mma_tf32(tmem + 128, umma_desc(dh + o, LBO, SBO), Bhd, idesc, ks > 0);
-                mma_tf32(tmem + 128, umma_desc(dh + o, LBO, SBO), Bld, idesc, 1);
-                mma_tf32(tmem + 128, umma_desc(dl + o, LBO, SBO), Bhd, idesc, 1);
+            for (int t = 0; t < 6; t++) {
+#pragma unroll
+                for (int ks = 0; ks < KP / 8; ks++) {
+                    const uint32_t o = ks * 256;   // two core matrices along K per step
+                    const uint64_t bd = umma_desc(bs + pb[t] * BB + o, LBO, SBO);
+                    const int accum = ks > 0 || t > 0;
+                    mma_tf32(tmem, umma_desc(xs + pa[t] * AB + o, LBO, SBO), bd, idesc, accum);
+                    mma_tf32(tmem + 128, umma_desc(ds + pa[t] * AB + o, LBO, SBO), bd, idesc, accum);
+                }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 smem_u32(&s_bar)));
@@ -349,7 +359,7 @@ template <int R>
 void launch_tc_r(const BatchView& B, cudaStream_t st) {
     constexpr int KP = tc3_kpad(R);
     constexpr int NP = tc3_npad(R);
-    size_t smem = sizeof(float) * (4 * (size_t)kTcTile * KP + 2 * (size_t)NP * KP);
+    size_t smem = sizeof(float) * (6 * (size_t)kTcTile * KP + kTc3Parts * (size_t)NP * KP);
     if (smem < kTcMinSmem) smem = kTcMinSmem;
     auto kern = k_forcetc3<R>;
     // the kernel's own dynamic size (its static shared memory counts against
