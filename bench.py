@@ -244,7 +244,7 @@ def run_ours(args):
         calc.stage(packed)
         calc.autotune()
     else:   # a fixed launch shape (profiler runs): no autotuning
-        calc.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0}[args.contraction])
+        calc.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0, "tensor": 4}[args.contraction])
         if args.tuning:
             calc.set_tuning(*[int(v) for v in args.tuning.split(",")])
         calc.stage(packed)
@@ -785,7 +785,7 @@ def profile_batched(args):
     if args.contraction == "auto":
         c.autotune()
     else:   # one contraction form at a fixed launch shape, no autotuning
-        c.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0}[args.contraction])
+        c.set_contraction({"factored": 1, "nocache": 2, "noy": 3, "percoef": 0, "tensor": 4}[args.contraction])
         if args.tuning:
             c.set_tuning(*[int(v) for v in args.tuning.split(",")])
         c.stage(c.pack([(x.pos, x.types, x.cell) for x in cfgs]))
@@ -946,7 +946,7 @@ def main():
     ap.add_argument("--profile-batched", action="store_true",
                     help="profiler run of the batched workload (--batch-configs configurations, "
                          "--precision): autotune, 3 warm-up + 2 launches")
-    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "nocache", "noy", "percoef"],
+    ap.add_argument("--contraction", default="auto", choices=["auto", "factored", "nocache", "noy", "percoef", "tensor"],
                     help="autotune (auto) or one fixed 3-/4-body contraction form (profiler runs)")
     ap.add_argument("--tuning", default="",
                     help="with a fixed --contraction: tpc3,tpc4,blocks_per_sm (ck_set_tuning)")

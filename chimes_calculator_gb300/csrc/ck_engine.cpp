@@ -234,8 +234,13 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     // it pays for itself while its tables stay near L2 (measured: ~10% on the
     // 3-body kernel for 25k list entries, nothing for 11M), so large batches
     // compute every pair in the cluster kernel
+    // The tensor-core 3-body kernel reads its ij and ik tables from the cache
+    // at every size: there the cache replaces FP64 work (geometry and Morse
+    // exponential of two of the three pairs, the kernel's bound) with loads
+    // that stay far below the memory bandwidth.
     const bool pc_size = n2_est <= 2.0e6;
-    avail_pc3_ = avail_fact3_ && pc3 && !enum_serial && pc_size;
+    pc_small_ = pc_size;
+    avail_pc3_ = avail_fact3_ && pc3 && !enum_serial && (pc_size || avail_tc3_);
     avail_pc4_ = avail_fact4_ && pc4 && !enum_serial && pc_size;
     tuning.rf3 = rf3;
     tuning.rf4 = rf4;
@@ -371,7 +376,7 @@ static cudaError_t record_stage_event(cudaEvent_t ev, cudaStream_t st) {
 
 Status Engine::enqueue(std::string& err) {
     BatchView B = V_;
-    B.use_pc3 = avail_pc3_ && tuning.fact3 && !tuning.tc3 ? 1 : 0;
+    B.use_pc3 = avail_pc3_ && tuning.fact3 && (tuning.tc3 || pc_small_) ? 1 : 0;
     B.bk_pad3 = tuning.tc3 ? 128 : 32;
     B.use_pc4 = avail_pc4_ && tuning.fact4 ? 1 : 0;
     cudaStream_t st = stream_;
@@ -418,6 +423,7 @@ Status Engine::enqueue(std::string& err) {
     auto body3 = [&](cudaStream_t q) {
         if (L.stride3 <= 0) return;
         if (L.fact3 && L.tc3) {
+            launch_pair_tables(B, d_l2_owner_.p, 3, L, q);
             launch_bucket(B, 3, q);
             launch_force3tc(B, L, q);
         } else if (L.fact3) {

@@ -193,6 +193,7 @@ private:
     bool avail_tc3_ = false;                           // ... and tensor-core 3-body images (mixed form)
     bool enum_serial_ = false;                         // staged batch needs the sequential enumeration
     bool avail_pc3_ = false, avail_pc4_ = false;       // pair-table cache usable for the staged batch
+    bool pc_small_ = false;                            // list small enough for the cache to stay near L2
     DevBuf<int> d_c3e_, d_c4e_;
     DevBuf<double> d_pcd3_, d_pcd4_;
     DevBuf<unsigned char> d_pct3_, d_pct4_;

@@ -684,7 +684,17 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
 #pragma unroll
             for (int p = 0; p < NP; p++) Gp[p] += __shfl_xor_sync(kFull, Gp[p], off);
         }
-        if (active && gl == 0) {
+        if (sizeof(CT) == 4 && active && gl == 0) {   // mixed form: the epilogue in FP32
+            float drf[NP][3], rinv[NP], fcf[NP], fcdf[NP], Gf[NP];
+            for (int p = 0; p < NP; p++) {
+                for (int k = 0; k < 3; k++) drf[p][k] = float(geo[(4 * p + k) * G + grp]);
+                rinv[p] = 1.0f / float(geo[(4 * p + 3) * G + grp]);
+                fcf[p] = float(fcs[p * G + grp]);
+                fcdf[p] = float(fcds[p * G + grp]);
+                Gf[p] = float(Gp[p]);
+            }
+            cluster_epilogue_f32<NB>(B, id, s, drf, rinv, fcf, fcdf, float(S), Gf, acc);
+        } else if (active && gl == 0) {
             double dr[NP][4], fc[NP], fcd[NP], Gd[NP];
             for (int p = 0; p < NP; p++) {
                 for (int k = 0; k < 4; k++) dr[p][k] = geo[(4 * p + k) * G + grp];

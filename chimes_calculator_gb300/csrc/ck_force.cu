@@ -227,7 +227,19 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
 #pragma unroll
             for (int p = 0; p < NP; p++) Gp[p] += __shfl_xor_sync(kFull, Gp[p], off);
         }
-        if (nc > 0 && gl == 0) {
+        if constexpr (sizeof(CT) == 4) {   // mixed form: the epilogue in FP32 (cluster_epilogue_f32)
+            if (nc > 0 && gl == 0) {
+                float drf[NP][3], rinv[NP], fcf[NP], fcdf[NP], Gf[NP];
+                for (int p = 0; p < NP; p++) {
+                    for (int k = 0; k < 3; k++) drf[p][k] = float(geo[4 * p + k]);
+                    rinv[p] = 1.0f / float(geo[4 * p + 3]);
+                    fcf[p] = float(fcs[p]);
+                    fcdf[p] = float(fcds[p]);
+                    Gf[p] = float(Gp[p]);
+                }
+                cluster_epilogue_f32<NB>(B, id, s, drf, rinv, fcf, fcdf, float(S), Gf, acc);
+            }
+        } else if (nc > 0 && gl == 0) {
             double fc[NP], fcd[NP], pre[NP + 1], suf[NP + 1];
             for (int p = 0; p < NP; p++) { fc[p] = fcs[p]; fcd[p] = fcds[p]; }
             pre[0] = 1.0;

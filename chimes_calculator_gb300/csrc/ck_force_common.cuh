@@ -194,5 +194,51 @@ __device__ __forceinline__ void cluster_epilogue(const BatchView& B, const int* 
     tally_atoms(B, id, NB, pre[NP] * S, vir);
 }
 
+// The same for the mixed form, in FP32: the cluster's force scalars, forces
+// and virial derive from the FP32 contraction sums, so they are formed in
+// FP32 (GB300's FP64 pipe issues one warp instruction per 16 cycles per SM,
+// and this epilogue was most of a mixed cluster kernel's FP64 work); the
+// per-atom forces (FP64 atomics) and the system's energy and virial (FP64)
+// are accumulated in FP64.  dr: the pairs' vectors, rinv: 1 / distance.
+template <int NB>
+__device__ __forceinline__ void cluster_epilogue_f32(const BatchView& B, const int* id, int sys, const float (*dr)[3],
+                                                     const float* rinv, const float* fc, const float* fcd, float S,
+                                                     const float* G, EVAcc& acc) {
+    constexpr int NP = Topo<NB>::NP;
+    float pre[NP + 1], suf[NP + 1];
+    pre[0] = 1.0f;
+#pragma unroll
+    for (int p = 0; p < NP; p++) pre[p + 1] = pre[p] * fc[p];
+    suf[NP] = 1.0f;
+#pragma unroll
+    for (int p = NP - 1; p >= 0; p--) suf[p] = suf[p + 1] * fc[p];
+    float f[NB][3];
+#pragma unroll
+    for (int k = 0; k < NB; k++) f[k][0] = f[k][1] = f[k][2] = 0.0f;
+    float v[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        const float fsp = pre[p] * suf[p + 1] * rinv[p] * (fc[p] * G[p] + fcd[p] * S);
+        const int a = Topo<NB>::a(p), b = Topo<NB>::b(p);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            f[a][k] += fsp * dr[p][k];
+            f[b][k] -= fsp * dr[p][k];
+        }
+        v[0] -= fsp * dr[p][0] * dr[p][0];
+        v[1] -= fsp * dr[p][0] * dr[p][1];
+        v[2] -= fsp * dr[p][0] * dr[p][2];
+        v[3] -= fsp * dr[p][1] * dr[p][1];
+        v[4] -= fsp * dr[p][1] * dr[p][2];
+        v[5] -= fsp * dr[p][2] * dr[p][2];
+    }
+#pragma unroll
+    for (int k = 0; k < NB; k++) add_force(B, id[k], double(f[k][0]), double(f[k][1]), double(f[k][2]));
+    const double vir[6] = {double(v[0]), double(v[1]), double(v[2]), double(v[3]), double(v[4]), double(v[5])};
+    const double e = double(pre[NP] * S);
+    acc.add(B, sys, e, vir);
+    tally_atoms(B, id, NB, e, vir);
+}
+
 }  // namespace
 }  // namespace ck

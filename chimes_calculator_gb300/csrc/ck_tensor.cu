@@ -14,8 +14,7 @@
 //   S = sum_b V[b] T_ik[b],   G_ij = sum_b V'[b] T_ik[b],
 //   G_ik = sum_b V[b] dT_ik[b],   G_jk = sum_b V2[b] T_ik[b]
 // which are the sums of compute_3B (chimesFF/src/chimesFF.cpp:2068-2169) in
-// another association order; the force and virial epilogue is the other
-// contraction kernels' (cluster_epilogue, FP64).
+// another association order.
 //
 // Precision: TF32 keeps 10 mantissa bits, so both operands are split into
 // three TF32 parts (high h, middle m, low l: each the TF32 rounding of what
@@ -23,9 +22,14 @@
 // Xm.Am (six MMAs per product; the dropped terms are ~2^-33 relative), with
 // FP32 accumulation: the FP32 contraction's accuracy.  (With two parts and
 // three MMAs the error is ~2^-21 per product, 3e-6 of the stress of the
-// reference's HN3 force field.)  Geometry, the Morse exponential and
-// the epilogue stay in FP64, the Chebyshev recursion and cutoff in FP32, as
-// in the other kernels of the mixed form.
+// reference's HN3 force field.)  Distances (minimum image) and the Morse
+// exponential stay in FP64; the Chebyshev recursion, cutoff and the
+// cluster's force scalars, forces and virial are FP32 (they derive from the
+// FP32 sums); the per-atom force, energy and virial accumulation is FP64.
+// GB300 issues one FP64 warp instruction per 16 cycles per SM, so FP64 work
+// bounds this kernel: with the pair-table cache (k_pair_tables) the geometry,
+// exponential and tables of the pairs ij and ik -- list entries of the
+// cluster's first atom -- are read instead of recomputed per cluster.
 //
 // Work: persistent CTAs of 128 threads (one cluster per thread) take
 // 128-cluster tiles from an atomic queue over the clusters bucketed by
@@ -236,36 +240,63 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
             loaded = Rt->tc_off;
             loaded_set = P;
         }
-        // this thread's cluster: geometry, cutoff early-outs, tables
+        // this thread's cluster: geometry, cutoff early-outs, tables; with
+        // the cache, pairs ij and ik (list entries of atom i) come from it
         const int c = perm[base + tid];
         bool active = c >= 0;
         int id[3] = {0, 0, 0};
         int s = 0;
-        double dr[3][4];
-        double fcd64[3] = {0, 0, 0}, fc64[3] = {0, 0, 0};
+        float drf[3][3], rinv[3] = {0, 0, 0}, fcf[3] = {0, 0, 0}, fcdf[3] = {0, 0, 0};
+        double rr[3] = {0, 0, 0};
+        long long ent[2] = {0, 0};
         float T0[R], D0[R], T1[R], D1[R], T2[R], D2[R];
 #pragma unroll
         for (int q = 0; q < R; q++) T0[q] = D0[q] = T1[q] = D1[q] = T2[q] = D2[q] = 0.0f;
+        const bool use_pc = B.use_pc3 != 0;
         if (active) {
             for (int k = 0; k < 3; k++) id[k] = clusters[3LL * c + k];
             s = B.atom_sys[B.ghost_parent[id[0]]];
-            const double* h = B.sys[s].h;
 #pragma unroll
             for (int p = 0; p < 3; p++) {
                 double d[3], r;
-                pair_geom(B, h, id[Topo<3>::a(p)], id[Topo<3>::b(p)], d, r);
-                dr[p][0] = d[0]; dr[p][1] = d[1]; dr[p][2] = d[2]; dr[p][3] = r;
+                if (use_pc && p < 2) {
+                    ent[p] = B.c3e[2LL * c + p];
+                    const double* g = B.pcd3 + 8 * ent[p];
+                    d[0] = g[0]; d[1] = g[1]; d[2] = g[2]; r = g[3];
+                } else {
+                    pair_geom(B, B.sys[s].h, id[Topo<3>::a(p)], id[Topo<3>::b(p)], d, r);
+                }
+                drf[p][0] = float(d[0]); drf[p][1] = float(d[1]); drf[p][2] = float(d[2]);
+                rr[p] = r;
                 if (r >= Rt->rout[p]) active = false;   // compute_3B's early-outs
             }
         }
         if (active) {
-            float fc, fcd;
-            pair_regs<R>(*P, *Rt, 0, dr[0][3], T0, D0, fc, fcd, B.flags);
-            fc64[0] = fc; fcd64[0] = fcd;
-            pair_regs<R>(*P, *Rt, 1, dr[1][3], T1, D1, fc, fcd, B.flags);
-            fc64[1] = fc; fcd64[1] = fcd;
-            pair_regs<R>(*P, *Rt, 2, dr[2][3], T2, D2, fc, fcd, B.flags);
-            fc64[2] = fc; fcd64[2] = fcd;
+            const int R3 = P->R3;   // the set's own powers; entries above it multiply zero coefficients
+            if (use_pc) {
+                const float* pct = reinterpret_cast<const float*>(B.pct3);
+#pragma unroll
+                for (int p = 0; p < 2; p++) {
+                    const double* g = B.pcd3 + 8 * ent[p];
+                    const float* tab = pct + ent[p] * 2 * R;
+                    float* T = p == 0 ? T0 : T1;
+                    float* D = p == 0 ? D0 : D1;
+#pragma unroll
+                    for (int q = 0; q < R; q++) {
+                        T[q] = q < R3 ? tab[q] : 0.0f;
+                        D[q] = q < R3 ? tab[R + q] : 0.0f;
+                    }
+                    fcf[p] = float(g[4]);
+                    fcdf[p] = float(g[5]);
+                    if (g[6] != 0.0) atomicAdd(&B.flags[4], 1);
+                }
+            } else {
+                pair_regs<R>(*P, *Rt, 0, rr[0], T0, D0, fcf[0], fcdf[0], B.flags);
+                pair_regs<R>(*P, *Rt, 1, rr[1], T1, D1, fcf[1], fcdf[1], B.flags);
+            }
+            pair_regs<R>(*P, *Rt, 2, rr[2], T2, D2, fcf[2], fcdf[2], B.flags);
+#pragma unroll
+            for (int p = 0; p < 3; p++) rinv[p] = 1.0f / float(rr[p]);
         }
         put_row<R, KP>(Xs, tid, T0, active);
         put_row<R, KP>(Ds, tid, D0, active);
@@ -341,8 +372,8 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
                 G1 += V[b] * D1[b];
                 G2 += V2[b] * T1[b];
             }
-            const double G[3] = {double(G0), double(G1), double(G2)};
-            cluster_epilogue<3>(B, id, s, dr, fc64, fcd64, double(S), G, acc);
+            const float G[3] = {G0, G1, G2};
+            cluster_epilogue_f32<3>(B, id, s, drf, rinv, fcf, fcdf, S, G, acc);
         }
         // TMEM and the operand images are rewritten by the next tile
         asm volatile("tcgen05.fence::before_thread_sync;");
