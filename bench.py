@@ -727,7 +727,7 @@ def serving(args):
     arrivals at 1x and 4x the plain path's request rate and at saturation;
     p50/p99 latency and throughput per rate."""
     from chimes_calculator_gb300 import Calculator, synth
-    from chimes_calculator_gb300.serving import Server, poisson_run, serial_run, serving_workload
+    from chimes_calculator_gb300.serving import Server, replay_run, serial_run, serving_workload
     tmp = tempfile.mkdtemp(prefix="cks")
     specs, reqs = serving_workload(args.serve_requests, processes=gen_processes())
     paths = [synth.write_param_file(os.path.join(tmp, "p%d.txt" % k), sp) for k, sp in enumerate(specs)]
@@ -755,10 +755,10 @@ def serving(args):
         tuned = srv.autotune([(cf.pos, tidx(sl, cf), cf.cell) for sl, cf in sample], [sl for sl, _ in sample])
         # warm-up: every request once, back to back, so the workspaces and
         # list capacities reach their steady-state sizes before the timed sweeps
-        poisson_run(srv, reqs, tidx, rate_hz=1e6)
+        replay_run(srv, reqs, tidx, rate_hz=1e6)
         runs = []
         for mult in mults:
-            r = poisson_run(srv, reqs, tidx, rate_hz=mult * base["throughput_req_per_s"])
+            r = replay_run(srv, reqs, tidx, rate_hz=mult * base["throughput_req_per_s"])
             r["offered_over_plain"] = mult if mult < 1e3 else "saturation"
             runs.append(r)
         srv.close()

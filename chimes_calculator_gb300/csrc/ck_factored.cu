@@ -693,7 +693,9 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
                 fcdf[p] = float(fcds[p * G + grp]);
                 Gf[p] = float(Gp[p]);
             }
-            cluster_epilogue_f32<NB>(B, id, s, drf, rinv, fcf, fcdf, float(S), Gf, acc);
+            double e_c, vir_c[6];
+            cluster_epilogue_f32<NB>(B, id, drf, rinv, fcf, fcdf, float(S), Gf, e_c, vir_c);
+            acc.add(B, s, e_c, vir_c);
         } else if (active && gl == 0) {
             double dr[NP][4], fc[NP], fcd[NP], Gd[NP];
             for (int p = 0; p < NP; p++) {

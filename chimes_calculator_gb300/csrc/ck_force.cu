@@ -47,9 +47,15 @@ template <typename CT>
 __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner) {
     const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
     EVAcc acc;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     const long long ntot = n2 > B.n_atoms_total ? n2 : B.n_atoms_total;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ntot; e += stride) {
+    // each block takes one contiguous range of entries (threads striding by
+    // the block size, so loads stay coalesced): a thread's entries then belong
+    // to the same atom and system for long runs, and its energy/virial
+    // accumulator reaches the system's totals with few atomics even when a
+    // batch holds many systems
+    const long long per = ((ntot + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const long long e_end = min(ntot, per * (blockIdx.x + 1));
+    for (long long e = per * blockIdx.x + threadIdx.x; e < e_end; e += blockDim.x) {
         double vir[6] = {0, 0, 0, 0, 0, 0};
         if (e < B.n_atoms_total) {   // compute_1B (chimesFF.cpp:1636-1641)
             const int s = B.atom_sys[e];
@@ -237,7 +243,9 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
                     fcdf[p] = float(fcds[p]);
                     Gf[p] = float(Gp[p]);
                 }
-                cluster_epilogue_f32<NB>(B, id, s, drf, rinv, fcf, fcdf, float(S), Gf, acc);
+                double e_c, vir_c[6];
+                cluster_epilogue_f32<NB>(B, id, drf, rinv, fcf, fcdf, float(S), Gf, e_c, vir_c);
+                acc.add(B, s, e_c, vir_c);
             }
         } else if (nc > 0 && gl == 0) {
             double fc[NP], fcd[NP], pre[NP + 1], suf[NP + 1];

@@ -84,6 +84,28 @@ struct EVAcc {
         v[0] += e;
         for (int k = 0; k < 6; k++) v[1 + k] += vir[k];
     }
+    // Warp-collective (all 32 lanes call it): one interaction's energy and
+    // virial per lane (valid lanes), summed over the warp first when every
+    // valid lane's interaction belongs to one system, so that one lane's
+    // accumulator takes the sum (atomics only when that lane changes system);
+    // otherwise each valid lane adds its own.  Keeps batches of many systems
+    // from turning every interaction into seven atomics on a few addresses.
+    __device__ void add_warp(const BatchView& B, int sys, double e, const double* vir, bool valid) {
+        const int lane = threadIdx.x & 31;
+        const unsigned have = __ballot_sync(kFull, valid);
+        if (!have) return;
+        const int s0 = __shfl_sync(kFull, sys, __ffs(have) - 1);
+        if (__all_sync(kFull, !valid || sys == s0)) {
+            double x[7];
+            x[0] = valid ? e : 0.0;
+            for (int k = 0; k < 6; k++) x[1 + k] = valid ? vir[k] : 0.0;
+            for (int k = 0; k < 7; k++)
+                for (int off = 16; off; off >>= 1) x[k] += __shfl_xor_sync(kFull, x[k], off);
+            if (lane == 0) add(B, s0, x[0], x + 1);
+        } else if (valid) {
+            add(B, sys, e, vir);
+        }
+    }
     // end of kernel: one set of atomics per warp when the warp holds one system
     __device__ void flush_warp(const BatchView& B) {
         const int lane = threadIdx.x & 31;
@@ -200,10 +222,12 @@ __device__ __forceinline__ void cluster_epilogue(const BatchView& B, const int* 
 // and this epilogue was most of a mixed cluster kernel's FP64 work); the
 // per-atom forces (FP64 atomics) and the system's energy and virial (FP64)
 // are accumulated in FP64.  dr: the pairs' vectors, rinv: 1 / distance.
+// The cluster's energy and virial are returned for the caller's (warp-wide)
+// accumulation.
 template <int NB>
-__device__ __forceinline__ void cluster_epilogue_f32(const BatchView& B, const int* id, int sys, const float (*dr)[3],
+__device__ __forceinline__ void cluster_epilogue_f32(const BatchView& B, const int* id, const float (*dr)[3],
                                                      const float* rinv, const float* fc, const float* fcd, float S,
-                                                     const float* G, EVAcc& acc) {
+                                                     const float* G, double& e_out, double* vir_out) {
     constexpr int NP = Topo<NB>::NP;
     float pre[NP + 1], suf[NP + 1];
     pre[0] = 1.0f;
@@ -234,10 +258,9 @@ __device__ __forceinline__ void cluster_epilogue_f32(const BatchView& B, const i
     }
 #pragma unroll
     for (int k = 0; k < NB; k++) add_force(B, id[k], double(f[k][0]), double(f[k][1]), double(f[k][2]));
-    const double vir[6] = {double(v[0]), double(v[1]), double(v[2]), double(v[3]), double(v[4]), double(v[5])};
-    const double e = double(pre[NP] * S);
-    acc.add(B, sys, e, vir);
-    tally_atoms(B, id, NB, e, vir);
+    for (int k = 0; k < 6; k++) vir_out[k] = double(v[k]);
+    e_out = double(pre[NP] * S);
+    tally_atoms(B, id, NB, e_out, vir_out);
 }
 
 }  // namespace

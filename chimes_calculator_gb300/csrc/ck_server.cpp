@@ -191,6 +191,75 @@ public:
         return kOk;
     }
 
+    // Offers a trace of requests at given arrival times (seconds from the
+    // start) from one native thread and takes their results in order from
+    // another, so that a client's own overhead does not cap what the server
+    // shows; writes each request's latency (submit to result) and energy.
+    // Returns the wall time from the first submission to the last result.
+    Status replay(int nreq, const int* slots, const int* natoms, const double* pos, const int* types,
+                  const double* cells, const int* small, const double* arrival, double* latency, double* energy,
+                  double& wall, std::string& err) {
+        std::vector<long long> off(nreq + 1, 0);
+        for (int q = 0; q < nreq; q++) off[q + 1] = off[q] + natoms[q];
+        std::vector<long long> ids(nreq, 0);
+        std::vector<char> ready(nreq, 0);
+        std::mutex mu;
+        std::condition_variable cv;
+        Status sub_status = kOk;
+        std::string sub_err;
+        const double t0 = now_s();
+        std::thread submitter([&] {
+            for (int q = 0; q < nreq; q++) {
+                for (;;) {
+                    const double dt = t0 + arrival[q] - now_s();
+                    if (dt <= 0) break;
+                    if (dt > 2e-4) std::this_thread::sleep_for(std::chrono::duration<double>(dt - 1e-4));
+                }
+                std::string e;
+                long long id = submit(slots[q], natoms[q], pos + 3 * off[q], types + off[q], cells + 9LL * q,
+                                      small ? small[q] != 0 : false, e);
+                std::lock_guard<std::mutex> g(mu);
+                if (id < 0) {
+                    sub_status = (Status)id;
+                    sub_err = e;
+                    for (int r = q; r < nreq; r++) ready[r] = 2;
+                    cv.notify_all();
+                    return;
+                }
+                ids[q] = id;
+                ready[q] = 1;
+                cv.notify_all();
+            }
+        });
+        Status st = kOk;
+        std::vector<double> force;
+        for (int q = 0; q < nreq; q++) {
+            {
+                std::unique_lock<std::mutex> g(mu);
+                cv.wait(g, [&] { return ready[q] != 0; });
+                if (ready[q] == 2) {
+                    st = sub_status;
+                    err = sub_err;
+                    break;
+                }
+            }
+            force.resize(3 * (size_t)natoms[q]);
+            double stress[9], e = 0.0, lat = 0.0;
+            std::string terr;
+            const int r = take(ids[q], true, 600.0, &e, force.data(), stress, &lat, terr);
+            if (r != 1) {
+                st = r < 0 ? (Status)r : kErrTimeout;
+                err = r < 0 ? terr : "request not finished within 600 s";
+                break;
+            }
+            if (latency) latency[q] = lat;
+            if (energy) energy[q] = e;
+        }
+        wall = now_s() - t0;
+        submitter.join();
+        return st;
+    }
+
     void stats(long long* out) {
         std::lock_guard<std::mutex> g(mu_);
         out[0] = submitted_;
@@ -398,6 +467,21 @@ int ck_server_autotune(void* s, int nsys, const int* natoms, const double* pos, 
     }
     std::string err;
     ck::Status st = static_cast<ck::Server*>(s)->autotune(specs, chosen, err);
+    if (st != ck::kOk) return ck::report_error(st, err);
+    return ck::kOk;
+}
+
+int ck_server_replay(void* s, int nreq, const int* slots, const int* natoms, const double* pos, const int* types,
+                     const double* cells, const int* small, const double* arrival_s, double* latency_s,
+                     double* energy, double* wall_s) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    if (nreq <= 0 || !slots || !natoms || !pos || !types || !cells || !arrival_s)
+        return ck::report_error(ck::kErrInput, "empty request trace");
+    std::string err;
+    double wall = 0.0;
+    ck::Status st = static_cast<ck::Server*>(s)->replay(nreq, slots, natoms, pos, types, cells, small, arrival_s,
+                                                        latency_s, energy, wall, err);
+    if (wall_s) *wall_s = wall;
     if (st != ck::kOk) return ck::report_error(st, err);
     return ck::kOk;
 }

@@ -363,6 +363,7 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
                 }
             }
         }
+        double e_c = 0.0, vir_c[6] = {0, 0, 0, 0, 0, 0};
         if (active) {
             float S = 0.0f, G0 = 0.0f, G1 = 0.0f, G2 = 0.0f;
 #pragma unroll
@@ -373,8 +374,9 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
                 G2 += V2[b] * T1[b];
             }
             const float G[3] = {G0, G1, G2};
-            cluster_epilogue_f32<3>(B, id, s, drf, rinv, fcf, fcdf, S, G, acc);
+            cluster_epilogue_f32<3>(B, id, drf, rinv, fcf, fcdf, S, G, e_c, vir_c);
         }
+        acc.add_warp(B, s, e_c, vir_c, active);
         // TMEM and the operand images are rewritten by the next tile
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();

@@ -173,19 +173,57 @@ def poisson_run(server: Server, requests: Sequence[Tuple[int, object]], type_idx
             "mean_ms": 1e3 * float(lat.mean()), "stats": server.stats()}
 
 
+def replay_run(server: Server, requests: Sequence[Tuple[int, object]], type_idx, rate_hz: float,
+               seed: int = 7) -> dict:
+    """Poisson arrivals (mean rate rate_hz) offered by the server's native
+    replay driver (ck_server_replay): the same measurement as poisson_run
+    without the Python client's per-request cost."""
+    rng = np.random.default_rng(seed)
+    arrival = np.cumsum(rng.exponential(1.0 / rate_hz, size=len(requests)))
+    slots = np.array([s for s, _ in requests], dtype=np.int32)
+    natoms = np.array([c.n_atoms for _, c in requests], dtype=np.int32)
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(c.pos, dtype=np.float64) for _, c in requests]))
+    types = np.ascontiguousarray(np.concatenate([np.asarray(type_idx(s, c), dtype=np.int32) for s, c in requests]))
+    cells = np.ascontiguousarray(np.stack([np.asarray(c.cell, dtype=np.float64).reshape(9) for _, c in requests]))
+    lat = np.zeros(len(requests))
+    wall = ctypes.c_double()
+    rc = server.lib.ck_server_replay(server.h, len(requests), _ip(slots), _ip(natoms), _dp(pos), _ip(types),
+                                     _dp(cells), None, _dp(arrival), _dp(lat), None, ctypes.byref(wall))
+    if rc != 0:
+        raise ChimesError(server.lib.ck_last_error().decode())
+    atoms = int(natoms.sum())
+    return {"offered_rate_hz": rate_hz, "requests": len(requests), "wall_s": wall.value,
+            "throughput_atoms_per_s": atoms / wall.value, "throughput_req_per_s": len(requests) / wall.value,
+            "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "mean_ms": 1e3 * float(lat.mean()), "client": "native replay (ck_server_replay)",
+            "stats": server.stats()}
+
+
 def serial_run(calc: Calculator, requests: Sequence[Tuple[int, object]], type_idx) -> dict:
-    """The plain per-request GPU path: one evaluation at a time."""
-    lat = []
-    atoms = 0
-    t0 = time.perf_counter()
+    """The plain per-request GPU path: one evaluation at a time through the
+    C ABI (ck_calculate_batch with one configuration, host arrays in and
+    out).  Each request's arguments are marshalled before the timing, so the
+    times hold the library call alone."""
+    prepared = []
     for slot, cfg in requests:
-        ty = type_idx(slot, cfg)
-        a = time.perf_counter()
-        calc.evaluate(cfg.pos, ty, cfg.cell, slot=slot)
-        lat.append(time.perf_counter() - a)
-        atoms += cfg.n_atoms
+        n = cfg.n_atoms
+        prepared.append((np.array([n], dtype=np.int32), np.ascontiguousarray(cfg.pos, dtype=np.float64),
+                         np.ascontiguousarray(type_idx(slot, cfg), dtype=np.int32),
+                         np.ascontiguousarray(np.asarray(cfg.cell, dtype=np.float64).reshape(9)),
+                         np.zeros(1, dtype=np.int32), np.array([slot], dtype=np.int32), np.zeros(1),
+                         np.zeros((n, 3)), np.zeros(9)))
+    args = [tuple(_ip(a) if a.dtype == np.int32 else _dp(a) for a in pr) for pr in prepared]
+    lib, h = calc.lib, calc.h
+    lat = np.zeros(len(requests))
+    t0 = time.perf_counter()
+    for q, a in enumerate(args):
+        t = time.perf_counter()
+        rc = lib.ck_calculate_batch(h, 1, *a)
+        lat[q] = time.perf_counter() - t
+        if rc != 0:
+            raise ChimesError(lib.ck_last_error().decode())
     wall = time.perf_counter() - t0
-    lat = np.array(lat)
+    atoms = sum(c.n_atoms for _, c in requests)
     return {"requests": len(requests), "wall_s": wall, "throughput_atoms_per_s": atoms / wall,
             "throughput_req_per_s": len(requests) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99))}
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "api": "ck_calculate_batch, one configuration per call"}

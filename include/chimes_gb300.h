@@ -202,6 +202,15 @@ int ck_server_take(void *server, long long id, int wait, double timeout_s, doubl
  * 4-body cluster, resident blocks per SM. */
 int ck_server_autotune(void *server, int nsys, const int *natoms, const double *pos, const int *types,
                        const double *cells, const int *small, const int *pset, int *chosen);
+/* Offers a trace of nreq requests (arrays as for ck_calculate_batch, plus
+ * their parameter slots) at arrival_s[q] seconds after the call starts, from
+ * a native submitting thread, and takes the results in order on the calling
+ * thread: latency_s[q] (submit to result) and energy[q] (either may be NULL),
+ * wall_s = first submission to last result.  Measures the server without a
+ * client's per-request overhead. */
+int ck_server_replay(void *server, int nreq, const int *slots, const int *natoms, const double *pos,
+                     const int *types, const double *cells, const int *small, const double *arrival_s,
+                     double *latency_s, double *energy, double *wall_s);
 /* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
 int ck_server_stats(void *server, long long *out);
 

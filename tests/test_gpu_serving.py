@@ -95,3 +95,40 @@ def test_admission_under_tiny_budget_and_failure_isolation(workload, native_lib)
     for a, b in zip(solo, got):
         assert abs(a["energy"] - b["energy"]) <= E_REL_TOL * max(1.0, abs(a["energy"]))
     assert st["largest_batch"] == 1          # the budget admits one request at a time
+
+
+def test_native_replay_driver(workload, native_lib):
+    """ck_server_replay (the native client the serving measurement uses) serves
+    every request of a Poisson trace, after autotuning on a sample (which may
+    pick another contraction form than the default), with the energies of the
+    requests evaluated alone within the mixed form's budget and positive
+    latencies."""
+    import ctypes
+
+    from chimes_calculator_gb300.serving import Server, _dp, _ip
+    paths, reqs = workload
+    calc, solo = _solo(paths, reqs, 1)
+    srv = Server(workers=3, precision=1, max_batch_atoms=2000)
+    try:
+        for p in paths:
+            srv.load_params(p)
+        srv.autotune([(cfg.pos, calc.type_indices(cfg.types, s), cfg.cell) for s, cfg in reqs[:6]],
+                     [s for s, _ in reqs[:6]])
+        arrival = np.cumsum(np.random.default_rng(3).exponential(1e-4, size=len(reqs)))
+        slots = np.array([s for s, _ in reqs], dtype=np.int32)
+        natoms = np.array([c.n_atoms for _, c in reqs], dtype=np.int32)
+        pos = np.ascontiguousarray(np.concatenate([c.pos for _, c in reqs]))
+        types = np.ascontiguousarray(np.concatenate([calc.type_indices(c.types, s) for s, c in reqs]).astype(np.int32))
+        cells = np.ascontiguousarray(np.stack([c.cell.reshape(9) for _, c in reqs]))
+        lat, en = np.zeros(len(reqs)), np.zeros(len(reqs))
+        wall = ctypes.c_double()
+        rc = srv.lib.ck_server_replay(srv.h, len(reqs), _ip(slots), _ip(natoms), _dp(pos), _ip(types), _dp(cells),
+                                      None, _dp(arrival), _dp(lat), _dp(en), ctypes.byref(wall))
+        assert rc == 0, srv.lib.ck_last_error()
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st["completed"] == len(reqs)
+    assert np.all(lat > 0) and wall.value > 0
+    for a, e in zip(solo, en):
+        assert abs(a["energy"] - e) <= MIXED_E_REL_TOL * max(1.0, abs(a["energy"]))
