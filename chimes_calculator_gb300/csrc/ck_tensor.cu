@@ -81,7 +81,8 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
     float* Bs = Ds + 3 * AFL;                           // coefficient parts
     __shared__ uint32_t s_tmem;
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ long long s_tile;
+    __shared__ long long s_tile, s_next;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const long long n = min(*perm_n, perm_cap);
@@ -206,9 +207,9 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    asm volatile("tcgen05.fence::before_thread_sync;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
                            ((uint32_t)(kTcTile >> 4) << 24);
@@ -217,10 +218,17 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
     const DevParamSet* loaded_set = nullptr;
     EVAcc acc;
 
+    // tiles are claimed one ahead, so that each thread can prefetch its next
+    // cluster's data into L2 while the current tile's MMAs run
+    if (tid == 0) s_next = (long long)atomicAdd(&B.queue[0], 1ull);
     for (;;) {
-        if (tid == 0) s_tile = (long long)atomicAdd(&B.queue[0], 1ull);
+        if (tid == 0) {
+            s_tile = s_next;
+            s_next = s_next < ntiles ? (long long)atomicAdd(&B.queue[0], 1ull) : ntiles;
+        }
         __syncthreads();
         const long long tile = s_tile;
+        const long long next = s_next;
         if (tile >= ntiles) break;
         const long long base = tile * kTcTile;
         const int c0 = perm[base];
@@ -301,10 +309,10 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
         put_row<R, KP>(Xs, tid, T0, active);
         put_row<R, KP>(Ds, tid, D0, active);
         // generic-proxy writes of the operands -> visible to the tensor core
-        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t xs = smem_u32(Xs), ds = smem_u32(Ds), bs = smem_u32(Bs);
             constexpr uint32_t AB = AFL * 4, BB = BFL * 4;   // bytes per part image
             // part pairs (operand part, coefficient part), smallest first so
@@ -324,7 +332,31 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(&s_bar)));
+                             smem_u32(&s_bar))
+                         : "memory");
+        }
+        // prefetch the next tile's cluster data (list, pair-table entries,
+        // positions) into L2 while the MMAs run
+        if (next < ntiles) {
+            const int cn = perm[next * kTcTile + tid];
+            if (cn >= 0) {
+                const int* ids = clusters + 3LL * cn;
+                const int g0 = ids[0], g2 = ids[2];
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(B.ghost_fs + 3LL * g0));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(B.ghost_fs + 3LL * ids[1]));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(B.ghost_fs + 3LL * g2));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(B.ghost_parent + g0));
+                if (use_pc) {
+                    const long long e0 = B.c3e[2LL * cn], e1 = B.c3e[2LL * cn + 1];
+                    const float* pct = reinterpret_cast<const float*>(B.pct3);
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(B.pcd3 + 8 * e0));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(B.pcd3 + 8 * e1));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pct + e0 * 2 * R));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pct + e0 * 2 * R + R + R - 1));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pct + e1 * 2 * R));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(pct + e1 * 2 * R + R + R - 1));
+                }
+            }
         }
         // bounded wait for the MMAs of this tile (non-blocking polls, then a back-off)
         uint32_t done = 0;
@@ -332,7 +364,8 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
             asm volatile(
                 "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                 : "=r"(done)
-                : "r"(smem_u32(&s_bar)), "r"(phase));
+                : "r"(smem_u32(&s_bar)), "r"(phase)
+                : "memory");
             if (!done && it > 256) __nanosleep(32);
         }
         phase ^= 1u;
@@ -340,7 +373,7 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
             if (tid == 0) atomicOr(&B.flags[7], 1);
             break;
         }
-        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         // this thread's TMEM row (lane = tid): W at columns [0, NP), W' at [128, 128 + NP)
         float V[R], V2[R], Vp[R];
 #pragma unroll
@@ -351,7 +384,7 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
             float w[16], wp[16];
             tmem_ld16(row + 16 * q, w);
             tmem_ld16(row + 128 + 16 * q, wp);
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
             for (int u = 0; u < 16; u++) {
                 const int j = 16 * q + u;
@@ -378,13 +411,13 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
         }
         acc.add_warp(B, s, e_c, vir_c, active);
         // TMEM and the operand images are rewritten by the next tile
-        asm volatile("tcgen05.fence::before_thread_sync;");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
     }
     acc.flush_warp(B);
-    asm volatile("tcgen05.fence::before_thread_sync;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
 }
 
