@@ -102,14 +102,17 @@ SIGNATURES = {
 
 
 def load() -> ctypes.CDLL:
-    """Loads the native library (raises if it has not been built)."""
+    """Loads the native library (raises if it has not been built).  The
+    environment variable CHIMES_GB300_LIB selects another build of it (the
+    checked build, libchimescalc_bounds.so, for instance)."""
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
+    path = os.environ.get("CHIMES_GB300_LIB") or LIB_PATH
+    if not os.path.exists(path):
         raise RuntimeError("native library %s is missing: build it with "
-                           "chimes_calculator_gb300.build.build() (there is no CPU fallback)" % LIB_PATH)
-    lib = ctypes.CDLL(LIB_PATH)
+                           "chimes_calculator_gb300.build.build() (there is no CPU fallback)" % path)
+    lib = ctypes.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name, None)
         if fn is None:

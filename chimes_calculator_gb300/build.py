@@ -50,8 +50,14 @@ def _compile(cmd):
     return p.stderr
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles the library if needed and returns its path."""
+BOUNDS_LIB = os.path.join(HERE, "libchimescalc_bounds.so")
+
+
+def build(force: bool = False, verbose: bool = False, bounds: bool = False) -> str:
+    """Compiles the library if needed and returns its path.  bounds=True
+    builds the checked variant libchimescalc_bounds.so instead: the CUDA
+    sources compiled with -DCK_BOUNDS (index checks that raise an error flag
+    and skip the access), the host objects shared with the normal build."""
     if not os.path.exists(NVCC):
         raise RuntimeError("nvcc not found at %s" % NVCC)
     os.makedirs(BUILD, exist_ok=True)
@@ -68,25 +74,28 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if force or _stale(o, s, headers):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                          *inc, "-c", s, "-o", o])
+    cu_dir = os.path.join(BUILD, "bounds") if bounds else BUILD
+    os.makedirs(cu_dir, exist_ok=True)
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
         if not os.path.exists(s):
             continue
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(cu_dir, src + ".o")
         objs.append(o)
         if force or _stale(o, s, headers):
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                         *inc, "-c", s, "-o", o])
+                         *(["-DCK_BOUNDS"] if bounds else []), *inc, "-c", s, "-o", o])
     if jobs:
         with concurrent.futures.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
             for err in ex.map(_compile, jobs):
                 if verbose and err.strip():
                     print(err, file=sys.stderr)
-    if jobs or force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        tmp = LIB + ".tmp"
+    lib = BOUNDS_LIB if bounds else LIB
+    if jobs or force or not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        tmp = lib + ".tmp"
         _compile([NVCC, *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt"])
-        shutil.move(tmp, LIB)
-    return LIB
+        shutil.move(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

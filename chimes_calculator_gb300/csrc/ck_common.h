@@ -181,6 +181,9 @@ struct DevParamSet {
     // tc3_k, tc3_n = K and N at Rw = R3; null when R3 is 0 or above kTc3MaxR
     int tc3_k, tc3_n;
     const float* tc3;
+    // table lengths, for the index checks of the checked build (CK_BOUNDS):
+    // 3-/4-body coefficients, factored entries, tensor-core image floats
+    long long n_c3, n_c4, n_fe3, n_fe4, n_tc3;
     const FactRow* fr3; const FactEntD* fe3d; const FactEntF* fe3f;
     const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
     // per-pair-type tables [npairs] (null when some tuple's cutoffs differ by tuple)

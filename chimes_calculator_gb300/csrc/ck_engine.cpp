@@ -556,6 +556,10 @@ Status Engine::collect(double* force_out, std::vector<SystemResult>& res, std::s
         err = "tensor-core contraction: a bounded wait for the matrix units expired";
         return kErrTimeout;
     }
+    if (f[7] & 2) {
+        err = "checked build: an index outside its array was found and the access skipped";
+        return kErrState;
+    }
     if (f[1]) {
         err = f[1] == 1 ? "negative bin computed (check box lengths and atom coordinates)"
                         : f[1] == 3 ? "bad bin computed for a real atom (check box lengths and atom coordinates)"

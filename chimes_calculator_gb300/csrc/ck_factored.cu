@@ -491,7 +491,9 @@ __global__ void __launch_bounds__(32) k_forcef(BatchView B, const int* clusters,
 
         const auto* ent = fact_ent<CT, NB>(*P);
         const FactRow* rows = (NB == 3 ? P->fr3 : P->fr4) + R->f_row;
-        const int nrow = R->f_nrow, ncol = R->f_ncol;
+        int nrow = R->f_nrow, ncol = R->f_ncol;
+        if (!ck_bound(B, R->f_ent >= 0 && R->f_ent + 2LL * R->ncoef <= (NB == 3 ? P->n_fe3 : P->n_fe4)))
+            nrow = ncol = 0;
         CT S = CT(0), Gp[NP];
 #pragma unroll
         for (int p = 0; p < NP; p++) Gp[p] = CT(0);

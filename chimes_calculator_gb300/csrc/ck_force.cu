@@ -70,7 +70,9 @@ __global__ void __launch_bounds__(256) k_force2(BatchView B, const int* l2_owner
         const int gi = B.atom_self[r];
         const int gj = B.l2_ghost[e];
         const int t0 = B.atom_type[r], t1 = B.atom_type[B.ghost_parent[gj]];
-        const PairRec pr = P.pairs[P.pair_map[t0 * P.ntypes + t1]];
+        int pidx = P.pair_map[t0 * P.ntypes + t1];
+        if (!ck_bound(B, pidx >= 0 && pidx < P.npairs)) continue;
+        const PairRec pr = P.pairs[pidx];
         double dr[3], dist;
         pair_geom(B, d.h, gi, gj, dr, dist);
         if (dist >= pr.rout) continue;
@@ -203,13 +205,15 @@ __global__ void __launch_bounds__(128) k_forcen(BatchView B, const int* clusters
         if (nc > 0) {
             const CT* cf = coefn<CT, NB>(*P) + R->coef_off;
             const uint32_t* pw = (NB == 3 ? P->p3 : P->p4) + R->coef_off;
+            if (!ck_bound(B, R->coef_off >= 0 && R->coef_off + (long long)nc <= (NB == 3 ? P->n_c3 : P->n_c4))) nc = 0;
             for (int k = gl; k < nc; k += TPC) {
                 const CT a = cf[k];
                 const uint32_t pk = pw[k];
                 CT t[NP], dd[NP];
 #pragma unroll
                 for (int p = 0; p < NP; p++) {
-                    const int q = (pk >> (kPowBits * p)) & 31u;
+                    int q = (pk >> (kPowBits * p)) & 31u;
+                    if (!ck_bound(B, q < stride)) q = 0;
                     t[p] = T[p * stride + q];
                     dd[p] = D[p * stride + q];
                 }

@@ -19,7 +19,27 @@ cudaError_t allow_max_smem(const void* kernel);
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+
+// Checked build (compiled with -DCK_BOUNDS, libchimescalc_bounds.so): index
+// checks on the arrays the cluster kernels index with computed values --
+// ghost slots, caller atoms, type tuples, coefficient and factored-entry
+// ranges, Chebyshev powers, tensor-core images.  A failed check raises bit 2
+// of flags[7] and the access is skipped (the call then returns an error); it
+// never traps.  In the normal build the checks compile to nothing.
+#ifdef CK_BOUNDS
+__device__ __forceinline__ bool ck_bound(const BatchView& B, bool ok) {
+    if (!ok) atomicOr(&B.flags[7], 2);
+    return ok;
+}
+#else
+__device__ __forceinline__ bool ck_bound(const BatchView&, bool) { return true; }
+#endif
 __device__ __forceinline__ void pair_geom(const BatchView& B, const double* h, int ga, int gb, double* dr, double& r) {
+    if (!ck_bound(B, ga >= 0 && ga < B.n_ghost_total && gb >= 0 && gb < B.n_ghost_total)) {
+        dr[0] = dr[1] = dr[2] = 0.0;
+        r = 1e300;   // beyond every cutoff: the cluster is dropped
+        return;
+    }
     const double* fa = &B.ghost_fs[3 * (long long)ga];
     const double* fb = &B.ghost_fs[3 * (long long)gb];
     const double dx = fb[0] - fa[0], dy = fb[1] - fa[1], dz = fb[2] - fa[2];
@@ -33,16 +53,23 @@ __device__ __forceinline__ void pair_geom(const BatchView& B, const double* h, i
 template <int NB>
 __device__ __forceinline__ const TupleRec* cluster_tuple(const BatchView& B, const int* clusters, long long c,
                                                          int* id, int& s, const DevParamSet*& P, int& u) {
-    for (int k = 0; k < NB; k++) id[k] = clusters[(long long)NB * c + k];
+    for (int k = 0; k < NB; k++) {
+        id[k] = clusters[(long long)NB * c + k];
+        if (!ck_bound(B, id[k] >= 0 && id[k] < B.n_ghost_total)) id[k] = 0;
+    }
     s = B.atom_sys[B.ghost_parent[id[0]]];
     P = &B.psets[B.sys[s].pset];
     u = 0;
     for (int k = 0; k < NB; k++) u = u * P->ntypes + B.atom_type[B.ghost_parent[id[k]]];
+    int ntup = 1;
+    for (int k = 0; k < NB; k++) ntup *= P->ntypes;
+    if (!ck_bound(B, u >= 0 && u < ntup)) u = 0;
     return (NB == 3 ? P->t3 : P->t4) + u;
 }
 
 __device__ __forceinline__ void add_force(const BatchView& B, int ghost, double fx, double fy, double fz) {
     const int o = B.atom_orig[B.ghost_parent[ghost]];
+    if (!ck_bound(B, o >= 0 && o < B.n_in_total)) return;
     atomicAdd(&B.force[3 * (long long)o + 0], fx);
     atomicAdd(&B.force[3 * (long long)o + 1], fy);
     atomicAdd(&B.force[3 * (long long)o + 2], fz);

@@ -338,6 +338,10 @@ Status calculate_noalloc(Engine& eng, int slot, int natom, const double* d_pos, 
               "; the outputs are not valid";
         return kErrInput;
     }
+    if (flags[7] & 2) {
+        err = "ck_calculate_noalloc: checked build: an index outside its array was found and the access skipped";
+        return kErrState;
+    }
     if (flags[0] & 1) {
         err = "ck_calculate_noalloc: the bin grid exceeds its capacity (" + std::to_string(kNaBins) +
               " bins); the outputs are not valid";

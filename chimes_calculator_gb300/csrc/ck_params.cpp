@@ -1027,8 +1027,11 @@ ParamImage pack_params(const HostParams& P) {
             H.tc3_k = tc3_kpad(R_pow);
             H.tc3_n = tc3_npad(R_pow);
             H.tc3 = as_off<const float>(B.add(tcimg.data(), tcimg.size()));
+            H.n_tc3 = (long long)tcimg.size();
         }
         if (nb == 3) {
+            H.n_c3 = (long long)cd.size();
+            H.n_fe3 = (long long)fed.size();
             H.t3 = as_off<const TupleRec>(tro); H.c3d = as_off<const double>(cdo);
             H.c3f = as_off<const float>(cfo); H.p3 = as_off<const uint32_t>(pwo);
             H.R3 = Rf;
@@ -1036,6 +1039,8 @@ ParamImage pack_params(const HostParams& P) {
             H.fr3 = as_off<const FactRow>(fro); H.fe3d = as_off<const FactEntD>(fdo);
             H.fe3f = as_off<const FactEntF>(ffo);
         } else {
+            H.n_c4 = (long long)cd.size();
+            H.n_fe4 = (long long)fed.size();
             H.t4 = as_off<const TupleRec>(tro); H.c4d = as_off<const double>(cdo);
             H.c4f = as_off<const float>(cfo); H.p4 = as_off<const uint32_t>(pwo);
             H.R4 = Rf;

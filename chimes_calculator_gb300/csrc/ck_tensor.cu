@@ -242,7 +242,9 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
         // the tuple's coefficient image at this kernel's width, when it is not
         // the one in shared memory
         if (Rt->tc_off != loaded || P != loaded_set) {
-            const float4* src = reinterpret_cast<const float4*>(P->tc3 + Rt->tc_off + tc3_offset(P->R3, R));
+            const long long img = Rt->tc_off + tc3_offset(P->R3, R);
+            const bool img_ok = ck_bound(B, Rt->tc_off >= 0 && img + (long long)kTc3Parts * BFL <= P->n_tc3);
+            const float4* src = reinterpret_cast<const float4*>(P->tc3 + (img_ok ? img : 0));
             float4* dst = reinterpret_cast<float4*>(Bs);
             for (int q = tid; q < kTc3Parts * BFL / 4; q += kTcTile) dst[q] = src[q];
             loaded = Rt->tc_off;
