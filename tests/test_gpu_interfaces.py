@@ -209,3 +209,37 @@ def test_error_reporting(golden, native_lib):
         c.evaluate(g.cfg.pos[:2], g.cfg.types[:2], np.diag([9.0, 9.0, 0.0]))
     r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell)   # the handle stays usable
     assert abs(r["energy"] - g.energy) <= E_REL_TOL * abs(g.energy)
+
+
+def test_badness_and_diagnostics(golden, native_lib):
+    """The penalty fixture has pairs inside the penalty region and below the inner
+    cutoff: the badness the GPU reports (get_badness, chimesFF.h:388-429) equals
+    the oracle's, and penalty hits and below-rin pairs are counted."""
+    from chimes_calculator_gb300 import Calculator
+    from oracle.oracle import Oracle
+    g = golden["penalty"]
+    c = Calculator()
+    c.load_params(g.params)
+    r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell)
+    d = c.diagnostics()
+    ref = Oracle(g.params).calculate(g.cfg.pos, g.cfg.types, g.cfg.cell)
+    assert d["badness"] == ref["badness"] and d["badness"] > 0
+    assert d["penalty_hits"] > 0
+    assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
+
+
+@pytest.mark.parametrize("name", ["c2", "ref_hn3", "triclinic"])
+def test_parameter_cache_evaluates_like_text(golden, native_lib, tmp_path, name):
+    """A set loaded from the binary parameter cache (ck_convert_params) gives the
+    reference's results, as the text file does."""
+    from chimes_calculator_gb300 import Calculator
+    g = golden[name]
+    native_lib.ck_set_error_mode(1)
+    cache = str(tmp_path / "p.ckpc")
+    assert native_lib.ck_convert_params(g.params.encode(), cache.encode()) == 0, native_lib.ck_last_error()
+    c = Calculator()
+    c.load_params(cache)
+    r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell, small=g.small)
+    assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
+    assert g.force_error(r["force"]) <= F_ABS_TOL
+    assert np.abs(r["stress"] - g.stress).max() <= S_ABS_TOL
