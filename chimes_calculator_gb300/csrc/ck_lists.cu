@@ -614,120 +614,265 @@ __global__ void k_enum(BatchView B, const int* l2_owner) {
     }
 }
 
-// Warp-per-entry form of the same enumeration.  When the 4-body outer cutoff
+// Per-entry warp form of the same enumeration.  When the 4-body outer cutoff
 // does not exceed the 3-body one (or a system lacks one of the two), the
 // valid_3mer / valid_4mer flags are restored before every k (the reference's
 // reset branch), so each k -- and each l -- is decided on its own: lanes take
 // consecutive k (then l) of the atom's list and a ballot plus prefix count
 // emits the clusters in the reference's (k, l) order.  Systems with 3- and
-// 4-body terms and rc4 > rc3 keep the sequential carry-over (k_enum).
+// 4-body terms and rc4 > rc3 keep the sequential carry-over (k_enum).  Used
+// by k_enuma for atoms whose list is longer than its bit matrices hold.
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_enumw(BatchView B, const int* l2_owner) {
-    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+__device__ void enumw_entry(const BatchView& B, long long e, int r, const SysDesc& d, int lane, unsigned lt) {
     const float4* vec = reinterpret_cast<const float4*>(B.l2_vec);
-    for (long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < B.n2_cap; e += nwarps) {
-        if (e >= n2) {
-            if (!FILL && lane == 0) { B.e_cnt3[e] = 0; B.e_cnt4[e] = 0; }
+    const double c3 = d.c3, c4 = d.c4;
+    const float4 vj = vec[e];
+    const unsigned wj = __float_as_uint(vj.w);
+    const bool want3 = d.has3 && (wj & kL2In3), want4 = d.has4 && (wj & kL2In4);
+    long long n3 = 0, n4 = 0;
+    long long o3 = 0, o4 = 0;
+    if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
+    if (want3 || want4) {
+        const double* hn = d.hn;   // read in place: the exact distances are rare
+        const float c3lo = d.c3lo, c3hi = d.c3hi, c4lo = d.c4lo, c4hi = d.c4hi;
+        const int gi = B.atom_self[r];
+        const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
+        const int jj = B.l2_ghost[e];
+        const double* fj = &B.ghost_fn[3 * (long long)jj];
+        const int pj = (int)(wj & kL2Parent);
+        for (long long kb = b0; kb < b1; kb += 32) {
+            const long long k = kb + lane;
+            bool ok3 = false, ok4 = false;
+            int kk = -1, pk = 0;
+            float4 vk = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < b1) {
+                kk = B.l2_ghost[k];
+                vk = vec[k];
+                const unsigned wk = __float_as_uint(vk.w);
+                pk = (int)(wk & kL2Parent);
+                if (kk != jj && pj <= pk) {
+                    const PairDistF jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk)};
+                    ok3 = want3 && (wk & kL2In3) && !jk.ge(c3, c3lo, c3hi);
+                    ok4 = want4 && (wk & kL2In4) && !jk.ge(c4, c4lo, c4hi);
+                }
+            }
+            const unsigned m3 = __ballot_sync(kFull, ok3);
+            if (FILL && ok3) {
+                const long long q = o3 + n3 + __popc(m3 & lt);
+                if (q < B.n3_cap) {
+                    int* out = B.c3 + 3 * q;
+                    out[0] = gi; out[1] = jj; out[2] = kk;
+                    if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)k; }
+                }
+            }
+            n3 += __popc(m3);
+            unsigned m4 = __ballot_sync(kFull, ok4);
+            while (m4) {
+                const int src = __ffs(m4) - 1;
+                m4 &= m4 - 1;
+                const int ks = __shfl_sync(kFull, kk, src);
+                const int pks = __shfl_sync(kFull, pk, src);
+                float4 vks;
+                vks.x = __shfl_sync(kFull, vk.x, src);
+                vks.y = __shfl_sync(kFull, vk.y, src);
+                vks.z = __shfl_sync(kFull, vk.z, src);
+                vks.w = 0.f;
+                const double* fk = &B.ghost_fn[3 * (long long)ks];
+                for (long long lb = b0; lb < b1; lb += 32) {
+                    const long long l = lb + lane;
+                    bool okl = false;
+                    int ll = -1;
+                    if (l < b1) {
+                        ll = B.l2_ghost[l];
+                        const float4 vl = vec[l];
+                        if (ll != jj && ll != ks) {
+                            const unsigned wl = __float_as_uint(vl.w);
+                            const int pl = (int)(wl & kL2Parent);
+                            if (pj <= pl && pks <= pl && (wl & kL2In4)) {
+                                const double* fl = &B.ghost_fn[3 * (long long)ll];
+                                const PairDistF jl{hn, fj, fl, vdist(vj, vl)};
+                                if (!jl.ge(c4, c4lo, c4hi)) {
+                                    const PairDistF kl{hn, fk, fl, vdist(vks, vl)};
+                                    okl = !kl.ge(c4, c4lo, c4hi);
+                                }
+                            }
+                        }
+                    }
+                    const unsigned ml = __ballot_sync(kFull, okl);
+                    if (FILL && okl) {
+                        const long long q = o4 + n4 + __popc(ml & lt);
+                        if (q < B.n4_cap) {
+                            int* out = B.c4 + 4 * q;
+                            out[0] = gi; out[1] = jj; out[2] = ks; out[3] = ll;
+                            if (B.c4e) {
+                                B.c4e[3 * q] = (int)e;
+                                B.c4e[3 * q + 1] = (int)(kb + src);
+                                B.c4e[3 * q + 2] = (int)l;
+                            }
+                        }
+                    }
+                    n4 += __popc(ml);
+                }
+            }
+        }
+    }
+    if (!FILL && lane == 0) { B.e_cnt3[e] = (int)n3; B.e_cnt4[e] = (int)n4; }
+}
+
+// Bit-matrix form (one block per atom i, atoms with at most kEnumRows list
+// entries).  With the reset semantics above, membership depends only on pair
+// tests among the entries of i's list:
+//   T[j][k] = want3(j) && in3(k) && j != k && parent(j) <= parent(k) && |r_jk| < rc3
+//   Q[j][k] = want4(j) && in4(k) && j != k && parent(j) <= parent(k) && |r_jk| < rc4
+// (i, j, k) is a triplet iff T[j][k]; (i, j, k, l) a quadruplet iff Q[j][k]
+// && Q[j][l] && Q[k][l] (Q[j][k] implies want4(k), which Q[k][l] carries).
+// The block tests every ordered pair of entries once -- the FP32 distance
+// with the same thresholds and, inside the margin, the same exact FP64
+// distance as the per-entry form -- and keeps the rows T[j], Q[j] as bit
+// masks in shared memory.  The count pass then takes n3(j) = popc T[j] and
+// n4(j) = sum over k in Q[j] of popc(Q[j] & Q[k]); the fill pass emits the
+// clusters from the masks in the same order (k ascending, then l ascending).
+// The per-entry form walks k and, for every 4-body k, all l again, once per
+// pass; here both passes cost one test per ordered pair.
+constexpr int kEnumRows = 128;
+constexpr int kEnumWords = kEnumRows / 32;
+constexpr int kEnumStride = kEnumWords + 1;   // odd row stride: column reads hit distinct banks
+constexpr int kEnumWarps = 4;
+
+template <bool FILL>
+__global__ void __launch_bounds__(32 * kEnumWarps, 8) k_enuma(BatchView B) {
+    __shared__ float4 sv[kEnumRows];
+    __shared__ int sg[kEnumRows];
+    __shared__ unsigned rt[kEnumRows * kEnumStride];
+    __shared__ unsigned rq[kEnumRows * kEnumStride];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
+    if (!FILL) {
+        for (long long e = n2 + (long long)blockIdx.x * blockDim.x + threadIdx.x; e < B.n2_cap;
+             e += (long long)gridDim.x * blockDim.x) {
+            B.e_cnt3[e] = 0;
+            B.e_cnt4[e] = 0;
+        }
+    }
+    const float4* vec = reinterpret_cast<const float4*>(B.l2_vec);
+    for (long long r = blockIdx.x; r < B.n_atoms_total; r += gridDim.x) {
+        const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
+        const int L = (int)(b1 - b0);
+        if (L <= 0) continue;
+        const SysDesc& d = B.sys[B.atom_sys[r]];
+        if (!d.has3 && !d.has4) {
+            if (!FILL)
+                for (int a = threadIdx.x; a < L; a += blockDim.x) { B.e_cnt3[b0 + a] = 0; B.e_cnt4[b0 + a] = 0; }
             continue;
         }
-        const int r = l2_owner[e];
-        const SysDesc& d = B.sys[B.atom_sys[r]];
-        const double c3 = d.c3, c4 = d.c4;
-        const float4 vj = vec[e];
-        const unsigned wj = __float_as_uint(vj.w);
-        const bool want3 = d.has3 && (wj & kL2In3), want4 = d.has4 && (wj & kL2In4);
-        long long n3 = 0, n4 = 0;
-        long long o3 = 0, o4 = 0;
-        if (FILL) { o3 = B.e_off3[e]; o4 = B.e_off4[e]; }
-        if (want3 || want4) {
-            double hn[9];
-            for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
+        if (L > kEnumRows) {
+            for (long long e = b0 + w; e < b1; e += kEnumWarps) enumw_entry<FILL>(B, e, (int)r, d, lane, lt);
+            continue;
+        }
+        __syncthreads();   // the previous atom's masks are no longer read
+        for (int a = threadIdx.x; a < L; a += blockDim.x) {
+            sv[a] = vec[b0 + a];
+            sg[a] = B.l2_ghost[b0 + a];
+        }
+        __syncthreads();
+        const int nw = (L + 31) >> 5;
+        {
+            const double* hn = d.hn;   // read in place: the exact distances are rare
+            const double c3 = d.c3, c4 = d.c4;
             const float c3lo = d.c3lo, c3hi = d.c3hi, c4lo = d.c4lo, c4hi = d.c4hi;
+            for (int a = w; a < L; a += kEnumWarps) {
+                const float4 va = sv[a];
+                const unsigned wa = __float_as_uint(va.w);
+                const bool want3 = d.has3 && (wa & kL2In3), want4 = d.has4 && (wa & kL2In4);
+                const int pa = (int)(wa & kL2Parent), ga = sg[a];
+                for (int c = 0; c < nw; c++) {
+                    const int b = 32 * c + lane;
+                    bool t = false, q = false;
+                    if (b < L && (want3 || want4)) {
+                        const float4 vb = sv[b];
+                        const unsigned wb = __float_as_uint(vb.w);
+                        const int gb = sg[b];
+                        if (gb != ga && pa <= (int)(wb & kL2Parent)) {
+                            const bool t0 = want3 && (wb & kL2In3), q0 = want4 && (wb & kL2In4);
+                            if (t0 || q0) {
+                                const float df = vdist(va, vb);
+                                // inside the margin of a cutoff: decided by the exact distance
+                                const bool x3 = t0 && !(df < c3lo) && !(df >= c3hi);
+                                const bool x4 = q0 && !(df < c4lo) && !(df >= c4hi);
+                                double dx = 0.0;
+                                if (x3 || x4)
+                                    dx = dist_frac(hn, &B.ghost_fn[3 * (long long)ga], &B.ghost_fn[3 * (long long)gb]);
+                                t = t0 && (x3 ? dx < c3 : df < c3lo);
+                                q = q0 && (x4 ? dx < c4 : df < c4lo);
+                            }
+                        }
+                    }
+                    const unsigned bt = __ballot_sync(kFull, t), bq = __ballot_sync(kFull, q);
+                    if (lane == 0) { rt[a * kEnumStride + c] = bt; rq[a * kEnumStride + c] = bq; }
+                }
+            }
+        }
+        __syncthreads();
+        if (!FILL) {
+            for (int a = threadIdx.x; a < L; a += blockDim.x) {
+                int n3 = 0, n4 = 0;
+                for (int c = 0; c < nw; c++) n3 += __popc(rt[a * kEnumStride + c]);
+                for (int c = 0; c < nw; c++) {
+                    unsigned m = rq[a * kEnumStride + c];
+                    while (m) {
+                        const int b = 32 * c + __ffs(m) - 1;
+                        m &= m - 1;
+                        for (int c2 = 0; c2 < nw; c2++) n4 += __popc(rq[a * kEnumStride + c2] & rq[b * kEnumStride + c2]);
+                    }
+                }
+                B.e_cnt3[b0 + a] = n3;
+                B.e_cnt4[b0 + a] = n4;
+            }
+        } else {
             const int gi = B.atom_self[r];
-            const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
-            const int jj = B.l2_ghost[e];
-            const double* fj = &B.ghost_fn[3 * (long long)jj];
-            const int pj = (int)(wj & kL2Parent);
-            for (long long kb = b0; kb < b1; kb += 32) {
-                const long long k = kb + lane;
-                bool ok3 = false, ok4 = false;
-                int kk = -1, pk = 0;
-                float4 vk = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (k < b1) {
-                    kk = B.l2_ghost[k];
-                    vk = vec[k];
-                    const unsigned wk = __float_as_uint(vk.w);
-                    pk = (int)(wk & kL2Parent);
-                    if (kk != jj && pj <= pk) {
-                        const PairDistF jk{hn, fj, &B.ghost_fn[3 * (long long)kk], vdist(vj, vk)};
-                        ok3 = want3 && (wk & kL2In3) && !jk.ge(c3, c3lo, c3hi);
-                        ok4 = want4 && (wk & kL2In4) && !jk.ge(c4, c4lo, c4hi);
+            for (int a = w; a < L; a += kEnumWarps) {
+                const long long e = b0 + a;
+                long long o3 = B.e_off3[e], o4 = B.e_off4[e];
+                const int ga = sg[a];
+                for (int c = 0; c < nw; c++) {
+                    const unsigned m = rt[a * kEnumStride + c];
+                    if ((m >> lane) & 1u) {
+                        const long long q = o3 + __popc(m & lt);
+                        if (q < B.n3_cap) {
+                            int* out = B.c3 + 3 * q;
+                            out[0] = gi; out[1] = ga; out[2] = sg[32 * c + lane];
+                            if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)(b0 + 32 * c + lane); }
+                        }
                     }
+                    o3 += __popc(m);
                 }
-                const unsigned m3 = __ballot_sync(kFull, ok3);
-                if (FILL && ok3) {
-                    const long long q = o3 + n3 + __popc(m3 & lt);
-                    if (q < B.n3_cap) {
-                        int* out = B.c3 + 3 * q;
-                        out[0] = gi; out[1] = jj; out[2] = kk;
-                        if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)k; }
-                    }
-                }
-                n3 += __popc(m3);
-                unsigned m4 = __ballot_sync(kFull, ok4);
-                while (m4) {
-                    const int src = __ffs(m4) - 1;
-                    m4 &= m4 - 1;
-                    const int ks = __shfl_sync(kFull, kk, src);
-                    const int pks = __shfl_sync(kFull, pk, src);
-                    float4 vks;
-                    vks.x = __shfl_sync(kFull, vk.x, src);
-                    vks.y = __shfl_sync(kFull, vk.y, src);
-                    vks.z = __shfl_sync(kFull, vk.z, src);
-                    vks.w = 0.f;
-                    const double* fk = &B.ghost_fn[3 * (long long)ks];
-                    for (long long lb = b0; lb < b1; lb += 32) {
-                        const long long l = lb + lane;
-                        bool okl = false;
-                        int ll = -1;
-                        if (l < b1) {
-                            ll = B.l2_ghost[l];
-                            const float4 vl = vec[l];
-                            if (ll != jj && ll != ks) {
-                                const unsigned wl = __float_as_uint(vl.w);
-                                const int pl = (int)(wl & kL2Parent);
-                                if (pj <= pl && pks <= pl && (wl & kL2In4)) {
-                                    const double* fl = &B.ghost_fn[3 * (long long)ll];
-                                    const PairDistF jl{hn, fj, fl, vdist(vj, vl)};
-                                    if (!jl.ge(c4, c4lo, c4hi)) {
-                                        const PairDistF kl{hn, fk, fl, vdist(vks, vl)};
-                                        okl = !kl.ge(c4, c4lo, c4hi);
+                for (int c = 0; c < nw; c++) {
+                    unsigned mb = rq[a * kEnumStride + c];
+                    while (mb) {
+                        const int b = 32 * c + __ffs(mb) - 1;
+                        mb &= mb - 1;
+                        const int gb = sg[b];
+                        for (int c2 = 0; c2 < nw; c2++) {
+                            const unsigned m = rq[a * kEnumStride + c2] & rq[b * kEnumStride + c2];
+                            if ((m >> lane) & 1u) {
+                                const long long q = o4 + __popc(m & lt);
+                                if (q < B.n4_cap) {
+                                    int* out = B.c4 + 4 * q;
+                                    out[0] = gi; out[1] = ga; out[2] = gb; out[3] = sg[32 * c2 + lane];
+                                    if (B.c4e) {
+                                        B.c4e[3 * q] = (int)e;
+                                        B.c4e[3 * q + 1] = (int)(b0 + b);
+                                        B.c4e[3 * q + 2] = (int)(b0 + 32 * c2 + lane);
                                     }
                                 }
                             }
+                            o4 += __popc(m);
                         }
-                        const unsigned ml = __ballot_sync(kFull, okl);
-                        if (FILL && okl) {
-                            const long long q = o4 + n4 + __popc(ml & lt);
-                            if (q < B.n4_cap) {
-                                int* out = B.c4 + 4 * q;
-                                out[0] = gi; out[1] = jj; out[2] = ks; out[3] = ll;
-                                if (B.c4e) {
-                                    B.c4e[3 * q] = (int)e;
-                                    B.c4e[3 * q + 1] = (int)(kb + src);
-                                    B.c4e[3 * q + 2] = (int)l;
-                                }
-                            }
-                        }
-                        n4 += __popc(ml);
                     }
                 }
             }
         }
-        if (!FILL && lane == 0) { B.e_cnt3[e] = (int)n3; B.e_cnt4[e] = (int)n4; }
     }
 }
 
@@ -947,11 +1092,11 @@ void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_
         else count_launch(), k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
         return;
     }
-    long long want = (long long)sm_count() * 8;      // 8 blocks of 8 warps per SM
-    long long need = (B.n2_cap + 7) / 8;             // one warp per list entry
+    long long want = (long long)sm_count() * 16;     // 16 blocks of 4 warps per SM
+    const long long need = B.n_atoms_total;          // one block per atom
     const unsigned grid = (unsigned)(want < need ? want : need);
-    if (fill) count_launch(), k_enumw<true><<<grid, 256, 0, st>>>(B, l2_owner);
-    else count_launch(), k_enumw<false><<<grid, 256, 0, st>>>(B, l2_owner);
+    if (fill) count_launch(), k_enuma<true><<<grid, 32 * kEnumWarps, 0, st>>>(B);
+    else count_launch(), k_enuma<false><<<grid, 32 * kEnumWarps, 0, st>>>(B);
 }
 void launch_check(const BatchView& B, cudaStream_t st) { count_launch(), k_check<<<1, 1, 0, st>>>(B); }
 void launch_reset(const BatchView& B, cudaStream_t st) {
