@@ -719,33 +719,60 @@ __device__ void enumw_entry(const BatchView& B, long long e, int r, const SysDes
     if (!FILL && lane == 0) { B.e_cnt3[e] = (int)n3; B.e_cnt4[e] = (int)n4; }
 }
 
-// Bit-matrix form (one block per atom i, atoms with at most kEnumRows list
+// Bit-matrix form (G warps per atom i, atoms with at most kEnumRows list
 // entries).  With the reset semantics above, membership depends only on pair
 // tests among the entries of i's list:
 //   T[j][k] = want3(j) && in3(k) && j != k && parent(j) <= parent(k) && |r_jk| < rc3
 //   Q[j][k] = want4(j) && in4(k) && j != k && parent(j) <= parent(k) && |r_jk| < rc4
 // (i, j, k) is a triplet iff T[j][k]; (i, j, k, l) a quadruplet iff Q[j][k]
 // && Q[j][l] && Q[k][l] (Q[j][k] implies want4(k), which Q[k][l] carries).
-// The block tests every ordered pair of entries once -- the FP32 distance
-// with the same thresholds and, inside the margin, the same exact FP64
-// distance as the per-entry form -- and keeps the rows T[j], Q[j] as bit
-// masks in shared memory.  The count pass then takes n3(j) = popc T[j] and
-// n4(j) = sum over k in Q[j] of popc(Q[j] & Q[k]); the fill pass emits the
-// clusters from the masks in the same order (k ascending, then l ascending).
-// The per-entry form walks k and, for every 4-body k, all l again, once per
-// pass; here both passes cost one test per ordered pair.
-constexpr int kEnumRows = 128;
-constexpr int kEnumWords = kEnumRows / 32;
-constexpr int kEnumStride = kEnumWords + 1;   // odd row stride: column reads hit distinct banks
-constexpr int kEnumWarps = 4;
+// The warps test every ordered pair of entries once -- the FP32 distance with
+// the same thresholds and, inside the margin, the same exact FP64 distance as
+// the per-entry form -- and keep the rows T[j], Q[j] as bit masks in shared
+// memory.  The count pass then takes n3(j) = popc T[j] and n4(j) = sum over
+// k in Q[j] of popc(Q[j] & Q[k]); the fill pass emits the clusters from the
+// masks in the same order (k ascending, then l ascending), each entry at the
+// offset of the atom's first entry plus the counts of the entries before it
+// (which the masks give).  The per-entry form walks k and, for every 4-body
+// k, all l again, once per pass; here both passes cost one test per ordered
+// pair.  G = 1 for batches with many atoms; small ones spread an atom over
+// up to a whole block so that the launch still fills the GPU.
+constexpr int kEnumRows = 96;
+constexpr int kEnumWords = kEnumRows / 32;   // odd: column reads of the masks hit distinct banks
+constexpr int kEnumWarps = 8;
 
-template <bool FILL>
-__global__ void __launch_bounds__(32 * kEnumWarps, 8) k_enuma(BatchView B) {
-    __shared__ float4 sv[kEnumRows];
-    __shared__ int sg[kEnumRows];
-    __shared__ unsigned rt[kEnumRows * kEnumStride];
-    __shared__ unsigned rq[kEnumRows * kEnumStride];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+template <int G>
+__device__ __forceinline__ void group_sync(int grp) {
+    if (G == 1) __syncwarp();
+    else if (G == kEnumWarps) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(32 * G) : "memory");
+}
+
+// n3 and n4 of entry a from the masks
+__device__ __forceinline__ void mask_counts(const unsigned* rt, const unsigned* rq, int a, int nw, int& n3, int& n4) {
+    n3 = 0;
+    n4 = 0;
+    for (int c = 0; c < nw; c++) n3 += __popc(rt[a * kEnumWords + c]);
+    for (int c = 0; c < nw; c++) {
+        unsigned m = rq[a * kEnumWords + c];
+        while (m) {
+            const int b = 32 * c + __ffs(m) - 1;
+            m &= m - 1;
+            for (int c2 = 0; c2 < nw; c2++) n4 += __popc(rq[a * kEnumWords + c2] & rq[b * kEnumWords + c2]);
+        }
+    }
+}
+
+template <bool FILL, int G>
+__global__ void __launch_bounds__(32 * kEnumWarps, 4) k_enuma(BatchView B) {
+    constexpr int NG = kEnumWarps / G;   // atoms a block works on at a time
+    __shared__ float4 s_v[NG][kEnumRows];
+    __shared__ int s_g[NG][kEnumRows];
+    __shared__ unsigned s_t[NG][kEnumRows * kEnumWords];
+    __shared__ unsigned s_q[NG][kEnumRows * kEnumWords];
+    __shared__ int s_o[G > 1 && FILL ? NG : 1][G > 1 && FILL ? 2 * kEnumRows : 1];   // per-entry offsets
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int grp = wib / G, w = wib % G;
     const unsigned lt = (1u << lane) - 1u;
     const long long n2 = min(B.l2_off[B.n_atoms_total], B.n2_cap);
     if (!FILL) {
@@ -756,35 +783,43 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 8) k_enuma(BatchView B) {
         }
     }
     const float4* vec = reinterpret_cast<const float4*>(B.l2_vec);
-    for (long long r = blockIdx.x; r < B.n_atoms_total; r += gridDim.x) {
+    float4* sv = s_v[grp];
+    int* sg = s_g[grp];
+    unsigned* rt = s_t[grp];
+    unsigned* rq = s_q[grp];
+    const long long ngroups = (long long)gridDim.x * NG;
+    for (long long r = (long long)blockIdx.x * NG + grp; r < B.n_atoms_total; r += ngroups) {
         const long long b0 = min(B.l2_off[r], B.n2_cap), b1 = min(B.l2_off[r + 1], B.n2_cap);
         const int L = (int)(b1 - b0);
         if (L <= 0) continue;
         const SysDesc& d = B.sys[B.atom_sys[r]];
         if (!d.has3 && !d.has4) {
             if (!FILL)
-                for (int a = threadIdx.x; a < L; a += blockDim.x) { B.e_cnt3[b0 + a] = 0; B.e_cnt4[b0 + a] = 0; }
+                for (int a = 32 * w + lane; a < L; a += 32 * G) { B.e_cnt3[b0 + a] = 0; B.e_cnt4[b0 + a] = 0; }
             continue;
         }
         if (L > kEnumRows) {
-            for (long long e = b0 + w; e < b1; e += kEnumWarps) enumw_entry<FILL>(B, e, (int)r, d, lane, lt);
+            for (long long e = b0 + w; e < b1; e += G) enumw_entry<FILL>(B, e, (int)r, d, lane, lt);
             continue;
         }
-        __syncthreads();   // the previous atom's masks are no longer read
-        for (int a = threadIdx.x; a < L; a += blockDim.x) {
+        long long o3 = 0, o4 = 0;
+        if (FILL) { o3 = B.e_off3[b0]; o4 = B.e_off4[b0]; }
+        group_sync<G>(grp);   // the previous atom's masks are no longer read
+        for (int a = 32 * w + lane; a < L; a += 32 * G) {
             sv[a] = vec[b0 + a];
             sg[a] = B.l2_ghost[b0 + a];
         }
-        __syncthreads();
+        group_sync<G>(grp);
         const int nw = (L + 31) >> 5;
         {
             const double* hn = d.hn;   // read in place: the exact distances are rare
             const double c3 = d.c3, c4 = d.c4;
             const float c3lo = d.c3lo, c3hi = d.c3hi, c4lo = d.c4lo, c4hi = d.c4hi;
-            for (int a = w; a < L; a += kEnumWarps) {
+            const bool has3 = d.has3, has4 = d.has4;
+            for (int a = w; a < L; a += G) {
                 const float4 va = sv[a];
                 const unsigned wa = __float_as_uint(va.w);
-                const bool want3 = d.has3 && (wa & kL2In3), want4 = d.has4 && (wa & kL2In4);
+                const bool want3 = has3 && (wa & kL2In3), want4 = has4 && (wa & kL2In4);
                 const int pa = (int)(wa & kL2Parent), ga = sg[a];
                 for (int c = 0; c < nw; c++) {
                     const int b = 32 * c + lane;
@@ -809,71 +844,99 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 8) k_enuma(BatchView B) {
                         }
                     }
                     const unsigned bt = __ballot_sync(kFull, t), bq = __ballot_sync(kFull, q);
-                    if (lane == 0) { rt[a * kEnumStride + c] = bt; rq[a * kEnumStride + c] = bq; }
+                    if (lane == 0) { rt[a * kEnumWords + c] = bt; rq[a * kEnumWords + c] = bq; }
                 }
             }
         }
-        __syncthreads();
+        group_sync<G>(grp);
         if (!FILL) {
-            for (int a = threadIdx.x; a < L; a += blockDim.x) {
-                int n3 = 0, n4 = 0;
-                for (int c = 0; c < nw; c++) n3 += __popc(rt[a * kEnumStride + c]);
-                for (int c = 0; c < nw; c++) {
-                    unsigned m = rq[a * kEnumStride + c];
-                    while (m) {
-                        const int b = 32 * c + __ffs(m) - 1;
-                        m &= m - 1;
-                        for (int c2 = 0; c2 < nw; c2++) n4 += __popc(rq[a * kEnumStride + c2] & rq[b * kEnumStride + c2]);
-                    }
-                }
+            for (int a = 32 * w + lane; a < L; a += 32 * G) {
+                int n3, n4;
+                mask_counts(rt, rq, a, nw, n3, n4);
                 B.e_cnt3[b0 + a] = n3;
                 B.e_cnt4[b0 + a] = n4;
             }
-        } else {
-            const int gi = B.atom_self[r];
-            for (int a = w; a < L; a += kEnumWarps) {
-                const long long e = b0 + a;
-                long long o3 = B.e_off3[e], o4 = B.e_off4[e];
-                const int ga = sg[a];
-                for (int c = 0; c < nw; c++) {
-                    const unsigned m = rt[a * kEnumStride + c];
-                    if ((m >> lane) & 1u) {
-                        const long long q = o3 + __popc(m & lt);
-                        if (q < B.n3_cap) {
-                            int* out = B.c3 + 3 * q;
-                            out[0] = gi; out[1] = ga; out[2] = sg[32 * c + lane];
-                            if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)(b0 + 32 * c + lane); }
-                        }
+            continue;
+        }
+        if (G > 1) {
+            // offsets of the entries relative to the first one, for the warps that emit them
+            int* so = s_o[G > 1 ? grp : 0];
+            if (w == 0) {
+                int c3 = 0, c4 = 0;
+                for (int a0 = 0; a0 < L; a0 += 32) {
+                    const int a = a0 + lane;
+                    int n3 = 0, n4 = 0;
+                    if (a < L) mask_counts(rt, rq, a, nw, n3, n4);
+                    int i3 = n3, i4 = n4;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y3 = __shfl_up_sync(kFull, i3, o), y4 = __shfl_up_sync(kFull, i4, o);
+                        if (lane >= o) { i3 += y3; i4 += y4; }
                     }
-                    o3 += __popc(m);
+                    if (a < L) { so[2 * a] = c3 + i3 - n3; so[2 * a + 1] = c4 + i4 - n4; }
+                    c3 += __shfl_sync(kFull, i3, 31);
+                    c4 += __shfl_sync(kFull, i4, 31);
                 }
-                for (int c = 0; c < nw; c++) {
-                    unsigned mb = rq[a * kEnumStride + c];
-                    while (mb) {
-                        const int b = 32 * c + __ffs(mb) - 1;
-                        mb &= mb - 1;
-                        const int gb = sg[b];
-                        for (int c2 = 0; c2 < nw; c2++) {
-                            const unsigned m = rq[a * kEnumStride + c2] & rq[b * kEnumStride + c2];
-                            if ((m >> lane) & 1u) {
-                                const long long q = o4 + __popc(m & lt);
-                                if (q < B.n4_cap) {
-                                    int* out = B.c4 + 4 * q;
-                                    out[0] = gi; out[1] = ga; out[2] = gb; out[3] = sg[32 * c2 + lane];
-                                    if (B.c4e) {
-                                        B.c4e[3 * q] = (int)e;
-                                        B.c4e[3 * q + 1] = (int)(b0 + b);
-                                        B.c4e[3 * q + 2] = (int)(b0 + 32 * c2 + lane);
-                                    }
+            }
+            group_sync<G>(grp);
+        }
+        const int gi = B.atom_self[r];
+        for (int a = w; a < L; a += G) {
+            const long long e = b0 + a;
+            long long p3 = o3, p4 = o4;
+            if (G > 1) {
+                const int* so = s_o[G > 1 ? grp : 0];
+                p3 += so[2 * a];
+                p4 += so[2 * a + 1];
+            }
+            const int ga = sg[a];
+            for (int c = 0; c < nw; c++) {
+                const unsigned m = rt[a * kEnumWords + c];
+                if ((m >> lane) & 1u) {
+                    const long long q = p3 + __popc(m & lt);
+                    if (q < B.n3_cap) {
+                        int* out = B.c3 + 3 * q;
+                        out[0] = gi; out[1] = ga; out[2] = sg[32 * c + lane];
+                        if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)(b0 + 32 * c + lane); }
+                    }
+                }
+                p3 += __popc(m);
+            }
+            for (int c = 0; c < nw; c++) {
+                unsigned mb = rq[a * kEnumWords + c];
+                while (mb) {
+                    const int b = 32 * c + __ffs(mb) - 1;
+                    mb &= mb - 1;
+                    const int gb = sg[b];
+                    for (int c2 = 0; c2 < nw; c2++) {
+                        const unsigned m = rq[a * kEnumWords + c2] & rq[b * kEnumWords + c2];
+                        if ((m >> lane) & 1u) {
+                            const long long q = p4 + __popc(m & lt);
+                            if (q < B.n4_cap) {
+                                int* out = B.c4 + 4 * q;
+                                out[0] = gi; out[1] = ga; out[2] = gb; out[3] = sg[32 * c2 + lane];
+                                if (B.c4e) {
+                                    B.c4e[3 * q] = (int)e;
+                                    B.c4e[3 * q + 1] = (int)(b0 + b);
+                                    B.c4e[3 * q + 2] = (int)(b0 + 32 * c2 + lane);
                                 }
                             }
-                            o4 += __popc(m);
                         }
+                        p4 += __popc(m);
                     }
                 }
             }
+            if (G == 1) { o3 = p3; o4 = p4; }
         }
     }
+}
+
+template <bool FILL, int G>
+void launch_enuma(const BatchView& B, cudaStream_t st) {
+    constexpr int NG = kEnumWarps / G;
+    const long long want = (long long)sm_count() * 4;   // 4 blocks of 8 warps per SM
+    const long long need = (B.n_atoms_total + NG - 1) / NG;
+    const unsigned grid = (unsigned)(want < need ? want : need);
+    count_launch(), k_enuma<FILL, G><<<grid, 32 * kEnumWarps, 0, st>>>(B);
 }
 
 // --- capacity checks and accumulator reset ---------------------------------
@@ -1092,11 +1155,17 @@ void launch_enum(const BatchView& B, const int* l2_owner, bool fill, cudaStream_
         else count_launch(), k_enum<false><<<grid, 128, 0, st>>>(B, l2_owner);
         return;
     }
-    long long want = (long long)sm_count() * 16;     // 16 blocks of 4 warps per SM
-    const long long need = B.n_atoms_total;          // one block per atom
-    const unsigned grid = (unsigned)(want < need ? want : need);
-    if (fill) count_launch(), k_enuma<true><<<grid, 32 * kEnumWarps, 0, st>>>(B);
-    else count_launch(), k_enuma<false><<<grid, 32 * kEnumWarps, 0, st>>>(B);
+    // warps per atom: the fewest that still give about two warps per
+    // resident warp slot (32 per SM)
+    const long long target = 64LL * sm_count();
+    const long long n = B.n_atoms_total;
+    const int G = n >= target ? 1 : 2 * n >= target ? 2 : 4 * n >= target ? 4 : 8;
+    switch (G) {
+    case 1: fill ? launch_enuma<true, 1>(B, st) : launch_enuma<false, 1>(B, st); break;
+    case 2: fill ? launch_enuma<true, 2>(B, st) : launch_enuma<false, 2>(B, st); break;
+    case 4: fill ? launch_enuma<true, 4>(B, st) : launch_enuma<false, 4>(B, st); break;
+    default: fill ? launch_enuma<true, 8>(B, st) : launch_enuma<false, 8>(B, st); break;
+    }
 }
 void launch_check(const BatchView& B, cudaStream_t st) { count_launch(), k_check<<<1, 1, 0, st>>>(B); }
 void launch_reset(const BatchView& B, cudaStream_t st) {

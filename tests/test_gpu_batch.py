@@ -115,3 +115,23 @@ def test_batch_of_parameter_sets_with_different_orders(golden, native_lib, facto
         g = golden[n]
         assert abs(r["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy)), n
         assert g.force_error(r["force"]) <= mixed_force_tol(np.abs(g.force).max()), n
+
+
+@pytest.mark.parametrize("copies", [1, 3, 6, 10])
+def test_enumeration_warps_per_atom(golden, native_lib, copies):
+    """The cluster enumeration spreads one atom over 8, 4, 2 or 1 warps,
+    fewer as the batch's atom count grows (on 152 SMs these batches of 1536,
+    3584, 6656 and 10752 atoms take 8, 4, 2 and 1).  c2 repeated and ref_hn3,
+    whose atoms have up to 251 list entries (beyond the bit-matrix form, so
+    enumerated entry by entry), give the reference's result in every copy."""
+    from chimes_calculator_gb300 import Calculator
+    names = ["c2"] * copies + ["ref_hn3"]
+    c = Calculator()
+    slot = {n: c.load_params(golden[n].params) for n in set(names)}
+    res = c.evaluate_batch([(golden[n].cfg.pos, c.type_indices(golden[n].cfg.types, slot[n]), golden[n].cfg.cell)
+                            for n in names], slots=[slot[n] for n in names])
+    for n, r in zip(names, res):
+        g = golden[n]
+        assert abs(r["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy)), n
+        assert g.force_error(r["force"]) <= F_ABS_TOL, n
+        assert np.abs(r["stress"] - g.stress).max() <= S_ABS_TOL, n
