@@ -250,6 +250,7 @@ struct BatchView {
     long long* bin_start;          // [n_bins_total+1] positions in bin_items (global exclusive scan)
     int* bin_fill;
     int* bin_items;                // [g] global ghost ids sorted by (bin, id)
+    float* bin_xp;                 // [g][4] ghost_xf and ghost_parent (int bits) of bin_items, same order; or null
     // 2B lists
     int* l2_count;                 // [n_atoms_total]
     long long* l2_off;             // [n_atoms_total+1]

@@ -270,6 +270,7 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     CK_TRY(d_ghost_xn_.reserve(3 * ghost_off));
     CK_TRY(d_ghost_fn_.reserve(3 * ghost_off));
     CK_TRY(d_bin_items_.reserve(ghost_off));
+    CK_TRY(d_bin_xp_.reserve(4 * ghost_off));
     CK_TRY(d_minmax_.reserve(6 * S));
     CK_TRY(d_bin_count_.reserve(bin_off));
     CK_TRY(d_bin_fill_.reserve(bin_off));
@@ -343,6 +344,7 @@ Status Engine::ensure_lists(std::string& err) {
     B.ghost_bin = d_ghost_bin_.p;
     B.bin_count = d_bin_count_.p; B.bin_start = d_bin_start_.p; B.bin_fill = d_bin_fill_.p;
     B.bin_items = d_bin_items_.p;
+    B.bin_xp = d_bin_xp_.p;
     B.l2_count = d_l2_count_.p; B.l2_off = d_l2_off_.p; B.l2_ghost = d_l2_ghost_.p; B.l2_dist = d_l2_dist_.p;
     B.l2_vec = d_l2_vec_.p;
     B.n2_cap = n2_cap_;

@@ -176,7 +176,7 @@ private:
     DevBuf<int> d_in_type_;
     DevBuf<int> d_atom_sys_, d_atom_type_, d_atom_orig_;
     DevBuf<int> d_atom_self_, d_ghost_id_;
-    DevBuf<float> d_ghost_xf_, d_l2_vec_;
+    DevBuf<float> d_ghost_xf_, d_l2_vec_, d_bin_xp_;
     DevBuf<int> d_ghost_parent_, d_ghost_bin_;
     DevBuf<double> d_ghost_fs_, d_ghost_xn_, d_ghost_fn_;
     DevBuf<unsigned long long> d_minmax_;

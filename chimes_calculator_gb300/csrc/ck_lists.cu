@@ -301,6 +301,13 @@ __global__ void k_bin_scatter(BatchView B, const long long* bin_start) {
     B.bin_items[pos] = (int)q;
 }
 
+// FP32 coordinates and parent atom of ghost q at bin position pos (read by
+// the pair-list kernel in bin order instead of gathered by ghost id)
+__device__ __forceinline__ void put_xp(const BatchView& B, long long pos, int q) {
+    const float* x = &B.ghost_xf[3 * (long long)q];
+    reinterpret_cast<float4*>(B.bin_xp)[pos] = make_float4(x[0], x[1], x[2], __int_as_float(B.ghost_parent[q]));
+}
+
 // each bin's members in ascending ghost id (the reference pushes ghosts into
 // bins in index order): one warp per bin; a member's place is the number of
 // members with a smaller id (ids are unique), counted over the warp's
@@ -312,7 +319,11 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
     const long long s0 = bin_start[b];
     const int n = B.bin_count[b];
     int* v = B.bin_items + s0;
-    if (n <= 1) return;
+    if (n <= 0) return;
+    if (n == 1) {
+        if (lane == 0 && B.bin_xp) put_xp(B, s0, v[0]);
+        return;
+    }
     if (n > 64) {
         if (lane == 0)
             for (int i = 1; i < n; i++) {
@@ -321,6 +332,9 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
                 while (j >= 0 && B.ghost_id[v[j]] > kid) { v[j + 1] = v[j]; j--; }
                 v[j + 1] = key;
             }
+        __syncwarp();
+        if (B.bin_xp)
+            for (int i = lane; i < n; i += 32) put_xp(B, s0 + i, v[i]);
         return;
     }
     const int big = 0x7fffffff;
@@ -333,8 +347,14 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
         r1 += (o0 < k1) + (o1 < k1);
     }
     __syncwarp();
-    if (q0 >= 0) v[r0] = q0;
-    if (q1 >= 0) v[r1] = q1;
+    if (q0 >= 0) {
+        v[r0] = q0;
+        if (B.bin_xp) put_xp(B, s0 + r0, q0);
+    }
+    if (q1 >= 0) {
+        v[r1] = q1;
+        if (B.bin_xp) put_xp(B, s0 + r1, q1);
+    }
 }
 
 // --- 5. 2B neighbour lists (:680-731): one warp per atom --------------------
@@ -456,9 +476,20 @@ __global__ void __launch_bounds__(kL2Block) k_l2(BatchView B, const long long* b
         bool exact = false, sure = false;
         int ajj = -1, par = -1;
         if (t < ncand) {
-            ajj = B.bin_items[st + (t - first)];
-            if (ajj != gi && r <= (par = B.ghost_parent[ajj])) {
-                const float* xj = &B.ghost_xf[3 * (long long)ajj];
+            const long long it = st + (t - first);
+            ajj = B.bin_items[it];
+            float xj[3];
+            if (B.bin_xp) {   // the candidate's coordinates and parent stored in bin order
+                const float4 p = reinterpret_cast<const float4*>(B.bin_xp)[it];
+                xj[0] = p.x; xj[1] = p.y; xj[2] = p.z;
+                par = __float_as_int(p.w);
+            } else {
+                par = B.ghost_parent[ajj];
+                xj[0] = B.ghost_xf[3 * (long long)ajj];
+                xj[1] = B.ghost_xf[3 * (long long)ajj + 1];
+                xj[2] = B.ghost_xf[3 * (long long)ajj + 2];
+            }
+            if (ajj != gi && r <= par) {
                 const float ex = xj[0] - xi[0], ey = xj[1] - xi[1], ez = xj[2] - xi[2];
                 const float e2 = ex * ex + ey * ey + ez * ez;
                 if (e2 < far2) {   // else certainly >= sd
