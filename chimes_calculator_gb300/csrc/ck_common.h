@@ -216,6 +216,7 @@ struct SysDesc {
     double ulo[3], uhi[3];     // kept fractional range per axis of the reoriented cell
     double eps;                // margin of the FP32 distance prefilter (Angstrom)
     float c3lo, c3hi, c4lo, c4hi;   // c3 -/+ eps and c4 -/+ eps as FP32, rounded outward
+    float far2, near2;         // (search +/- eps)^2 as FP32: the pair lists' squared-distance prefilter
     // device-completed
     double minpos[3];
     int nb[3];

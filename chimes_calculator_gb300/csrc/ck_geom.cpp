@@ -241,6 +241,8 @@ Status system_geometry(const double* ca, const double* cb, const double* cc, int
     d.c3hi = up(d.c3 + d.eps);
     d.c4lo = down(d.c4 - d.eps);
     d.c4hi = up(d.c4 + d.eps);
+    d.far2 = (float)((d.search + d.eps) * (d.search + d.eps));
+    d.near2 = d.search > d.eps ? (float)((d.search - d.eps) * (d.search - d.eps)) : 0.0f;
     return kOk;
 }
 

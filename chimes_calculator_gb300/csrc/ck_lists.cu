@@ -389,10 +389,16 @@ __global__ void __launch_bounds__(kL2Block) k_l2(BatchView B, const long long* b
     double hn[9];
     for (int c = 0; c < 9; c++) hn[c] = d.hn[c];
     const double sd = d.search;
-    const float far2 = (float)((sd + d.eps) * (sd + d.eps));
-    const float near2 = sd > d.eps ? (float)((sd - d.eps) * (sd - d.eps)) : 0.0f;
-    int bx, by, bz;
-    bin_of(d, &B.ghost_xn[3 * gi], bx, by, bz);
+    const float far2 = d.far2, near2 = d.near2;
+    // the atom's bin, as k_bin_count placed it (bin_of of the same coordinates;
+    // recomputing it would cost three FP64 divisions per atom)
+    const int ib0 = B.ghost_bin[gi];
+    int bx = -1, by = -1, bz = -1;
+    if (ib0 >= 0) {
+        bx = ib0 % d.nb[0];
+        by = (ib0 / d.nb[0]) % d.nb[1];
+        bz = ib0 / (d.nb[0] * d.nb[1]);
+    }
     if (bx < 1 || by < 1 || bz < 1) {
         if (lane == 0) { atomicExch(&B.flags[1], 3); if (!FILL) B.l2_count[r] = 0; }
         return;
@@ -864,13 +870,17 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 4) k_enuma(BatchView B) {
                             if (t0 || q0) {
                                 const float df = vdist(va, vb);
                                 // inside the margin of a cutoff: decided by the exact distance
+                                // (FP64 only on that rare branch: GB300 issues FP64 at a small
+                                // fraction of the FP32 rate)
                                 const bool x3 = t0 && !(df < c3lo) && !(df >= c3hi);
                                 const bool x4 = q0 && !(df < c4lo) && !(df >= c4hi);
-                                double dx = 0.0;
-                                if (x3 || x4)
-                                    dx = dist_frac(hn, &B.ghost_fn[3 * (long long)ga], &B.ghost_fn[3 * (long long)gb]);
-                                t = t0 && (x3 ? dx < c3 : df < c3lo);
-                                q = q0 && (x4 ? dx < c4 : df < c4lo);
+                                t = t0 && df < c3lo;
+                                q = q0 && df < c4lo;
+                                if (x3 || x4) {
+                                    const double dx = dist_frac(hn, &B.ghost_fn[3 * (long long)ga], &B.ghost_fn[3 * (long long)gb]);
+                                    if (x3) t = dx < c3;
+                                    if (x4) q = dx < c4;
+                                }
                             }
                         }
                     }
