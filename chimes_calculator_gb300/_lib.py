@@ -96,6 +96,7 @@ SIGNATURES = {
     "ck_server_submit": (LL, [P, I, I, DP, IP, DP, I]),
     "ck_server_take": (I, [P, LL, I, D, DP, DP, DP, DP]),
     "ck_server_stats": (I, [P, LLP]),
+    "ck_server_worker_tuning": (I, [P, I, IP]),
     "ck_server_autotune": (I, [P, I, IP, DP, IP, DP, IP, IP, IP]),
     "ck_server_replay": (I, [P, I, IP, IP, DP, IP, DP, IP, DP, DP, DP, DP]),
 }

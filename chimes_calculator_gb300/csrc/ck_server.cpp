@@ -187,6 +187,7 @@ public:
             d.tpc3 = t.tpc3, d.tpc4 = t.tpc4, d.blocks_per_sm = t.blocks_per_sm;
             d.ftpc3 = t.ftpc3, d.ftpc4 = t.ftpc4, d.fbps3 = t.fbps3, d.fbps4 = t.fbps4;
             d.want_fact3 = t.want_fact3, d.want_fact4 = t.want_fact4, d.noy3 = t.noy3;
+            d.want_tc3 = t.want_tc3;
         }
         return kOk;
     }
@@ -258,6 +259,21 @@ public:
         wall = now_s() - t0;
         submitter.join();
         return st;
+    }
+
+    // worker w's launch preferences (the values ck_get_tuning reports, with
+    // the contraction-form entries as preferences)
+    Status worker_tuning(int w, int* out, std::string& err) {
+        if (w < 0 || w >= (int)engines_.size()) {
+            err = "no such worker";
+            return kErrInput;
+        }
+        std::lock_guard<std::mutex> ge(*engine_mu_[w]);
+        const ForceLaunch& L = engines_[w]->tuning;
+        const int v[11] = {L.tpc3, L.tpc4, L.blocks_per_sm, L.want_fact3, L.want_fact4, L.ftpc3,
+                           L.ftpc4, L.fbps3, L.fbps4, L.noy3, L.want_tc3};
+        for (int k = 0; k < 11; k++) out[k] = v[k];
+        return kOk;
     }
 
     void stats(long long* out) {
@@ -482,6 +498,14 @@ int ck_server_replay(void* s, int nreq, const int* slots, const int* natoms, con
     ck::Status st = static_cast<ck::Server*>(s)->replay(nreq, slots, natoms, pos, types, cells, small, arrival_s,
                                                         latency_s, energy, wall, err);
     if (wall_s) *wall_s = wall;
+    if (st != ck::kOk) return ck::report_error(st, err);
+    return ck::kOk;
+}
+
+int ck_server_worker_tuning(void* s, int worker, int* out) {
+    if (!s) return ck::report_error(ck::kErrState, "no server");
+    std::string err;
+    const ck::Status st = static_cast<ck::Server*>(s)->worker_tuning(worker, out, err);
     if (st != ck::kOk) return ck::report_error(st, err);
     return ck::kOk;
 }

@@ -218,13 +218,23 @@ __global__ void __launch_bounds__(128) k_forcetc3(BatchView B, const int* cluste
     const DevParamSet* loaded_set = nullptr;
     EVAcc acc;
 
-    // tiles are claimed one ahead, so that each thread can prefetch its next
-    // cluster's data into L2 while the current tile's MMAs run
-    if (tid == 0) s_next = (long long)atomicAdd(&B.queue[0], 1ull);
+    // Tiles: first a contiguous block per CTA (consecutive tiles share the
+    // tuple's coefficient image, so the image is seldom reloaded, and the
+    // pair-cache entries and positions of the same atoms), then the last
+    // eighth claimed one at a time so that the CTAs finish together.  Claimed
+    // one ahead, so that each thread can prefetch its next cluster's data into
+    // L2 while the current tile's MMAs run.
+    const long long per = ntiles * 7 / 8 / gridDim.x;
+    long long own = (long long)blockIdx.x * per;        // thread 0's next tile of its block
+    const long long own_end = own + per, shared0 = per * gridDim.x;
+    auto claim = [&]() -> long long {
+        return own < own_end ? own++ : shared0 + (long long)atomicAdd(&B.queue[0], 1ull);
+    };
+    if (tid == 0) s_next = claim();
     for (;;) {
         if (tid == 0) {
             s_tile = s_next;
-            s_next = s_next < ntiles ? (long long)atomicAdd(&B.queue[0], 1ull) : ntiles;
+            s_next = s_next < ntiles ? claim() : ntiles;
         }
         __syncthreads();
         const long long tile = s_tile;

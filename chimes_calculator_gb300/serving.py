@@ -37,6 +37,7 @@ class Server:
         self.lib = _lib.load()
         self.lib.ck_set_error_mode(1)
         self.h = self.lib.ck_server_open(workers, hbm_budget_gb, max_batch_atoms, precision)
+        self.workers = workers
         if not self.h:
             raise ChimesError(self.lib.ck_last_error().decode())
         self._natoms: Dict[int, int] = {}
@@ -103,6 +104,17 @@ class Server:
         if rc != 0:
             raise ChimesError(self.lib.ck_last_error().decode())
         return tuple(int(v) for v in chosen)
+
+    def worker_tunings(self) -> list:
+        """Each worker's launch preferences (11 values, ck_get_tuning's order
+        with the contraction-form entries as preferences)."""
+        out = []
+        for w in range(self.workers):
+            buf = (ctypes.c_int * 11)()
+            if self.lib.ck_server_worker_tuning(self.h, w, buf) != 0:
+                raise ChimesError(self.lib.ck_last_error().decode())
+            out.append(tuple(buf))
+        return out
 
     def stats(self) -> dict:
         out = (ctypes.c_longlong * 6)()

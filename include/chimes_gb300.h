@@ -213,6 +213,10 @@ int ck_server_replay(void *server, int nreq, const int *slots, const int *natoms
                      double *latency_s, double *energy, double *wall_s);
 /* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
 int ck_server_stats(void *server, long long *out);
+/* out[11] = worker's launch preferences, in ck_get_tuning's order with the
+ * factored and tensor-core entries as preferences (want_fact3, want_fact4,
+ * want_tc3): after ck_server_autotune every worker holds worker 0's. */
+int ck_server_worker_tuning(void *server, int worker, int *out);
 
 /* Pair-style evaluation on a caller's full neighbour list with ghost atoms:
  * the GPU form of LAMMPS pair_style chimesFF (etc/lmp/src/pair_chimes.cpp:

@@ -100,7 +100,8 @@ def test_admission_under_tiny_budget_and_failure_isolation(workload, native_lib)
 def test_native_replay_driver(workload, native_lib):
     """ck_server_replay (the native client the serving measurement uses) serves
     every request of a Poisson trace, after autotuning on a sample (which may
-    pick another contraction form than the default), with the energies of the
+    pick another contraction form than the default, and which every worker
+    takes, the tensor-core preference included), with the energies of the
     requests evaluated alone within the mixed form's budget and positive
     latencies."""
     import ctypes
@@ -114,6 +115,8 @@ def test_native_replay_driver(workload, native_lib):
             srv.load_params(p)
         srv.autotune([(cfg.pos, calc.type_indices(cfg.types, s), cfg.cell) for s, cfg in reqs[:6]],
                      [s for s, _ in reqs[:6]])
+        tunings = srv.worker_tunings()   # every worker takes worker 0's choices, the contraction form included
+        assert len(tunings) == 3 and tunings[1] == tunings[0] and tunings[2] == tunings[0]
         arrival = np.cumsum(np.random.default_rng(3).exponential(1e-4, size=len(reqs)))
         slots = np.array([s for s, _ in reqs], dtype=np.int32)
         natoms = np.array([c.n_atoms for _, c in reqs], dtype=np.int32)
