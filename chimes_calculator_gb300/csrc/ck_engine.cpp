@@ -9,6 +9,7 @@
 #include <string>
 
 #include "ck_geom.h"
+#include "nvtx3/nvToolsExt.h"
 
 namespace ck {
 
@@ -376,6 +377,21 @@ static cudaError_t record_stage_event(cudaEvent_t ev, cudaStream_t st) {
     return cudaEventRecord(ev, st);
 }
 
+// NVTX range over the enqueue of one stage: a profiler that records NVTX
+// (Nsight Systems) shows the stage's kernels under its name; without one
+// attached the calls return at once.
+namespace {
+struct NvtxRange {
+    bool open = true;
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    void end() {
+        if (open) nvtxRangePop();
+        open = false;
+    }
+    ~NvtxRange() { end(); }
+};
+}  // namespace
+
 Status Engine::enqueue(std::string& err) {
     BatchView B = V_;
     B.use_pc3 = avail_pc3_ && tuning.fact3 && (tuning.tc3 || pc_small_) ? 1 : 0;
@@ -388,6 +404,7 @@ Status Engine::enqueue(std::string& err) {
             if (!e) CK_TRY(cudaEventCreate(&e));
         CK_TRY(record_stage_event(ev_[0], st));
     }
+    NvtxRange lists_range("chimes: list build");
     CK_TRY(cudaMemsetAsync(B.bin_count, 0, sizeof(int) * B.n_bins_total, st));
     CK_TRY(cudaMemsetAsync(B.bin_fill, 0, sizeof(int) * B.n_bins_total, st));
     launch_reset(B, st);
@@ -411,12 +428,14 @@ Status Engine::enqueue(std::string& err) {
     if (conc) {
         CK_TRY(cudaEventRecord(fork_, st));
         CK_TRY(cudaStreamWaitEvent(stream2_, fork_, 0));
+        NvtxRange r("chimes: 1B+2B");
         launch_force2(B, d_l2_owner_.p, L, stream2_);
     }
     launch_enum(B, d_l2_owner_.p, false, st);
     exclusive_scan2(B.e_cnt3, B.e_off3, B.e_cnt4, B.e_off4, B.n2_cap, d_scan_tmp_.p, st);
     launch_enum(B, d_l2_owner_.p, true, st);
     launch_check(B, st);
+    lists_range.end();
     if (profile) CK_TRY(record_stage_event(ev_[1], st));
     if ((L.stride3 > 0 && L.fact3) || (L.stride4 > 0 && L.fact4)) {
         CK_TRY(cudaMemsetAsync(B.bk_count, 0, sizeof(int) * (B.nbk3 + B.nbk4), st));
@@ -424,6 +443,7 @@ Status Engine::enqueue(std::string& err) {
     }
     auto body3 = [&](cudaStream_t q) {
         if (L.stride3 <= 0) return;
+        NvtxRange r("chimes: 3B");
         if (L.fact3 && L.tc3) {
             launch_pair_tables(B, d_l2_owner_.p, 3, L, q);
             launch_bucket(B, 3, q);
@@ -438,6 +458,7 @@ Status Engine::enqueue(std::string& err) {
     };
     auto body4 = [&](cudaStream_t q) {
         if (L.stride4 <= 0) return;
+        NvtxRange r("chimes: 4B");
         if (L.fact4) {
             launch_pair_tables(B, d_l2_owner_.p, 4, L, q);
             launch_bucket(B, 4, q);
@@ -456,7 +477,10 @@ Status Engine::enqueue(std::string& err) {
         body3(st);
         CK_TRY(cudaStreamWaitEvent(st, join_, 0));
     } else {
-        launch_force2(B, d_l2_owner_.p, L, st);
+        {
+            NvtxRange r("chimes: 1B+2B");
+            launch_force2(B, d_l2_owner_.p, L, st);
+        }
         if (profile) CK_TRY(record_stage_event(ev_[2], st));
         body3(st);
         if (profile) CK_TRY(record_stage_event(ev_[3], st));
