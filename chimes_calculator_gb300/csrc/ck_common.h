@@ -217,6 +217,7 @@ struct SysDesc {
     double eps;                // margin of the FP32 distance prefilter (Angstrom)
     float c3lo, c3hi, c4lo, c4hi;   // c3 -/+ eps and c4 -/+ eps as FP32, rounded outward
     float far2, near2;         // (search +/- eps)^2 as FP32: the pair lists' squared-distance prefilter
+    float c3lo2, c3hi2, c4lo2, c4hi2;   // the same thresholds squared, rounded outward (-1: none below)
     // device-completed
     double minpos[3];
     int nb[3];

@@ -241,6 +241,12 @@ Status system_geometry(const double* ca, const double* cb, const double* cc, int
     d.c3hi = up(d.c3 + d.eps);
     d.c4lo = down(d.c4 - d.eps);
     d.c4hi = up(d.c4 + d.eps);
+    auto sq_down = [&](float v) { return v > 0.0f ? down((double)v * v) : -1.0f; };
+    auto sq_up = [&](float v) { return up((double)v * v); };
+    d.c3lo2 = sq_down(d.c3lo);
+    d.c3hi2 = sq_up(d.c3hi);
+    d.c4lo2 = sq_down(d.c4lo);
+    d.c4hi2 = sq_up(d.c4hi);
     d.far2 = (float)((d.search + d.eps) * (d.search + d.eps));
     d.near2 = d.search > d.eps ? (float)((d.search - d.eps) * (d.search - d.eps)) : 0.0f;
     return kOk;

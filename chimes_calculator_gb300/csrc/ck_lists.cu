@@ -851,37 +851,39 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 4) k_enuma(BatchView B) {
         {
             const double* hn = d.hn;   // read in place: the exact distances are rare
             const double c3 = d.c3, c4 = d.c4;
-            const float c3lo = d.c3lo, c3hi = d.c3hi, c4lo = d.c4lo, c4hi = d.c4hi;
+            // squared FP32 thresholds: the prefilter needs no square root
+            const float c3lo2 = d.c3lo2, c3hi2 = d.c3hi2, c4lo2 = d.c4lo2, c4hi2 = d.c4hi2;
             const bool has3 = d.has3, has4 = d.has4;
-            for (int a = w; a < L; a += G) {
-                const float4 va = sv[a];
-                const unsigned wa = __float_as_uint(va.w);
-                const bool want3 = has3 && (wa & kL2In3), want4 = has4 && (wa & kL2In4);
-                const int pa = (int)(wa & kL2Parent), ga = sg[a];
-                for (int c = 0; c < nw; c++) {
-                    const int b = 32 * c + lane;
+            for (int c = 0; c < nw; c++) {
+                // this lane's candidate k (column b of every row) stays in registers
+                const int b = 32 * c + lane;
+                float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
+                int gb = -1;
+                if (b < L) { vb = sv[b]; gb = sg[b]; }
+                const unsigned wb = __float_as_uint(vb.w);
+                const int pb = (int)(wb & kL2Parent);
+                const bool in3 = has3 && (wb & kL2In3), in4 = has4 && (wb & kL2In4);
+                for (int a = w; a < L; a += G) {
+                    const float4 va = sv[a];
+                    const unsigned wa = __float_as_uint(va.w);
+                    const int ga = sg[a];
+                    const bool t0 = in3 && (wa & kL2In3) && b < L && gb != ga && (int)(wa & kL2Parent) <= pb;
+                    const bool q0 = in4 && (wa & kL2In4) && b < L && gb != ga && (int)(wa & kL2Parent) <= pb;
                     bool t = false, q = false;
-                    if (b < L && (want3 || want4)) {
-                        const float4 vb = sv[b];
-                        const unsigned wb = __float_as_uint(vb.w);
-                        const int gb = sg[b];
-                        if (gb != ga && pa <= (int)(wb & kL2Parent)) {
-                            const bool t0 = want3 && (wb & kL2In3), q0 = want4 && (wb & kL2In4);
-                            if (t0 || q0) {
-                                const float df = vdist(va, vb);
-                                // inside the margin of a cutoff: decided by the exact distance
-                                // (FP64 only on that rare branch: GB300 issues FP64 at a small
-                                // fraction of the FP32 rate)
-                                const bool x3 = t0 && !(df < c3lo) && !(df >= c3hi);
-                                const bool x4 = q0 && !(df < c4lo) && !(df >= c4hi);
-                                t = t0 && df < c3lo;
-                                q = q0 && df < c4lo;
-                                if (x3 || x4) {
-                                    const double dx = dist_frac(hn, &B.ghost_fn[3 * (long long)ga], &B.ghost_fn[3 * (long long)gb]);
-                                    if (x3) t = dx < c3;
-                                    if (x4) q = dx < c4;
-                                }
-                            }
+                    if (t0 || q0) {
+                        const float ex = vb.x - va.x, ey = vb.y - va.y, ez = vb.z - va.z;
+                        const float e2 = ex * ex + ey * ey + ez * ez;
+                        // inside the margin of a cutoff: decided by the exact distance
+                        // (FP64 only on that rare branch: GB300 issues FP64 at a small
+                        // fraction of the FP32 rate)
+                        const bool x3 = t0 && !(e2 < c3lo2) && !(e2 >= c3hi2);
+                        const bool x4 = q0 && !(e2 < c4lo2) && !(e2 >= c4hi2);
+                        t = t0 && e2 < c3lo2;
+                        q = q0 && e2 < c4lo2;
+                        if (x3 || x4) {
+                            const double dx = dist_frac(hn, &B.ghost_fn[3 * (long long)ga], &B.ghost_fn[3 * (long long)gb]);
+                            if (x3) t = dx < c3;
+                            if (x4) q = dx < c4;
                         }
                     }
                     const unsigned bt = __ballot_sync(kFull, t), bq = __ballot_sync(kFull, q);
