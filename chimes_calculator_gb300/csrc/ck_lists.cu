@@ -309,32 +309,43 @@ __device__ __forceinline__ void put_xp(const BatchView& B, long long pos, int q)
 }
 
 // each bin's members in ascending ghost id (the reference pushes ghosts into
-// bins in index order): one warp per bin; a member's place is the number of
-// members with a smaller id (ids are unique), counted over the warp's
-// registers; bins above 64 members fall back to an insertion sort by one lane
-__global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* bin_start) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (b >= B.n_bins_total) return;   // whole warp
-    const long long s0 = bin_start[b];
-    const int n = B.bin_count[b];
+// bins in index order): a warp takes one bin, or 32 in a large batch (most of
+// the reserved bins are empty); a bin of one member needs no sort, larger
+// ones are ranked by the whole warp in turn: a member's place is the number of members with a
+// smaller id (ids are unique), counted over the warp's registers up to 64
+// members, over a shared-memory copy of the ids up to kRankSmem; larger
+// bins (none in practice) fall back to an insertion sort by one lane
+constexpr int kRankSmem = 256;
+__device__ __forceinline__ void rank_bin(const BatchView& B, long long s0, int n, int lane, int* key, int* val) {
     int* v = B.bin_items + s0;
-    if (n <= 0) return;
-    if (n == 1) {
-        if (lane == 0 && B.bin_xp) put_xp(B, s0, v[0]);
+    if (n > 64 && n <= kRankSmem) {
+        for (int i = lane; i < n; i += 32) {
+            val[i] = v[i];
+            key[i] = B.ghost_id[val[i]];
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            const int k = key[i];
+            int r = 0;
+            for (int j = 0; j < n; j++) r += key[j] < k;
+            v[r] = val[i];
+            if (B.bin_xp) put_xp(B, s0 + r, val[i]);
+        }
+        __syncwarp();
         return;
     }
     if (n > 64) {
         if (lane == 0)
             for (int i = 1; i < n; i++) {
-                const int key = v[i], kid = B.ghost_id[key];
+                const int k2 = v[i], kid = B.ghost_id[k2];
                 int j = i - 1;
                 while (j >= 0 && B.ghost_id[v[j]] > kid) { v[j + 1] = v[j]; j--; }
-                v[j + 1] = key;
+                v[j + 1] = k2;
             }
         __syncwarp();
         if (B.bin_xp)
             for (int i = lane; i < n; i += 32) put_xp(B, s0 + i, v[i]);
+        __syncwarp();
         return;
     }
     const int big = 0x7fffffff;
@@ -354,6 +365,28 @@ __global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* 
     if (q1 >= 0) {
         v[r1] = q1;
         if (B.bin_xp) put_xp(B, s0 + r1, q1);
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) k_bin_rank(BatchView B, const long long* bin_start, int per) {
+    __shared__ int s_key[8][kRankSmem], s_val[8][kRankSmem];
+    const long long b0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * per;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    if (b0 >= B.n_bins_total) return;   // whole warp
+    const long long b = b0 + lane;
+    int n = 0;
+    long long st = 0;
+    if (lane < per && b < B.n_bins_total) {
+        n = B.bin_count[b];
+        if (n > 0) st = bin_start[b];
+    }
+    if (n == 1 && B.bin_xp) put_xp(B, st, B.bin_items[st]);
+    unsigned many = __ballot_sync(kFull, n > 1);
+    while (many) {
+        const int src = __ffs(many) - 1;
+        many &= many - 1;
+        rank_bin(B, __shfl_sync(kFull, st, src), __shfl_sync(kFull, n, src), lane, s_key[wib], s_val[wib]);
     }
 }
 
@@ -1180,7 +1213,13 @@ void launch_bin_scatter(const BatchView& B, cudaStream_t st) {
     if (B.n_ghost_total) count_launch(), k_bin_scatter<<<grid_for(B.n_ghost_total, 256), 256, 0, st>>>(B, B.bin_start);
 }
 void launch_bin_sort(const BatchView& B, cudaStream_t st) {
-    if (B.n_bins_total) count_launch(), k_bin_rank<<<grid_for(B.n_bins_total * 32, 256), 256, 0, st>>>(B, B.bin_start);
+    if (!B.n_bins_total) return;
+    // bins per warp: one while that still gives a few warps per resident slot
+    // (a small batch's bins are few and mostly occupied), else 32 (a large
+    // batch reserves many times the bins its ghost clouds occupy)
+    const int per = B.n_bins_total > 64LL * 32 * sm_count() ? 32 : 1;
+    const long long warps = (B.n_bins_total + per - 1) / per;
+    count_launch(), k_bin_rank<<<grid_for(warps * 32, 256), 256, 0, st>>>(B, B.bin_start, per);
 }
 void launch_l2(const BatchView& B, int* l2_owner, bool fill, cudaStream_t st) {
     if (!B.n_atoms_total) return;
