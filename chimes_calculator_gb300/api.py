@@ -109,8 +109,11 @@ class Calculator:
     def tuning(self) -> dict:
         v = np.zeros(11, dtype=np.int32)
         self._check(self.lib.ck_get_tuning(self.h, _ip(v)))
-        keys = ["tpc3", "tpc4", "blocks_per_sm", "fact3", "fact4", "ftpc3", "ftpc4", "fbps3", "fbps4", "noy3", "tc3"]
-        return {k: int(x) for k, x in zip(keys, v)}
+        keys = ["tpc3", "tpc4", "blocks_per_sm", "fact3", "fact4", "ftpc3", "ftpc4", "fbps3", "fbps4", "noy3"]
+        out = {k: int(x) for k, x in zip(keys, v)}
+        out["tc3"] = int(v[10]) & 1      # tensor-core 3-body contraction in use
+        out["tc4"] = (int(v[10]) >> 1) & 1
+        return out
 
     def type_indices(self, types: Sequence[str], slot: int = 0) -> np.ndarray:
         cache = self._types[slot]

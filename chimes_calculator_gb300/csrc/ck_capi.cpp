@@ -318,7 +318,7 @@ int ck_get_tuning(void* h, int* out) {
     if (int st = check_handle(h)) return st;
     const ck::ForceLaunch& L = static_cast<Instance*>(h)->eng.tuning;
     const int v[11] = {L.tpc3,  L.tpc4,  L.blocks_per_sm, L.fact3, L.fact4, L.ftpc3,
-                       L.ftpc4, L.fbps3, L.fbps4,         L.noy3,  L.tc3};
+                       L.ftpc4, L.fbps3, L.fbps4,         L.noy3,  L.tc3 | (L.tc4 << 1)};
     for (int k = 0; k < 11; k++) out[k] = v[k];
     return ck::kOk;
 }
@@ -360,7 +360,7 @@ int ck_set_contraction(void* h, int factored) {
     e.factored = factored != 0;
     e.pair_cache = factored != 2;
     e.tuning.noy3 = factored == 3 ? 1 : 0;
-    e.tuning.want_tc3 = factored == 4 ? 1 : 0;
+    e.tuning.want_tc3 = e.tuning.want_tc4 = factored == 4 ? 1 : 0;
     return ck::kOk;
 }
 

@@ -68,8 +68,9 @@ struct TupleRec {
     // right after them (f_ncol); row entries at [f_ent, f_ent+ncoef), column
     // entries at [f_ent+ncoef, f_ent+2*ncoef)
     int f_row, f_nrow, f_ncol, f_ent;
-    // tensor-core form (3-body): offset of the tuple's coefficient matrix
-    // images in DevParamSet::tc3 (floats), -1 when absent
+    // tensor-core form: offset of the tuple's coefficient matrix images in
+    // DevParamSet::tc3 (3-body tuples) or tc4 (4-body tuples), in floats; -1
+    // when absent
     int tc_off, tc_pad;
     double rin[6], rout[6], lam[6], xavg[6], xdiff[6];
     // reciprocals for the factored kernels: 1/lam, 1/xdiff, and the cutoff's
@@ -104,6 +105,13 @@ constexpr int kTc3MaxR = 11;
 constexpr int kTc3Parts = 3;
 CK_HD constexpr int tc3_kpad(int Rw) { return Rw <= 8 ? 8 : 16; }
 CK_HD constexpr int tc3_npad(int Rw) { return ((Rw * Rw + 15) / 16) * 16; }
+// Tensor-core 4-body images (DevParamSet::tc4): with R powers per pair the
+// rows I = (q_ij, q_ik, q_il) and columns J = (q_jk, q_jl, q_kl) number
+// n3 = R^3 each; K = n3 padded to 8, N = n3 padded to 16 (shared memory keeps
+// R <= kTc4MaxR); one image per tuple at the set's own R, kTc3Parts parts.
+constexpr int kTc4MaxR = 4;
+CK_HD constexpr int tc4_kpad(int n3) { return (n3 + 7) / 8 * 8; }
+CK_HD constexpr int tc4_npad(int n3) { return (n3 + 15) / 16 * 16; }
 CK_HD inline long long tc3_offset(int R, int Rw) {
     long long o = 0;
     for (int r = R; r < Rw; r++) o += (long long)kTc3Parts * tc3_kpad(r) * tc3_npad(r);
@@ -181,9 +189,14 @@ struct DevParamSet {
     // tc3_k, tc3_n = K and N at Rw = R3; null when R3 is 0 or above kTc3MaxR
     int tc3_k, tc3_n;
     const float* tc3;
+    // tensor-core 4-body contraction (mixed form): per tuple, A[I][J] with
+    // I = (q_ij, q_ik, q_il), J = (q_jk, q_jl, q_kl) as the B operand, at
+    // tc4_r = R4 powers per pair; null when R4 is below 2 or above kTc4MaxR
+    int tc4_r, tc4_pad;
+    const float* tc4;
     // table lengths, for the index checks of the checked build (CK_BOUNDS):
     // 3-/4-body coefficients, factored entries, tensor-core image floats
-    long long n_c3, n_c4, n_fe3, n_fe4, n_tc3;
+    long long n_c3, n_c4, n_fe3, n_fe4, n_tc3, n_tc4;
     const FactRow* fr3; const FactEntD* fe3d; const FactEntF* fe3f;
     const FactRow* fr4; const FactEntD* fe4d; const FactEntF* fe4f;
     // per-pair-type tables [npairs] (null when some tuple's cutoffs differ by tuple)

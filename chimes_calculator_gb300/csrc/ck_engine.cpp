@@ -120,6 +120,7 @@ int Engine::load_params(const std::string& path, std::string& err) {
     rel(h.fr4); rel(h.fe4d); rel(h.fe4f);
     rel(h.pt3); rel(h.pt4);
     rel(h.tc3);
+    rel(h.tc4);
     rel(h.t2rec); rel(h.tab2r); rel(h.tab2c);
     rel(h.t3rec); rel(h.tab3r); rel(h.tab3v);
     // this set's cluster buckets follow those of the sets loaded before it
@@ -158,7 +159,8 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     bool fact3 = factored, fact4 = factored;
     bool pc3 = pair_cache, pc4 = pair_cache;
     int rf3 = 0, rf4 = 0;
-    bool tc3 = precision == kMixed;
+    bool tc3 = precision == kMixed, tc4 = precision == kMixed;
+    int r4_lo = 1 << 30;   // the 4-body tensor-core kernel needs one R over the batch's sets
     bool enum_serial = false;
     double n2_est = 0.0, n3_est = 0.0, n4_est = 0.0;
     for (int s = 0; s < S; s++) {
@@ -211,7 +213,13 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
             pc3 = pc3 && V.pt3;
             tc3 = tc3 && V.tc3 != nullptr;
         }
-        if (P.o4 > 0) { fact4 = fact4 && V.R4 > 0; rf4 = std::max(rf4, V.R4); pc4 = pc4 && V.pt4; }
+        if (P.o4 > 0) {
+            fact4 = fact4 && V.R4 > 0;
+            rf4 = std::max(rf4, V.R4);
+            r4_lo = std::min(r4_lo, V.R4);
+            pc4 = pc4 && V.pt4;
+            tc4 = tc4 && V.tc4 != nullptr;
+        }
         // list-size estimates for the first capacity guess
         const double rho = d.n_atoms / (vols_[s] > 0 ? vols_[s] : 1.0);
         const double m = rho * 4.18879 * d.search * d.search * d.search;
@@ -231,6 +239,8 @@ Status Engine::stage(const std::vector<SystemSpec>& sys, std::string& err) {
     avail_fact4_ = fact4 && rf4 > 0;
     avail_tc3_ = avail_fact3_ && tc3 && tc3_supported(rf3);
     tuning.tc3 = tuning.fact3 && avail_tc3_ && tuning.want_tc3 ? 1 : 0;
+    avail_tc4_ = avail_fact4_ && tc4 && r4_lo == rf4 && tc4_supported(rf4);
+    tuning.tc4 = tuning.fact4 && avail_tc4_ && tuning.want_tc4 ? 1 : 0;
     // the pair-table cache needs the enumeration that records entry indices;
     // it pays for itself while its tables stay near L2 (measured: ~10% on the
     // 3-body kernel for 25k list entries, nothing for 11M), so large batches
@@ -396,7 +406,7 @@ Status Engine::enqueue(std::string& err) {
     BatchView B = V_;
     B.use_pc3 = avail_pc3_ && tuning.fact3 && (tuning.tc3 || pc_small_) ? 1 : 0;
     B.bk_pad3 = tuning.tc3 ? 128 : 32;
-    B.use_pc4 = avail_pc4_ && tuning.fact4 ? 1 : 0;
+    B.use_pc4 = avail_pc4_ && tuning.fact4 && !tuning.tc4 ? 1 : 0;
     cudaStream_t st = stream_;
     const long long k0 = launch_counter();
     if (profile) {
@@ -459,7 +469,10 @@ Status Engine::enqueue(std::string& err) {
     auto body4 = [&](cudaStream_t q) {
         if (L.stride4 <= 0) return;
         NvtxRange r("chimes: 4B");
-        if (L.fact4) {
+        if (L.fact4 && L.tc4) {
+            launch_bucket(B, 4, q);
+            launch_force4tc(B, L, q);
+        } else if (L.fact4) {
             launch_pair_tables(B, d_l2_owner_.p, 4, L, q);
             launch_bucket(B, 4, q);
             launch_force4f(B, L, q);
@@ -522,7 +535,7 @@ Status Engine::launch(std::string& err) {
                                   tuning.stride3, tuning.stride4, tuning.blocks_per_sm, profile ? 1 : 0,
                                   tuning.fact3, tuning.fact4, tuning.rf3, tuning.rf4, tuning.ftpc3, tuning.ftpc4,
                                   tuning.fbps3, tuning.fbps4, nbk3_, nbk4_, concurrent ? 1 : 0, tuning.noy3,
-                                  tuning.tc3};
+                                  tuning.tc3, tuning.tc4};
     for (const void* p : {(const void*)V_.sys, (const void*)V_.in_pos, (const void*)V_.ghost_fs,
                           (const void*)V_.bin_items, (const void*)V_.l2_ghost, (const void*)V_.c3,
                           (const void*)V_.c4, (const void*)V_.force, (const void*)d_scan_tmp_.p,
@@ -665,9 +678,11 @@ Status Engine::autotune(int* chosen, std::string& err) {
             tuning.want_fact4 = kv.second.want_fact4;
             tuning.noy3 = kv.second.noy3;
             tuning.want_tc3 = kv.second.want_tc3;
+            tuning.want_tc4 = kv.second.want_tc4;
             tuning.fact3 = avail_fact3_ && tuning.want_fact3;
             tuning.fact4 = avail_fact4_ && tuning.want_fact4;
             tuning.tc3 = tuning.fact3 && avail_tc3_ && tuning.want_tc3;
+            tuning.tc4 = tuning.fact4 && avail_tc4_ && tuning.want_tc4;
             report();
             return kOk;
         }
@@ -707,7 +722,7 @@ Status Engine::autotune(int* chosen, std::string& err) {
     // in shared memory per cluster, so each is tried at 8 and at up to 16
     // resident one-warp blocks per SM (capped by its occupancy); the per-SM
     // count is refined below.
-    // (3-body in the mixed form also the tensor-core contraction)
+    // (in the mixed form also the tensor-core contractions)
     struct Cand { int fact, tpc, noy, fbps, tc; };
     auto cands = [](bool can_fact, bool with_noy, bool with_tc) {
         std::vector<Cand> v;
@@ -722,7 +737,7 @@ Status Engine::autotune(int* chosen, std::string& err) {
         for (int t : {1, 2, 4, 8, 16, 32}) v.push_back({0, t, 0, 0, 0});
         return v;
     };
-    const std::vector<Cand> c3 = cands(avail_fact3_, true, avail_tc3_), c4 = cands(avail_fact4_, false, false);
+    const std::vector<Cand> c3 = cands(avail_fact3_, true, avail_tc3_), c4 = cands(avail_fact4_, false, avail_tc4_);
     auto apply = [&](int nb, const Cand& c) {
         if (nb == 3) {
             tuning.fact3 = c.fact;
@@ -733,12 +748,13 @@ Status Engine::autotune(int* chosen, std::string& err) {
         } else {
             tuning.fact4 = c.fact;
             (c.fact ? tuning.ftpc4 : tuning.tpc4) = c.tpc;
+            tuning.tc4 = c.tc;
             if (c.fbps > 0) tuning.fbps4 = c.fbps;
         }
     };
     double best3 = 1e300, best4 = 1e300;
     Cand b3 = {tuning.fact3, tuning.fact3 ? tuning.ftpc3 : tuning.tpc3, tuning.noy3, tuning.fbps3, tuning.tc3};
-    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0, tuning.fbps4, 0};
+    Cand b4 = {tuning.fact4, tuning.fact4 ? tuning.ftpc4 : tuning.tpc4, 0, tuning.fbps4, tuning.tc4};
     const size_t nc = std::max(c3.size(), c4.size());
     for (size_t i = 0; i < nc && st == kOk; i++) {
         const bool need3 = do3 && i < c3.size(), need4 = do4 && i < c4.size();
@@ -759,8 +775,9 @@ Status Engine::autotune(int* chosen, std::string& err) {
     tuning.want_fact3 = b3.fact;
     tuning.want_fact4 = b4.fact;
     tuning.want_tc3 = b3.tc;
-    // (the tensor-core form's occupancy is fixed by its shared memory: two blocks per SM)
-    const bool f3 = tuning.fact3 != 0 && !tuning.tc3, f4 = tuning.fact4 != 0;
+    tuning.want_tc4 = b4.tc;
+    // (the tensor-core forms' occupancy is fixed by their shared memory)
+    const bool f3 = tuning.fact3 != 0 && !tuning.tc3, f4 = tuning.fact4 != 0 && !tuning.tc4;
     // resident blocks per SM: 4-warp blocks for the per-coefficient kernels,
     // one-warp blocks for the factored ones (capped by their occupancy)
     const int bps[] = {1, 2, 4, 8};

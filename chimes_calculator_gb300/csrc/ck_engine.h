@@ -191,6 +191,7 @@ private:
     int nbk3_ = 0, nbk4_ = 0;     // cluster buckets over all loaded parameter sets
     bool avail_fact3_ = false, avail_fact4_ = false;   // staged batch has factored tables
     bool avail_tc3_ = false;                           // ... and tensor-core 3-body images (mixed form)
+    bool avail_tc4_ = false;                           // ... and tensor-core 4-body images at one R
     bool enum_serial_ = false;                         // staged batch needs the sequential enumeration
     bool avail_pc3_ = false, avail_pc4_ = false;       // pair-table cache usable for the staged batch
     bool pc_small_ = false;                            // list small enough for the cache to stay near L2

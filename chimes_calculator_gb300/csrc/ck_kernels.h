@@ -53,6 +53,8 @@ struct ForceLaunch {
     // tensor-core 3-body contraction (mixed form only; ck_tensor.cu): tc3 = in
     // use for this launch, want_tc3 = preference (autotuner or forced)
     int tc3 = 0, want_tc3 = 0;
+    // tensor-core 4-body contraction (mixed form, one R <= kTc4MaxR over the batch)
+    int tc4 = 0, want_tc4 = 0;
 };
 
 // Cluster counts are read on the device (l2_off[n_atoms], e_off3/4[n2_cap]) and
@@ -73,6 +75,10 @@ void launch_force4f(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // pair in [2, kTc3MaxR]; clusters bucketed with 128-slot padding (bk_pad3).
 bool tc3_supported(int rf3);
 void launch_force3tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
+// Tensor-core 4-body contraction (ck_tensor.cu): mixed form, R4 powers per
+// pair in [2, kTc4MaxR]; tiles of 32 clusters (the 4-body buckets' padding).
+bool tc4_supported(int rf4);
+void launch_force4tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st);
 // dynamic shared memory of one factored-kernel block (one warp)
 size_t factored_smem_bytes(int nbody, int precision, int tpc, int rs);
 

@@ -795,6 +795,27 @@ void tc3_image(const std::vector<double>& dense, int R, int Rw, std::vector<floa
             }
 }
 
+// Tensor-core image of one 4-body tuple's dense coefficient matrix
+// A[I][J] (I = (q_ij, q_ik, q_il), J = (q_jk, q_jl, q_kl), n3 = R^3 each):
+// the B operand of W = X . A, N = tc4_npad(n3) rows (J) of K = tc4_kpad(n3)
+// values (I), in tc3_image's layout and parts.
+void tc4_image(const std::vector<double>& dense, int n3, std::vector<float>& out) {
+    const int kpad = tc4_kpad(n3), npad = tc4_npad(n3);
+    const size_t base = out.size();
+    const size_t part = (size_t)kpad * npad;
+    out.resize(base + kTc3Parts * part, 0.0f);
+    for (int n = 0; n < n3; n++)
+        for (int k = 0; k < n3; k++) {
+            double rest = dense[(size_t)k * n3 + n];
+            const size_t off = ((size_t)(n / 8) * (kpad / 4) + k / 4) * 32 + (n % 8) * 4 + (k % 4);
+            for (int t = 0; t < kTc3Parts; t++) {
+                const float v = t + 1 < kTc3Parts ? tf32_hi_host((float)rest) : (float)rest;
+                out[base + t * part + off] = v;
+                rest -= (double)v;
+            }
+        }
+}
+
 // set_cheby_polys' Morse-map constants (chimesFF.h:553-559)
 void morse_consts(double rin, double rout, double lam, double& xavg, double& xdiff) {
     double x_min = std::exp(-1 * rin / lam);
@@ -892,7 +913,8 @@ ParamImage pack_params(const HostParams& P) {
         // tensor-core images (3-body, R <= kTc3MaxR: N = R^2 <= 128 TMEM columns
         // per accumulator), one per working width Rw = R .. kTc3MaxR so that a
         // batch mixing sets of different orders runs at its largest R
-        const bool tc = nb == 3 && fact && R_pow >= 2 && R_pow <= kTc3MaxR;
+        const bool tc = nb == 3 ? fact && R_pow >= 2 && R_pow <= kTc3MaxR
+                                : fact && R_pow >= 2 && R_pow <= kTc4MaxR;
         std::vector<float> tcimg;
         struct Shared { int coef_off, f_row, f_nrow, f_ncol, f_ent, tc_off; };
         std::map<std::pair<int, std::vector<int>>, Shared> shared;  // (type, mapping) -> tables
@@ -984,11 +1006,18 @@ ParamImage pack_params(const HostParams& P) {
                     if (pass == 0) R.f_nrow = nrec; else R.f_ncol = nrec;
                 }
             }
-            if (tc && R.ncoef > 0) {
+            if (tc && R.ncoef > 0 && nb == 3) {
                 std::vector<double> dense((size_t)R_pow * R_pow * R_pow, 0.0);
                 for (int c = 0; c < R.ncoef; c++) dense[(size_t)rowi[c] * R_pow * R_pow + coli[c]] += Bd.coef[ti][c];
                 R.tc_off = (int)tcimg.size();
                 for (int Rw = R_pow; Rw <= kTc3MaxR; Rw++) tc3_image(dense, R_pow, Rw, tcimg);
+            }
+            if (tc && R.ncoef > 0 && nb == 4) {
+                const int n3 = R_pow * R_pow * R_pow;
+                std::vector<double> dense((size_t)n3 * n3, 0.0);
+                for (int c = 0; c < R.ncoef; c++) dense[(size_t)rowi[c] * n3 + coli[c]] += Bd.coef[ti][c];
+                R.tc_off = (int)tcimg.size();
+                tc4_image(dense, n3, tcimg);
             }
             shared[key] = Shared{R.coef_off, R.f_row, R.f_nrow, R.f_ncol, R.f_ent, R.tc_off};
         }
@@ -1028,6 +1057,11 @@ ParamImage pack_params(const HostParams& P) {
             H.tc3_n = tc3_npad(R_pow);
             H.tc3 = as_off<const float>(B.add(tcimg.data(), tcimg.size()));
             H.n_tc3 = (long long)tcimg.size();
+        }
+        if (nb == 4 && tc && Rf > 0 && !tcimg.empty()) {
+            H.tc4_r = R_pow;
+            H.tc4 = as_off<const float>(B.add(tcimg.data(), tcimg.size()));
+            H.n_tc4 = (long long)tcimg.size();
         }
         if (nb == 3) {
             H.n_c3 = (long long)cd.size();

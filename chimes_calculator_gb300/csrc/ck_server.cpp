@@ -188,6 +188,7 @@ public:
             d.ftpc3 = t.ftpc3, d.ftpc4 = t.ftpc4, d.fbps3 = t.fbps3, d.fbps4 = t.fbps4;
             d.want_fact3 = t.want_fact3, d.want_fact4 = t.want_fact4, d.noy3 = t.noy3;
             d.want_tc3 = t.want_tc3;
+            d.want_tc4 = t.want_tc4;
         }
         return kOk;
     }
@@ -271,7 +272,7 @@ public:
         std::lock_guard<std::mutex> ge(*engine_mu_[w]);
         const ForceLaunch& L = engines_[w]->tuning;
         const int v[11] = {L.tpc3, L.tpc4, L.blocks_per_sm, L.want_fact3, L.want_fact4, L.ftpc3,
-                           L.ftpc4, L.fbps3, L.fbps4, L.noy3, L.want_tc3};
+                           L.ftpc4, L.fbps3, L.fbps4, L.noy3, L.want_tc3 | (L.want_tc4 << 1)};
         for (int k = 0; k < 11; k++) out[k] = v[k];
         return kOk;
     }

@@ -451,9 +451,351 @@ void launch_tc_r(const BatchView& B, cudaStream_t st) {
     count_launch(), kern<<<grid, kTcTile, smem, st>>>(B, B.c3, B.perm3, pn, B.perm3_cap);
 }
 
+
+// ---------------------------------------------------------------------------
+// Tensor-core 4-body contraction (mixed form).  With R powers per pair a
+// tuple's coefficients form a dense matrix A[I][J], I = (q_ij, q_ik, q_il) and
+// J = (q_jk, q_jl, q_kl) (R^3 each).  For a cluster, X_I = T_ij T_ik T_il and
+// Y_J = T_jk T_jl T_kl: S = X.A.Y, and the pair gradients are
+//   G_ij = dX_ij.A.Y, G_ik = dX_ik.A.Y, G_il = dX_il.A.Y  (dX_p: T_p -> dT_p/dr)
+//   G_jk, G_jl, G_kl = W.dY_p with W = X.A.
+// A tile is 32 clusters of one tuple and the MMA's 128 rows are the four row
+// vectors X, dX_ij, dX_ik, dX_il of each (row 32 v + c: warp v builds variant
+// v of cluster c and reads its TMEM row back), so one M = 128, N = R^3 MMA
+// chain gives W, W_ij, W_ik, W_il for all 32 clusters; each row is then
+// contracted with the cluster's column tables, and warp 0 forms the forces.
+// Operands in three TF32 parts as in the 3-body kernel (six part products,
+// smallest first).  Pair tables are computed by the four threads of a
+// cluster (pairs v and v + 4), after the early-outs of all six pairs.
+constexpr int kTc4Tile = 32;              // clusters per tile
+
+template <int R>
+__global__ void __launch_bounds__(128, 2) k_forcetc4(BatchView B, const int* clusters, const int* perm,
+                                                     const long long* perm_n, long long perm_cap) {
+    constexpr int N3 = R * R * R;
+    constexpr int KP = tc4_kpad(N3);                    // K padded to whole MMA steps
+    constexpr int NP = tc4_npad(N3);                    // N padded to 16
+    // the A operand goes in K halves of KH through one buffer (two CTAs per
+    // SM fit in shared memory that way)
+    constexpr int KH = KP > 32 ? KP / 2 : KP;
+    constexpr int NH = KP / KH;
+    constexpr int AFL = 128 * KH;                       // floats per A part image (one K half)
+    constexpr int BFL = NP * KP;                        // floats per B part image
+    constexpr uint32_t LBO = 128, SBOA = KH * 32, SBOB = KP * 32;   // bytes: next core matrix in K; next 8 rows
+    // TMEM: the large (h.h) and the small part products in separate
+    // accumulators, summed in FP32 at the end (each accumulates its own terms
+    // in order of size, whatever the K half)
+    constexpr uint32_t DCOL = NP <= 32 ? 32 : (NP <= 64 ? 64 : 128);
+    constexpr uint32_t COLS = 2 * DCOL;
+    constexpr int C = kTc4Tile;
+    static_assert(kTc3Parts == 3, "the MMA sequence below pairs three parts");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float* As = reinterpret_cast<float*>(smem);         // rows X / dX parts h, m, l
+    float* Bs = As + 3 * AFL;                           // coefficient parts
+    __shared__ float s_tab[6][2 * R][C];                // T, then dT/dr, per pair and cluster
+    __shared__ float s_fc[6][C], s_fcd[6][C], s_rinv[6][C], s_dr[6][3][C];
+    __shared__ double s_r[6][C];
+    __shared__ int s_far[6][C];
+    __shared__ float s_res[7][C];                       // S, G_0 .. G_5
+    __shared__ uint32_t s_tmem;
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ long long s_tile, s_next;
+
+    const int tid = threadIdx.x, warp = tid >> 5, c = tid & 31;
+    const long long n = min(*perm_n, perm_cap);
+    const long long ntiles = n / C;
+    if (tid < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s_tmem;
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                           ((uint32_t)(128 >> 4) << 24);
+    uint32_t phase = 0;
+    int loaded = -1;                                    // tc_off of the B image in shared memory
+    const DevParamSet* loaded_set = nullptr;
+    EVAcc acc;
+
+    // tiles: a contiguous block per CTA, then the last eighth one at a time
+    // (as in the 3-body kernel), claimed one ahead
+    const long long per = ntiles * 7 / 8 / gridDim.x;
+    long long own = (long long)blockIdx.x * per;
+    const long long own_end = own + per, shared0 = per * gridDim.x;
+    auto claim = [&]() -> long long {
+        return own < own_end ? own++ : shared0 + (long long)atomicAdd(&B.queue[1], 1ull);
+    };
+    if (tid == 0) s_next = claim();
+    for (;;) {
+        if (tid == 0) {
+            s_tile = s_next;
+            s_next = s_next < ntiles ? claim() : ntiles;
+        }
+        __syncthreads();
+        const long long tile = s_tile;
+        if (tile >= ntiles) break;
+        const long long base = tile * C;
+        const int c0 = perm[base];
+        if (c0 < 0) {               // uniform: a tile never starts in a bucket's padding
+            __syncthreads();
+            continue;
+        }
+        int id0[4], s0, u0;
+        const DevParamSet* P;
+        const TupleRec* Rt = cluster_tuple<4>(B, clusters, c0, id0, s0, P, u0);
+        if (Rt->tc_off != loaded || P != loaded_set) {
+            const long long img = Rt->tc_off;
+            const bool img_ok = ck_bound(B, img >= 0 && img + (long long)kTc3Parts * BFL <= P->n_tc4);
+            const float4* src = reinterpret_cast<const float4*>(P->tc4 + (img_ok ? img : 0));
+            float4* dst = reinterpret_cast<float4*>(Bs);
+            for (int q = tid; q < kTc3Parts * BFL / 4; q += 128) dst[q] = src[q];
+            loaded = Rt->tc_off;
+            loaded_set = P;
+        }
+        // this cluster's geometry: pairs warp and warp + 4 (the four warps
+        // cover the six pairs)
+        const int cl = perm[base + c];
+        int id[4] = {0, 0, 0, 0};
+        int s = 0;
+        if (cl >= 0) {
+            for (int k = 0; k < 4; k++) id[k] = clusters[4LL * cl + k];
+            s = B.atom_sys[B.ghost_parent[id[0]]];
+        }
+        for (int p = warp; p < 6; p += 4) {
+            double d[3] = {0, 0, 0}, r = 1e300;
+            if (cl >= 0) pair_geom(B, B.sys[s].h, id[Topo<4>::a(p)], id[Topo<4>::b(p)], d, r);
+            s_far[p][c] = cl < 0 || r >= Rt->rout[p];   // compute_4B's early-outs
+            s_r[p][c] = r;
+            s_dr[p][0][c] = float(d[0]);
+            s_dr[p][1][c] = float(d[1]);
+            s_dr[p][2][c] = float(d[2]);
+        }
+        __syncthreads();
+        bool active = true;
+#pragma unroll
+        for (int p = 0; p < 6; p++) active = active && !s_far[p][c];
+        for (int p = warp; p < 6; p += 4) {
+            float T[R], D[R], fc = 0.0f, fcd = 0.0f;
+#pragma unroll
+            for (int q = 0; q < R; q++) T[q] = D[q] = 0.0f;
+            if (active) pair_regs<R>(*P, *Rt, p, s_r[p][c], T, D, fc, fcd, B.flags);
+            const int R4 = P->R4;   // the set's own powers; entries above it multiply zero coefficients
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                s_tab[p][q][c] = q < R4 ? T[q] : 0.0f;
+                s_tab[p][R + q][c] = q < R4 ? D[q] : 0.0f;
+            }
+            s_fc[p][c] = fc;
+            s_fcd[p][c] = fcd;
+            s_rinv[p][c] = active ? 1.0f / float(s_r[p][c]) : 0.0f;
+        }
+        __syncthreads();
+        // row 32 warp + c of the A operand: X (warp 0) or dX_ij, dX_ik, dX_il
+        {
+            float f0[R], f1[R], f2[R];
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                f0[q] = s_tab[0][(warp == 1 ? R : 0) + q][c];
+                f1[q] = s_tab[1][(warp == 2 ? R : 0) + q][c];
+                f2[q] = s_tab[2][(warp == 3 ? R : 0) + q][c];
+            }
+            float* r0 = As + (tid >> 3) * (KH * 8) + (tid & 7) * 4;
+            bool ok = true;
+            for (int hf = 0; hf < NH && ok; hf++) {
+                if (hf > 0) {
+                    // the previous half's MMAs have read the buffer
+                    uint32_t done = 0;
+                    for (int it = 0; it < kTcSpin && !done; it++) {
+                        asm volatile(
+                            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                            : "=r"(done)
+                            : "r"(smem_u32(&s_bar)), "r"(phase)
+                            : "memory");
+                        if (!done && it > 256) __nanosleep(32);
+                    }
+                    phase ^= 1u;
+                    ok = __syncthreads_and(done);
+                    if (!ok) break;
+                }
+#pragma unroll
+                for (int j = 0; j < KH / 4; j++) {
+                    float h[4], md[4], l[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int k = hf * KH + 4 * j + u;
+                        const int kk = k < N3 ? k : 0;
+                        const float x = (active && k < N3) ? f0[kk / (R * R)] * f1[(kk / R) % R] * f2[kk % R] : 0.0f;
+                        h[u] = tf32_hi(x);
+                        const float rest = x - h[u];
+                        md[u] = tf32_hi(rest);
+                        l[u] = rest - md[u];
+                    }
+                    *reinterpret_cast<float4*>(r0 + j * 32) = make_float4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<float4*>(r0 + AFL + j * 32) = make_float4(md[0], md[1], md[2], md[3]);
+                    *reinterpret_cast<float4*>(r0 + 2 * AFL + j * 32) = make_float4(l[0], l[1], l[2], l[3]);
+                }
+                // generic-proxy writes of the operands -> visible to the tensor core
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncthreads();
+                if (tid == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t as = smem_u32(As), bs = smem_u32(Bs);
+                    constexpr uint32_t AB = AFL * 4, BB = BFL * 4;   // bytes per part image
+                    // small part products smallest first (m.m, h.l, l.h, h.m, m.h) into
+                    // the first accumulator, h.h into the second
+                    constexpr int pa[6] = {1, 0, 2, 0, 1, 0}, pb[6] = {1, 2, 0, 1, 0, 0};
+#pragma unroll
+                    for (int t = 0; t < 6; t++) {
+#pragma unroll
+                        for (int ks = 0; ks < KH / 8; ks++) {
+                            const uint32_t oa = ks * 256;                       // two core matrices along K per step
+                            const uint32_t ob = (hf * (KH / 8) + ks) * 256;
+                            const uint32_t d = t < 5 ? tmem : tmem + DCOL;
+                            const int acc = hf > 0 || ks > 0 || (t > 0 && t < 5);
+                            mma_tf32(d, umma_desc(as + pa[t] * AB + oa, LBO, SBOA),
+                                     umma_desc(bs + pb[t] * BB + ob, LBO, SBOB), idesc, acc);
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(&s_bar))
+                                 : "memory");
+                }
+            }
+            // bounded wait for the last half's MMAs
+            if (ok) {
+                uint32_t done = 0;
+                for (int it = 0; it < kTcSpin && !done; it++) {
+                    asm volatile(
+                        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                        : "=r"(done)
+                        : "r"(smem_u32(&s_bar)), "r"(phase)
+                        : "memory");
+                    if (!done && it > 256) __nanosleep(32);
+                }
+                phase ^= 1u;
+                ok = __syncthreads_and(done);
+            }
+            if (!ok) {
+                if (tid == 0) atomicOr(&B.flags[7], 1);
+                break;
+            }
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // this thread's TMEM row (small + large products), contracted with the
+        // cluster's column tables (jk: d, jl: e, kl: f; J = (d R + e) R + f)
+        float W[NP];
+        const uint32_t row = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int q = 0; q < NP / 16; q++) {
+            float big[16];
+            tmem_ld16(row + 16 * q, W + 16 * q);
+            tmem_ld16(row + DCOL + 16 * q, big);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int u = 0; u < 16; u++) W[16 * q + u] += big[u];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        {
+            float T3[R], D3[R], T4[R], D4[R], T5[R], D5[R];
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                T3[q] = s_tab[3][q][c]; D3[q] = s_tab[3][R + q][c];
+                T4[q] = s_tab[4][q][c]; D4[q] = s_tab[4][R + q][c];
+                T5[q] = s_tab[5][q][c]; D5[q] = s_tab[5][R + q][c];
+            }
+            float S = 0.0f, G3 = 0.0f, G4 = 0.0f, G5 = 0.0f;
+#pragma unroll
+            for (int d = 0; d < R; d++) {
+                float w = 0.0f, w1 = 0.0f, w2 = 0.0f;
+#pragma unroll
+                for (int e = 0; e < R; e++) {
+                    float u = 0.0f, u1 = 0.0f;
+#pragma unroll
+                    for (int f = 0; f < R; f++) {
+                        const float x = W[(d * R + e) * R + f];
+                        u += x * T5[f];
+                        u1 += x * D5[f];
+                    }
+                    w += u * T4[e];
+                    w1 += u * D4[e];
+                    w2 += u1 * T4[e];
+                }
+                S += w * T3[d];
+                G3 += w * D3[d];
+                G4 += w1 * T3[d];
+                G5 += w2 * T3[d];
+            }
+            if (warp == 0) {
+                s_res[0][c] = S;
+                s_res[4][c] = G3;
+                s_res[5][c] = G4;
+                s_res[6][c] = G5;
+            } else {
+                s_res[warp][c] = S;   // G_ij, G_ik, G_il from the derivative rows
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double e_c = 0.0, vir_c[6] = {0, 0, 0, 0, 0, 0};
+            if (active) {
+                float dr[6][3], rinv[6], fc[6], fcd[6], G[6];
+#pragma unroll
+                for (int p = 0; p < 6; p++) {
+                    dr[p][0] = s_dr[p][0][c]; dr[p][1] = s_dr[p][1][c]; dr[p][2] = s_dr[p][2][c];
+                    rinv[p] = s_rinv[p][c];
+                    fc[p] = s_fc[p][c];
+                    fcd[p] = s_fcd[p][c];
+                    G[p] = s_res[1 + p][c];
+                }
+                cluster_epilogue_f32<4>(B, id, dr, rinv, fc, fcd, s_res[0][c], G, e_c, vir_c);
+            }
+            acc.add_warp(B, s, e_c, vir_c, active);
+        }
+    }
+    if (warp == 0) acc.flush_warp(B);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(COLS));
+}
+
+template <int R>
+void launch_tc4_r(const BatchView& B, cudaStream_t st) {
+    constexpr int N3 = R * R * R;
+    constexpr int KP = tc4_kpad(N3);
+    constexpr int NP = tc4_npad(N3);
+    constexpr int KH = KP > 32 ? KP / 2 : KP;
+    const size_t smem = sizeof(float) * (3 * (size_t)128 * KH + kTc3Parts * (size_t)NP * KP);
+    auto kern = k_forcetc4<R>;
+    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const long long tiles = B.perm4_cap / kTc4Tile;
+    const long long want = 2LL * sm_count();   // two CTAs per SM (shared memory)
+    const unsigned grid = (unsigned)(want < tiles ? want : (tiles > 0 ? tiles : 1));
+    const long long* pn = B.bk_start + B.nbk3 + 1 + B.nbk4;
+    count_launch(), kern<<<grid, 128, smem, st>>>(B, B.c4, B.perm4, pn, B.perm4_cap);
+}
+
 }  // namespace
 
 bool tc3_supported(int rf3) { return rf3 >= 2 && rf3 <= kTc3MaxR; }
+bool tc4_supported(int rf4) { return rf4 >= 2 && rf4 <= kTc4MaxR; }
+
+void launch_force4tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
+    if (B.perm4_cap <= 0 || B.nbk4 <= 0) return;
+    switch (L.rf4) {
+        case 2: launch_tc4_r<2>(B, st); break;
+        case 3: launch_tc4_r<3>(B, st); break;
+        case 4: launch_tc4_r<4>(B, st); break;
+        default: break;
+    }
+}
 
 void launch_force3tc(const BatchView& B, const ForceLaunch& L, cudaStream_t st) {
     if (B.perm3_cap <= 0 || B.nbk3 <= 0) return;

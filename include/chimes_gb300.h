@@ -65,8 +65,8 @@ int ck_tuple_factored(void *h, int slot, int nbody, int *nrow, int *ncol, int *R
  * 4B in use for the staged batch (0/1), their threads per cluster and one-warp
  * blocks per SM (ftpc3, ftpc4, fbps3, fbps4), whether the factored 3-body
  * kernel forms its column products per coefficient instead of keeping a table
- * of them (noy3), and whether the 3-body contraction runs on the tensor cores
- * (tc3, mixed form) */
+ * of them (noy3), and which contractions run on the tensor cores (mixed
+ * form): bit 0 the 3-body one, bit 1 the 4-body one */
 int ck_get_tuning(void *h, int *out);
 /* index of an atom type name in a slot, or -1 */
 int ck_type_index(void *h, int slot, const char *name);
@@ -89,10 +89,11 @@ int ck_set_tuning(void *h, int tpc3, int tpc4, int blocks_per_sm);
  * tuple uses the same cutoffs for a given pair type); 3 = factored with the
  * 3-body kernel forming its column products per coefficient instead of
  * keeping a table of them (ck_autotune also tries this); 4 = factored with
- * the 3-body contraction on the tensor cores (tcgen05 TF32 MMAs with a
- * high/remainder split of both operands) in the mixed form, where every
- * parameter set of the batch has 2-11 powers per pair (ck_autotune also
- * tries this in the mixed form).  All give the same sums in another rounding
+ * the 3-body and 4-body contractions on the tensor cores (tcgen05 TF32 MMAs
+ * with a three-part split of both operands) in the mixed form, where every
+ * parameter set of the batch has 2-11 powers per pair (3-body) and one
+ * count of 2-4 powers per pair (4-body) (ck_autotune also tries these in the
+ * mixed form).  All give the same sums in another rounding
  * order. */
 int ck_set_contraction(void *h, int factored);
 /* Autotuner for the batch staged with ck_stage_batch: times the 3-body and
@@ -214,8 +215,9 @@ int ck_server_replay(void *server, int nreq, const int *slots, const int *natoms
 /* out[6] = submitted, completed, batches, largest batch, bytes in flight, peak bytes in flight */
 int ck_server_stats(void *server, long long *out);
 /* out[11] = worker's launch preferences, in ck_get_tuning's order with the
- * factored and tensor-core entries as preferences (want_fact3, want_fact4,
- * want_tc3): after ck_server_autotune every worker holds worker 0's. */
+ * factored and tensor-core entries as preferences (want_fact3, want_fact4;
+ * out[10] bit 0 the 3-body, bit 1 the 4-body tensor-core preference): after
+ * ck_server_autotune every worker holds worker 0's. */
 int ck_server_worker_tuning(void *server, int worker, int *out);
 
 /* Pair-style evaluation on a caller's full neighbour list with ghost atoms:

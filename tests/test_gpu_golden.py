@@ -64,17 +64,21 @@ def test_mixed_precision_error(golden, native_lib, name, factored):
 
 
 def test_tensor_core_form_runs(golden, native_lib):
-    """The tensor-core 3-body contraction is the one that runs when asked for
-    in the mixed form (3-body orders 2-11), gives the reference's results
-    within the mixed budget, and leaves the FP64 form on the CUDA cores."""
-    for name in ("c3_cut", "c2_small", "c1", "smallbox"):
+    """The tensor-core 3-body and 4-body contractions are the ones that run
+    when asked for in the mixed form (3-body orders 2-11; 4-body with 2-4
+    powers per pair: c3_cut, c2_small and smallbox have 4, rc4_gt_rc3 3, c1 no
+    4-body term), give the reference's results within the mixed budget, and
+    leave the FP64 form on the CUDA cores."""
+    for name, tc4 in (("c3_cut", 1), ("c2_small", 1), ("c1", 0), ("smallbox", 1), ("rc4_gt_rc3", 1),
+                      ("ref_hn3", 1)):
         g = golden[name]
         c, r = evaluate(g, precision=1, factored=4)
         assert c.tuning()["tc3"] == 1, name
+        assert c.tuning()["tc4"] == tc4, name
         assert abs(r["energy"] - g.energy) <= MIXED_E_REL_TOL * max(1.0, abs(g.energy)), name
-        assert g.force_error(r["force"]) <= MIXED_F_ABS_TOL, name
+        assert g.force_error(r["force"]) <= mixed_force_tol(np.abs(g.force).max()), name
         c64, r64 = evaluate(g, precision=0, factored=4)
-        assert c64.tuning()["tc3"] == 0
+        assert c64.tuning()["tc3"] == 0 and c64.tuning()["tc4"] == 0
         assert abs(r64["energy"] - g.energy) <= E_REL_TOL * max(1.0, abs(g.energy))
 
 
