@@ -818,6 +818,16 @@ __device__ __forceinline__ void group_sync(int grp) {
     else asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(32 * G) : "memory");
 }
 
+// position of the k-th (from 0) set bit of m
+__device__ __forceinline__ int select_bit(unsigned m, int k) {
+    int pos = 0;
+    for (int sh = 16; sh; sh >>= 1) {
+        const int c = __popc(m & ((1u << sh) - 1u));
+        if (k >= c) { k -= c; m >>= sh; pos += sh; }
+    }
+    return pos;
+}
+
 // n3 and n4 of entry a from the masks
 __device__ __forceinline__ void mask_counts(const unsigned* rt, const unsigned* rq, int a, int nw, int& n3, int& n4) {
     n3 = 0;
@@ -840,7 +850,7 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 4) k_enuma(BatchView B) {
     __shared__ int s_g[NG][kEnumRows];
     __shared__ unsigned s_t[NG][kEnumRows * kEnumWords];
     __shared__ unsigned s_q[NG][kEnumRows * kEnumWords];
-    __shared__ int s_o[G > 1 && FILL ? NG : 1][G > 1 && FILL ? 2 * kEnumRows : 1];   // per-entry offsets
+    __shared__ int s_o[FILL ? NG : 1][FILL ? 2 * kEnumRows + 2 : 1];   // per-entry offsets, then the totals
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = wib / G, w = wib % G;
     const unsigned lt = (1u << lane) - 1u;
@@ -934,74 +944,87 @@ __global__ void __launch_bounds__(32 * kEnumWarps, 4) k_enuma(BatchView B) {
             }
             continue;
         }
-        if (G > 1) {
-            // offsets of the entries relative to the first one, for the warps that emit them
-            int* so = s_o[G > 1 ? grp : 0];
-            if (w == 0) {
-                int c3 = 0, c4 = 0;
-                for (int a0 = 0; a0 < L; a0 += 32) {
-                    const int a = a0 + lane;
-                    int n3 = 0, n4 = 0;
-                    if (a < L) mask_counts(rt, rq, a, nw, n3, n4);
-                    int i3 = n3, i4 = n4;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int y3 = __shfl_up_sync(kFull, i3, o), y4 = __shfl_up_sync(kFull, i4, o);
-                        if (lane >= o) { i3 += y3; i4 += y4; }
-                    }
-                    if (a < L) { so[2 * a] = c3 + i3 - n3; so[2 * a + 1] = c4 + i4 - n4; }
-                    c3 += __shfl_sync(kFull, i3, 31);
-                    c4 += __shfl_sync(kFull, i4, 31);
+        // offsets of the entries within the atom (triplets, quadruplets) and
+        // the atom's totals
+        int* so = s_o[FILL ? grp : 0];
+        if (w == 0) {
+            int c3 = 0, c4 = 0;
+            for (int a0 = 0; a0 < L; a0 += 32) {
+                const int a = a0 + lane;
+                int n3 = 0, n4 = 0;
+                if (a < L) mask_counts(rt, rq, a, nw, n3, n4);
+                int i3 = n3, i4 = n4;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y3 = __shfl_up_sync(kFull, i3, o), y4 = __shfl_up_sync(kFull, i4, o);
+                    if (lane >= o) { i3 += y3; i4 += y4; }
                 }
+                if (a < L) { so[2 * a] = c3 + i3 - n3; so[2 * a + 1] = c4 + i4 - n4; }
+                c3 += __shfl_sync(kFull, i3, 31);
+                c4 += __shfl_sync(kFull, i4, 31);
             }
-            group_sync<G>(grp);
+            if (lane == 0) { so[2 * L] = c3; so[2 * L + 1] = c4; }
         }
+        group_sync<G>(grp);
+        // the atom's clusters in the reference's order, one per lane: the t-th
+        // triplet belongs to the last entry whose offset is <= t and is that
+        // entry's (t - offset)-th set bit of T; the t-th quadruplet likewise,
+        // walking the entry's k in Q and the set bits of Q[j] & Q[k]
         const int gi = B.atom_self[r];
-        for (int a = w; a < L; a += G) {
-            const long long e = b0 + a;
-            long long p3 = o3, p4 = o4;
-            if (G > 1) {
-                const int* so = s_o[G > 1 ? grp : 0];
-                p3 += so[2 * a];
-                p4 += so[2 * a + 1];
+        const long long base3 = B.e_off3[b0], base4 = B.e_off4[b0];
+        const int t3 = so[2 * L], t4 = so[2 * L + 1];
+        for (int t = 32 * w + lane; t < t3; t += 32 * G) {
+            int lo = 0, hi = L - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (so[2 * mid] <= t) lo = mid; else hi = mid - 1;
             }
-            const int ga = sg[a];
+            const int a = lo;
+            int rk = t - so[2 * a], bk = 0;
             for (int c = 0; c < nw; c++) {
                 const unsigned m = rt[a * kEnumWords + c];
-                if ((m >> lane) & 1u) {
-                    const long long q = p3 + __popc(m & lt);
-                    if (q < B.n3_cap) {
-                        int* out = B.c3 + 3 * q;
-                        out[0] = gi; out[1] = ga; out[2] = sg[32 * c + lane];
-                        if (B.c3e) { B.c3e[2 * q] = (int)e; B.c3e[2 * q + 1] = (int)(b0 + 32 * c + lane); }
-                    }
-                }
-                p3 += __popc(m);
+                const int pc = __popc(m);
+                if (rk < pc) { bk = 32 * c + select_bit(m, rk); break; }
+                rk -= pc;
             }
-            for (int c = 0; c < nw; c++) {
+            const long long q = base3 + t;
+            if (q < B.n3_cap) {
+                int* out = B.c3 + 3 * q;
+                out[0] = gi; out[1] = sg[a]; out[2] = sg[bk];
+                if (B.c3e) { B.c3e[2 * q] = (int)(b0 + a); B.c3e[2 * q + 1] = (int)(b0 + bk); }
+            }
+        }
+        for (int t = 32 * w + lane; t < t4; t += 32 * G) {
+            int lo = 0, hi = L - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (so[2 * mid + 1] <= t) lo = mid; else hi = mid - 1;
+            }
+            const int a = lo;
+            int rk = t - so[2 * a + 1], bk = 0, lk = 0;
+            bool found = false;
+            for (int c = 0; c < nw && !found; c++) {
                 unsigned mb = rq[a * kEnumWords + c];
-                while (mb) {
-                    const int b = 32 * c + __ffs(mb) - 1;
+                while (mb && !found) {
+                    const int bb = 32 * c + __ffs(mb) - 1;
                     mb &= mb - 1;
-                    const int gb = sg[b];
                     for (int c2 = 0; c2 < nw; c2++) {
-                        const unsigned m = rq[a * kEnumWords + c2] & rq[b * kEnumWords + c2];
-                        if ((m >> lane) & 1u) {
-                            const long long q = p4 + __popc(m & lt);
-                            if (q < B.n4_cap) {
-                                int* out = B.c4 + 4 * q;
-                                out[0] = gi; out[1] = ga; out[2] = gb; out[3] = sg[32 * c2 + lane];
-                                if (B.c4e) {
-                                    B.c4e[3 * q] = (int)e;
-                                    B.c4e[3 * q + 1] = (int)(b0 + b);
-                                    B.c4e[3 * q + 2] = (int)(b0 + 32 * c2 + lane);
-                                }
-                            }
-                        }
-                        p4 += __popc(m);
+                        const unsigned x = rq[a * kEnumWords + c2] & rq[bb * kEnumWords + c2];
+                        const int pc = __popc(x);
+                        if (rk < pc) { bk = bb; lk = 32 * c2 + select_bit(x, rk); found = true; break; }
+                        rk -= pc;
                     }
                 }
             }
-            if (G == 1) { o3 = p3; o4 = p4; }
+            const long long q = base4 + t;
+            if (q < B.n4_cap) {
+                int* out = B.c4 + 4 * q;
+                out[0] = gi; out[1] = sg[a]; out[2] = sg[bk]; out[3] = sg[lk];
+                if (B.c4e) {
+                    B.c4e[3 * q] = (int)(b0 + a);
+                    B.c4e[3 * q + 1] = (int)(b0 + bk);
+                    B.c4e[3 * q + 2] = (int)(b0 + lk);
+                }
+            }
         }
     }
 }
