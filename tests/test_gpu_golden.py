@@ -121,3 +121,25 @@ def test_graph_replay(golden, native_lib):
         r = c.evaluate(g.cfg.pos, g.cfg.types, g.cfg.cell)
         assert abs(r["energy"] - g.energy) <= E_REL_TOL * abs(g.energy)
         assert np.abs(r["force"] - g.force).max() <= F_ABS_TOL
+
+
+def test_tensor_core_4body_two_powers(tmp_path, native_lib):
+    """4-body order 2 runs the tensor-core 4-body kernel at its smallest width
+    (two powers per pair: rows and columns of 8, K = 8, N = 16) and gives the
+    oracle's result within the mixed budget; the FP64 form matches it within
+    the FP64 tolerances."""
+    from chimes_calculator_gb300 import FP64, MIXED, Calculator, synth
+    from oracle.oracle import Oracle
+    spec = synth.ParamSpec(elements=["C", "N"], orders=(10, 4, 2), rin=0.9, rout=5.0, lam=(1.3, 1.6),
+                           fcut=("TERSOFF", 0.5), s3max=4.0, s4max=3.2, seed=4343)
+    p = synth.write_param_file(str(tmp_path / "p.txt"), spec)
+    cfg = synth.random_config(160, np.diag([12.0, 12.0, 12.0]), ["C", "N"], 1.0, seed=4344)
+    ref = Oracle(p).calculate(cfg.pos, cfg.types, cfg.cell)
+    for prec, etol, ftol in ((MIXED, MIXED_E_REL_TOL, MIXED_F_ABS_TOL), (FP64, E_REL_TOL, F_ABS_TOL)):
+        c = Calculator(precision=prec)
+        c.set_contraction(4)
+        c.load_params(p)
+        r = c.evaluate(cfg.pos, cfg.types, cfg.cell)
+        assert c.tuning()["tc4"] == (1 if prec == MIXED else 0)
+        assert abs(r["energy"] - ref["energy"]) <= etol * max(1.0, abs(ref["energy"]))
+        assert np.abs(r["force"] - ref["force"]).max() <= ftol
