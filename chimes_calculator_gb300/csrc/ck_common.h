@@ -54,6 +54,9 @@ struct PairRec {
     double xavg, xdiff;    // Morse-map constants 0.5*(xmax+xmin), -0.5*(xmax-xmin)
     int ncoef;             // = 2B order
     int coef_off;          // offset into c2d/c2f/p2
+    // reciprocals for the 2-body kernels (as TupleRec): 1/lam, 1/xdiff, and the
+    // cutoff's 1/rc (cubic) or Tersoff threshold rc - f*rc and 1/(rc - threshold)
+    double inv_lam, inv_xdiff, fc_th, fc_inv;
 };
 
 // One ordered atom-type tuple of a 3- or 4-body cluster.  Cutoffs, lambdas and

@@ -173,9 +173,14 @@ __device__ __forceinline__ void virial_add(double* vir, double f, const double* 
 template <typename CT>
 __device__ __forceinline__ void pair_2b(const DevParamSet& P, const PairRec& pr, double dist, int* flags, double& E,
                                         double& fs) {
-    double xd, dxdr;
-    bool oor;
-    morse_x(dist, pr.rin, pr.lam, pr.xavg, pr.xdiff, xd, dxdr, oor);
+    // the Morse map with the pair type's reciprocals (no FP64 divisions:
+    // GB300 issues FP64 at a small fraction of the FP32 rate, and a division
+    // is several FP64 instructions)
+    const bool oor = dist < pr.rin;
+    const double rr = oor ? pr.rin : dist;
+    const double ex = exp(-rr * pr.inv_lam);
+    const double xd = (ex - pr.xavg) * pr.inv_xdiff;
+    const double dxdr = -ex * pr.inv_lam * pr.inv_xdiff;
     const CT* a = coef2<CT>(P) + pr.coef_off;   // dense a_n, n = 0..o2
     const CT x = CT(xd), tx = CT(2) * x;
     CT t0c = CT(1), t1c = x, u0 = CT(1), u1 = tx;
@@ -195,9 +200,24 @@ __device__ __forceinline__ void pair_2b(const DevParamSet& P, const PairRec& pr,
         Sd += P.inner_smooth * (damp - 1.0) * Gd;
         Gd *= damp;
     }
-    CT fcc, fcdc;
-    fcut_eval<CT>(P, dist, pr.rout, fcc, fcdc);
-    const double fc = double(fcc), fcd = double(fcdc);
+    double fc, fcd;
+    if (!P.tersoff) {
+        const double f0 = 1.0 - dist * pr.fc_inv;
+        fc = f0 * f0 * f0;
+        fcd = f0 * f0 * (-3.0 * pr.fc_inv);
+    } else if (dist < pr.fc_th) {
+        fc = 1.0;
+        fcd = 0.0;
+    } else if (dist > pr.rout) {
+        fc = 0.0;
+        fcd = 0.0;
+    } else {
+        const double f0 = (dist - pr.fc_th) * pr.fc_inv * kPi + kPi / 2.0;
+        double sn, cs;
+        sincos(f0, &sn, &cs);
+        fc = 0.5 + 0.5 * sn;
+        fcd = 0.5 * cs * (kPi * pr.fc_inv);
+    }
     E = fc * Sd;
     const double dx_inv = dist > 0.0 ? 1.0 / dist : 1e20;
     fs = (fc * Gd + fcd * Sd) * dx_inv;

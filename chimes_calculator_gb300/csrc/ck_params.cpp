@@ -868,6 +868,15 @@ ParamImage pack_params(const HostParams& P) {
     for (int p = 0; p < P.npairs; p++) {
         pr[p].rin = P.rin[p]; pr[p].rout = P.rout[p]; pr[p].lam = P.lam[p];
         morse_consts(P.rin[p], P.rout[p], P.lam[p], pr[p].xavg, pr[p].xdiff);
+        pr[p].inv_lam = 1.0 / pr[p].lam;
+        pr[p].inv_xdiff = 1.0 / pr[p].xdiff;
+        if (P.tersoff) {
+            pr[p].fc_th = pr[p].rout - P.fcut_var * pr[p].rout;
+            pr[p].fc_inv = 1.0 / (pr[p].rout - pr[p].fc_th);
+        } else {
+            pr[p].fc_th = 0.0;
+            pr[p].fc_inv = 1.0 / pr[p].rout;
+        }
         // dense table a_n (n = 0..o2) with a_{pow+1} = sum of the coefficients of
         // that power: the 2B kernel sums along the Chebyshev recursion
         pr[p].ncoef = P.o2 + 1;
