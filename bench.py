@@ -14,12 +14,12 @@ value : atom-evaluations/s with the inputs resident in HBM, CUDA events on
         before every step;
 e2e   : the same metric through the reference-facing C ABI
         (calculate_chimes_instance) with host arrays, timed on the host.
-the benchmark spec (default, one GPU): the batched mixed-size workload in FP64 and
+targets (default, one GPU): the batched mixed-size workload in FP64 and
         mixed against the plain FP64 path one configuration per call, the
         serving loop (p50/p99 latency at three offered rates) against the
         plain path one request at a time, and the mixed form's error against
         the reference's FP64 results in the committed fixtures; about a
-        minute (--no-north-star skips it).
+        minute (--no-targets skips it).
 Under torchrun each rank runs an independent replica (weak scaling; the path
 has no exchange step, so there is no collective on the data path).
 
@@ -429,8 +429,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "check": check,
         }
-        if world == 1 and not args.no_north_star and not args.profile_run:
-            line["north_star"] = north_star(args)
+        if world == 1 and not args.no_targets and not args.profile_run:
+            line["targets"] = targets(args)
         if args.extras:
             line["extras"] = extras(args)
         print(json.dumps(line))
@@ -485,7 +485,7 @@ def gen_processes():
     return max(1, min(8, os.cpu_count() or 1))
 
 
-def north_star(args):
+def targets(args):
     """The comparisons the path is built for, on bounded samples of their
     workloads (seeded synthetic configurations):
       batched : the 4096-configuration mixed-size workload (8-512 atoms,
@@ -953,7 +953,7 @@ def main():
     ap.add_argument("--extras", action="store_true",
                     help="also time the mixed form on C2, the 32768-atom configuration, the pair-style path "
                          "and the fingerprint pipeline")
-    ap.add_argument("--no-north-star", action="store_true",
+    ap.add_argument("--no-targets", action="store_true",
                     help="skip the batched / plain / serving / error block of the default line")
     ap.add_argument("--serve-requests", type=int, default=6000)
     ap.add_argument("--serve-workers", type=int, default=4)
