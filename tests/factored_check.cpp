@@ -3,6 +3,8 @@
 // the same S = sum a prod T and G_p = sum a dT_p prod_{q!=p} T through the
 // per-coefficient packed powers and through the row/column factored lists
 // (whose last entry per record carries the record-end bit).
+// The tensor-core images of the tuples (3-body at its own width, 4-body) hold
+// the same coefficient matrix: X . A . Y reproduces S, and the padding is zero.
 // With a second argument (a binary parameter cache of the same file) it also
 // checks that the cache packs into the same device image as the text file.
 // Usage: factored_check <params> [cache]; prints "ok <tuples checked>" or a mismatch.
@@ -45,7 +47,7 @@ int main(int argc, char** argv) {
     }
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> U(-1.0, 1.0);
-    int checked = 0;
+    int checked = 0, tc_checked = 0;
     for (int nb = 3; nb <= 4; nb++) {
         const int order = nb == 3 ? H.o3 : H.o4;
         const int Rp = nb == 3 ? H.R3 : H.R4;
@@ -161,9 +163,39 @@ int main(int argc, char** argv) {
                 std::printf("mismatch %d-body tuple %d: S %.17g vs %.17g\n", nb, u, S1, S0);
                 return 1;
             }
+            // tensor-core image (the B operand: N rows of K values, core-matrix
+            // layout, kTc3Parts parts): the parts' sum is the coefficient matrix
+            // (rows = the first K pairs' powers, columns = the rest), zero in
+            // the padding, and S = X . A . Y reproduces the per-coefficient sum
+            const float* tcimg = nb == 3 ? (H.tc3 ? at(img.bytes, H.tc3) : nullptr)
+                                         : (H.tc4 ? at(img.bytes, H.tc4) : nullptr);
+            const long long ntc = nb == 3 ? H.n_tc3 : H.n_tc4;
+            if (tcimg && R.tc_off >= 0) {
+                const int nrow = nx, ncol = ny;   // R^K rows (I), R^(P-K) columns (J)
+                const int kpad = nb == 3 ? tc3_kpad(Rp) : tc4_kpad(nrow);
+                const int npad = nb == 3 ? tc3_npad(Rp) : tc4_npad(ncol);
+                const long long part = (long long)kpad * npad;
+                if (R.tc_off + kTc3Parts * part > ntc) { std::printf("tensor-core image out of range\n"); return 1; }
+                double S2 = 0, pad = 0;
+                for (int n = 0; n < npad; n++)
+                    for (int k = 0; k < kpad; k++) {
+                        const long long off = ((long long)(n / 8) * (kpad / 4) + k / 4) * 32 + (n % 8) * 4 + (k % 4);
+                        double a = 0;
+                        for (int t = 0; t < kTc3Parts; t++) a += (double)tcimg[R.tc_off + t * part + off];
+                        // 3-body columns at Rw = R are q1 * R + q2, i.e. J itself
+                        if (n >= ncol || k >= nrow) { pad += std::fabs(a); continue; }
+                        S2 += prod_of(k, 0, K, -1) * a * prod_of(n, K, np, -1);
+                    }
+                if (pad != 0.0 || std::fabs(S2 - S0) > 1e-6 * scale) {
+                    std::printf("tensor-core image mismatch %d-body tuple %d: S %.17g vs %.17g (padding %g)\n", nb, u,
+                                S2, S0, pad);
+                    return 1;
+                }
+                tc_checked++;
+            }
             checked++;
         }
     }
-    std::printf("ok %d\n", checked);
+    std::printf("ok %d (tensor-core images %d)\n", checked, tc_checked);
     return 0;
 }

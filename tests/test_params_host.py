@@ -124,6 +124,8 @@ def factored_check(tmp_path_factory):
 
 
 def test_factored_tables_reproduce_the_coefficient_sums(factored_check, golden, tmp_path):
+    """Per tuple of every parameter file: the factored lists and the tensor-core
+    images (3-body and 4-body) give the per-coefficient sums."""
     import subprocess
     paths = [g.params for g in golden.values()]
     for k, spec in enumerate([synth.spec_c3(), synth.spec_c4()] + list(synth.specs_c5())):
