@@ -464,9 +464,12 @@ void launch_tc_r(const BatchView& B, cudaStream_t st) {
 // v of cluster c and reads its TMEM row back), so one M = 128, N = R^3 MMA
 // chain gives W, W_ij, W_ik, W_il for all 32 clusters; each row is then
 // contracted with the cluster's column tables, and warp 0 forms the forces.
-// Operands in three TF32 parts as in the 3-body kernel (six part products,
-// smallest first).  Pair tables are computed by the four threads of a
-// cluster (pairs v and v + 4), after the early-outs of all six pairs.
+// Operands in three TF32 parts as in the 3-body kernel: the five small part
+// products (smallest first) and the large one go into two accumulators that
+// are summed in FP32.  The A operand passes through one shared-memory buffer
+// in K halves (R = 4: 2 x 32), which lets two CTAs share an SM.  Pair tables
+// are computed by the four threads of a cluster (pairs v and v + 4), after
+// the early-outs of all six pairs.
 constexpr int kTc4Tile = 32;              // clusters per tile
 
 template <int R>
