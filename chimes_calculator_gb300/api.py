@@ -220,7 +220,8 @@ class Calculator:
         """3-/4-body contraction kernels: True/1 factored (default), False/0
         per-coefficient, 2 factored without the per-entry pair-table cache,
         3 factored with the 3-body column products formed per coefficient,
-        4 factored with the 3-body contraction on the tensor cores (mixed form)."""
+        4 factored with the 3-body and 4-body contractions on the tensor cores
+        (mixed form; tuning()["tc3"] and ["tc4"] report which run)."""
         self._check(self.lib.ck_set_contraction(self.h, int(factored)))
 
     def autotune(self, packed=None):
